@@ -1,0 +1,28 @@
+// Launch interface of the McICA sub-column generator (lw_mcica.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+enum McicaMode {
+  MCICA_PERCOL_MT = 0,    // Mersenne twister, column c seeded with seed + c (reference called per column)
+  MCICA_STREAM_MT = 1,    // Mersenne twister, one sequence for the whole call (the reference's own call)
+  MCICA_PERCOL_KISS = 2,  // KISS, seeds from each column's bottom pressures (irng = 0)
+};
+
+// Device pointers, Fortran layouts with column leading dimension ld:
+// cldfrac/ciwp/clwp/rei/rel/play/alpha (ld, nlay); tauc (16, ld, nlay);
+// cldfmcl/ciwpmcl/clwpmcl/taucmcl (140, ld, nlay); reicmcl/relqmcl (ld, nlay).
+struct McicaArgs {
+  int mode, ncol, nlay, icld, seed, ncol_call, ndraw_per_col;
+  long long ld;
+  const double *play, *cldfrac, *ciwp, *clwp, *rei, *rel, *tauc, *alpha;
+  double *cldfmcl, *ciwpmcl, *clwpmcl, *taucmcl, *reicmcl, *relqmcl;
+  int ngb[140];
+};
+
+// Number of doubles of draw scratch the launch needs.
+size_t gb_mcica_draw_count(int ncol, int nlay, int icld);
+// seed_per_column: column c of the launch uses seed + c (MT) or warms KISS up
+// seed + c times, reproducing one reference call per column.
+cudaError_t gb_mcica_launch(const McicaArgs& a, double* d_draws, int* d_err, cudaStream_t stream,
+                            bool seed_per_column);

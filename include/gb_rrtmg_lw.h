@@ -1,0 +1,155 @@
+/*
+ * gb_rrtmg_lw.h -- C ABI of the GB300-native RRTMG_LW longwave column solver.
+ *
+ * Drop-in boundary for BRAMS's radiation driver: each entry point replaces
+ * one routine of the reference (luflarois/brams, src/rrtmg/RRTMG_LW/src/)
+ * and keeps its argument list, units and Fortran (column-major) layouts.
+ * All reals are double precision as in the reference (kind_rb).  Arrays that
+ * the reference declares (ncol, ...) take an explicit leading dimension
+ * (ld_in / ld_out >= ncol), so callers can pass BRAMS's wider allocations
+ * (e.g. outputs allocated (nofcols, nlay+2), rtm_driver.f90:913-922).
+ *
+ * Return value: 0 on success.  Positive values are the reference's STOP
+ * conditions (GB_LW_E_*), reported instead of stopping the process;
+ * negative values are argument, memory or CUDA errors.
+ *
+ * Threading: a context may be used by one host thread at a time.  Separate
+ * contexts (or separate streams with the *_device entry points) run
+ * concurrently.
+ */
+#ifndef GB_RRTMG_LW_H
+#define GB_RRTMG_LW_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gb_lw_context gb_lw_context;
+
+/* status codes */
+#define GB_LW_OK 0
+#define GB_LW_E_INFLAG1 2      /* cldprmc: 'INFLAG = 1 OPTION NOT AVAILABLE WITH MCICA'   */
+#define GB_LW_E_ICE_SMALL 3    /* cldprmc/cldprop: 'ICE RADIUS TOO SMALL'               */
+#define GB_LW_E_ICE_BOUNDS 4   /* cldprmc/cldprop: 'ICE RADIUS OUT OF BOUNDS'           */
+#define GB_LW_E_DGE_BOUNDS 5   /* cldprmc/cldprop: 'ICE GENERALIZED EFFECTIVE SIZE ...'  */
+#define GB_LW_E_LIQ_BOUNDS 6   /* cldprmc/cldprop: 'LIQUID EFFECTIVE RADIUS OUT OF BOUNDS' */
+#define GB_LW_E_ICLD 7         /* mcica_subcol_lw: 'INVALID ICLD'                        */
+#define GB_LW_E_KISS_PMID 8    /* generate_stochastic_clouds: KISS seed needs pmid(1) >= pmid(2) */
+#define GB_LW_E_LAYTROP 9      /* pressure does not decrease with layer index            */
+#define GB_LW_E_BADVAL 11      /* non-positive or non-finite layer pressure/temperature  */
+#define GB_LW_E_ARGS (-1)      /* invalid sizes, flags or null pointers                  */
+#define GB_LW_E_CUDA (-2)      /* CUDA runtime error (see gb_rrtmg_lw_last_error)        */
+#define GB_LW_E_TABLES (-3)    /* table files missing or malformed                       */
+#define GB_LW_E_NOMEM (-4)     /* device or pinned-host allocation failed                */
+
+/* Replaces rrtmg_lw_ini(cpdair) (rrtmg_lw_init.f90:47; called from
+ * mem_rrtm.f90:114).  Loads the tables from table_dir (NULL: the directory
+ * installed next to this library) onto CUDA device `device` and returns a
+ * context.  cpdair is the specific heat of dry air used in heatfac
+ * (BRAMS: cp = 1004.). */
+int gb_rrtmg_lw_ini(double cpdair, const char* table_dir, int device, gb_lw_context** ctx);
+
+/* Releases all device memory, streams and events of the context. */
+int gb_rrtmg_lw_free(gb_lw_context* ctx);
+
+/* Replaces rrtmg_lw (rrtmg_lw_rad.f90:99-108, called at rtm_driver.f90:1313)
+ * for HOST arrays.  icld is in/out as in the reference (values outside 0..3
+ * become 2).  Layout (ld = ld_in for inputs, ld_out for outputs):
+ *   play tlay h2ovmr o3vmr co2vmr ch4vmr n2ovmr o2vmr cfc11vmr cfc12vmr
+ *   cfc22vmr ccl4vmr reicmcl relqmcl             (ld, nlay)
+ *   plev tlev                                     (ld, nlay+1)
+ *   tsfc (ncol), emis (ld, 16), tauaer (ld, nlay, 16)
+ *   cldfmcl taucmcl ciwpmcl clwpmcl               (140, ld, nlay)
+ *   uflx dflx uflxc dflxc duflx_dt duflxc_dt      (ld_out, nlay+1)
+ *   hr hrc                                        (ld_out, nlay)
+ * duflx_dt / duflxc_dt are written only when idrv == 1 (may be NULL
+ * otherwise); the McICA arrays may be NULL when icld == 0.  Columns are
+ * streamed to the GPU in chunks; page-locked host buffers are copied by DMA
+ * while earlier chunks compute. */
+int gb_rrtmg_lw(gb_lw_context* ctx, int ncol, int nlay, int* icld, int idrv,
+                const double* play, const double* plev, const double* tlay, const double* tlev,
+                const double* tsfc, const double* h2ovmr, const double* o3vmr, const double* co2vmr,
+                const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+                const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr,
+                const double* ccl4vmr, const double* emis, int inflglw, int iceflglw, int liqflglw,
+                const double* cldfmcl, const double* taucmcl, const double* ciwpmcl,
+                const double* clwpmcl, const double* reicmcl, const double* relqmcl,
+                const double* tauaer, double* uflx, double* dflx, double* hr, double* uflxc,
+                double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt,
+                int64_t ld_in, int64_t ld_out);
+
+/* Same computation on DEVICE arrays, enqueued on `stream` (a cudaStream_t,
+ * NULL for the default stream) without host synchronisation.  Per-column
+ * status codes go to d_col_status (device, ncol ints) when not NULL; the
+ * maximum status of all calls since the last gb_rrtmg_lw_sync_status is
+ * kept on the device. */
+int gb_rrtmg_lw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int* icld, int idrv,
+                       const double* play, const double* plev, const double* tlay,
+                       const double* tlev, const double* tsfc, const double* h2ovmr,
+                       const double* o3vmr, const double* co2vmr, const double* ch4vmr,
+                       const double* n2ovmr, const double* o2vmr, const double* cfc11vmr,
+                       const double* cfc12vmr, const double* cfc22vmr, const double* ccl4vmr,
+                       const double* emis, int inflglw, int iceflglw, int liqflglw,
+                       const double* cldfmcl, const double* taucmcl, const double* ciwpmcl,
+                       const double* clwpmcl, const double* reicmcl, const double* relqmcl,
+                       const double* tauaer, double* uflx, double* dflx, double* hr,
+                       double* uflxc, double* dflxc, double* hrc, double* duflx_dt,
+                       double* duflxc_dt, int64_t ld_in, int64_t ld_out, int* d_col_status);
+
+/* Waits for `stream` and returns (then clears) the maximum column status of
+ * the device calls made since the previous call. */
+int gb_rrtmg_lw_sync_status(gb_lw_context* ctx, void* stream);
+
+/* Replaces mcica_subcol_lw (mcica_subcol_gen_lw.f90:183-185, called at
+ * rtm_driver.f90:1262) for HOST arrays.  icld 0..5, irng 0 (KISS) or 1
+ * (Mersenne twister); draws are bit-identical to the reference's.
+ *   play cldfrac ciwp clwp rei rel alpha          (ld, nlay)
+ *   tauc                                          (16, ld, nlay)
+ *   cldfmcl ciwpmcl clwpmcl taucmcl               (140, ld, nlay)
+ *   reicmcl relqmcl                               (ld, nlay)
+ * seed_per_column = 0 reproduces one reference call over all columns
+ * (seed = permuteseed); 1 reproduces one reference call per column with
+ * seed = permuteseed + (column index, 0-based).  alpha may be NULL unless
+ * icld is 4 or 5. */
+int gb_mcica_subcol_lw(gb_lw_context* ctx, int ncol, int nlay, int icld, int permuteseed,
+                       int* irng, const double* play, const double* cldfrac, const double* ciwp,
+                       const double* clwp, const double* rei, const double* rel,
+                       const double* tauc, const double* alpha, double* cldfmcl,
+                       double* ciwpmcl, double* clwpmcl, double* reicmcl, double* relqmcl,
+                       double* taucmcl, int64_t ld, int seed_per_column);
+
+/* Same on DEVICE arrays, enqueued on `stream`. */
+int gb_mcica_subcol_lw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int icld,
+                              int permuteseed, int* irng, const double* play,
+                              const double* cldfrac, const double* ciwp, const double* clwp,
+                              const double* rei, const double* rel, const double* tauc,
+                              const double* alpha, double* cldfmcl, double* ciwpmcl,
+                              double* clwpmcl, double* reicmcl, double* relqmcl,
+                              double* taucmcl, int64_t ld, int seed_per_column);
+
+/* Diagnostics (no counterpart in the reference's interface): runs the same
+ * column kernel on host arrays (tight layout, ld = ncol) and also returns
+ * the gas-plus-aerosol optical depth taut and the Planck fraction of every
+ * (column, layer, g-point) in single precision, g fastest:
+ * taut[(icol*nlay + lay)*140 + g].  Used to check taumol band by band. */
+int gb_rrtmg_lw_gas_optics_diag(gb_lw_context* ctx, int ncol, int nlay, const double* play,
+                                const double* plev, const double* tlay, const double* tlev,
+                                const double* tsfc, const double* h2ovmr, const double* o3vmr,
+                                const double* co2vmr, const double* ch4vmr, const double* n2ovmr,
+                                const double* o2vmr, const double* cfc11vmr,
+                                const double* cfc12vmr, const double* cfc22vmr,
+                                const double* ccl4vmr, const double* emis, const double* tauaer,
+                                float* taut, float* fracs);
+
+/* Human-readable text of a status code (static storage). */
+const char* gb_rrtmg_lw_strerror(int code);
+/* Detail of the last failing call on this context (CUDA error text etc.). */
+const char* gb_rrtmg_lw_last_error(gb_lw_context* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GB_RRTMG_LW_H */

@@ -1,0 +1,184 @@
+"""ctypes front end of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this module; the product library never does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+DATA = os.path.join(ROOT, "brams_gb300", "data")
+_lib = {}
+
+_D = np.ctypeslib.ndpointer(dtype=np.float64, flags="F_CONTIGUOUS")
+
+
+def build(native: bool = False) -> str:
+    target = "native" if native else "all"
+    subprocess.run(["make", "-s", "-C", HERE, target], check=True)
+    return os.path.join(HERE, "_build", "liblworacle_native.so" if native else "liblworacle.so")
+
+
+def lib(native: bool = False):
+    key = "native" if native else "portable"
+    if key in _lib:
+        return _lib[key]
+    path = os.path.join(HERE, "_build", "liblworacle_native.so" if native else "liblworacle.so")
+    src = os.path.join(HERE, "lw_oracle.cpp")
+    if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+        build(native)
+    L = C.CDLL(path)
+    L.ora_init.restype = C.c_int
+    L.ora_init.argtypes = [C.c_double, C.c_char_p, C.c_char_p]
+    L.ora_error_string.restype = C.c_char_p
+    rc = L.ora_init(1004.0, os.path.join(DATA, "lw_ref_tables.gblw").encode(),
+                    os.path.join(DATA, "lw_ktables.gblw").encode())
+    if rc != 0:
+        raise RuntimeError(f"oracle init failed: {rc}")
+    _lib[key] = L
+    return L
+
+
+def _p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def _f(a):
+    return np.asfortranarray(a, dtype=np.float64)
+
+
+STATE_ORDER = ["play", "plev", "tlay", "tlev", "tsfc", "h2ovmr", "o3vmr", "co2vmr", "ch4vmr",
+               "n2ovmr", "o2vmr", "cfc11vmr", "cfc12vmr", "cfc22vmr", "ccl4vmr", "emis"]
+CLOUD_ORDER = ["cldfmcl", "taucmcl", "ciwpmcl", "clwpmcl", "reicmcl", "relqmcl"]
+
+
+def rrtmg_lw(state: dict, mc: dict, icld: int = 3, idrv: int = 1, inflglw: int = 2,
+             iceflglw: int = 3, liqflglw: int = 1, nthreads: int = 1, native: bool = False) -> dict:
+    """Reference-order FP64 rrtmg_lw on Fortran-ordered arrays; returns the outputs."""
+    L = lib(native)
+    ncol, nlay = state["play"].shape
+    st = [_f(state[k]) for k in STATE_ORDER]
+    cl = [_f(mc[k]) for k in CLOUD_ORDER]
+    tauaer = _f(state["tauaer"])
+    out = {k: np.zeros((ncol, nlay + 1), order="F") for k in ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt")}
+    out["hr"] = np.zeros((ncol, nlay), order="F")
+    out["hrc"] = np.zeros((ncol, nlay), order="F")
+    ic = C.c_int(icld)
+    args = [C.c_int(ncol), C.c_int(nlay), C.byref(ic), C.c_int(idrv)] + [_p(a) for a in st]
+    args += [C.c_int(inflglw), C.c_int(iceflglw), C.c_int(liqflglw)] + [_p(a) for a in cl] + [_p(tauaer)]
+    args += [_p(out[k]) for k in ("uflx", "dflx", "hr", "uflxc", "dflxc", "hrc", "duflx_dt", "duflxc_dt")]
+    args += [C.c_int(nthreads)]
+    rc = L.ora_rrtmg_lw(*args)
+    if rc != 0:
+        raise RuntimeError(f"oracle rrtmg_lw: {L.ora_error_string(rc).decode()}")
+    out["icld"] = ic.value
+    return out
+
+
+def column_intermediates(state: dict, mc: dict, icol: int, icld: int = 3, inflglw: int = 2,
+                         iceflglw: int = 3, liqflglw: int = 1) -> dict:
+    L = lib()
+    ncol, nlay = state["play"].shape
+    st = [_f(state[k]) for k in STATE_ORDER]
+    cl = [_f(mc[k]) for k in CLOUD_ORDER]
+    o = {"taug": np.zeros((nlay, 140), order="F"), "fracs": np.zeros((nlay, 140), order="F"),
+         "taut": np.zeros((nlay, 140), order="F"), "planklay": np.zeros((nlay, 16), order="F"),
+         "planklev": np.zeros((nlay + 1, 16), order="F"), "plankbnd": np.zeros(16),
+         "taucmc": np.zeros((140, nlay), order="F")}
+    lt = C.c_int(0)
+    args = [C.c_int(ncol), C.c_int(nlay), C.c_int(icol), C.c_int(icld)] + [_p(a) for a in st]
+    args += [C.c_int(inflglw), C.c_int(iceflglw), C.c_int(liqflglw)] + [_p(a) for a in cl]
+    args += [_p(_f(state["tauaer"]))]
+    args += [_p(o[k]) for k in ("taug", "fracs", "taut", "planklay", "planklev", "plankbnd", "taucmc")]
+    args += [C.byref(lt)]
+    rc = L.ora_column_intermediates(*args)
+    if rc != 0:
+        raise RuntimeError(f"oracle intermediates: {L.ora_error_string(rc).decode()}")
+    o["laytrop"] = lt.value
+    return o
+
+
+def cldprop_columns(state: dict, inflag: int = 2, iceflag: int = 3, liqflag: int = 1) -> np.ndarray:
+    """BRAMS's per-column cldprop call (rtm_driver.f90:1250-1258): tauc (16, ncol, nlay)."""
+    L = lib()
+    ncol, nlay = state["play"].shape
+    tauc_in = np.zeros((16, nlay), order="F")
+    out = np.zeros((16, ncol, nlay), order="F")
+    tc = np.zeros((nlay, 16), order="F")
+    nb = C.c_int(0)
+    for i in range(ncol):
+        cf = np.ascontiguousarray(state["cldfrac"][i, :])
+        ci = np.ascontiguousarray(state["ciwp"][i, :])
+        cw = np.ascontiguousarray(state["clwp"][i, :])
+        re = np.ascontiguousarray(state["rei"][i, :])
+        rl = np.ascontiguousarray(state["rel"][i, :])
+        rc = L.ora_cldprop(C.c_int(nlay), C.c_int(inflag), C.c_int(iceflag), C.c_int(liqflag),
+                           _p(cf), _p(tauc_in), _p(ci), _p(cw), _p(re), _p(rl), C.byref(nb), _p(tc))
+        if rc != 0:
+            raise RuntimeError(f"oracle cldprop: {L.ora_error_string(rc).decode()}")
+        out[:, i, :] = tc.T
+    return out
+
+
+def mcica_subcol_lw(state: dict, tauc: np.ndarray, icld: int, permuteseed: int, irng: int = 1,
+                    alpha: np.ndarray | None = None) -> dict:
+    """One call of mcica_subcol_lw over all columns (BRAMS draw order)."""
+    L = lib()
+    ncol, nlay = state["play"].shape
+    o = {k: np.zeros((140, ncol, nlay), order="F") for k in ("cldfmcl", "ciwpmcl", "clwpmcl", "taucmcl")}
+    o["reicmcl"] = np.zeros((ncol, nlay), order="F")
+    o["relqmcl"] = np.zeros((ncol, nlay), order="F")
+    ir = C.c_int(irng)
+    rc = L.ora_mcica_subcol_lw(C.c_int(ncol), C.c_int(nlay), C.c_int(icld), C.c_int(permuteseed), C.byref(ir),
+                               _p(_f(state["play"])), _p(_f(state["cldfrac"])), _p(_f(state["ciwp"])),
+                               _p(_f(state["clwp"])), _p(_f(state["rei"])), _p(_f(state["rel"])),
+                               _p(_f(tauc)), _p(_f(alpha) if alpha is not None else None),
+                               _p(o["cldfmcl"]), _p(o["ciwpmcl"]), _p(o["clwpmcl"]), _p(o["reicmcl"]),
+                               _p(o["relqmcl"]), _p(o["taucmcl"]))
+    if rc != 0:
+        raise RuntimeError(f"oracle mcica: {L.ora_error_string(rc).decode()}")
+    return o
+
+
+def mcica_per_column(state: dict, tauc: np.ndarray, icld: int, base_seed: int, irng: int = 1) -> dict:
+    """Per-column seeding (seed = base + column index, 0-based): the reference
+    generator called with ncol = 1 for each column."""
+    ncol, nlay = state["play"].shape
+    o = {k: np.zeros((140, ncol, nlay), order="F") for k in ("cldfmcl", "ciwpmcl", "clwpmcl", "taucmcl")}
+    o["reicmcl"] = np.asfortranarray(state["rei"].copy())
+    o["relqmcl"] = np.asfortranarray(state["rel"].copy())
+    for i in range(ncol):
+        sub = {k: np.asfortranarray(state[k][i:i + 1, :]) for k in ("play", "cldfrac", "ciwp", "clwp", "rei", "rel")}
+        r = mcica_subcol_lw(sub, np.asfortranarray(tauc[:, i:i + 1, :]), icld, base_seed + i, irng)
+        for k in ("cldfmcl", "ciwpmcl", "clwpmcl", "taucmcl"):
+            o[k][:, i, :] = r[k][:, 0, :]
+    return o
+
+
+def mt_draws(seed: int, n: int):
+    L = lib()
+    ints = np.zeros(n, dtype=np.uint32)
+    reals = np.zeros(n)
+    L.ora_mt_draws(C.c_int32(seed), C.c_int(n), ints.ctypes.data_as(C.POINTER(C.c_uint32)), _p(reals))
+    return ints, reals
+
+
+def kiss_draws(s1: int, s2: int, s3: int, s4: int, n: int) -> np.ndarray:
+    L = lib()
+    reals = np.zeros(n)
+    L.ora_kiss_draws(C.c_int32(s1), C.c_int32(s2), C.c_int32(s3), C.c_int32(s4), C.c_int(n), _p(reals))
+    return reals
+
+
+def lookup_tables():
+    L = lib()
+    tau, ex, tfn = np.zeros(10001), np.zeros(10001), np.zeros(10001)
+    hf, ff = C.c_double(0), C.c_double(0)
+    L.ora_get_tables(_p(tau), _p(ex), _p(tfn), C.byref(hf), C.byref(ff))
+    return tau, ex, tfn, hf.value, ff.value
