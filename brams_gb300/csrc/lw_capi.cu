@@ -557,6 +557,7 @@ const char* gb_rrtmg_lw_strerror(int code) {
     case GB_LW_E_CUDA: return "CUDA error";
     case GB_LW_E_TABLES: return "table files missing or malformed";
     case GB_LW_E_NOMEM: return "allocation failed";
+    case GB_LW_E_SCRATCH: return "call exceeds the fixed scratch of gb_mcica_subcol_lw_noalloc (4,194,304 draws)";
   }
   return "unknown status";
 }

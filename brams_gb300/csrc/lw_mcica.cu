@@ -16,6 +16,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
+#include "../../include/gb_rrtmg_lw.h"
 #include "lw_common.h"
 #include "lw_mcica.h"
 
@@ -278,4 +281,95 @@ cudaError_t gb_mcica_launch(const McicaArgs& a, double* d_draws, int* d_err, cud
 size_t gb_mcica_draw_count(int ncol, int nlay, int icld) {
   const int per = icld == 3 ? 1 : (icld <= 2 ? nlay : 2 * nlay);
   return (size_t)GB_NGPT * per * (size_t)ncol;
+}
+
+// ----------------------------------------------------------------------------
+// Allocation-free McICA entry point.
+//
+// Some callers must not allocate device memory while a model runs: a host
+// model whose device memory is owned by another runtime (an OpenACC or
+// OpenMP-offload data region, or a pooled allocator that forbids allocations
+// outside its pool), and time-stepping codes that cannot afford the implicit
+// device-wide synchronisation of cudaMalloc/cudaFree in the middle of a step.
+// gb_mcica_subcol_lw_noalloc serves them: its draw buffer is this fixed
+// file-scope array, so a call allocates nothing.  Every GPU that loads the
+// library holds the array until the process exits.
+//
+// Layout: the first 256 bytes hold the status word, the rest holds draws.
+// All calls share the array and it keeps the previous call's contents: the
+// status word is cleared at the start of every call, and every draw slot a
+// call reads is written by that call first.  Calls whose kernels overlap on
+// the GPU (different streams without ordering, or several host threads)
+// race on the array and must be serialised by the caller.
+static __device__ __align__(256) double g_mcica_scratch[GB_MCICA_NOALLOC_STATUS_DOUBLES + GB_MCICA_NOALLOC_MAX_DRAWS];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mutex;
+double* g_scratch_ptr[kMaxDevices] = {nullptr};
+
+// Device address of g_mcica_scratch on the current device.  In host code the
+// array's name stands for a host-side shadow, not a device address, so the
+// address is queried once per device (with that device current) and cached.
+cudaError_t scratch_on_current_device(double** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_mcica_scratch);
+    if (e != cudaSuccess) return e;
+    g_scratch_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_scratch_ptr[dev];
+  return cudaSuccess;
+}
+}  // namespace
+
+extern "C" int gb_mcica_subcol_lw_noalloc(void* stream, int ncol, int nlay, int icld, int permuteseed, int* irng,
+                                          const double* play, const double* cldfrac, const double* ciwp,
+                                          const double* clwp, const double* rei, const double* rel,
+                                          const double* tauc, const double* alpha, double* cldfmcl,
+                                          double* ciwpmcl, double* clwpmcl, double* reicmcl, double* relqmcl,
+                                          double* taucmcl, int64_t ld, int seed_per_column, int* d_status) {
+  if (!irng) return GB_LW_E_ARGS;
+  if (icld == 0) return GB_LW_OK;
+  if (icld < 0 || icld > 5) return GB_LW_E_ICLD;
+  if (ncol < 0 || nlay < 1 || ld < ncol) return GB_LW_E_ARGS;
+  if (*irng != 0) *irng = 1;
+  if (icld >= 4 && !alpha) return GB_LW_E_ARGS;
+  if (*irng == 0 && nlay < 4) return GB_LW_E_ARGS;
+  if (!play || !cldfrac || !ciwp || !clwp || !rei || !rel || !tauc || !cldfmcl || !ciwpmcl || !clwpmcl ||
+      !reicmcl || !relqmcl || !taucmcl)
+    return GB_LW_E_ARGS;
+  if (ncol == 0) return GB_LW_OK;
+  if (gb_mcica_draw_count(ncol, nlay, icld) > (size_t)GB_MCICA_NOALLOC_MAX_DRAWS) return GB_LW_E_SCRATCH;
+  double* scratch = nullptr;
+  if (scratch_on_current_device(&scratch) != cudaSuccess) return GB_LW_E_CUDA;
+  cudaStream_t s = (cudaStream_t)stream;
+  int* status = reinterpret_cast<int*>(scratch);
+  if (cudaMemsetAsync(status, 0, sizeof(int), s) != cudaSuccess) return GB_LW_E_CUDA;
+  McicaArgs a{};
+  a.mode = *irng == 0 ? MCICA_PERCOL_KISS : (seed_per_column ? MCICA_PERCOL_MT : MCICA_STREAM_MT);
+  a.ncol = ncol;
+  a.nlay = nlay;
+  a.icld = icld;
+  a.seed = permuteseed;
+  a.ncol_call = seed_per_column ? 1 : ncol;
+  a.ld = ld;
+  a.play = play; a.cldfrac = cldfrac; a.ciwp = ciwp; a.clwp = clwp; a.rei = rei; a.rel = rel;
+  a.tauc = tauc; a.alpha = alpha;
+  a.cldfmcl = cldfmcl; a.ciwpmcl = ciwpmcl; a.clwpmcl = clwpmcl; a.taucmcl = taucmcl;
+  a.reicmcl = reicmcl; a.relqmcl = relqmcl;
+  // g-point -> band map (rrtmg_lw_init.f90:359-374): band b owns ng(b) consecutive g-points
+  static const int ng_list[16] = GB_NG_LIST;
+  for (int b = 0, g = 0; b < 16; ++b)
+    for (int k = 0; k < ng_list[b]; ++k) a.ngb[g++] = b + 1;
+  if (gb_mcica_launch(a, scratch + GB_MCICA_NOALLOC_STATUS_DOUBLES, status, s, seed_per_column != 0) != cudaSuccess)
+    return GB_LW_E_CUDA;
+  if (d_status && cudaMemcpyAsync(d_status, status, sizeof(int), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return GB_LW_E_CUDA;
+  return GB_LW_OK;
 }

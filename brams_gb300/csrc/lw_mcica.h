@@ -20,6 +20,11 @@ struct McicaArgs {
   int ngb[140];
 };
 
+// Fixed scratch of the allocation-free entry point: a 256-byte status area
+// followed by GB_MCICA_NOALLOC_MAX_DRAWS doubles (4 Mi draws, 32 MiB in all).
+#define GB_MCICA_NOALLOC_STATUS_DOUBLES 32
+#define GB_MCICA_NOALLOC_MAX_DRAWS (4 * 1024 * 1024)
+
 // Number of doubles of draw scratch the launch needs.
 size_t gb_mcica_draw_count(int ncol, int nlay, int icld);
 // seed_per_column: column c of the launch uses seed + c (MT) or warms KISS up

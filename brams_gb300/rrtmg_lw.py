@@ -35,6 +35,7 @@ EXPORTS = [
     "gb_rrtmg_lw_ini", "gb_rrtmg_lw_free", "gb_rrtmg_lw", "gb_rrtmg_lw_device",
     "gb_rrtmg_lw_sync_status", "gb_mcica_subcol_lw", "gb_mcica_subcol_lw_device",
     "gb_rrtmg_lw_strerror", "gb_rrtmg_lw_last_error", "gb_rrtmg_lw_gas_optics_diag",
+    "gb_mcica_subcol_lw_noalloc",
 ]
 
 
@@ -67,6 +68,7 @@ def load_library(path: str = LIB_PATH):
         L.gb_mcica_subcol_lw.argtypes = [P, I, I, I, I, IP] + [P] * 8 + [P] * 6 + [LL, I]
         L.gb_mcica_subcol_lw_device.argtypes = [P, P, I, I, I, I, IP] + [P] * 8 + [P] * 6 + [LL, I]
         L.gb_rrtmg_lw_gas_optics_diag.argtypes = [P, I, I] + [P] * 17 + [P, P]
+        L.gb_mcica_subcol_lw_noalloc.argtypes = [P, I, I, I, I, IP] + [P] * 8 + [P] * 6 + [LL, I, P]
         L.gb_rrtmg_lw_strerror.restype = C.c_char_p
         L.gb_rrtmg_lw_strerror.argtypes = [I]
         L.gb_rrtmg_lw_last_error.restype = C.c_char_p

@@ -43,6 +43,7 @@ typedef struct gb_lw_context gb_lw_context;
 #define GB_LW_E_CUDA (-2)      /* CUDA runtime error (see gb_rrtmg_lw_last_error)        */
 #define GB_LW_E_TABLES (-3)    /* table files missing or malformed                       */
 #define GB_LW_E_NOMEM (-4)     /* device or pinned-host allocation failed                */
+#define GB_LW_E_SCRATCH (-5)   /* call too large for the fixed scratch of gb_mcica_subcol_lw_noalloc */
 
 /* Replaces rrtmg_lw_ini(cpdair) (rrtmg_lw_init.f90:47; called from
  * mem_rrtm.f90:114).  Loads the tables from table_dir (NULL: the directory
@@ -142,6 +143,33 @@ int gb_rrtmg_lw_gas_optics_diag(gb_lw_context* ctx, int ncol, int nlay, const do
                                 const double* cfc12vmr, const double* cfc22vmr,
                                 const double* ccl4vmr, const double* emis, const double* tauaer,
                                 float* taut, float* fracs);
+
+/* Allocation-free variant of gb_mcica_subcol_lw_device.  It has no
+ * counterpart in the reference: it exists for callers that cannot allocate
+ * device memory during a run -- models whose device memory belongs to
+ * another runtime (OpenACC / OpenMP-offload data regions, pooled allocators)
+ * and time-stepping codes that cannot take the device-wide synchronisation
+ * that cudaMalloc/cudaFree may cause.  The caller passes device inputs and
+ * outputs as for gb_mcica_subcol_lw_device; no context is needed.  Draws go
+ * to a fixed array inside the library of 4 Mi doubles (32 MiB, held by every
+ * GPU that loads the library until exit), so
+ *   140 * ncol          (icld 3)
+ *   140 * ncol * nlay   (icld 1, 2)
+ *   280 * ncol * nlay   (icld 4, 5)
+ * must not exceed 4,194,304; larger calls return GB_LW_E_SCRATCH.  The first
+ * call on a device looks up the array's device address (once per device,
+ * with that device current); make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race,
+ * so order them (one stream, or events).  The reference's STOP status of the
+ * call (e.g. GB_LW_E_KISS_PMID) is copied to d_status (device int) when not
+ * NULL.  Enqueued on `stream` without host synchronisation. */
+int gb_mcica_subcol_lw_noalloc(void* stream, int ncol, int nlay, int icld, int permuteseed,
+                               int* irng, const double* play, const double* cldfrac,
+                               const double* ciwp, const double* clwp, const double* rei,
+                               const double* rel, const double* tauc, const double* alpha,
+                               double* cldfmcl, double* ciwpmcl, double* clwpmcl,
+                               double* reicmcl, double* relqmcl, double* taucmcl, int64_t ld,
+                               int seed_per_column, int* d_status);
 
 /* Human-readable text of a status code (static storage). */
 const char* gb_rrtmg_lw_strerror(int code);
