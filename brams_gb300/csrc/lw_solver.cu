@@ -30,7 +30,7 @@
 
 #include "lw_common.h"
 #include "lw_solver.h"
-#include "lw_taumol.cuh"
+#include "lw_gasoptics.cuh"
 
 namespace gb {
 
@@ -42,6 +42,7 @@ constexpr float BPADE = 1.0f / 0.278f;
 struct Smem {
   float* f;        // [NF][nl]   per-layer coefficients (phase 1-2)
   int* iv;         // [NI][nl]
+  float2* terms;   // [nl][MAXT_ALL] gas-optics terms of the current band (phase 2)
   float* part;     // [NWARP][nl+1][6] warp partial fluxes (aliases f/iv in phase 3-4)
   float* taut;     // [nl][140]
   float* taua;     // [nl][16]
@@ -58,7 +59,7 @@ struct Smem {
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
 __host__ __device__ inline size_t smem_bytes(int nl) {
-  size_t coef = (size_t)NF * nl * 4 + (size_t)NI * nl * 4;
+  size_t coef = (((size_t)(NF + NI) * nl * 4 + 7) & ~size_t(7)) + (size_t)nl * MAXT_ALL * 8;
   size_t part = (size_t)NWARP * (nl + 1) * 6 * 4;
   size_t a = align16(coef > part ? coef : part);
   a += align16((size_t)nl * GB_NGPT * 4);
@@ -74,11 +75,12 @@ __host__ __device__ inline size_t smem_bytes(int nl) {
 
 __device__ inline Smem carve(char* base, int nl) {
   Smem s;
-  size_t coef = (size_t)NF * nl * 4 + (size_t)NI * nl * 4;
+  size_t coef = (((size_t)(NF + NI) * nl * 4 + 7) & ~size_t(7)) + (size_t)nl * MAXT_ALL * 8;
   size_t part = (size_t)NWARP * (nl + 1) * 6 * 4;
   char* p = base;
   s.f = (float*)p;
   s.iv = (int*)(p + (size_t)NF * nl * 4);
+  s.terms = (float2*)(p + (((size_t)(NF + NI) * nl * 4 + 7) & ~size_t(7)));
   s.part = (float*)p;
   p += align16(coef > part ? coef : part);
   s.taut = (float*)p; p += align16((size_t)nl * GB_NGPT * 4);
@@ -111,7 +113,7 @@ struct TblEntry {
   float tau, trans, tfn;
 };
 __device__ __forceinline__ TblEntry tbl(float od) {
-  float tblind = od / (BPADE + od);
+  float tblind = __fdividef(od, BPADE + od);
   int itr = (int)(10000.0f * tblind + 0.5f);
   itr = itr < 0 ? 0 : (itr > 10000 ? 10000 : itr);
   TblEntry e;
@@ -120,13 +122,13 @@ __device__ __forceinline__ TblEntry tbl(float od) {
   } else if (itr == 10000) {
     e.tau = 1.0e10f; e.trans = 1.0e-20f; e.tfn = 1.0f;
   } else {
-    float t = __fdiv_rn((float)itr, 10000.0f);
-    float tau = BPADE * t / (1.0f - t);
+    float t = (float)itr * 1.0e-4f;
+    float tau = BPADE * __fdividef(t, 1.0f - t);
     float ex = __expf(-tau);
     ex = ex <= 1.0e-20f ? 1.0e-20f : ex;
     e.tau = tau;
     e.trans = ex;
-    e.tfn = tau < 0.06f ? tau / 6.0f : 1.0f - 2.0f * (1.0f / tau - ex / (1.0f - ex));
+    e.tfn = tau < 0.06f ? tau * (1.0f / 6.0f) : 1.0f - 2.0f * (__fdividef(1.0f, tau) - __fdividef(ex, 1.0f - ex));
   }
   return e;
 }
@@ -238,25 +240,39 @@ __device__ __forceinline__ float cell_cloud(const LwArgs& a, long long icol, int
       tauc = (float)tin;
     }
     odcld = secdiff_b * tauc;
-    efcl = (1.0f - __expf(-odcld));
+    efcl = 1.0f - __expf(-odcld);
   }
   return (float)cf;
 }
 
-// ------------------------------------------------------------------ taumol dispatch
+// ------------------------------------------------------------------ gas optics of one band
+// Prologue once per layer (terms into shared memory), barrier, then one
+// generic weighted gather per (layer, g) cell.
 template <int b>
-__device__ __forceinline__ void taumol_band(const Smem& s, int nl, int laytrop, const float* __restrict__ T) {
-  const int ng = c_T.band[b - 1].ng, g0 = c_T.band[b - 1].g0;
-  const int ncell = nl * ng;
-  Cell c{s.f, s.iv, nl, 0};
-  for (int cell = threadIdx.x; cell < ncell; cell += NT) {
-    int lay = cell / ng, gi = cell - lay * ng;
-    c.lay = lay;
-    FracRec rec;
-    float t = tau_band<b>(c, lay < laytrop, gi, T, gi == 0 ? &rec : nullptr);
-    s.taut[lay * GB_NGPT + g0 + gi] = t + s.taua[lay * 16 + (b - 1)];
-    if (gi == 0) s.frec[lay * 16 + (b - 1)] = rec;
+__device__ __forceinline__ void gas_optics_band(const Smem& s, int nl, int laytrop, const float* __restrict__ T) {
+  constexpr int NG = ngb_const(b), G0 = g0_const(b), M = maxt(b);
+  const int pad_off = c_T.band[b - 1].sr;
+  for (int lay = threadIdx.x; lay < nl; lay += NT) {
+    Cell c{s.f, s.iv, nl, lay};
+    Terms t{s.terms + lay * MAXT_ALL, 0};
+    FracRec r = prologue<b>(c, lay < laytrop, t);
+    t.pad(M, pad_off);
+    s.frec[lay * 16 + (b - 1)] = r;
   }
+  __syncthreads();
+  for (int cell = threadIdx.x; cell < nl * NG; cell += NT) {
+    const int lay = cell / NG, gi = cell - lay * NG;
+    const float2* tp = s.terms + lay * MAXT_ALL;
+    float acc = 0.0f;
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      float2 w = tp[k];
+      acc = fmaf(w.x, __ldg(T + __float_as_int(w.y) + gi), acc);
+    }
+    if ((b == 4 || b == 7) && lay >= laytrop) acc *= gscale(b, gi);
+    s.taut[lay * GB_NGPT + G0 + gi] = acc + s.taua[lay * 16 + (b - 1)];
+  }
+  __syncthreads();
 }
 
 // ------------------------------------------------------------------ the kernel
@@ -458,24 +474,23 @@ __global__ void __launch_bounds__(NT) lw_column_kernel(LwArgs a, const float* __
   }
   __syncthreads();
 
-  // ---------------- phase 2: taumol, band by band (no barrier between bands)
-  taumol_band<1>(s, nl, laytrop, T);
-  taumol_band<2>(s, nl, laytrop, T);
-  taumol_band<3>(s, nl, laytrop, T);
-  taumol_band<4>(s, nl, laytrop, T);
-  taumol_band<5>(s, nl, laytrop, T);
-  taumol_band<6>(s, nl, laytrop, T);
-  taumol_band<7>(s, nl, laytrop, T);
-  taumol_band<8>(s, nl, laytrop, T);
-  taumol_band<9>(s, nl, laytrop, T);
-  taumol_band<10>(s, nl, laytrop, T);
-  taumol_band<11>(s, nl, laytrop, T);
-  taumol_band<12>(s, nl, laytrop, T);
-  taumol_band<13>(s, nl, laytrop, T);
-  taumol_band<14>(s, nl, laytrop, T);
-  taumol_band<15>(s, nl, laytrop, T);
-  taumol_band<16>(s, nl, laytrop, T);
-  __syncthreads();
+  // ---------------- phase 2: taumol, band by band
+  gas_optics_band<1>(s, nl, laytrop, T);
+  gas_optics_band<2>(s, nl, laytrop, T);
+  gas_optics_band<3>(s, nl, laytrop, T);
+  gas_optics_band<4>(s, nl, laytrop, T);
+  gas_optics_band<5>(s, nl, laytrop, T);
+  gas_optics_band<6>(s, nl, laytrop, T);
+  gas_optics_band<7>(s, nl, laytrop, T);
+  gas_optics_band<8>(s, nl, laytrop, T);
+  gas_optics_band<9>(s, nl, laytrop, T);
+  gas_optics_band<10>(s, nl, laytrop, T);
+  gas_optics_band<11>(s, nl, laytrop, T);
+  gas_optics_band<12>(s, nl, laytrop, T);
+  gas_optics_band<13>(s, nl, laytrop, T);
+  gas_optics_band<14>(s, nl, laytrop, T);
+  gas_optics_band<15>(s, nl, laytrop, T);
+  gas_optics_band<16>(s, nl, laytrop, T);
   if (a.dbg_taut) {
     for (int c = tid; c < nl * GB_NGPT; c += NT) {
       int lay = c / GB_NGPT, g = c - lay * GB_NGPT;
