@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -39,8 +40,25 @@ struct gb_lw_context {
   int chunk_cols = 0, chunk_nlay = 0;
   double* d_draws = nullptr;
   size_t draws_elems = 0;
+  float4* d_scratch[2] = {nullptr, nullptr};  // cell-coefficient slots (one set per chunk stream)
+  size_t scratch_bytes = 0;
+  int scratch_slots = 0, scratch_nlay = 0;
   std::string last_error;
   size_t max_smem = 0;
+  int num_sms = 0;
+  float4* d_bscratch = nullptr;  // scratch of batched launches
+  size_t bscratch_bytes = 0;
+  std::vector<gb_lw_tuning> tuned;  // autotuned shapes, parallel to tuned_nlay (largest nlay of the batch)
+  std::vector<int> tuned_nlay;
+};
+
+static_assert(sizeof(gb_lw_grid) == 344, "gb_lw_grid layout is part of the ABI (Python mirror: GridDesc)");
+
+struct gb_lw_graph {
+  gb_lw_context* ctx = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  float4* scratch = nullptr;
 };
 
 namespace {
@@ -142,9 +160,120 @@ cudaError_t copy2d(double* dst, size_t dpitch, const double* src, size_t spitch,
   return cudaMemcpy2DAsync(dst, dpitch * 8, src, spitch * 8, width * 8, rows, kind, s);
 }
 
+// scratch slots for the column kernel at this nlay (grown on demand)
+int ensure_scratch(gb_lw_context* ctx, int nlay) {
+  if (ctx->d_scratch[0] && ctx->scratch_nlay >= nlay) return 0;
+  int slots = gb_lw_slots(nlay);
+  size_t bytes = gb_lw_scratch_bytes(nlay, slots);
+  for (auto& p : ctx->d_scratch) {
+    cudaFree(p);
+    p = nullptr;
+  }
+  ctx->scratch_bytes = 0;
+  for (auto& p : ctx->d_scratch) {
+    if (cudaMalloc(&p, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      ctx->last_error = "device allocation of the cell-coefficient scratch failed";
+      return GB_LW_E_NOMEM;
+    }
+  }
+  ctx->scratch_bytes = bytes;
+  ctx->scratch_slots = slots;
+  ctx->scratch_nlay = nlay;
+  return 0;
+}
+
 bool flags_ok(int idrv, int inflglw, int iceflglw, int liqflglw) {
   return (idrv == 0 || idrv == 1) && inflglw >= 0 && inflglw <= 2 && iceflglw >= 0 && iceflglw <= 3 &&
          liqflglw >= 0 && liqflglw <= 1;
+}
+
+// Validates the grids of a batched call and fills the launch descriptor.
+// frac < 1 keeps only that fraction of each grid's columns (autotuner sample).
+int make_batch(gb_lw_context* ctx, int ngrid, const gb_lw_grid* grids, double frac, LwBatch& b) {
+  if (ngrid < 1 || ngrid > GB_LW_MAX_GRIDS || !grids) return GB_LW_E_ARGS;
+  b = LwBatch{};
+  b.ngrid = ngrid;
+  b.nsmax = 1;
+  b.col0[0] = 0;
+  for (int i = 0; i < ngrid; ++i) {
+    const gb_lw_grid& g = grids[i];
+    if (g.ncol < 0 || g.nlay < 1 || g.nlay > GB_MAXLAY || g.ld_in < g.ncol || g.ld_out < g.ncol) return GB_LW_E_ARGS;
+    if (!flags_ok(g.idrv, g.inflglw, g.iceflglw, g.liqflglw)) return GB_LW_E_ARGS;
+    int icld = (g.icld < 0 || g.icld > 3) ? 2 : g.icld;  // rrtmg_lw_rad.f90:465
+    const bool fused = g.cloud_mode == GB_LW_CLOUD_FUSED;
+    if (g.cloud_mode != GB_LW_CLOUD_SUBCOL && !fused) return GB_LW_E_ARGS;
+    if (fused && icld != 0 && icld != 3) return GB_LW_E_ARGS;
+    const double* req[] = {g.play, g.plev, g.tlay, g.tlev, g.tsfc, g.h2ovmr, g.o3vmr, g.co2vmr, g.ch4vmr,
+                           g.n2ovmr, g.o2vmr, g.cfc11vmr, g.cfc12vmr, g.cfc22vmr, g.ccl4vmr, g.emis,
+                           g.tauaer, g.uflx, g.dflx, g.hr, g.uflxc, g.dflxc, g.hrc};
+    if (g.ncol > 0) {
+      for (const double* p : req)
+        if (!p) return GB_LW_E_ARGS;
+      if (icld >= 1 && (!g.reicmcl || !g.relqmcl)) return GB_LW_E_ARGS;
+      if (icld >= 1 && !fused && (!g.cldfmcl || !g.taucmcl || !g.ciwpmcl || !g.clwpmcl)) return GB_LW_E_ARGS;
+      if (icld >= 1 && fused && (!g.cldfrac || !g.ciwp || !g.clwp || !g.tauc)) return GB_LW_E_ARGS;
+      if (g.idrv == 1 && (!g.duflx_dt || !g.duflxc_dt)) return GB_LW_E_ARGS;
+    }
+    int nc = g.ncol;
+    if (frac < 1.0 && nc > 0) nc = std::max(1, std::min(nc, (int)std::ceil(frac * nc)));
+    LwArgs& a = b.g[i];
+    a = LwArgs{};
+    a.ncol = nc; a.nlay = g.nlay; a.ld = g.ld_in; a.ldo = g.ld_out;
+    a.icld = icld; a.idrv = g.idrv; a.inflag = g.inflglw; a.iceflag = g.iceflglw; a.liqflag = g.liqflglw;
+    a.cloud_mode = fused ? LW_CLOUD_FUSED : LW_CLOUD_SUBCOL;
+    a.seed0 = g.seed0;
+    a.play = g.play; a.plev = g.plev; a.tlay = g.tlay; a.tlev = g.tlev; a.tsfc = g.tsfc;
+    a.h2ovmr = g.h2ovmr; a.o3vmr = g.o3vmr; a.co2vmr = g.co2vmr; a.ch4vmr = g.ch4vmr; a.n2ovmr = g.n2ovmr;
+    a.o2vmr = g.o2vmr; a.cfc11vmr = g.cfc11vmr; a.cfc12vmr = g.cfc12vmr; a.cfc22vmr = g.cfc22vmr;
+    a.ccl4vmr = g.ccl4vmr; a.emis = g.emis; a.tauaer = g.tauaer;
+    a.cldfmcl = g.cldfmcl; a.taucmcl = g.taucmcl; a.ciwpmcl = g.ciwpmcl; a.clwpmcl = g.clwpmcl;
+    a.cldfrac = g.cldfrac; a.ciwp = g.ciwp; a.clwp = g.clwp; a.tauc = g.tauc;
+    a.reicmcl = g.reicmcl; a.relqmcl = g.relqmcl;
+    a.uflx = g.uflx; a.dflx = g.dflx; a.hr = g.hr; a.uflxc = g.uflxc; a.dflxc = g.dflxc; a.hrc = g.hrc;
+    a.duflx_dt = g.duflx_dt; a.duflxc_dt = g.duflxc_dt;
+    a.col_err = g.d_col_status;
+    a.err_flag = ctx->d_err;
+    b.col0[i + 1] = b.col0[i] + nc;
+    b.nsmax = std::max(b.nsmax, g.nlay);
+  }
+  if (gb_lw_smem_bytes(b.nsmax) > ctx->max_smem) {
+    ctx->last_error = "nlay too large for one thread block's shared memory";
+    return GB_LW_E_ARGS;
+  }
+  return 0;
+}
+
+gb_lw_tuning default_tuning(gb_lw_context* ctx, int nlay) {
+  gb_lw_tuning t{};
+  t.variant = 0;
+  t.threads = gb_lw_variant(0).threads;
+  t.min_blocks = gb_lw_variant(0).min_blocks;
+  t.blocks_per_sm = std::max(1, gb_lw_slots(nlay, 0) / std::max(1, ctx->num_sms));
+  t.blocks = t.blocks_per_sm * ctx->num_sms;
+  t.ms = 0.0;
+  return t;
+}
+
+gb_lw_tuning tuning_for(gb_lw_context* ctx, int nlay) {
+  for (size_t i = 0; i < ctx->tuned_nlay.size(); ++i)
+    if (ctx->tuned_nlay[i] == nlay) return ctx->tuned[i];
+  return default_tuning(ctx, nlay);
+}
+
+int ensure_bscratch(gb_lw_context* ctx, int nlay, int blocks) {
+  size_t bytes = gb_lw_scratch_bytes(nlay, blocks);
+  if (bytes <= ctx->bscratch_bytes) return 0;
+  cudaFree(ctx->d_bscratch);
+  ctx->d_bscratch = nullptr;
+  ctx->bscratch_bytes = 0;
+  if (cudaMalloc(&ctx->d_bscratch, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->last_error = "device allocation of the batch scratch failed";
+    return GB_LW_E_NOMEM;
+  }
+  ctx->bscratch_bytes = bytes;
+  return 0;
 }
 
 }  // namespace
@@ -175,6 +304,7 @@ int gb_rrtmg_lw_ini(double cpdair, const char* table_dir, int device, gb_lw_cont
   int dev_smem = 0;
   cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
   ctx->max_smem = (size_t)dev_smem;
+  cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (cudaMalloc(&ctx->d_tables, blob.size() * 4) != cudaSuccess || cudaMalloc(&ctx->d_err, 8) != cudaSuccess) {
     cudaGetLastError();
     gb_rrtmg_lw_free(ctx);
@@ -205,6 +335,8 @@ int gb_rrtmg_lw_free(gb_lw_context* ctx) {
   cudaFree(ctx->d_tables);
   cudaFree(ctx->d_err);
   cudaFree(ctx->d_draws);
+  for (auto& p : ctx->d_scratch) cudaFree(p);
+  cudaFree(ctx->d_bscratch);
   delete ctx;
   return GB_LW_OK;
 }
@@ -255,7 +387,9 @@ int gb_rrtmg_lw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int
   a.col_err = d_col_status;
   a.err_flag = ctx->d_err;
   cudaSetDevice(ctx->device);
-  CK(gb_lw_launch(a, ctx->d_tables, (cudaStream_t)stream));
+  int rs = ensure_scratch(ctx, nlay);
+  if (rs) return rs;
+  CK(gb_lw_launch(a, ctx->d_tables, ctx->d_scratch[0], ctx->scratch_slots, (cudaStream_t)stream));
   return GB_LW_OK;
 }
 
@@ -293,6 +427,8 @@ int gb_rrtmg_lw(gb_lw_context* ctx, int ncol, int nlay, int* icld, int idrv, con
   const size_t per_col = (size_t)(600 * nlay + 64) * 8;
   int C = (int)std::max<size_t>(1, std::min<size_t>((size_t)ncol, (size_t)(2ull << 30) / per_col));
   int rc = ensure_chunks(ctx, C, nlay);
+  if (rc) return rc;
+  rc = ensure_scratch(ctx, nlay);
   if (rc) return rc;
   const InLayout li = in_layout(C, nlay);
   const OutLayout lo = out_layout(C, nlay);
@@ -349,7 +485,7 @@ int gb_rrtmg_lw(gb_lw_context* ctx, int ncol, int nlay, int* icld, int idrv, con
     a.duflx_dt = O + lo.duflx; a.duflxc_dt = O + lo.duflxc; a.hr = O + lo.hr; a.hrc = O + lo.hrc;
     a.col_err = nullptr;
     a.err_flag = ctx->d_err_host;
-    CK(gb_lw_launch(a, ctx->d_tables, s));
+    CK(gb_lw_launch(a, ctx->d_tables, ctx->d_scratch[k & 1], ctx->scratch_slots, s));
     auto D2H = [&](double* dst, size_t soff, size_t rows) {
       return copy2d(dst + c0, (size_t)ld_out, O + soff, P, nc, rows, cudaMemcpyDeviceToHost, s);
     };
@@ -530,8 +666,13 @@ int gb_rrtmg_lw_gas_optics_diag(gb_lw_context* ctx, int ncol, int nlay, const do
   a.err_flag = ctx->d_err_host;
   a.dbg_taut = dt;
   a.dbg_fracs = dt + n2 * GB_NGPT;
-  int rc = GB_LW_OK;
-  cudaError_t e = gb_lw_launch(a, ctx->d_tables, 0);
+  int rc = ensure_scratch(ctx, nlay);
+  if (rc) {
+    cudaFree(d);
+    cudaFree(dt);
+    return rc;
+  }
+  cudaError_t e = gb_lw_launch(a, ctx->d_tables, ctx->d_scratch[0], ctx->scratch_slots, 0);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e == cudaSuccess) e = cudaMemcpy(taut, dt, n2 * GB_NGPT * 4, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(fracs, dt + n2 * GB_NGPT, n2 * GB_NGPT * 4, cudaMemcpyDeviceToHost);
@@ -539,6 +680,180 @@ int gb_rrtmg_lw_gas_optics_diag(gb_lw_context* ctx, int ncol, int nlay, const do
   cudaFree(d);
   cudaFree(dt);
   return rc;
+}
+
+int gb_rrtmg_lw_batch_device(gb_lw_context* ctx, void* stream, int ngrid, const gb_lw_grid* grids) {
+  if (!ctx) return GB_LW_E_ARGS;
+  LwBatch b;
+  int rc = make_batch(ctx, ngrid, grids, 1.0, b);
+  if (rc) return rc;
+  if (b.col0[ngrid] == 0) return GB_LW_OK;
+  cudaSetDevice(ctx->device);
+  const gb_lw_tuning t = tuning_for(ctx, b.nsmax);
+  rc = ensure_bscratch(ctx, b.nsmax, t.blocks);
+  if (rc) return rc;
+  b.scratch = ctx->d_bscratch;
+  CK(gb_lw_launch_batch(b, ctx->d_tables, t.variant, t.blocks, (cudaStream_t)stream));
+  return GB_LW_OK;
+}
+
+int gb_rrtmg_lw_tuning_get(gb_lw_context* ctx, int nlay, gb_lw_tuning* out) {
+  if (!ctx || !out || nlay < 1 || nlay > GB_MAXLAY) return GB_LW_E_ARGS;
+  cudaSetDevice(ctx->device);
+  *out = tuning_for(ctx, nlay);
+  return GB_LW_OK;
+}
+
+int gb_rrtmg_lw_num_variants(void) { return gb_lw_num_variants(); }
+
+int gb_rrtmg_lw_tuning_set(gb_lw_context* ctx, int nlay, const gb_lw_tuning* shape) {
+  if (!ctx || !shape || nlay < 1 || nlay > GB_MAXLAY) return GB_LW_E_ARGS;
+  if (shape->variant < 0 || shape->variant >= gb_lw_num_variants()) return GB_LW_E_ARGS;
+  cudaSetDevice(ctx->device);
+  const int occ = gb_lw_slots(nlay, shape->variant) / std::max(1, ctx->num_sms);
+  if (shape->blocks_per_sm < 1 || shape->blocks_per_sm > occ) {
+    ctx->last_error = "blocks_per_sm exceeds what fits on an SM for this nlay and variant";
+    return GB_LW_E_ARGS;
+  }
+  gb_lw_tuning t{};
+  t.variant = shape->variant;
+  t.threads = gb_lw_variant(t.variant).threads;
+  t.min_blocks = gb_lw_variant(t.variant).min_blocks;
+  t.blocks_per_sm = shape->blocks_per_sm;
+  t.blocks = t.blocks_per_sm * ctx->num_sms;
+  t.ms = shape->ms;
+  for (size_t i = 0; i < ctx->tuned_nlay.size(); ++i)
+    if (ctx->tuned_nlay[i] == nlay) {
+      ctx->tuned[i] = t;
+      return GB_LW_OK;
+    }
+  ctx->tuned_nlay.push_back(nlay);
+  ctx->tuned.push_back(t);
+  return GB_LW_OK;
+}
+
+int gb_rrtmg_lw_autotune(gb_lw_context* ctx, void* stream, int ngrid, const gb_lw_grid* grids, int sample_cols,
+                         int reps, gb_lw_tuning* best) {
+  if (!ctx) return GB_LW_E_ARGS;
+  LwBatch full;
+  int rc = make_batch(ctx, ngrid, grids, 1.0, full);
+  if (rc) return rc;
+  const long long total = full.col0[ngrid];
+  if (total == 0) return GB_LW_E_ARGS;
+  const double frac = sample_cols > 0 && sample_cols < total ? (double)sample_cols / (double)total : 1.0;
+  LwBatch b;
+  rc = make_batch(ctx, ngrid, grids, frac, b);
+  if (rc) return rc;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  reps = std::max(1, reps);
+  // candidate shapes: every variant at 1 .. max resident blocks per SM
+  struct Cand { int v, per; };
+  std::vector<Cand> cands;
+  int max_blocks = 1;
+  for (int v = 0; v < gb_lw_num_variants(); ++v) {
+    const int occ = gb_lw_slots(b.nsmax, v) / std::max(1, ctx->num_sms);
+    for (int per = 1; per <= occ; ++per) {
+      cands.push_back({v, per});
+      max_blocks = std::max(max_blocks, per * ctx->num_sms);
+    }
+  }
+  if (cands.empty()) return GB_LW_E_ARGS;
+  rc = ensure_bscratch(ctx, b.nsmax, max_blocks);
+  if (rc) return rc;
+  b.scratch = ctx->d_bscratch;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  gb_lw_tuning bt{};
+  bt.ms = 1e30;
+  cudaError_t err = cudaSuccess;
+  for (const Cand& c : cands) {
+    const int nb = c.per * ctx->num_sms;
+    err = gb_lw_launch_batch(b, ctx->d_tables, c.v, nb, st);  // warm-up
+    if (err == cudaSuccess) err = cudaEventRecord(e0, st);
+    for (int r = 0; r < reps && err == cudaSuccess; ++r) err = gb_lw_launch_batch(b, ctx->d_tables, c.v, nb, st);
+    if (err == cudaSuccess) err = cudaEventRecord(e1, st);
+    if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+    float ms = 0.0f;
+    if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+    if (err != cudaSuccess) break;
+    const double per_launch = ms / reps;
+    if (per_launch < bt.ms) {
+      bt.variant = c.v;
+      bt.threads = gb_lw_variant(c.v).threads;
+      bt.min_blocks = gb_lw_variant(c.v).min_blocks;
+      bt.blocks_per_sm = c.per;
+      bt.blocks = nb;
+      bt.ms = per_launch;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (err != cudaSuccess) return cuda_fail(ctx, err, "autotune");
+  bool stored = false;
+  for (size_t i = 0; i < ctx->tuned_nlay.size(); ++i)
+    if (ctx->tuned_nlay[i] == b.nsmax) {
+      ctx->tuned[i] = bt;
+      stored = true;
+    }
+  if (!stored) {
+    ctx->tuned_nlay.push_back(b.nsmax);
+    ctx->tuned.push_back(bt);
+  }
+  if (best) *best = bt;
+  return GB_LW_OK;
+}
+
+int gb_rrtmg_lw_batch_graph_create(gb_lw_context* ctx, int ngrid, const gb_lw_grid* grids, gb_lw_graph** out) {
+  if (!ctx || !out) return GB_LW_E_ARGS;
+  *out = nullptr;
+  LwBatch b;
+  int rc = make_batch(ctx, ngrid, grids, 1.0, b);
+  if (rc) return rc;
+  if (b.col0[ngrid] == 0) return GB_LW_E_ARGS;
+  cudaSetDevice(ctx->device);
+  const gb_lw_tuning t = tuning_for(ctx, b.nsmax);
+  gb_lw_graph* g = new gb_lw_graph();
+  g->ctx = ctx;
+  if (cudaMalloc(&g->scratch, gb_lw_scratch_bytes(b.nsmax, t.blocks)) != cudaSuccess) {
+    cudaGetLastError();
+    delete g;
+    return GB_LW_E_NOMEM;
+  }
+  b.scratch = g->scratch;
+  cudaStream_t s = ctx->streams[0];
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed);
+  if (e == cudaSuccess) {
+    cudaError_t le = gb_lw_launch_batch(b, ctx->d_tables, t.variant, t.blocks, s);
+    e = cudaStreamEndCapture(s, &g->graph);
+    if (le != cudaSuccess) e = le;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+  if (e != cudaSuccess) {
+    gb_rrtmg_lw_graph_destroy(g);
+    return cuda_fail(ctx, e, "batch graph capture");
+  }
+  *out = g;
+  return GB_LW_OK;
+}
+
+int gb_rrtmg_lw_graph_launch(gb_lw_graph* g, void* stream) {
+  if (!g || !g->exec) return GB_LW_E_ARGS;
+  gb_lw_context* ctx = g->ctx;
+  cudaSetDevice(ctx->device);
+  CK(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+  return GB_LW_OK;
+}
+
+int gb_rrtmg_lw_graph_destroy(gb_lw_graph* g) {
+  if (!g) return GB_LW_OK;
+  cudaSetDevice(g->ctx->device);
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  cudaFree(g->scratch);
+  delete g;
+  return GB_LW_OK;
 }
 
 const char* gb_rrtmg_lw_strerror(int code) {

@@ -41,6 +41,10 @@ __constant__ GbTables c_T;
 
 // most terms any band needs in one layer (band 13, lower atmosphere)
 constexpr int MAXT_ALL = 24;
+// Bands are processed in groups that share one prologue pass and one cell
+// pass; a group's term lists fit TGROUP terms per layer.
+constexpr int NGROUP = 6;
+constexpr int TGROUP = 48;
 // per band: max over lower and upper atmosphere
 __host__ __device__ constexpr int maxt(int b) {
   constexpr int m[17] = {0, 10, 8, 20, 16, 21, 12, 20, 16, 20, 8, 10, 16, 24, 8, 20, 16};
@@ -72,12 +76,18 @@ struct FracRec {
 };
 
 // A term list under construction: weights and absolute table offsets of row starts.
+// Term k of the layer lives at t[k * stride] (term-major storage, so the
+// threads of consecutive layers write and read consecutive words).
 struct Terms {
-  float2* t;  // MAXT_ALL slots of this layer
+  float2* t;
+  int stride;
   int n;
-  __device__ __forceinline__ void add(float w, int off) { t[n++] = make_float2(w, __int_as_float(off)); }
+  __device__ __forceinline__ void add(float w, int off) {
+    t[n * stride] = make_float2(w, __int_as_float(off));
+    ++n;
+  }
   __device__ __forceinline__ void scale(float s) {
-    for (int k = 0; k < n; ++k) t[k].x *= s;
+    for (int k = 0; k < n; ++k) t[k * stride].x *= s;
   }
   __device__ __forceinline__ void pad(int maxt, int off) {
     while (n < maxt) add(0.0f, off);
@@ -550,13 +560,8 @@ __device__ FracRec prologue<16>(const Cell& c, bool lower, Terms& t) {
 
 // band-4 / band-7 upper-atmosphere g-point factors (default-real literals in
 // the reference, taumol.f90:1044-1050 and 1687-1692)
-__device__ __forceinline__ float gscale(int b, int gi) {
-  if (b == 4) {
-    constexpr float f[14] = {1, 1, 1, 1, 1, 1, 1, 0.92f, 0.88f, 1.07f, 1.1f, 0.99f, 0.88f, 0.943f};
-    return f[gi];
-  }
-  constexpr float f[12] = {1, 1, 1, 1, 1, 0.92f, 0.88f, 1.07f, 1.1f, 0.99f, 0.855f, 1};
-  return f[gi];
-}
+__constant__ float c_gscale4[14] = {1, 1, 1, 1, 1, 1, 1, 0.92f, 0.88f, 1.07f, 1.1f, 0.99f, 0.88f, 0.943f};
+__constant__ float c_gscale7[12] = {1, 1, 1, 1, 1, 0.92f, 0.88f, 1.07f, 1.1f, 0.99f, 0.855f, 1};
+__device__ __forceinline__ float gscale(int b, int gi) { return b == 4 ? c_gscale4[gi] : c_gscale7[gi]; }
 
 }  // namespace gb

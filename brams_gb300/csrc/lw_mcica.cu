@@ -21,37 +21,16 @@
 #include "../../include/gb_rrtmg_lw.h"
 #include "lw_common.h"
 #include "lw_mcica.h"
+#include "lw_mt.cuh"
 
 namespace gbm {
 
 // ---------------------------------------------------------------- Mersenne twister
-__device__ __forceinline__ uint32_t mt_temper(uint32_t y) {
-  uint32_t x = y ^ (y >> 11);
-  x ^= (x << 7) & 0x9d2c5680u;
-  x ^= (x << 15) & 0xefc60000u;
-  return x ^ (x >> 18);
-}
-__device__ __forceinline__ uint32_t mt_twist(uint32_t u, uint32_t v) {
-  return (((u & 0x80000000u) | (v & 0x7fffffffu)) >> 1) ^ ((v & 1u) ? 0x9908b0dfu : 0u);
-}
-// getRandomReal (:276-295): u32 / (2^32 - 1) in double precision
-__device__ __forceinline__ double mt_real(uint32_t u) { return (double)u / 4294967295.0; }
-
-// First n <= 227 outputs of MT(seed): they need the initial state words
-// 0..n and 397..396+n only (nextState's first loop, :129-132).
-__device__ void mt_first(uint32_t seed, int n, uint32_t* lo /* n+1 words */, double* out, int stride) {
-  uint32_t s = seed;
-  lo[0] = s;
-  for (int i = 1; i <= n; ++i) {
-    s = 1812433253u * (s ^ (s >> 30)) + (uint32_t)i;
-    lo[i] = s;
-  }
-  for (int i = n + 1; i < 397; ++i) s = 1812433253u * (s ^ (s >> 30)) + (uint32_t)i;
-  for (int k = 0; k < n; ++k) {
-    s = 1812433253u * (s ^ (s >> 30)) + (uint32_t)(397 + k);  // word 397 + k
-    out[(long long)k * stride] = mt_real(mt_temper(s ^ mt_twist(lo[k], lo[k + 1])));
-  }
-}
+using gbmt::temper;
+using gbmt::real;
+__device__ __forceinline__ uint32_t mt_temper(uint32_t y) { return gbmt::temper(y); }
+__device__ __forceinline__ uint32_t mt_twist(uint32_t u, uint32_t v) { return gbmt::twist(u, v); }
+__device__ __forceinline__ double mt_real(uint32_t u) { return gbmt::real(u); }
 
 // Full-state generator for longer per-column sequences.
 struct MtState {
@@ -81,7 +60,7 @@ __global__ void mt_percol_kernel(int ncol, int seed0, int ndraw, double* __restr
   uint32_t seed = (uint32_t)(seed0 + c);
   if (ndraw <= 226) {
     uint32_t lo[227];
-    mt_first(seed, ndraw, lo, out, 1);
+    gbmt::first_reals(seed, ndraw, lo, out, 1);
     return;
   }
   MtState m;

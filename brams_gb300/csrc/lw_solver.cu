@@ -1,23 +1,37 @@
 // Fused RRTMG_LW column kernel for GB300 (sm_103a).
 //
-// One thread block solves one column (the reference's column loop,
-// rrtmg_lw_rad.f90:486-593).  Phases, separated by block barriers:
+// A persistent grid of thread blocks; each block solves one column at a time
+// (the reference's column loop, rrtmg_lw_rad.f90:486-593) and owns one slot
+// of an L2-resident scratch area.  One launch covers a batch of grids (nested
+// grids, ensemble members) with their own column and layer counts: the batch
+// columns are numbered grid after grid and each block walks them with stride
+// gridDim.x.  Phases per column, separated by barriers:
 //   1. inatm + setcoef (rrtmg_lw_rad.f90:598-924, rrtmg_lw_setcoef.f90:50-434):
 //      one thread per layer, coefficients into shared memory; Planck
-//      interpolation with one thread per (level, band); column sums for pwvcm.
-//      In parallel the 140 g-point threads scan the McICA cloud fractions to
-//      mark cloudy layers (rtrnmc.f90:292-331) and check the cloud particle
-//      sizes exactly where cldprmc would (cldprmc.f90:178-266).
-//   2. taumol (rrtmg_lw_taumol.f90): one thread per (layer, g) cell, band by
-//      band, writing taut = taug + aerosol (rrtmg_lw_rad.f90:548-553) to shared
-//      memory, plus one Planck-fraction record per (layer, band).
-//   3. rtrnmc (rrtmg_lw_rtrnmc.f90:51-595): one thread per g-point; downward
-//      then upward sweep.  The upward sweep recomputes the layer
-//      transmittances from taut instead of storing them, which keeps shared
-//      memory per column near 40 KB.  Lookup-table entries exp_tbl/tfn_tbl/
-//      tau_tbl (rrtmg_lw_init.f90:125-142) are evaluated at the quantised
-//      table index instead of being loaded.  Per-level g-point sums are
-//      weighted by 0.5*delwave*fluxfac and reduced across each warp in fp32.
+//      interpolation with one thread per (level, band); column sums for
+//      pwvcm.  All threads also scan the McICA cloud fractions to mark cloudy
+//      layers and cells (rtrnmc.f90:292-331) and to check the particle sizes
+//      where cldprmc would stop (cldprmc.f90:178-266).  In the fused cloud
+//      mode the block instead draws the column's 140 McICA random numbers
+//      (mcica_subcol_gen_lw.f90:484-512 with icld 3, Mersenne twister seeded
+//      seed0 + column) and marks cell (lay, g) cloudy iff cdf(g) >= 1 -
+//      cldf(lay) (:650), with the cloud optical depth of each (layer, band)
+//      computed once -- the values mcica_subcol_lw would have copied into
+//      every sub-column of that band.
+//   2. gas optics and cell transfer coefficients, band by band: a prologue
+//      per (layer, band) builds the taumol term list (lw_gasoptics.cuh), then
+//      one thread per (layer, g) cell evaluates taug, adds the aerosol depth
+//      (rrtmg_lw_rad.f90:548-553), takes the Planck fraction and computes the
+//      cell's layer transmittance and down/up sources exactly as rtrnmc's
+//      down sweep does (rtrnmc.f90:350-455): clear-sky coefficients for every
+//      cell and cloudy-layer coefficients where cldfmc /= 0.  They go to the
+//      block's scratch slot.  Lookup-table entries exp_tbl/tfn_tbl/tau_tbl
+//      (rrtmg_lw_init.f90:125-142) are evaluated at the quantised index.
+//   3. rtrnmc sweeps, one thread per g-point: each layer is then an affine
+//      update radiance*A + B (rtrnmc.f90:347-529); the clear-sky stream and
+//      the surface-temperature derivatives follow with their own
+//      coefficients.  Per-level g-point sums are weighted by
+//      0.5*delwave*fluxfac and reduced across each warp in fp32.
 //   4. fp64 epilogue: per-warp partial sums added in fp64, net fluxes and
 //      heating rates heatfac*dF/dp in fp64 (rtrnmc.f90:566-592).
 //
@@ -31,68 +45,82 @@
 #include "lw_common.h"
 #include "lw_solver.h"
 #include "lw_gasoptics.cuh"
+#include "lw_mt.cuh"
 
 namespace gb {
 
-constexpr int NT = 160;      // threads per column block (5 warps; 140 g-point lanes)
-constexpr int NWARP = NT / 32;
+constexpr int NSW = 5;  // warps of the g-point sweeps (140 lanes)
 constexpr float BPADE = 1.0f / 0.278f;
 
 // ------------------------------------------------------------------ shared memory layout
 struct Smem {
-  float* f;        // [NF][nl]   per-layer coefficients (phase 1-2)
+  float* f;        // [NF][nl]   per-layer coefficients (phases 1-2)
   int* iv;         // [NI][nl]
-  float2* terms;   // [nl][MAXT_ALL] gas-optics terms of the current band (phase 2)
-  float* part;     // [NWARP][nl+1][6] warp partial fluxes (aliases f/iv in phase 3-4)
-  float* taut;     // [nl][140]
-  float* taua;     // [nl][16]
-  float* plk_lay;  // [nl][16]
-  float* plk_lev;  // [nl+1][16]
-  FracRec* frec;   // [nl][16]
+  float2* terms;   // [TGROUP][nl] gas-optics terms of the current band group, term-major (phase 2)
+  float* part;     // [NSW][nl+1][6] warp partial fluxes (aliases f/iv/terms in phases 3-4)
+  float* taua;     // [16][nl]
+  float* plk_lay;  // [16][nl]
+  float* plk_lev;  // [16][nl+1]
+  FracRec* frec;   // [3][nl] Planck-fraction records of the current band group
   int* cldlay;     // [nl]
+  unsigned* cbits; // [nl][5] bit g set where cldfmcl == 1
+  unsigned* fbits; // [nl][5] bit g set where cldfmcl is neither 0 nor 1
+  float* frac1;    // [140] Planck fractions of the bottom layer (surface source)
   double* fnet;    // [nl+1][2] net fluxes (phase 4)
   float* misc;     // [64]: secdiff[16], plankbnd[16], dplankbnd[16], semiss[16]
-  float* scal;     // [4]: pwvcm pieces
-  int* iscal;      // [4]: laytrop, lower-count, error
+  float* scal;     // [4]
+  int* iscal;      // [4]: laytrop, sum of lower-layer indices, error, column error
+  double* cdf;     // [140] McICA draws of the column (fused cloud mode; compared as bit patterns)
+  uint32_t* mtlo;  // [141] Mersenne-twister state words (fused cloud mode)
+  float* tcl;      // [nl][16] cloud optical depth per (layer, band) (fused cloud mode)
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
+__host__ __device__ inline size_t region_a(int nl) {
+  size_t coef = (((size_t)(NF + NI) * nl * 4 + 15) & ~size_t(15)) + (size_t)nl * TGROUP * 8;
+  size_t part = (size_t)NSW * (nl + 1) * 6 * 4;
+  return align16(coef > part ? coef : part);
+}
+
 __host__ __device__ inline size_t smem_bytes(int nl) {
-  size_t coef = (((size_t)(NF + NI) * nl * 4 + 7) & ~size_t(7)) + (size_t)nl * MAXT_ALL * 8;
-  size_t part = (size_t)NWARP * (nl + 1) * 6 * 4;
-  size_t a = align16(coef > part ? coef : part);
-  a += align16((size_t)nl * GB_NGPT * 4);
-  a += align16((size_t)nl * 16 * 4);
-  a += align16((size_t)nl * 16 * 4);
-  a += align16((size_t)(nl + 1) * 16 * 4);
-  a += align16((size_t)nl * 16 * sizeof(FracRec));
+  size_t a = region_a(nl);
+  a += align16((size_t)nl * 16 * 4);         // taua
+  a += align16((size_t)nl * 16 * 4);         // plk_lay
+  a += align16((size_t)(nl + 1) * 16 * 4);   // plk_lev
+  a += align16((size_t)3 * nl * sizeof(FracRec));
   a += align16((size_t)nl * 4);
+  a += 2 * align16((size_t)nl * 5 * 4);
+  a += align16(GB_NGPT * 4);
   a += align16((size_t)(nl + 1) * 2 * 8);
   a += align16(64 * 4) + align16(4 * 4) + align16(4 * 4);
+  a += align16(GB_NGPT * 8) + align16((GB_NGPT + 1) * 4) + align16((size_t)nl * 16 * 4);
   return a;
 }
 
 __device__ inline Smem carve(char* base, int nl) {
   Smem s;
-  size_t coef = (((size_t)(NF + NI) * nl * 4 + 7) & ~size_t(7)) + (size_t)nl * MAXT_ALL * 8;
-  size_t part = (size_t)NWARP * (nl + 1) * 6 * 4;
   char* p = base;
   s.f = (float*)p;
   s.iv = (int*)(p + (size_t)NF * nl * 4);
-  s.terms = (float2*)(p + (((size_t)(NF + NI) * nl * 4 + 7) & ~size_t(7)));
+  s.terms = (float2*)(p + (((size_t)(NF + NI) * nl * 4 + 15) & ~size_t(15)));
   s.part = (float*)p;
-  p += align16(coef > part ? coef : part);
-  s.taut = (float*)p; p += align16((size_t)nl * GB_NGPT * 4);
+  p += region_a(nl);
   s.taua = (float*)p; p += align16((size_t)nl * 16 * 4);
   s.plk_lay = (float*)p; p += align16((size_t)nl * 16 * 4);
   s.plk_lev = (float*)p; p += align16((size_t)(nl + 1) * 16 * 4);
-  s.frec = (FracRec*)p; p += align16((size_t)nl * 16 * sizeof(FracRec));
+  s.frec = (FracRec*)p; p += align16((size_t)3 * nl * sizeof(FracRec));
   s.cldlay = (int*)p; p += align16((size_t)nl * 4);
+  s.cbits = (unsigned*)p; p += align16((size_t)nl * 5 * 4);
+  s.fbits = (unsigned*)p; p += align16((size_t)nl * 5 * 4);
+  s.frac1 = (float*)p; p += align16(GB_NGPT * 4);
   s.fnet = (double*)p; p += align16((size_t)(nl + 1) * 2 * 8);
   s.misc = (float*)p; p += align16(64 * 4);
   s.scal = (float*)p; p += align16(4 * 4);
-  s.iscal = (int*)p;
+  s.iscal = (int*)p; p += align16(4 * 4);
+  s.cdf = (double*)p; p += align16(GB_NGPT * 8);
+  s.mtlo = (uint32_t*)p; p += align16((GB_NGPT + 1) * 4);
+  s.tcl = (float*)p;
   return s;
 }
 
@@ -133,296 +161,452 @@ __device__ __forceinline__ TblEntry tbl(float od) {
   return e;
 }
 
-// Transfer quantities of one (layer, g) cell (rtrnmc.f90:350-455).
-struct CellRT {
-  float atrans, bbd, gassrc, atot, bbdtot, bbugas, bbutot;
-};
-__device__ __forceinline__ CellRT cell_rt(bool cloudy_layer, float odepth, float odcld, float plfrac, float blay,
-                                          float dplankup, float dplankdn) {
-  const float rec_6 = 0.166667f;
-  CellRT r;
-  if (cloudy_layer) {
-    float odtot = odepth + odcld;
-    if (odtot < 0.06f) {
-      r.atrans = odepth - 0.5f * odepth * odepth;
-      float odepth_rec = rec_6 * odepth;
-      r.gassrc = plfrac * (blay + dplankdn * odepth_rec) * r.atrans;
-      r.atot = odtot - 0.5f * odtot * odtot;
-      float odtot_rec = rec_6 * odtot;
-      r.bbdtot = plfrac * (blay + dplankdn * odtot_rec);
-      r.bbd = plfrac * (blay + dplankdn * odepth_rec);
-      r.bbugas = plfrac * (blay + dplankup * odepth_rec);
-      r.bbutot = plfrac * (blay + dplankup * odtot_rec);
-    } else if (odepth <= 0.06f) {
-      r.atrans = odepth - 0.5f * odepth * odepth;
-      float odepth_rec = rec_6 * odepth;
-      r.gassrc = plfrac * (blay + dplankdn * odepth_rec) * r.atrans;
-      TblEntry et = tbl(odtot);
-      r.bbdtot = plfrac * (blay + et.tfn * dplankdn);
-      r.bbd = plfrac * (blay + dplankdn * odepth_rec);
-      r.atot = 1.0f - et.trans;
-      r.bbugas = plfrac * (blay + dplankup * odepth_rec);
-      r.bbutot = plfrac * (blay + et.tfn * dplankup);
+__constant__ int c_maxt[17] = {0, maxt(1), maxt(2), maxt(3), maxt(4), maxt(5), maxt(6), maxt(7), maxt(8),
+                               maxt(9), maxt(10), maxt(11), maxt(12), maxt(13), maxt(14), maxt(15), maxt(16)};
+__constant__ int c_icb[16] = {1, 2, 3, 3, 3, 4, 4, 4, 5, 5, 5, 5, 5, 5, 5, 5};  // cldprmc.f90:133
+// diffusivity-angle coefficients (rtrnmc.f90:236-247)
+__constant__ float c_a0[16] = {1.66f, 1.55f, 1.58f, 1.66f, 1.54f, 1.454f, 1.89f, 1.33f, 1.668f, 1.66f, 1.66f, 1.66f, 1.66f, 1.66f, 1.66f, 1.66f};
+__constant__ float c_a1[16] = {0.f, 0.25f, 0.22f, 0.f, 0.13f, 0.446f, -0.10f, 0.40f, -0.006f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+__constant__ float c_a2[16] = {0.f, -12.0f, -11.7f, 0.f, -0.72f, -0.243f, 0.19f, -0.062f, 0.414f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+
+// cldprmc's optical depth ciwp*abscoice + clwp*abscoliq of one cell
+// (cldprmc.f90:194-266; the radius bounds are checked in the pre-pass).
+__device__ __forceinline__ float cloud_tau(const LwArgs& a, long long icol, int lay, int band,
+                                           const float* __restrict__ T, double ciwp, double clwp) {
+  float abscoice = 0.0f, abscoliq = 0.0f;
+  if (ciwp != 0.0) {
+    float radice = (float)in2(a.reicmcl, a.ld, icol, lay);
+    if (a.iceflag == 0) {
+      abscoice = T[c_T.absice0] + T[c_T.absice0 + 1] / radice;
+    } else if (a.iceflag == 1) {
+      int ib = c_icb[band];
+      abscoice = T[c_T.absice1 + 2 * (ib - 1)] + T[c_T.absice1 + 1 + 2 * (ib - 1)] / radice;
     } else {
-      TblEntry eg = tbl(odepth);
-      r.atrans = 1.0f - eg.trans;
-      r.gassrc = r.atrans * plfrac * (blay + eg.tfn * dplankdn);
-      TblEntry et = tbl(eg.tau + odcld);
-      r.bbdtot = plfrac * (blay + et.tfn * dplankdn);
-      r.bbd = plfrac * (blay + eg.tfn * dplankdn);
-      r.atot = 1.0f - et.trans;
-      r.bbugas = plfrac * (blay + eg.tfn * dplankup);
-      r.bbutot = plfrac * (blay + et.tfn * dplankup);
+      float factor = (radice - 2.0f) / 3.0f;
+      int nrow = a.iceflag == 2 ? 43 : 46;
+      int index = clampi((int)factor, 1, nrow - 1);
+      float fint = factor - (float)index;
+      const float* t = T + (a.iceflag == 2 ? c_T.absice2 : c_T.absice3) + nrow * band;
+      abscoice = t[index - 1] + fint * (t[index] - t[index - 1]);
     }
-  } else {
-    if (odepth <= 0.06f) {
-      r.atrans = odepth - 0.5f * odepth * odepth;
-      float o = rec_6 * odepth;
-      r.bbd = plfrac * (blay + dplankdn * o);
-      r.bbugas = plfrac * (blay + dplankup * o);
-    } else {
-      TblEntry e = tbl(odepth);
-      r.atrans = 1.0f - e.trans;
-      r.bbd = plfrac * (blay + e.tfn * dplankdn);
-      r.bbugas = plfrac * (blay + e.tfn * dplankup);
-    }
-    r.gassrc = 0.0f; r.atot = 0.0f; r.bbdtot = 0.0f; r.bbutot = 0.0f;
   }
-  return r;
+  if (clwp != 0.0) {
+    if (a.liqflag == 0) {
+      abscoliq = c_T.absliq0;
+    } else {
+      float radliq = (float)in2(a.relqmcl, a.ld, icol, lay);
+      int index = clampi((int)(radliq - 1.5f), 1, 57);
+      float fint = radliq - 1.5f - (float)index;
+      const float* t = T + c_T.absliq1 + 58 * band;
+      abscoliq = t[index - 1] + fint * (t[index] - t[index - 1]);
+    }
+  }
+  return (float)ciwp * abscoice + (float)clwp * abscoliq;
 }
 
 // McICA cloud optics of one cell: returns cldfmc and sets odcld/efcl
 // (cldprmc.f90:178-266 then rtrnmc.f90:300-312; computed only where
 // cldfmc == 1, the only cells whose optical depth rtrnmc reads).
-__device__ __forceinline__ float cell_cloud(const LwArgs& a, long long icol, int g, int lay, float secdiff_b,
-                                            int band, const float* __restrict__ T, float& odcld, float& efcl) {
-  long long o = (long long)g + GB_NGPT * (icol + (long long)a.ld * lay);
-  double cf = __ldg(a.cldfmcl + o);
+__device__ __forceinline__ float cell_cloud(const LwArgs& a, const Smem& s, long long icol, int g, int lay,
+                                            float secdiff_b, int band, const float* __restrict__ T, float& odcld,
+                                            float& efcl) {
+  const unsigned bit = 1u << (g & 31);
+  const bool one = s.cbits[lay * 5 + (g >> 5)] & bit;
   odcld = 0.0f;
   efcl = 0.0f;
-  if (cf == 1.0) {
-    double ciwp = __ldg(a.ciwpmcl + o), clwp = __ldg(a.clwpmcl + o);
-    float tauc;
-    double cwp = ciwp + clwp;
-    double tin = __ldg(a.taucmcl + o);
-    if (a.inflag == 2 && (cwp >= 1.e-20 || tin >= 1.e-20)) {
-      float abscoice = 0.0f, abscoliq = 0.0f;
-      if (ciwp != 0.0) {
-        float radice = (float)in2(a.reicmcl, a.ld, icol, lay);
-        if (a.iceflag == 0) {
-          abscoice = T[c_T.absice0] + T[c_T.absice0 + 1] / radice;
-        } else if (a.iceflag == 1) {
-          const int icb[16] = {1, 2, 3, 3, 3, 4, 4, 4, 5, 5, 5, 5, 5, 5, 5, 5};
-          int ib = icb[band];
-          abscoice = T[c_T.absice1 + 2 * (ib - 1)] + T[c_T.absice1 + 1 + 2 * (ib - 1)] / radice;
-        } else if (a.iceflag == 2 || a.iceflag == 3) {
-          float factor = (radice - 2.0f) / 3.0f;
-          int nrow = a.iceflag == 2 ? 43 : 46;
-          int index = clampi((int)factor, 1, nrow - 1);
-          float fint = factor - (float)index;
-          const float* t = T + (a.iceflag == 2 ? c_T.absice2 : c_T.absice3) + nrow * band;
-          abscoice = t[index - 1] + fint * (t[index] - t[index - 1]);
-        }
-      }
-      if (clwp != 0.0) {
-        if (a.liqflag == 0) {
-          abscoliq = c_T.absliq0;
-        } else {
-          float radliq = (float)in2(a.relqmcl, a.ld, icol, lay);
-          int index = clampi((int)(radliq - 1.5f), 1, 57);
-          float fint = radliq - 1.5f - (float)index;
-          const float* t = T + c_T.absliq1 + 58 * band;
-          abscoliq = t[index - 1] + fint * (t[index] - t[index - 1]);
-        }
-      }
-      tauc = (float)ciwp * abscoice + (float)clwp * abscoliq;
-    } else {
-      tauc = (float)tin;
-    }
-    odcld = secdiff_b * tauc;
+  if (a.cloud_mode == LW_CLOUD_FUSED) {  // sub-column clouds are 0 or 1; optical depth per (layer, band)
+    if (!one) return 0.0f;
+    odcld = secdiff_b * s.tcl[lay * 16 + band];
     efcl = 1.0f - __expf(-odcld);
+    return 1.0f;
   }
-  return (float)cf;
+  if (!one) {
+    if (!(s.fbits[lay * 5 + (g >> 5)] & bit)) return 0.0f;
+    // fractional cldfmc: enters the cloudy-layer formulas with zero cloud optical depth
+    return (float)__ldg(a.cldfmcl + (long long)g + GB_NGPT * (icol + (long long)a.ld * lay));
+  }
+  long long o = (long long)g + GB_NGPT * (icol + (long long)a.ld * lay);
+  double ciwp = __ldg(a.ciwpmcl + o), clwp = __ldg(a.clwpmcl + o);
+  float tauc;
+  double cwp = ciwp + clwp;
+  if (a.inflag == 2 && cwp >= 1.e-20) {
+    tauc = cloud_tau(a, icol, lay, band, T, ciwp, clwp);
+  } else {
+    double tin = __ldg(a.taucmcl + o);
+    if (a.inflag == 2 && tin >= 1.e-20) tauc = cloud_tau(a, icol, lay, band, T, ciwp, clwp);
+    else tauc = (float)tin;
+  }
+  odcld = secdiff_b * tauc;
+  efcl = 1.0f - __expf(-odcld);
+  return 1.0f;
 }
 
-// ------------------------------------------------------------------ gas optics of one band
-// Prologue once per layer (terms into shared memory), barrier, then one
-// generic weighted gather per (layer, g) cell.
-template <int b>
-__device__ __forceinline__ void gas_optics_band(const Smem& s, int nl, int laytrop, const float* __restrict__ T) {
-  constexpr int NG = ngb_const(b), G0 = g0_const(b), M = maxt(b);
-  const int pad_off = c_T.band[b - 1].sr;
-  for (int lay = threadIdx.x; lay < nl; lay += NT) {
-    Cell c{s.f, s.iv, nl, lay};
-    Terms t{s.terms + lay * MAXT_ALL, 0};
-    FracRec r = prologue<b>(c, lay < laytrop, t);
-    t.pad(M, pad_off);
-    s.frec[lay * 16 + (b - 1)] = r;
+
+__device__ __forceinline__ bool cell_is_cloudy(const Smem& s, int lay, int g) {
+  const unsigned bit = 1u << (g & 31);
+  return ((s.cbits[lay * 5 + (g >> 5)] | s.fbits[lay * 5 + (g >> 5)]) & bit) != 0u;
+}
+
+// Transfer coefficients of one cell (rtrnmc.f90:350-455 rearranged): the
+// clear-sky stream uses radiance*T + S (S = bbd*atrans down, bbugas*atrans
+// up); a cloudy cell uses radiance*A + Bd (down) / + Bu (up) and scales the
+// surface-temperature derivative by D.
+struct CellCoef {
+  float4 clr;  // T, Sd, Su, 0
+  float4 cld;  // A, Bd, Bu, D
+};
+__device__ __forceinline__ CellCoef cell_coef(bool cloudy, float odepth, float odcld, float efcl, float cldf,
+                                              float plfrac, float blay, float dplankup, float dplankdn) {
+  const float rec_6 = 0.166667f;
+  CellCoef r;
+  float atrans, bbd, bbu, tau_q;
+  if (odepth <= 0.06f) {
+    atrans = odepth - 0.5f * odepth * odepth;
+    float o = rec_6 * odepth;
+    bbd = plfrac * (blay + dplankdn * o);
+    bbu = plfrac * (blay + dplankup * o);
+    tau_q = odepth;
+  } else {
+    TblEntry e = tbl(odepth);
+    atrans = 1.0f - e.trans;
+    bbd = plfrac * (blay + e.tfn * dplankdn);
+    bbu = plfrac * (blay + e.tfn * dplankup);
+    tau_q = e.tau;
   }
-  __syncthreads();
-  for (int cell = threadIdx.x; cell < nl * NG; cell += NT) {
-    const int lay = cell / NG, gi = cell - lay * NG;
-    const float2* tp = s.terms + lay * MAXT_ALL;
+  const float gsd = bbd * atrans, gsu = bbu * atrans;
+  r.clr = make_float4(1.0f - atrans, gsd, gsu, 0.0f);
+  if (cloudy) {
+    float atot, bbdtot, bbutot;
+    float odtot = odepth + odcld;
+    if (odtot < 0.06f) {
+      atot = odtot - 0.5f * odtot * odtot;
+      float o = rec_6 * odtot;
+      bbdtot = plfrac * (blay + dplankdn * o);
+      bbutot = plfrac * (blay + dplankup * o);
+    } else {
+      // odepth <= 0.06: table at odepth + odcld; otherwise at tau_tbl(itgas) + odcld
+      TblEntry et = tbl((odepth <= 0.06f ? odepth : tau_q) + odcld);
+      atot = 1.0f - et.trans;
+      bbdtot = plfrac * (blay + et.tfn * dplankdn);
+      bbutot = plfrac * (blay + et.tfn * dplankup);
+    }
+    float A = 1.0f - (atrans + efcl * (1.0f - atrans));
+    float Bd = gsd + cldf * (bbdtot * atot - gsd);
+    float Bu = gsu + cldf * (bbutot * atot - gsu);
+    float D = cldf * (1.0f - atot) + (1.0f - cldf) * (1.0f - atrans);
+    r.cld = make_float4(A, Bd, Bu, D);
+  } else {
+    r.cld = r.clr;
+  }
+  return r;
+}
+
+// ------------------------------------------------------------------ band groups
+// Groups of consecutive bands whose term lists share the TGROUP slots per
+// layer: {1,2,3} {4,5} {6,7,8} {9,10,11} {12,13} {14,15,16}.  c_toff[b] is the
+// first term slot of band b in its group.
+__constant__ int c_gfirst[NGROUP + 1] = {1, 4, 6, 9, 12, 14, 17};
+__constant__ int c_toff[17] = {0, 0, 10, 18, 0, 16, 0, 12, 32, 0, 20, 28, 0, 16, 0, 8, 28};
+static_assert(maxt(1) + maxt(2) + maxt(3) <= TGROUP && maxt(4) + maxt(5) <= TGROUP &&
+                  maxt(6) + maxt(7) + maxt(8) <= TGROUP && maxt(9) + maxt(10) + maxt(11) <= TGROUP &&
+                  maxt(12) + maxt(13) <= TGROUP && maxt(14) + maxt(15) + maxt(16) <= TGROUP,
+              "band group exceeds its term slots");
+static_assert(maxt(1) == 10 && maxt(1) + maxt(2) == 18 && maxt(4) == 16 && maxt(6) == 12 &&
+                  maxt(6) + maxt(7) == 32 && maxt(9) == 20 && maxt(9) + maxt(10) == 28 && maxt(12) == 16 &&
+                  maxt(14) == 8 && maxt(14) + maxt(15) == 28,
+              "c_toff out of date");
+
+// Prologue of band b for one layer: the band-specific per-layer code
+// (lw_gasoptics.cuh) writing the layer's terms and Planck-fraction record.
+template <int b>
+__device__ __forceinline__ void band_prologue(const Smem& s, int nl, int lay, bool lower, int slot) {
+  Cell c{s.f, s.iv, nl, lay};
+  Terms t{s.terms + (size_t)c_toff[b] * nl + lay, nl, 0};
+  FracRec r = prologue<b>(c, lower, t);
+  t.pad(maxt(b), c_T.band[b - 1].sr);
+  s.frec[slot * nl + lay] = r;
+}
+
+__device__ __noinline__ void prologue_dispatch(int b, const Smem& s, int nl, int lay, bool lower, int slot) {
+  switch (b) {
+    case 1: band_prologue<1>(s, nl, lay, lower, slot); break;
+    case 2: band_prologue<2>(s, nl, lay, lower, slot); break;
+    case 3: band_prologue<3>(s, nl, lay, lower, slot); break;
+    case 4: band_prologue<4>(s, nl, lay, lower, slot); break;
+    case 5: band_prologue<5>(s, nl, lay, lower, slot); break;
+    case 6: band_prologue<6>(s, nl, lay, lower, slot); break;
+    case 7: band_prologue<7>(s, nl, lay, lower, slot); break;
+    case 8: band_prologue<8>(s, nl, lay, lower, slot); break;
+    case 9: band_prologue<9>(s, nl, lay, lower, slot); break;
+    case 10: band_prologue<10>(s, nl, lay, lower, slot); break;
+    case 11: band_prologue<11>(s, nl, lay, lower, slot); break;
+    case 12: band_prologue<12>(s, nl, lay, lower, slot); break;
+    case 13: band_prologue<13>(s, nl, lay, lower, slot); break;
+    case 14: band_prologue<14>(s, nl, lay, lower, slot); break;
+    case 15: band_prologue<15>(s, nl, lay, lower, slot); break;
+    default: band_prologue<16>(s, nl, lay, lower, slot); break;
+  }
+}
+
+// All (band, layer) prologues of group gr, spread over the block's threads.
+template <int NT>
+__device__ __forceinline__ void group_prologues(int gr, const Smem& s, int nl, int laytrop) {
+  const int b0 = c_gfirst[gr], nb = c_gfirst[gr + 1] - b0;
+  for (int it = threadIdx.x; it < nb * nl; it += NT) {
+    const int slot = it / nl, lay = it - slot * nl;
+    prologue_dispatch(b0 + slot, s, nl, lay, lay < laytrop, slot);
+  }
+}
+
+// One thread per (band, layer, g) cell of group gr: optical depth, Planck
+// fraction and transfer coefficients into the scratch slot.
+template <int NT>
+__device__ __forceinline__ void group_cells(int gr, const LwArgs& a, const Smem& s, int nl, int laytrop,
+                                            const float* __restrict__ T, long long icol, float4* __restrict__ scr) {
+  const int b0 = c_gfirst[gr], b1 = c_gfirst[gr + 1];
+  int ncell = 0;
+  for (int b = b0; b < b1; ++b) ncell += nl * c_T.band[b - 1].ng;
+  const bool clouds = a.icld >= 1;
+  for (int cell = threadIdx.x; cell < ncell; cell += NT) {
+    int b = b0, c = cell, NG = c_T.band[b0 - 1].ng;
+    while (c >= nl * NG) {
+      c -= nl * NG;
+      ++b;
+      NG = c_T.band[b - 1].ng;
+    }
+    const int slot = b - b0;
+    const int lay = (int)(((float)c + 0.5f) * __frcp_rn((float)NG)), gi = c - lay * NG, g = c_T.band[b - 1].g0 + gi;
+    const int M = c_maxt[b];
+    const float2* tp = s.terms + (size_t)c_toff[b] * nl + lay;
+    const float* Tg = T + gi;
     float acc = 0.0f;
-#pragma unroll
     for (int k = 0; k < M; ++k) {
-      float2 w = tp[k];
-      acc = fmaf(w.x, __ldg(T + __float_as_int(w.y) + gi), acc);
+      const float2 w = tp[k * nl];
+      acc = fmaf(w.x, __ldg(Tg + __float_as_int(w.y)), acc);
     }
     if ((b == 4 || b == 7) && lay >= laytrop) acc *= gscale(b, gi);
-    s.taut[lay * GB_NGPT + G0 + gi] = acc + s.taua[lay * 16 + (b - 1)];
+    const float taut = acc + s.taua[(b - 1) * nl + lay];
+    const FracRec fr = s.frec[slot * nl + lay];
+    const float* fp = T + fr.off + gi;
+    const float f0 = __ldg(fp);
+    const float plfrac = f0 + fr.fpl * (__ldg(fp + NG) - f0);
+    if (lay == 0) s.frac1[g] = plfrac;
+    if (a.dbg_taut) {
+      a.dbg_taut[(icol * nl + lay) * GB_NGPT + g] = taut;
+      a.dbg_fracs[(icol * nl + lay) * GB_NGPT + g] = plfrac;
+    }
+    const float secdiff = s.misc[b - 1];
+    const float blay = s.plk_lay[(b - 1) * nl + lay];
+    const float dplankup = s.plk_lev[(b - 1) * (nl + 1) + lay + 1] - blay;
+    const float dplankdn = s.plk_lev[(b - 1) * (nl + 1) + lay] - blay;
+    const float odepth = fmaxf(secdiff * taut, 0.0f);
+    bool cloudy = false;
+    float odcld = 0.0f, efcl = 0.0f, cldf = 0.0f;
+    if (clouds && s.cldlay[lay]) {
+      cldf = cell_cloud(a, s, icol, g, lay, secdiff, b - 1, T, odcld, efcl);
+      cloudy = cell_is_cloudy(s, lay, g);
+    }
+    CellCoef cc = cell_coef(cloudy, odepth, odcld, efcl, cldf, plfrac, blay, dplankup, dplankdn);
+    scr[lay * GB_NGPT + g] = cc.clr;
+    if (cloudy) scr[(nl + lay) * GB_NGPT + g] = cc.cld;
   }
-  __syncthreads();
 }
 
-// ------------------------------------------------------------------ the kernel
-__global__ void __launch_bounds__(NT) lw_column_kernel(LwArgs a, const float* __restrict__ T) {
-  extern __shared__ __align__(16) char smem_raw[];
+// ------------------------------------------------------------------ one column
+template <int NT>
+__device__ __forceinline__ void solve_column(const LwArgs& a, long long icol, char* smem_raw,
+                                             float4* __restrict__ scr, const float* __restrict__ T) {
+  constexpr int NWARP = NT / 32;
   const int nl = a.nlay;
-  const long long icol = blockIdx.x;
-  if (icol >= a.ncol) return;
-  Smem s = carve(smem_raw, nl);
+  const Smem s = carve(smem_raw, nl);
   const int tid = threadIdx.x;
-  if (tid < 4) {
-    s.scal[tid] = 0.0f;
-    s.iscal[tid] = 0;
-  }
-  for (int l = tid; l < nl; l += NT) s.cldlay[l] = 0;
-  __syncthreads();
+  const bool fused = a.cloud_mode == LW_CLOUD_FUSED;
+  {
+    // fused clouds: the column's 140 draws, one thread (the last warp is the
+    // least busy one in phase 1)
+    if (fused && a.icld >= 1 && tid == NT - 1)
+      gbmt::first_reals(a.seed0 + (unsigned)icol, GB_NGPT, s.mtlo, s.cdf, 1);
+    if (tid < 4) {
+      s.scal[tid] = 0.0f;
+      s.iscal[tid] = 0;
+    }
+    for (int l = tid; l < nl; l += NT) s.cldlay[l] = 0;
+    for (int l = tid; l < nl * 5; l += NT) s.cbits[l] = s.fbits[l] = 0u;
+    __syncthreads();
 
-  // ---------------- phase 1: inatm + setcoef, one thread per layer
-  const float stpfac = 296.0f / 1013.0f;
-  const float amd = 28.9660f, amw = 18.0160f;
-  int my_bad = 0;
-  for (int lay = tid; lay < nl; lay += NT) {
-    double pd = in2(a.play, a.ld, icol, lay);
-    float pavel = (float)pd;
-    float tavel = (float)in2(a.tlay, a.ld, icol, lay);
-    double dpz = in2(a.plev, a.ld, icol, lay) - in2(a.plev, a.ld, icol, lay + 1);
-    float w1 = (float)in2(a.h2ovmr, a.ld, icol, lay);
-    float w2 = (float)in2(a.co2vmr, a.ld, icol, lay);
-    float w3 = (float)in2(a.o3vmr, a.ld, icol, lay);
-    float w4 = (float)in2(a.n2ovmr, a.ld, icol, lay);
-    float w6 = (float)in2(a.ch4vmr, a.ld, icol, lay);
-    float w7 = (float)in2(a.o2vmr, a.ld, icol, lay);
-    float amm = (1.0f - w1) * amd + w1 * amw;
-    float coldry = (float)dpz * 1.e3f * (float)c_T.avogad / (1.e2f * (float)c_T.grav * amm * (1.0f + w1));
-    float summol = w2 + w3 + w4 + 0.0f + w6 + w7;
-    float wbrodl = coldry * (1.0f - summol);
-    float wk1 = coldry * w1, wk2 = coldry * w2, wk3 = coldry * w3, wk4 = coldry * w4, wk6 = coldry * w6,
-          wk7 = coldry * w7;
-    float* F = s.f;
-    auto put = [&](int k, float v) { F[k * nl + lay] = v; };
-    put(F_COLDRY, coldry);
-    put(F_PAVEL, pavel);
-    put(F_WX1, coldry * (float)in2(a.ccl4vmr, a.ld, icol, lay) * 1.e-20f);
-    put(F_WX2, coldry * (float)in2(a.cfc11vmr, a.ld, icol, lay) * 1.e-20f);
-    put(F_WX3, coldry * (float)in2(a.cfc12vmr, a.ld, icol, lay) * 1.e-20f);
-    put(F_WX4, coldry * (float)in2(a.cfc22vmr, a.ld, icol, lay) * 1.e-20f);
-    if (!(pavel > 0.0f) || !(tavel > 0.0f) || !isfinite(pavel) || !isfinite(tavel)) my_bad = 1;
-    // setcoef (rrtmg_lw_setcoef.f90:275-430)
-    float plog = __logf(pavel);
-    bool lower = plog > 4.56f;
-    if (fabsf(plog - 4.56f) < 1.0e-4f) lower = log(pd) > 4.56;  // decide the regime in fp64 near the switch
-    int jp = clampi((int)(36.0f - 5.0f * (plog + 0.04f)), 1, 58);
-    jp = lower ? (jp > 12 ? 12 : jp) : (jp < 13 ? 13 : jp);
-    float fp = 5.0f * (c_T.preflog[jp - 1] - plog);
-    float dt0 = (tavel - c_T.tref[jp - 1]) / 15.0f;
-    int jt = clampi((int)(3.0f + dt0), 1, 4);
-    float ft = dt0 - (float)(jt - 3);
-    float dt1 = (tavel - c_T.tref[jp]) / 15.0f;
-    int jt1 = clampi((int)(3.0f + dt1), 1, 4);
-    float ft1 = dt1 - (float)(jt1 - 3);
-    float water = wk1 / coldry;
-    float scalefac = pavel * stpfac / tavel;
-    float forfac = scalefac / (1.0f + water), forfrac, selffrac = 0.0f;
-    int indfor, indself = 1;
-    if (lower) {
-      float factor = (332.0f - tavel) / 36.0f;
-      indfor = min(2, max(1, (int)factor));
-      forfrac = factor - (float)indfor;
-      factor = (tavel - 188.0f) / 7.2f;
-      indself = min(9, max(1, (int)factor - 7));
-      selffrac = factor - (float)(indself + 7);
-    } else {
-      float factor = (tavel - 188.0f) / 36.0f;
-      indfor = 3;
-      forfrac = factor - 1.0f;
+    // ---------------- phase 1: inatm + setcoef, one thread per layer
+    const float stpfac = 296.0f / 1013.0f;
+    const float amd = 28.9660f, amw = 18.0160f;
+    int my_bad = 0;
+    for (int lay = tid; lay < nl; lay += NT) {
+      double pd = in2(a.play, a.ld, icol, lay);
+      float pavel = (float)pd;
+      float tavel = (float)in2(a.tlay, a.ld, icol, lay);
+      double dpz = in2(a.plev, a.ld, icol, lay) - in2(a.plev, a.ld, icol, lay + 1);
+      float w1 = (float)in2(a.h2ovmr, a.ld, icol, lay);
+      float w2 = (float)in2(a.co2vmr, a.ld, icol, lay);
+      float w3 = (float)in2(a.o3vmr, a.ld, icol, lay);
+      float w4 = (float)in2(a.n2ovmr, a.ld, icol, lay);
+      float w6 = (float)in2(a.ch4vmr, a.ld, icol, lay);
+      float w7 = (float)in2(a.o2vmr, a.ld, icol, lay);
+      float amm = (1.0f - w1) * amd + w1 * amw;
+      float coldry = (float)dpz * 1.e3f * (float)c_T.avogad / (1.e2f * (float)c_T.grav * amm * (1.0f + w1));
+      float summol = w2 + w3 + w4 + 0.0f + w6 + w7;
+      float wbrodl = coldry * (1.0f - summol);
+      float wk1 = coldry * w1, wk2 = coldry * w2, wk3 = coldry * w3, wk4 = coldry * w4, wk6 = coldry * w6,
+            wk7 = coldry * w7;
+      float* F = s.f;
+      auto put = [&](int k, float v) { F[k * nl + lay] = v; };
+      put(F_COLDRY, coldry);
+      put(F_PAVEL, pavel);
+      put(F_WX1, coldry * (float)in2(a.ccl4vmr, a.ld, icol, lay) * 1.e-20f);
+      put(F_WX2, coldry * (float)in2(a.cfc11vmr, a.ld, icol, lay) * 1.e-20f);
+      put(F_WX3, coldry * (float)in2(a.cfc12vmr, a.ld, icol, lay) * 1.e-20f);
+      put(F_WX4, coldry * (float)in2(a.cfc22vmr, a.ld, icol, lay) * 1.e-20f);
+      if (!(pavel > 0.0f) || !(tavel > 0.0f) || !isfinite(pavel) || !isfinite(tavel)) my_bad = 1;
+      // setcoef (rrtmg_lw_setcoef.f90:275-430)
+      float plog = __logf(pavel);
+      bool lower = plog > 4.56f;
+      if (fabsf(plog - 4.56f) < 1.0e-4f) lower = log(pd) > 4.56;  // decide the regime in fp64 near the switch
+      int jp = clampi((int)(36.0f - 5.0f * (plog + 0.04f)), 1, 58);
+      jp = lower ? (jp > 12 ? 12 : jp) : (jp < 13 ? 13 : jp);
+      float fp = 5.0f * (c_T.preflog[jp - 1] - plog);
+      float dt0 = (tavel - c_T.tref[jp - 1]) / 15.0f;
+      int jt = clampi((int)(3.0f + dt0), 1, 4);
+      float ft = dt0 - (float)(jt - 3);
+      float dt1 = (tavel - c_T.tref[jp]) / 15.0f;
+      int jt1 = clampi((int)(3.0f + dt1), 1, 4);
+      float ft1 = dt1 - (float)(jt1 - 3);
+      float water = wk1 / coldry;
+      float scalefac = pavel * stpfac / tavel;
+      float forfac = scalefac / (1.0f + water), forfrac, selffrac = 0.0f;
+      int indfor, indself = 1;
+      if (lower) {
+        float factor = (332.0f - tavel) / 36.0f;
+        indfor = min(2, max(1, (int)factor));
+        forfrac = factor - (float)indfor;
+        factor = (tavel - 188.0f) / 7.2f;
+        indself = min(9, max(1, (int)factor - 7));
+        selffrac = factor - (float)(indself + 7);
+      } else {
+        float factor = (tavel - 188.0f) / 36.0f;
+        indfor = 3;
+        forfrac = factor - 1.0f;
+      }
+      float selffac = water * forfac;
+      float scaleminor = pavel / tavel;
+      float scaleminorn2 = scaleminor * (wbrodl / (coldry + wk1));
+      float factor = (tavel - 180.8f) / 7.2f;
+      int indminor = min(18, max(1, (int)factor));
+      float minorfrac = factor - (float)indminor;
+      float colh2o = 1.e-20f * wk1;
+      float colco2 = 1.e-20f * wk2, colo3 = 1.e-20f * wk3, coln2o = 1.e-20f * wk4, colco = 0.0f;
+      float colch4 = 1.e-20f * wk6, colo2 = 1.e-20f * wk7;
+      if (colco2 == 0.0f) colco2 = 1.e-32f * coldry;
+      if (colo3 == 0.0f) colo3 = 1.e-32f * coldry;
+      if (coln2o == 0.0f) coln2o = 1.e-32f * coldry;
+      if (colco == 0.0f) colco = 1.e-32f * coldry;
+      if (colch4 == 0.0f) colch4 = 1.e-32f * coldry;
+      float compfp = 1.0f - fp;
+      put(F_FAC10, compfp * ft);
+      put(F_FAC00, compfp * (1.0f - ft));
+      put(F_FAC11, fp * ft1);
+      put(F_FAC01, fp * (1.0f - ft1));
+      put(F_COLH2O, colh2o); put(F_COLCO2, colco2); put(F_COLO3, colo3); put(F_COLN2O, coln2o);
+      put(F_COLCO, colco); put(F_COLCH4, colch4); put(F_COLO2, colo2); put(F_COLBRD, 1.e-20f * wbrodl);
+      put(F_SELFFAC, colh2o * selffac); put(F_SELFFRAC, selffrac);
+      put(F_FORFAC, colh2o * forfac); put(F_FORFRAC, forfrac);
+      put(F_MINORFRAC, minorfrac); put(F_SCALEMINOR, scaleminor); put(F_SCALEMINORN2, scaleminorn2);
+      int* IV = s.iv;
+      IV[I_JP * nl + lay] = jp; IV[I_JT * nl + lay] = jt; IV[I_JT1 * nl + lay] = jt1;
+      IV[I_INDSELF * nl + lay] = indself; IV[I_INDFOR * nl + lay] = indfor; IV[I_INDMINOR * nl + lay] = indminor;
+      // lower layers must form the prefix 0..laytrop-1
+      if (lower) {
+        atomicAdd(&s.iscal[0], 1);        // laytrop
+        atomicAdd(&s.iscal[1], lay + 1);  // sum of 1-based indices of lower layers
+      }
     }
-    float selffac = water * forfac;
-    float scaleminor = pavel / tavel;
-    float scaleminorn2 = scaleminor * (wbrodl / (coldry + wk1));
-    float factor = (tavel - 180.8f) / 7.2f;
-    int indminor = min(18, max(1, (int)factor));
-    float minorfrac = factor - (float)indminor;
-    float colh2o = 1.e-20f * wk1;
-    float colco2 = 1.e-20f * wk2, colo3 = 1.e-20f * wk3, coln2o = 1.e-20f * wk4, colco = 0.0f;
-    float colch4 = 1.e-20f * wk6, colo2 = 1.e-20f * wk7;
-    if (colco2 == 0.0f) colco2 = 1.e-32f * coldry;
-    if (colo3 == 0.0f) colo3 = 1.e-32f * coldry;
-    if (coln2o == 0.0f) coln2o = 1.e-32f * coldry;
-    if (colco == 0.0f) colco = 1.e-32f * coldry;
-    if (colch4 == 0.0f) colch4 = 1.e-32f * coldry;
-    float compfp = 1.0f - fp;
-    put(F_FAC10, compfp * ft);
-    put(F_FAC00, compfp * (1.0f - ft));
-    put(F_FAC11, fp * ft1);
-    put(F_FAC01, fp * (1.0f - ft1));
-    put(F_COLH2O, colh2o); put(F_COLCO2, colco2); put(F_COLO3, colo3); put(F_COLN2O, coln2o);
-    put(F_COLCO, colco); put(F_COLCH4, colch4); put(F_COLO2, colo2); put(F_COLBRD, 1.e-20f * wbrodl);
-    put(F_SELFFAC, colh2o * selffac); put(F_SELFFRAC, selffrac);
-    put(F_FORFAC, colh2o * forfac); put(F_FORFRAC, forfrac);
-    put(F_MINORFRAC, minorfrac); put(F_SCALEMINOR, scaleminor); put(F_SCALEMINORN2, scaleminorn2);
-    int* IV = s.iv;
-    IV[I_JP * nl + lay] = jp; IV[I_JT * nl + lay] = jt; IV[I_JT1 * nl + lay] = jt1;
-    IV[I_INDSELF * nl + lay] = indself; IV[I_INDFOR * nl + lay] = indfor; IV[I_INDMINOR * nl + lay] = indminor;
-    // lower layers must form the prefix 0..laytrop-1
-    if (lower) {
-      atomicAdd(&s.iscal[0], 1);        // laytrop
-      atomicAdd(&s.iscal[1], lay + 1);  // sum of 1-based indices of lower layers
+    // aerosol optical depths (rrtmg_lw_rad.f90:548-553), all threads
+    for (int it = tid; it < 16 * nl; it += NT) {
+      const int ib = it / nl, lay = it - ib * nl;
+      s.taua[it] = (float)__ldg(a.tauaer + icol + (long long)a.ld * (lay + (long long)nl * ib));
     }
-    for (int ib = 0; ib < 16; ++ib)
-      s.taua[lay * 16 + ib] = (float)__ldg(a.tauaer + icol + (long long)a.ld * (lay + (long long)nl * ib));
-  }
-  // Planck interpolation per (level, band) (setcoef.f90:173-269, istart = 1)
-  for (int it = tid; it < (nl + 1) * 16; it += NT) {
-    int lev = it >> 4, ib = it & 15;
-    const float* tp = T + c_T.totplnk + ib * 181;
-    float tz = (float)in2(a.tlev, a.ld, icol, lev);
-    int ind = clampi((int)(tz - 159.0f), 1, 180);
-    float fr = tz - 159.0f - (float)ind;
-    s.plk_lev[lev * 16 + ib] = tp[ind - 1] + fr * (tp[ind] - tp[ind - 1]);
-    if (lev < nl) {
-      float tl = (float)in2(a.tlay, a.ld, icol, lev);
-      int il = clampi((int)(tl - 159.0f), 1, 180);
-      float fl = tl - 159.0f - (float)il;
-      s.plk_lay[lev * 16 + ib] = tp[il - 1] + fl * (tp[il] - tp[il - 1]);
+    // Planck interpolation per (level, band) (setcoef.f90:173-269, istart = 1)
+    for (int it = tid; it < (nl + 1) * 16; it += NT) {
+      int lev = it >> 4, ib = it & 15;
+      const float* tp = T + c_T.totplnk + ib * 181;
+      float tz = (float)in2(a.tlev, a.ld, icol, lev);
+      int ind = clampi((int)(tz - 159.0f), 1, 180);
+      float fr = tz - 159.0f - (float)ind;
+      s.plk_lev[ib * (nl + 1) + lev] = tp[ind - 1] + fr * (tp[ind] - tp[ind - 1]);
+      if (lev < nl) {
+        float tl = (float)in2(a.tlay, a.ld, icol, lev);
+        int il = clampi((int)(tl - 159.0f), 1, 180);
+        float fl = tl - 159.0f - (float)il;
+        s.plk_lay[ib * nl + lev] = tp[il - 1] + fl * (tp[il] - tp[il - 1]);
+      }
     }
-  }
-  if (tid < 16) {
-    float tb = (float)__ldg(a.tsfc + icol);
-    int ind = clampi((int)(tb - 159.0f), 1, 180);
-    float fr = tb - 159.0f - (float)ind;
-    float se = (float)__ldg(a.emis + icol + (long long)a.ld * tid);
-    const float* tp = T + c_T.totplnk + tid * 181;
-    const float* td = T + c_T.totplnkderiv + tid * 181;
-    s.misc[16 + tid] = se * (tp[ind - 1] + fr * (tp[ind] - tp[ind - 1]));
-    s.misc[32 + tid] = se * (td[ind - 1] + fr * (td[ind] - td[ind - 1]));
-    s.misc[48 + tid] = se;
-  }
-  // McICA pre-pass: cloudy layers and cldprmc's STOP conditions
-  if (tid < GB_NGPT && a.icld >= 1) {
-    int err = 0;
-    for (int lay = 0; lay < nl; ++lay) {
-      long long o = (long long)tid + GB_NGPT * (icol + (long long)a.ld * lay);
-      double cf = __ldg(a.cldfmcl + o);
-      if (cf == 1.0) s.cldlay[lay] = 1;
-      if (cf >= 1.e-20) {
-        double ciwp = __ldg(a.ciwpmcl + o), clwp = __ldg(a.clwpmcl + o);
-        if (ciwp + clwp >= 1.e-20 || __ldg(a.taucmcl + o) >= 1.e-20) {
+    if (tid < 16) {
+      float tb = (float)__ldg(a.tsfc + icol);
+      int ind = clampi((int)(tb - 159.0f), 1, 180);
+      float fr = tb - 159.0f - (float)ind;
+      float se = (float)__ldg(a.emis + icol + (long long)a.ld * tid);
+      const float* tp = T + c_T.totplnk + tid * 181;
+      const float* td = T + c_T.totplnkderiv + tid * 181;
+      s.misc[16 + tid] = se * (tp[ind - 1] + fr * (tp[ind] - tp[ind - 1]));
+      s.misc[32 + tid] = se * (td[ind - 1] + fr * (td[ind] - td[ind - 1]));
+      s.misc[48 + tid] = se;
+    }
+    // McICA pre-pass over every (layer, g) cell: cloudy layers, the per-cell
+    // "cldfmc == 1" / "cldfmc neither 0 nor 1" bits the later phases use to
+    // skip loads, and cldprmc's STOP conditions.
+    if (a.icld >= 1 && fused) {
+      __syncthreads();  // draws ready
+      // cloudy cells: cdf(g) >= 1 - cldf(lay) (mcica_subcol_gen_lw.f90:650), one warp per layer
+      const int warp = tid >> 5, lane = tid & 31;
+      const long long* cdfb = reinterpret_cast<const long long*>(s.cdf);
+      for (int lay = warp; lay < nl; lay += NWARP) {
+        double cf = in2(a.cldfrac, a.ld, icol, lay);
+        cf = cf < 1.0e-20 ? 0.0 : cf;  // :463-470
+        // cdf >= 1 - cf, compared on the bit patterns (cdf is in [0, 1], so
+        // for a threshold >= 0 the integer order is the floating-point order)
+        const double thr = 1.0 - cf;
+        const long long tb = __double_as_longlong(thr);
+        const bool all = thr < 0.0, none = !(thr == thr);
+        unsigned any = 0u;
+#pragma unroll
+        for (int w = 0; w < 5; ++w) {
+          const int g = w * 32 + lane;
+          const bool cl = g < GB_NGPT && !none && (all || cdfb[g] >= tb);
+          const unsigned m = __ballot_sync(0xffffffffu, cl);
+          if (lane == 0) s.cbits[lay * 5 + w] = m;
+          any |= m;
+        }
+        if (lane == 0) s.cldlay[lay] = any != 0u;
+      }
+      __syncthreads();
+      // cloud optical depth per (layer, band) where the band has a cloudy
+      // sub-column (the values cldprmc computes for every such cell), and
+      // cldprmc's STOP conditions
+      int err = 0;
+      for (int it = tid; it < nl * 16; it += NT) {
+        const int lay = it >> 4, band = it & 15;
+        if (!s.cldlay[lay]) continue;
+        const int g0 = c_T.band[band].g0, ng = c_T.band[band].ng;
+        bool any = false;
+        for (int g = g0; g < g0 + ng; ++g) any |= (s.cbits[lay * 5 + (g >> 5)] >> (g & 31)) & 1u;
+        if (!any) continue;
+        const double ciwp = in2(a.ciwp, a.ld, icol, lay), clwp = in2(a.clwp, a.ld, icol, lay);
+        const double tin = __ldg(a.tauc + band + 16 * (icol + a.ld * lay));
+        const double cwp = ciwp + clwp;
+        float tauc;
+        if (a.inflag == 2 && (cwp >= 1.e-20 || tin >= 1.e-20)) tauc = cloud_tau(a, icol, lay, band, T, ciwp, clwp);
+        else tauc = (float)tin;
+        s.tcl[lay * 16 + band] = tauc;
+        if (cwp >= 1.e-20 || tin >= 1.e-20) {
           if (a.inflag == 1) err = GB_COL_INFLAG1;
           if (a.inflag == 2) {
-            double rice = in2(a.reicmcl, a.ld, icol, lay), rliq = in2(a.relqmcl, a.ld, icol, lay);
+            const double rice = in2(a.reicmcl, a.ld, icol, lay), rliq = in2(a.relqmcl, a.ld, icol, lay);
             if (ciwp != 0.0) {
               if (a.iceflag == 0 && rice < 10.0) err = GB_COL_ICE_SMALL;
               if (a.iceflag == 1 && (rice < 13.0 || rice > 130.0)) err = GB_COL_ICE_BOUNDS;
@@ -433,224 +617,297 @@ __global__ void __launch_bounds__(NT) lw_column_kernel(LwArgs a, const float* __
           }
         }
       }
-    }
-    if (err) atomicMax(&s.iscal[2], err);
-  }
-  int anybad = __syncthreads_or(my_bad);
-  const int laytrop = s.iscal[0];
-  if (tid == 0) {
-    int err = s.iscal[2];
-    // sum of 1-based indices of lower layers equals laytrop*(laytrop+1)/2 iff they form a prefix
-    if (s.iscal[1] != laytrop * (laytrop + 1) / 2) err = GB_COL_LAYTROP;
-    if (anybad) err = GB_COL_BADVAL;
-    s.iscal[3] = err;
-    if (err) {
-      if (a.col_err) a.col_err[icol] = err;
-      atomicMax(a.err_flag, err);
-    } else if (a.col_err) {
-      a.col_err[icol] = 0;
-    }
-    // pwvcm (inatm :859-870, summed in layer order) and secdiff (rtrnmc.f90:258-266)
-    float amttl = 0.0f, wvttl = 0.0f;
-    for (int l = 0; l < nl; ++l) {
-      float wk1 = s.f[F_COLH2O * nl + l] * 1.e20f;
-      amttl = amttl + s.f[F_COLDRY * nl + l] + wk1;
-      wvttl = wvttl + wk1;
-    }
-    float wvsh = (amw * wvttl) / (amd * amttl);
-    float pz0 = (float)in2(a.plev, a.ld, icol, 0);
-    float pwvcm = wvsh * (1.e3f * pz0) / (1.e2f * (float)c_T.grav);
-    const float a0[16] = {1.66f, 1.55f, 1.58f, 1.66f, 1.54f, 1.454f, 1.89f, 1.33f, 1.668f, 1.66f, 1.66f, 1.66f, 1.66f, 1.66f, 1.66f, 1.66f};
-    const float a1[16] = {0.f, 0.25f, 0.22f, 0.f, 0.13f, 0.446f, -0.10f, 0.40f, -0.006f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    const float a2[16] = {0.f, -12.0f, -11.7f, 0.f, -0.72f, -0.243f, 0.19f, -0.062f, 0.414f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int ib = 0; ib < 16; ++ib) {
-      float sd = 1.66f;
-      if (!(ib == 0 || ib == 3 || ib >= 9)) {
-        sd = a0[ib] + a1[ib] * __expf(a2[ib] * pwvcm);
-        sd = fminf(fmaxf(sd, 1.50f), 1.80f);
+      if (err) atomicMax(&s.iscal[2], err);
+    } else if (a.icld >= 1) {
+      // one warp per layer: the layer's 140 cldfmcl values tested on their bit
+      // patterns (no fp64 pipe): == 1, /= 0, >= 1e-20
+      const int warp = tid >> 5, lane = tid & 31;
+      const long long kOne = 0x3FF0000000000000LL, kInf = 0x7FF0000000000000LL;
+      const long long kMin = __double_as_longlong(1.0e-20);
+      int err = 0;
+      for (int lay = warp; lay < nl; lay += NWARP) {
+        const long long base = GB_NGPT * (icol + (long long)a.ld * lay);
+        long long cb[5];
+#pragma unroll
+        for (int w = 0; w < 5; ++w) {
+          const int g = w * 32 + lane;
+          cb[w] = g < GB_NGPT ? __double_as_longlong(__ldcs(a.cldfmcl + base + g)) : 0LL;
+        }
+        unsigned any = 0u;
+#pragma unroll
+        for (int w = 0; w < 5; ++w) {
+          const bool one = cb[w] == kOne;
+          const bool frac = !one && (cb[w] << 1) != 0LL;  // neither +-0 nor 1 (NaN included, as /= 0 is)
+          const unsigned m1 = __ballot_sync(0xffffffffu, one), mf = __ballot_sync(0xffffffffu, frac);
+          if (lane == 0) {
+            s.cbits[lay * 5 + w] = m1;
+            s.fbits[lay * 5 + w] = mf;
+          }
+          any |= m1;
+          if (cb[w] >= kMin && cb[w] <= kInf) {  // cldfmc >= cldmin (cldprmc.f90:178)
+            const long long o = base + w * 32 + lane;
+            const double ciwp = __ldg(a.ciwpmcl + o), clwp = __ldg(a.clwpmcl + o);
+            if (ciwp + clwp >= 1.e-20 || __ldg(a.taucmcl + o) >= 1.e-20) {
+              if (a.inflag == 1) err = GB_COL_INFLAG1;
+              if (a.inflag == 2) {
+                const double rice = in2(a.reicmcl, a.ld, icol, lay), rliq = in2(a.relqmcl, a.ld, icol, lay);
+                if (ciwp != 0.0) {
+                  if (a.iceflag == 0 && rice < 10.0) err = GB_COL_ICE_SMALL;
+                  if (a.iceflag == 1 && (rice < 13.0 || rice > 130.0)) err = GB_COL_ICE_BOUNDS;
+                  if (a.iceflag == 2 && (rice < 5.0 || rice > 131.0)) err = GB_COL_ICE_BOUNDS;
+                  if (a.iceflag == 3 && (rice < 5.0 || rice > 140.0)) err = GB_COL_DGE_BOUNDS;
+                }
+                if (clwp != 0.0 && a.liqflag == 1 && (rliq < 2.5 || rliq > 60.0)) err = GB_COL_LIQ_BOUNDS;
+              }
+            }
+          }
+        }
+        if (lane == 0) s.cldlay[lay] = any != 0u;
       }
-      s.misc[ib] = sd;
+      if (err) atomicMax(&s.iscal[2], err);
     }
-  }
-  __syncthreads();
-
-  // ---------------- phase 2: taumol, band by band
-  gas_optics_band<1>(s, nl, laytrop, T);
-  gas_optics_band<2>(s, nl, laytrop, T);
-  gas_optics_band<3>(s, nl, laytrop, T);
-  gas_optics_band<4>(s, nl, laytrop, T);
-  gas_optics_band<5>(s, nl, laytrop, T);
-  gas_optics_band<6>(s, nl, laytrop, T);
-  gas_optics_band<7>(s, nl, laytrop, T);
-  gas_optics_band<8>(s, nl, laytrop, T);
-  gas_optics_band<9>(s, nl, laytrop, T);
-  gas_optics_band<10>(s, nl, laytrop, T);
-  gas_optics_band<11>(s, nl, laytrop, T);
-  gas_optics_band<12>(s, nl, laytrop, T);
-  gas_optics_band<13>(s, nl, laytrop, T);
-  gas_optics_band<14>(s, nl, laytrop, T);
-  gas_optics_band<15>(s, nl, laytrop, T);
-  gas_optics_band<16>(s, nl, laytrop, T);
-  if (a.dbg_taut) {
-    for (int c = tid; c < nl * GB_NGPT; c += NT) {
-      int lay = c / GB_NGPT, g = c - lay * GB_NGPT;
-      int b = c_T.ngb[g] - 1;
-      FracRec r = s.frec[lay * 16 + b];
-      const float* p = T + r.off + (g - c_T.band[b].g0);
-      a.dbg_taut[(icol * nl + lay) * GB_NGPT + g] = s.taut[c];
-      a.dbg_fracs[(icol * nl + lay) * GB_NGPT + g] = p[0] + r.fpl * (p[c_T.band[b].ng] - p[0]);
-    }
-  }
-
-  // ---------------- phase 3: transfer, one thread per g-point
-  const int warp = tid >> 5, lane = tid & 31;
-  const bool active = tid < GB_NGPT;
-  const int g = active ? tid : GB_NGPT - 1;
-  const int band = c_T.ngb[g] - 1;
-  const int ng = c_T.band[band].ng, gi = g - c_T.band[band].g0;
-  const float secdiff = s.misc[band];
-  const float wgt = active ? (float)(0.5 * (double)c_T.delwave[band] * c_T.fluxfac) : 0.0f;
-  const bool idrv = a.idrv == 1;
-  const bool clouds = a.icld >= 1;
-  auto frac = [&](int lay) {
-    FracRec r = s.frec[lay * 16 + band];
-    const float* p = T + r.off + gi;
-    float f0 = __ldg(p);
-    return f0 + r.fpl * (__ldg(p + ng) - f0);
-  };
-  float* part = s.part;  // [NWARP][nl+1][6]
-  auto emit = [&](int lev, int k, float v) {
-    float sum = warp_sum(v * wgt);
-    if (lane == 0) part[(warp * (nl + 1) + lev) * 6 + k] = sum;
-  };
-  // downward sweep (rtrnmc.f90:347-455)
-  float radld = 0.0f, radclrd = 0.0f;
-  bool iclddn = false;
-  for (int lev = nl; lev >= 1; --lev) {
-    const int L = lev - 1;  // 0-based layer
-    float plfrac = frac(L);
-    float blay = s.plk_lay[L * 16 + band];
-    float dplankup = s.plk_lev[lev * 16 + band] - blay;
-    float dplankdn = s.plk_lev[(lev - 1) * 16 + band] - blay;
-    float odepth = fmaxf(secdiff * s.taut[L * GB_NGPT + g], 0.0f);
-    bool cl = clouds && s.cldlay[L];
-    if (cl) {
-      iclddn = true;
-      float odcld, efcl;
-      float cldf = cell_cloud(a, icol, g, L, secdiff, band, T, odcld, efcl);
-      efcl *= (cldf == 1.0f ? cldf : 0.0f);
-      CellRT r = cell_rt(true, odepth, odcld, plfrac, blay, dplankup, dplankdn);
-      radld = radld - radld * (r.atrans + efcl * (1.0f - r.atrans)) + r.gassrc + cldf * (r.bbdtot * r.atot - r.gassrc);
-      radclrd = radclrd + (r.bbd - radclrd) * r.atrans;
-    } else {
-      CellRT r = cell_rt(false, odepth, 0.0f, plfrac, blay, dplankup, dplankdn);
-      radld = radld + (r.bbd - radld) * r.atrans;
-      if (iclddn) radclrd = radclrd + (r.bbd - radclrd) * r.atrans;
-      else radclrd = radld;
-    }
-    emit(lev - 1, 0, radld);
-    emit(lev - 1, 1, radclrd);
-  }
-  // surface (rtrnmc.f90:465-485)
-  float plfrac1 = frac(0);
-  float rad0 = plfrac1 * s.misc[16 + band];
-  float d_rad0 = plfrac1 * s.misc[32 + band];
-  float reflect = 1.0f - s.misc[48 + band];
-  float radlu = rad0 + reflect * radld;
-  float radclru = rad0 + reflect * radclrd;
-  float d_radlu = d_rad0, d_radclru = d_rad0;
-  emit(0, 2, radlu);
-  emit(0, 3, radclru);
-  if (idrv) {
-    emit(0, 4, d_radlu);
-    emit(0, 5, d_radclru);
-  }
-  // upward sweep (rtrnmc.f90:486-529)
-  for (int lev = 1; lev <= nl; ++lev) {
-    const int L = lev - 1;
-    float plfrac = frac(L);
-    float blay = s.plk_lay[L * 16 + band];
-    float dplankup = s.plk_lev[lev * 16 + band] - blay;
-    float dplankdn = s.plk_lev[(lev - 1) * 16 + band] - blay;
-    float odepth = fmaxf(secdiff * s.taut[L * GB_NGPT + g], 0.0f);
-    bool cl = clouds && s.cldlay[L];
-    if (cl) {
-      float odcld, efcl;
-      float cldf = cell_cloud(a, icol, g, L, secdiff, band, T, odcld, efcl);
-      efcl *= (cldf == 1.0f ? cldf : 0.0f);
-      CellRT r = cell_rt(true, odepth, odcld, plfrac, blay, dplankup, dplankdn);
-      float gassrc = r.bbugas * r.atrans;
-      radlu = radlu - radlu * (r.atrans + efcl * (1.0f - r.atrans)) + gassrc + cldf * (r.bbutot * r.atot - gassrc);
-      d_radlu = d_radlu * cldf * (1.0f - r.atot) + d_radlu * (1.0f - cldf) * (1.0f - r.atrans);
-      radclru = radclru + (r.bbugas - radclru) * r.atrans;
-      d_radclru = d_radclru * (1.0f - r.atrans);
-    } else {
-      CellRT r = cell_rt(false, odepth, 0.0f, plfrac, blay, dplankup, dplankdn);
-      radlu = radlu + (r.bbugas - radlu) * r.atrans;
-      d_radlu = d_radlu * (1.0f - r.atrans);
-      if (iclddn) {
-        radclru = radclru + (r.bbugas - radclru) * r.atrans;
-        d_radclru = d_radclru * (1.0f - r.atrans);
-      } else {
-        radclru = radlu;
-        d_radclru = d_radlu;
+    int anybad = __syncthreads_or(my_bad);
+    const int laytrop = s.iscal[0];
+    if (tid < 32) {
+      if (tid == 0) {
+        int err = s.iscal[2];
+        // sum of 1-based indices of lower layers equals laytrop*(laytrop+1)/2 iff they form a prefix
+        if (s.iscal[1] != laytrop * (laytrop + 1) / 2) err = GB_COL_LAYTROP;
+        if (anybad) err = GB_COL_BADVAL;
+        s.iscal[3] = err;
+        if (err) {
+          if (a.col_err) a.col_err[icol] = err;
+          atomicMax(a.err_flag, err);
+        } else if (a.col_err) {
+          a.col_err[icol] = 0;
+        }
+      }
+      // pwvcm (inatm :859-870; a fixed-order warp sum over layers) and
+      // secdiff (rtrnmc.f90:258-266), one band per lane
+      float amttl = 0.0f, wvttl = 0.0f;
+      for (int l = tid; l < nl; l += 32) {
+        const float wk1 = s.f[F_COLH2O * nl + l] * 1.e20f;
+        amttl += s.f[F_COLDRY * nl + l] + wk1;
+        wvttl += wk1;
+      }
+      amttl = __shfl_sync(0xffffffffu, warp_sum(amttl), 0);
+      wvttl = __shfl_sync(0xffffffffu, warp_sum(wvttl), 0);
+      if (tid < 16) {
+        const int ib = tid;
+        const float wvsh = (amw * wvttl) / (amd * amttl);
+        const float pz0 = (float)in2(a.plev, a.ld, icol, 0);
+        const float pwvcm = wvsh * (1.e3f * pz0) / (1.e2f * (float)c_T.grav);
+        float sd = 1.66f;
+        if (!(ib == 0 || ib == 3 || ib >= 9)) {
+          sd = c_a0[ib] + c_a1[ib] * __expf(c_a2[ib] * pwvcm);
+          sd = fminf(fmaxf(sd, 1.50f), 1.80f);
+        }
+        s.misc[ib] = sd;
       }
     }
-    emit(lev, 2, radlu);
-    emit(lev, 3, radclru);
-    if (idrv) {
-      emit(lev, 4, d_radlu);
-      emit(lev, 5, d_radclru);
+    __syncthreads();
+    // ---------------- phase 2: gas optics and cell coefficients, band by band
+    for (int gr = 0; gr < NGROUP; ++gr) {
+      group_prologues<NT>(gr, s, nl, laytrop);
+      __syncthreads();
+      group_cells<NT>(gr, a, s, nl, laytrop, T, icol, scr);
+      __syncthreads();
     }
-  }
-  __syncthreads();
 
-  // ---------------- phase 4: fp64 sums, net fluxes, heating rates, stores
-  const long long ldo = a.ldo;
-  for (int lev = tid; lev <= nl; lev += NT) {
-    double acc[6] = {0, 0, 0, 0, 0, 0};
-    for (int w = 0; w < NWARP; ++w)
-      for (int k = 0; k < 6; ++k) acc[k] += (double)part[(w * (nl + 1) + lev) * 6 + k];
-    if (lev == nl) acc[0] = acc[1] = 0.0;  // no downward radiation at the model top
-    long long o = icol + ldo * lev;
-    a.uflx[o] = acc[2];
-    a.dflx[o] = acc[0];
-    a.uflxc[o] = acc[3];
-    a.dflxc[o] = acc[1];
-    if (idrv) {
-      a.duflx_dt[o] = acc[4];
-      a.duflxc_dt[o] = acc[5];
+    // ---------------- phase 3: sweeps, one thread per g-point
+    if (tid < NSW * 32) {
+      const int warp = tid >> 5, lane = tid & 31;
+      const bool active = tid < GB_NGPT;
+      const int g = active ? tid : GB_NGPT - 1;
+      const int band = c_T.ngb[g] - 1;
+      const float wgt = active ? (float)(0.5 * (double)c_T.delwave[band] * c_T.fluxfac) : 0.0f;
+      const bool idrv = a.idrv == 1;
+      const bool clouds = a.icld >= 1;
+      float* part = s.part + warp * (nl + 1) * 6;  // this warp's [nl+1][6] partial sums
+      auto emit = [&](int lev, int k, float v) {
+        const float sum = warp_sum(v * wgt);
+        if (lane == 0) part[lev * 6 + k] = sum;
+      };
+      // downward (rtrnmc.f90:347-455): total stream and clear-sky stream
+      float radld = 0.0f, radclrd = 0.0f;
+      float4 cnext = scr[(nl - 1) * GB_NGPT + g];
+      for (int L = nl - 1; L >= 0; --L) {
+        const float4 c = cnext;
+        if (L > 0) cnext = scr[(L - 1) * GB_NGPT + g];
+        if (clouds && s.cldlay[L] && cell_is_cloudy(s, L, g)) {
+          const float4 k = scr[(nl + L) * GB_NGPT + g];
+          radld = fmaf(radld, k.x, k.y);
+        } else {
+          radld = fmaf(radld, c.x, c.y);
+        }
+        radclrd = fmaf(radclrd, c.x, c.y);
+        emit(L, 0, radld);
+        emit(L, 1, radclrd);
+      }
+      // surface emission and reflection (rtrnmc.f90:465-485)
+      const float plfrac1 = s.frac1[g];
+      const float rad0 = plfrac1 * s.misc[16 + band];
+      const float reflect = 1.0f - s.misc[48 + band];
+      float radlu = rad0 + reflect * radld;
+      float radclru = rad0 + reflect * radclrd;
+      float d_radlu = plfrac1 * s.misc[32 + band], d_radclru = d_radlu;
+      emit(0, 2, radlu);
+      emit(0, 3, radclru);
+      if (idrv) {
+        emit(0, 4, d_radlu);
+        emit(0, 5, d_radclru);
+      }
+      // upward (rtrnmc.f90:486-529)
+      cnext = scr[g];
+      for (int L = 0; L < nl; ++L) {
+        const float4 c = cnext;
+        if (L + 1 < nl) cnext = scr[(L + 1) * GB_NGPT + g];
+        if (clouds && s.cldlay[L] && cell_is_cloudy(s, L, g)) {
+          const float4 k = scr[(nl + L) * GB_NGPT + g];
+          radlu = fmaf(radlu, k.x, k.z);
+          d_radlu *= k.w;
+        } else {
+          radlu = fmaf(radlu, c.x, c.z);
+          d_radlu *= c.x;
+        }
+        radclru = fmaf(radclru, c.x, c.z);
+        d_radclru *= c.x;
+        emit(L + 1, 2, radlu);
+        emit(L + 1, 3, radclru);
+        if (idrv) {
+          emit(L + 1, 4, d_radlu);
+          emit(L + 1, 5, d_radclru);
+        }
+      }
     }
-    s.fnet[lev * 2 + 0] = acc[2] - acc[0];
-    s.fnet[lev * 2 + 1] = acc[3] - acc[1];
-  }
-  __syncthreads();
-  for (int l = tid; l < nl; l += NT) {
-    double dp = in2(a.plev, a.ld, icol, l) - in2(a.plev, a.ld, icol, l + 1);
-    long long o = icol + ldo * l;
-    a.hr[o] = c_T.heatfac * (s.fnet[l * 2] - s.fnet[(l + 1) * 2]) / dp;
-    a.hrc[o] = c_T.heatfac * (s.fnet[l * 2 + 1] - s.fnet[(l + 1) * 2 + 1]) / dp;
+    __syncthreads();
+
+    // ---------------- phase 4: fp64 sums, net fluxes, heating rates, stores
+    {
+      const long long ldo = a.ldo;
+      const bool idrv = a.idrv == 1;
+      for (int lev = tid; lev <= nl; lev += NT) {
+        double acc[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+        for (int w = 0; w < NSW; ++w)
+#pragma unroll
+          for (int k = 0; k < 6; ++k) acc[k] += (double)s.part[(w * (nl + 1) + lev) * 6 + k];
+        if (lev == nl) acc[0] = acc[1] = 0.0;  // no downward radiation at the model top
+        long long o = icol + ldo * lev;
+        a.uflx[o] = acc[2];
+        a.dflx[o] = acc[0];
+        a.uflxc[o] = acc[3];
+        a.dflxc[o] = acc[1];
+        if (idrv) {
+          a.duflx_dt[o] = acc[4];
+          a.duflxc_dt[o] = acc[5];
+        }
+        s.fnet[lev * 2 + 0] = acc[2] - acc[0];
+        s.fnet[lev * 2 + 1] = acc[3] - acc[1];
+      }
+      __syncthreads();
+      for (int l = tid; l < nl; l += NT) {
+        double dp = in2(a.plev, a.ld, icol, l) - in2(a.plev, a.ld, icol, l + 1);
+        long long o = icol + ldo * l;
+        a.hr[o] = c_T.heatfac * (s.fnet[l * 2] - s.fnet[(l + 1) * 2]) / dp;
+        a.hrc[o] = c_T.heatfac * (s.fnet[l * 2 + 1] - s.fnet[(l + 1) * 2 + 1]) / dp;
+      }
+      __syncthreads();
+    }
   }
 }
+
+// ------------------------------------------------------------------ the kernel
+// Persistent blocks walk the batch columns grid after grid; a block's columns
+// increase, so its grid index only moves forward.
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) lw_batch_kernel(const __grid_constant__ LwBatch B,
+                                                             const float* __restrict__ T) {
+  extern __shared__ __align__(16) char smem_raw[];
+  float4* __restrict__ scr = B.scratch + (size_t)blockIdx.x * ((size_t)2 * B.nsmax * GB_NGPT);
+  const long long total = B.col0[B.ngrid];
+  int gi = 0;
+  for (long long gc = blockIdx.x; gc < total; gc += gridDim.x) {
+    while (gc >= B.col0[gi + 1]) ++gi;
+    solve_column<NT>(B.g[gi], gc - B.col0[gi], smem_raw, scr, T);
+  }
+}
+
+// compiled shapes (threads per column, min blocks per SM); variant 0 is the default
+#define GB_LW_VARIANTS(X) X(0, 160, 6) X(1, 160, 4) X(2, 256, 4) X(3, 256, 3)
 
 }  // namespace gb
 
 // ------------------------------------------------------------------ host side
-size_t gb_lw_smem_bytes(int nlay) { return gb::smem_bytes(nlay); }
+namespace {
 
-cudaError_t gb_lw_set_tables(const GbTables& T) {
-  return cudaMemcpyToSymbol(gb::c_T, &T, sizeof(GbTables));
+struct VariantInfo {
+  int threads, min_blocks;
+  const void* fn;
+  cudaError_t (*launch)(const LwBatch&, const float*, int, size_t, cudaStream_t);
+};
+
+template <int NT, int MINB>
+cudaError_t launch_variant(const LwBatch& b, const float* T, int nblocks, size_t smem, cudaStream_t st) {
+  gb::lw_batch_kernel<NT, MINB><<<nblocks, NT, smem, st>>>(b, T);
+  return cudaGetLastError();
 }
 
-cudaError_t gb_lw_launch(const LwArgs& a, const float* d_tables, cudaStream_t stream) {
+#define GB_LW_VARIANT_ENTRY(i, nt, mb) {nt, mb, (const void*)gb::lw_batch_kernel<nt, mb>, launch_variant<nt, mb>},
+const VariantInfo kVariants[] = {GB_LW_VARIANTS(GB_LW_VARIANT_ENTRY)};
+constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+
+cudaError_t configure(int nlay, int variant, int* blocks_per_sm) {
+  const VariantInfo& v = kVariants[variant];
+  const size_t sm = gb::smem_bytes(nlay);
+  cudaError_t e = cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, v.fn, v.threads, sm);
+}
+
+}  // namespace
+
+int gb_lw_num_variants() { return kNumVariants; }
+
+LwVariant gb_lw_variant(int v) {
+  if (v < 0 || v >= kNumVariants) return LwVariant{0, 0};
+  return LwVariant{kVariants[v].threads, kVariants[v].min_blocks};
+}
+
+size_t gb_lw_smem_bytes(int nlay, int) { return gb::smem_bytes(nlay); }
+
+cudaError_t gb_lw_set_tables(const GbTables& T) { return cudaMemcpyToSymbol(gb::c_T, &T, sizeof(GbTables)); }
+
+int gb_lw_slots(int nlay, int variant) {
+  if (variant < 0 || variant >= kNumVariants) variant = 0;
+  int dev = 0, nsm = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (configure(nlay, variant, &per) != cudaSuccess || per < 1) per = 1;
+  return nsm * per;
+}
+
+size_t gb_lw_scratch_bytes(int nlay, int slots) { return (size_t)slots * 2 * nlay * GB_NGPT * sizeof(float4); }
+
+cudaError_t gb_lw_launch_batch(const LwBatch& b, const float* d_tables, int variant, int nblocks,
+                               cudaStream_t stream) {
+  if (variant < 0 || variant >= kNumVariants || b.ngrid < 1 || b.ngrid > GB_LW_MAX_GRIDS) return cudaErrorInvalidValue;
+  if (b.col0[b.ngrid] <= 0 || nblocks <= 0) return cudaSuccess;
+  int per = 0;
+  cudaError_t e = configure(b.nsmax, variant, &per);
+  if (e != cudaSuccess) return e;
+  if ((long long)nblocks > b.col0[b.ngrid]) nblocks = (int)b.col0[b.ngrid];
+  return kVariants[variant].launch(b, d_tables, nblocks, gb::smem_bytes(b.nsmax), stream);
+}
+
+cudaError_t gb_lw_launch(const LwArgs& a, const float* d_tables, float4* scratch, int nslots, cudaStream_t stream) {
   if (a.ncol <= 0) return cudaSuccess;
-  size_t sm = gb::smem_bytes(a.nlay);
-  static int configured_bytes = -1;
-  if ((int)sm > configured_bytes) {
-    cudaError_t e = cudaFuncSetAttribute(gb::lw_column_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    configured_bytes = (int)sm;
-  }
-  gb::lw_column_kernel<<<a.ncol, gb::NT, sm, stream>>>(a, d_tables);
-  return cudaGetLastError();
+  LwBatch b;
+  b.ngrid = 1;
+  b.nsmax = a.nlay;
+  b.col0[0] = 0;
+  b.col0[1] = a.ncol;
+  b.scratch = scratch;
+  b.g[0] = a;
+  return gb_lw_launch_batch(b, d_tables, 0, a.ncol < nslots ? a.ncol : nslots, stream);
 }

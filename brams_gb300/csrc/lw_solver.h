@@ -5,17 +5,29 @@
 
 #include "lw_common.h"
 
+// Where a grid's McICA sub-column clouds come from.
+enum LwCloudMode {
+  LW_CLOUD_SUBCOL = 0,  // caller-supplied (140, ld, nlay) arrays cldfmcl/ciwpmcl/clwpmcl/taucmcl
+  LW_CLOUD_FUSED = 1,   // generated inside the kernel from layer clouds (icld 3, Mersenne twister,
+                        // column c seeded with seed0 + c), as mcica_subcol_lw would for one column
+};
+
 // Device pointers in the reference's Fortran layout.  (ncol, .) arrays have
 // leading dimension ld (>= ncol); McICA arrays are (140, ld, nlay); tauaer is
-// (ld, nlay, 16); outputs (ldo, nlay+1) / (ldo, nlay).
+// (ld, nlay, 16); outputs (ldo, nlay+1) / (ldo, nlay).  In LW_CLOUD_FUSED mode
+// cldfrac/ciwp/clwp are (ld, nlay), tauc is (16, ld, nlay) and reicmcl/relqmcl
+// hold the layer radii rei/rel.
 struct LwArgs {
   int ncol, nlay;
   long long ld, ldo;
   int icld, idrv, inflag, iceflag, liqflag;
+  int cloud_mode;
+  unsigned seed0;
   const double *play, *plev, *tlay, *tlev, *tsfc;
   const double *h2ovmr, *o3vmr, *co2vmr, *ch4vmr, *n2ovmr, *o2vmr;
   const double *cfc11vmr, *cfc12vmr, *cfc22vmr, *ccl4vmr, *emis;
   const double *cldfmcl, *taucmcl, *ciwpmcl, *clwpmcl, *reicmcl, *relqmcl, *tauaer;
+  const double *cldfrac, *ciwp, *clwp, *tauc;
   double *uflx, *dflx, *hr, *uflxc, *dflxc, *hrc, *duflx_dt, *duflxc_dt;
   int* col_err;   // optional per-column status (ncol)
   int* err_flag;  // required: max status over the launch
@@ -23,6 +35,34 @@ struct LwArgs {
   float* dbg_fracs;  // (ncol, nlay, 140) with g fastest; NULL in production calls
 };
 
-size_t gb_lw_smem_bytes(int nlay);
+// Grids of one launch: grid i owns batch columns col0[i] .. col0[i+1]-1.  The
+// kernel takes this by value (kernel parameter space), so the launch carries
+// no device-side descriptor and can be captured in a CUDA graph as is.
+#define GB_LW_MAX_GRIDS 32
+struct LwBatch {
+  int ngrid;
+  int nsmax;                              // largest nlay (scratch-slot stride)
+  long long col0[GB_LW_MAX_GRIDS + 1];
+  float4* scratch;                        // >= gridDim.x slots of 2*nsmax*140 float4
+  LwArgs g[GB_LW_MAX_GRIDS];
+};
+
+// Compiled shapes of the column kernel: threads per column block and the
+// minimum resident blocks per SM the register allocation is sized for.
+struct LwVariant {
+  int threads, min_blocks;
+};
+int gb_lw_num_variants();
+LwVariant gb_lw_variant(int v);
+
+size_t gb_lw_smem_bytes(int nlay, int variant = 0);
+// thread blocks of `variant` that fit on the device at once for this nlay
+int gb_lw_slots(int nlay, int variant = 0);
+// bytes of scratch for `slots` slots: per slot 2*nlay*140 float4 (clear and cloudy cell coefficients)
+size_t gb_lw_scratch_bytes(int nlay, int slots);
 cudaError_t gb_lw_set_tables(const GbTables& T);
-cudaError_t gb_lw_launch(const LwArgs& a, const float* d_tables, cudaStream_t stream);
+// One grid, default variant, grid = min(ncol, nslots) blocks.
+cudaError_t gb_lw_launch(const LwArgs& a, const float* d_tables, float4* scratch, int nslots, cudaStream_t stream);
+// All grids of `b` in one launch of `nblocks` persistent blocks of `variant`.
+cudaError_t gb_lw_launch_batch(const LwBatch& b, const float* d_tables, int variant, int nblocks,
+                               cudaStream_t stream);

@@ -35,8 +35,57 @@ EXPORTS = [
     "gb_rrtmg_lw_ini", "gb_rrtmg_lw_free", "gb_rrtmg_lw", "gb_rrtmg_lw_device",
     "gb_rrtmg_lw_sync_status", "gb_mcica_subcol_lw", "gb_mcica_subcol_lw_device",
     "gb_rrtmg_lw_strerror", "gb_rrtmg_lw_last_error", "gb_rrtmg_lw_gas_optics_diag",
-    "gb_mcica_subcol_lw_noalloc",
+    "gb_mcica_subcol_lw_noalloc", "gb_rrtmg_lw_batch_device", "gb_rrtmg_lw_autotune",
+    "gb_rrtmg_lw_tuning_get", "gb_rrtmg_lw_batch_graph_create", "gb_rrtmg_lw_graph_launch",
+    "gb_rrtmg_lw_graph_destroy", "gb_rrtmg_lw_tuning_set", "gb_rrtmg_lw_num_variants",
 ]
+
+CLOUD_SUBCOL, CLOUD_FUSED = 0, 1
+MAX_GRIDS = 32
+
+_GRID_PTRS = ["play", "plev", "tlay", "tlev", "tsfc", "h2ovmr", "o3vmr", "co2vmr", "ch4vmr", "n2ovmr",
+              "o2vmr", "cfc11vmr", "cfc12vmr", "cfc22vmr", "ccl4vmr", "emis", "tauaer",
+              "cldfmcl", "taucmcl", "ciwpmcl", "clwpmcl", "cldfrac", "ciwp", "clwp", "tauc",
+              "reicmcl", "relqmcl", "uflx", "dflx", "hr", "uflxc", "dflxc", "hrc", "duflx_dt", "duflxc_dt",
+              "d_col_status"]
+
+
+class GridDesc(C.Structure):
+    """gb_lw_grid: one grid of a batched call (device arrays, Fortran layouts)."""
+    _fields_ = ([(k, C.c_int) for k in ("ncol", "nlay", "icld", "idrv", "inflglw", "iceflglw", "liqflglw",
+                                        "cloud_mode")]
+                + [("seed0", C.c_uint32), ("ld_in", C.c_int64), ("ld_out", C.c_int64)]
+                + [(k, C.c_void_p) for k in _GRID_PTRS])
+
+
+class Tuning(C.Structure):
+    """gb_lw_tuning: launch shape of the batched kernel."""
+    _fields_ = [(k, C.c_int) for k in ("variant", "threads", "min_blocks", "blocks_per_sm", "blocks")] + \
+        [("ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def grid_desc(ncol: int, nlay: int, arrays: dict, icld: int = 3, idrv: int = 1, inflglw: int = 2,
+              iceflglw: int = 3, liqflglw: int = 1, cloud_mode: int = CLOUD_SUBCOL, seed0: int = 0,
+              ld_in: int | None = None, ld_out: int | None = None) -> GridDesc:
+    """Descriptor of one grid from device arrays (torch tensors or raw pointers) keyed by argument name.
+    In CLOUD_FUSED mode the layer radii go under "reicmcl"/"relqmcl" (or "rei"/"rel")."""
+    g = GridDesc()
+    g.ncol, g.nlay, g.icld, g.idrv = ncol, nlay, icld, idrv
+    g.inflglw, g.iceflglw, g.liqflglw, g.cloud_mode = inflglw, iceflglw, liqflglw, cloud_mode
+    g.seed0 = seed0 & 0xFFFFFFFF
+    g.ld_in = ld_in or ncol
+    g.ld_out = ld_out or ncol
+    alias = {"reicmcl": "rei", "relqmcl": "rel"}
+    for k in _GRID_PTRS:
+        a = arrays.get(k)
+        if a is None and k in alias:
+            a = arrays.get(alias[k])
+        p = _ptr(a)
+        setattr(g, k, p.value if p is not None else None)
+    return g
 
 
 class RrtmgLwError(RuntimeError):
@@ -69,6 +118,15 @@ def load_library(path: str = LIB_PATH):
         L.gb_mcica_subcol_lw_device.argtypes = [P, P, I, I, I, I, IP] + [P] * 8 + [P] * 6 + [LL, I]
         L.gb_rrtmg_lw_gas_optics_diag.argtypes = [P, I, I] + [P] * 17 + [P, P]
         L.gb_mcica_subcol_lw_noalloc.argtypes = [P, I, I, I, I, IP] + [P] * 8 + [P] * 6 + [LL, I, P]
+        GP = C.POINTER(GridDesc)
+        L.gb_rrtmg_lw_batch_device.argtypes = [P, P, I, GP]
+        L.gb_rrtmg_lw_autotune.argtypes = [P, P, I, GP, I, I, C.POINTER(Tuning)]
+        L.gb_rrtmg_lw_tuning_get.argtypes = [P, I, C.POINTER(Tuning)]
+        L.gb_rrtmg_lw_batch_graph_create.argtypes = [P, I, GP, C.POINTER(P)]
+        L.gb_rrtmg_lw_graph_launch.argtypes = [P, P]
+        L.gb_rrtmg_lw_graph_destroy.argtypes = [P]
+        L.gb_rrtmg_lw_tuning_set.argtypes = [P, I, C.POINTER(Tuning)]
+        L.gb_rrtmg_lw_num_variants.argtypes = []
         L.gb_rrtmg_lw_strerror.restype = C.c_char_p
         L.gb_rrtmg_lw_strerror.argtypes = [I]
         L.gb_rrtmg_lw_last_error.restype = C.c_char_p
@@ -198,3 +256,63 @@ class Context:
             *[_ptr(ptrs[k]) for k in ("cldfmcl", "ciwpmcl", "clwpmcl", "reicmcl", "relqmcl", "taucmcl")],
             ld or ncol, 1 if seed_per_column else 0)
         _check(self.L, self.h, rc)
+
+    # ------------------------------------------------------------ batched grids
+    @staticmethod
+    def _grids(grids) -> tuple:
+        n = len(grids)
+        if not 1 <= n <= MAX_GRIDS:
+            raise ValueError(f"1..{MAX_GRIDS} grids per batch, got {n}")
+        arr = (GridDesc * n)(*grids)
+        return n, arr
+
+    def rrtmg_lw_batch_device(self, grids, stream=None) -> None:
+        """All grids (GridDesc list) in one persistent launch on `stream`."""
+        n, arr = self._grids(grids)
+        _check(self.L, self.h, self.L.gb_rrtmg_lw_batch_device(self.h, _ptr(stream or 0), n, arr))
+
+    def autotune(self, grids, sample_cols: int = 0, reps: int = 3, stream=None) -> dict:
+        """Time every kernel variant and grid size on a sample of the batch; keeps and returns the best."""
+        n, arr = self._grids(grids)
+        t = Tuning()
+        _check(self.L, self.h, self.L.gb_rrtmg_lw_autotune(self.h, _ptr(stream or 0), n, arr, sample_cols, reps,
+                                                           C.byref(t)))
+        return t.as_dict()
+
+    def tuning(self, nlay: int) -> dict:
+        t = Tuning()
+        _check(self.L, self.h, self.L.gb_rrtmg_lw_tuning_get(self.h, nlay, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, nlay: int, variant: int, blocks_per_sm: int) -> None:
+        t = Tuning(variant, 0, 0, blocks_per_sm, 0, 0.0)
+        _check(self.L, self.h, self.L.gb_rrtmg_lw_tuning_set(self.h, nlay, C.byref(t)))
+
+    def num_variants(self) -> int:
+        return self.L.gb_rrtmg_lw_num_variants()
+
+    def batch_graph(self, grids) -> "BatchGraph":
+        """CUDA graph of one batched launch (inputs updated in place between replays)."""
+        n, arr = self._grids(grids)
+        h = C.c_void_p()
+        _check(self.L, self.h, self.L.gb_rrtmg_lw_batch_graph_create(self.h, n, arr, C.byref(h)))
+        return BatchGraph(self, h)
+
+
+class BatchGraph:
+    def __init__(self, ctx: Context, h):
+        self.ctx, self.h = ctx, h
+
+    def launch(self, stream=None) -> None:
+        _check(self.ctx.L, self.ctx.h, self.ctx.L.gb_rrtmg_lw_graph_launch(self.h, _ptr(stream or 0)))
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.ctx.L.gb_rrtmg_lw_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -171,6 +171,80 @@ int gb_mcica_subcol_lw_noalloc(void* stream, int ncol, int nlay, int icld, int p
                                double* reicmcl, double* relqmcl, double* taucmcl, int64_t ld,
                                int seed_per_column, int* d_status);
 
+/* ---------------------------------------------------------------------------
+ * Batched calls (no counterpart in the reference, which BRAMS calls once per
+ * grid and MPI rank, rtm_driver.f90:1313): several grids -- nested grids,
+ * ensemble members -- with their own column and layer counts are solved in
+ * ONE persistent kernel launch.  Each grid is described by device arrays in
+ * the layouts of gb_rrtmg_lw_device.
+ *
+ * cloud_mode GB_LW_CLOUD_SUBCOL: McICA sub-column arrays as for
+ *   gb_rrtmg_lw_device (cldfmcl, taucmcl, ciwpmcl, clwpmcl, reicmcl,
+ *   relqmcl).
+ * cloud_mode GB_LW_CLOUD_FUSED: the kernel generates the sub-columns itself
+ *   from layer clouds, exactly as gb_mcica_subcol_lw with icld 3, irng 1 and
+ *   seed_per_column 1 (column c seeded seed0 + c) followed by rrtmg_lw would:
+ *   cldfrac ciwp clwp (ld, nlay), tauc (16, ld, nlay), and reicmcl/relqmcl
+ *   carry the layer radii rei/rel (ld, nlay).  Requires icld 0 or 3.  The
+ *   (140, ncol, nlay) arrays are never formed.
+ */
+#define GB_LW_CLOUD_SUBCOL 0
+#define GB_LW_CLOUD_FUSED 1
+#define GB_LW_MAX_GRIDS 32
+
+typedef struct gb_lw_grid {
+  int ncol, nlay, icld, idrv, inflglw, iceflglw, liqflglw;
+  int cloud_mode;
+  uint32_t seed0;
+  int64_t ld_in, ld_out;
+  const double *play, *plev, *tlay, *tlev, *tsfc, *h2ovmr, *o3vmr, *co2vmr, *ch4vmr, *n2ovmr,
+      *o2vmr, *cfc11vmr, *cfc12vmr, *cfc22vmr, *ccl4vmr, *emis, *tauaer;
+  const double *cldfmcl, *taucmcl, *ciwpmcl, *clwpmcl;   /* GB_LW_CLOUD_SUBCOL */
+  const double *cldfrac, *ciwp, *clwp, *tauc;            /* GB_LW_CLOUD_FUSED  */
+  const double *reicmcl, *relqmcl;
+  double *uflx, *dflx, *hr, *uflxc, *dflxc, *hrc, *duflx_dt, *duflxc_dt;
+  int* d_col_status; /* optional, ncol ints */
+} gb_lw_grid;
+
+/* Launch shape of the batched kernel: compiled variant (threads per column
+ * block, register budget) and resident blocks per SM of the persistent grid. */
+typedef struct gb_lw_tuning {
+  int variant, threads, min_blocks, blocks_per_sm, blocks;
+  double ms; /* measured time of the tuned shape on the sample batch (autotune only) */
+} gb_lw_tuning;
+
+/* All grids in one launch on `stream` (ngrid <= GB_LW_MAX_GRIDS), with the
+ * shape the context's autotuner chose for this batch (largest nlay), or the
+ * default shape.  Same status handling as gb_rrtmg_lw_device. */
+int gb_rrtmg_lw_batch_device(gb_lw_context* ctx, void* stream, int ngrid, const gb_lw_grid* grids);
+
+/* Times every compiled variant and persistent-grid size on a sample of the
+ * batch (each grid cut to the same fraction of its columns, about
+ * sample_cols columns in all; <= 0 for the whole batch), `reps` launches
+ * each after a warm-up, keeps the fastest for batches with this largest
+ * nlay and returns it in *best.  Overwrites the outputs of the sampled
+ * columns. */
+int gb_rrtmg_lw_autotune(gb_lw_context* ctx, void* stream, int ngrid, const gb_lw_grid* grids,
+                         int sample_cols, int reps, gb_lw_tuning* best);
+
+/* The shape gb_rrtmg_lw_batch_device would use for a batch whose largest
+ * layer count is nlay; _set pins one (e.g. a shape tuned in an earlier run:
+ * variant and blocks_per_sm are used, the other fields are derived). */
+int gb_rrtmg_lw_tuning_get(gb_lw_context* ctx, int nlay, gb_lw_tuning* out);
+int gb_rrtmg_lw_tuning_set(gb_lw_context* ctx, int nlay, const gb_lw_tuning* shape);
+/* Number of compiled kernel variants (valid gb_lw_tuning.variant values). */
+int gb_rrtmg_lw_num_variants(void);
+
+/* CUDA graph of one batched launch: the descriptor and a scratch area owned
+ * by the graph are fixed at creation, so the caller updates the input arrays
+ * in place between replays (a time-stepping model's resident state).  The
+ * graph holds the single persistent kernel. */
+typedef struct gb_lw_graph gb_lw_graph;
+int gb_rrtmg_lw_batch_graph_create(gb_lw_context* ctx, int ngrid, const gb_lw_grid* grids,
+                                   gb_lw_graph** graph);
+int gb_rrtmg_lw_graph_launch(gb_lw_graph* graph, void* stream);
+int gb_rrtmg_lw_graph_destroy(gb_lw_graph* graph);
+
 /* Human-readable text of a status code (static storage). */
 const char* gb_rrtmg_lw_strerror(int code);
 /* Detail of the last failing call on this context (CUDA error text etc.). */
