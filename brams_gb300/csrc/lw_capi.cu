@@ -20,53 +20,28 @@
 #include "lw_mcica.h"
 #include "lw_solver.h"
 #include "lw_tables.h"
+#include "lw_context.h"
 
 #include <dlfcn.h>
 
-struct ChunkBufs {
-  double* in = nullptr;   // all inputs of one chunk, packed
-  double* out = nullptr;  // all outputs of one chunk, packed
-  size_t in_elems = 0, out_elems = 0;
-};
-
-struct gb_lw_context {
-  int device = 0;
-  GbTables tabs;
-  float* d_tables = nullptr;
-  int* d_err = nullptr;      // max status of device calls
-  int* d_err_host = nullptr; // status of the current host call
-  cudaStream_t streams[2] = {nullptr, nullptr};
-  ChunkBufs bufs[2];
-  int chunk_cols = 0, chunk_nlay = 0;
-  double* d_draws = nullptr;
-  size_t draws_elems = 0;
-  float4* d_scratch[2] = {nullptr, nullptr};  // cell-coefficient slots (one set per chunk stream)
-  size_t scratch_bytes = 0;
-  int scratch_slots = 0, scratch_nlay = 0;
-  std::string last_error;
-  size_t max_smem = 0;
-  int num_sms = 0;
-  float4* d_bscratch = nullptr;  // scratch of batched launches
-  size_t bscratch_bytes = 0;
-  std::vector<gb_lw_tuning> tuned;  // autotuned shapes, parallel to tuned_nlay (largest nlay of the batch)
-  std::vector<int> tuned_nlay;
-};
-
-static_assert(sizeof(gb_lw_grid) == 344, "gb_lw_grid layout is part of the ABI (Python mirror: GridDesc)");
+static_assert(sizeof(gb_lw_grid) == 368, "gb_lw_grid layout is part of the ABI (Python mirror: GridDesc)");
 
 struct gb_lw_graph {
   gb_lw_context* ctx = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   float4* scratch = nullptr;
+  double* draws = nullptr;  // McICA draws of the fused-cloud grids
 };
 
-namespace {
-
-int cuda_fail(gb_lw_context* c, cudaError_t e, const char* where) {
+int gb_ctx_fail(gb_lw_context* c, cudaError_t e, const char* where) {
   if (c) c->last_error = std::string(where) + ": " + cudaGetErrorString(e);
   return GB_LW_E_CUDA;
 }
+
+namespace {
+
+int cuda_fail(gb_lw_context* c, cudaError_t e, const char* where) { return gb_ctx_fail(c, e, where); }
 #define CK(call)                                      \
   do {                                                \
     cudaError_t _e = (call);                          \
@@ -188,9 +163,43 @@ bool flags_ok(int idrv, int inflglw, int iceflglw, int liqflglw) {
          liqflglw >= 0 && liqflglw <= 1;
 }
 
+gb_lw_tuning default_tuning(gb_lw_context* ctx, int nlay) {
+  gb_lw_tuning t{};
+  t.variant = 0;
+  t.threads = gb_lw_variant(0).threads;
+  t.min_blocks = gb_lw_variant(0).min_blocks;
+  t.blocks_per_sm = std::max(1, gb_lw_slots(nlay, 0) / std::max(1, ctx->num_sms));
+  t.blocks = t.blocks_per_sm * ctx->num_sms;
+  t.ms = 0.0;
+  return t;
+}
+
+gb_lw_tuning tuning_for(gb_lw_context* ctx, int nlay) {
+  for (size_t i = 0; i < ctx->tuned_nlay.size(); ++i)
+    if (ctx->tuned_nlay[i] == nlay) return ctx->tuned[i];
+  return default_tuning(ctx, nlay);
+}
+
+int ensure_bscratch(gb_lw_context* ctx, int nlay, int blocks) {
+  size_t bytes = gb_lw_scratch_bytes(nlay, blocks);
+  if (bytes <= ctx->bscratch_bytes) return 0;
+  cudaFree(ctx->d_bscratch);
+  ctx->d_bscratch = nullptr;
+  ctx->bscratch_bytes = 0;
+  if (cudaMalloc(&ctx->d_bscratch, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->last_error = "device allocation of the batch scratch failed";
+    return GB_LW_E_NOMEM;
+  }
+  ctx->bscratch_bytes = bytes;
+  return 0;
+}
+
+}  // namespace
+
 // Validates the grids of a batched call and fills the launch descriptor.
 // frac < 1 keeps only that fraction of each grid's columns (autotuner sample).
-int make_batch(gb_lw_context* ctx, int ngrid, const gb_lw_grid* grids, double frac, LwBatch& b) {
+int gb_ctx_make_batch(gb_lw_context* ctx, int ngrid, const gb_lw_grid* grids, double frac, LwBatch& b) {
   if (ngrid < 1 || ngrid > GB_LW_MAX_GRIDS || !grids) return GB_LW_E_ARGS;
   b = LwBatch{};
   b.ngrid = ngrid;
@@ -234,6 +243,11 @@ int make_batch(gb_lw_context* ctx, int ngrid, const gb_lw_grid* grids, double fr
     a.duflx_dt = g.duflx_dt; a.duflxc_dt = g.duflxc_dt;
     a.col_err = g.d_col_status;
     a.err_flag = ctx->d_err;
+    a.sur_tau = g.sur_tau;
+    a.sur_frac = g.sur_frac;
+    a.sur_flag = g.sur_flag;
+    if ((g.sur_tau != nullptr) != (g.sur_frac != nullptr) || (g.sur_tau != nullptr) != (g.sur_flag != nullptr))
+      return GB_LW_E_ARGS;
     b.col0[i + 1] = b.col0[i] + nc;
     b.nsmax = std::max(b.nsmax, g.nlay);
   }
@@ -244,39 +258,54 @@ int make_batch(gb_lw_context* ctx, int ngrid, const gb_lw_grid* grids, double fr
   return 0;
 }
 
-gb_lw_tuning default_tuning(gb_lw_context* ctx, int nlay) {
-  gb_lw_tuning t{};
-  t.variant = 0;
-  t.threads = gb_lw_variant(0).threads;
-  t.min_blocks = gb_lw_variant(0).min_blocks;
-  t.blocks_per_sm = std::max(1, gb_lw_slots(nlay, 0) / std::max(1, ctx->num_sms));
-  t.blocks = t.blocks_per_sm * ctx->num_sms;
-  t.ms = 0.0;
-  return t;
+
+size_t gb_ctx_fused_draws(const LwBatch& b) {
+  size_t n = 0;
+  for (int i = 0; i < b.ngrid; ++i)
+    if (b.g[i].cloud_mode == LW_CLOUD_FUSED && b.g[i].icld >= 1) n += (size_t)b.g[i].ncol * GB_NGPT;
+  return n;
 }
 
-gb_lw_tuning tuning_for(gb_lw_context* ctx, int nlay) {
-  for (size_t i = 0; i < ctx->tuned_nlay.size(); ++i)
-    if (ctx->tuned_nlay[i] == nlay) return ctx->tuned[i];
-  return default_tuning(ctx, nlay);
-}
-
-int ensure_bscratch(gb_lw_context* ctx, int nlay, int blocks) {
-  size_t bytes = gb_lw_scratch_bytes(nlay, blocks);
-  if (bytes <= ctx->bscratch_bytes) return 0;
-  cudaFree(ctx->d_bscratch);
-  ctx->d_bscratch = nullptr;
-  ctx->bscratch_bytes = 0;
-  if (cudaMalloc(&ctx->d_bscratch, bytes) != cudaSuccess) {
-    cudaGetLastError();
-    ctx->last_error = "device allocation of the batch scratch failed";
-    return GB_LW_E_NOMEM;
+int gb_ctx_make_draws(gb_lw_context* ctx, LwBatch& b, double* buf, cudaStream_t stream) {
+  size_t off = 0;
+  for (int i = 0; i < b.ngrid; ++i) {
+    LwArgs& a = b.g[i];
+    if (a.cloud_mode != LW_CLOUD_FUSED || a.icld < 1) continue;
+    cudaError_t e = gb_mcica_percol_mt(a.ncol, a.seed0, GB_NGPT, buf + off, stream);
+    if (e != cudaSuccess) return gb_ctx_fail(ctx, e, "McICA draws");
+    a.draws = buf + off;
+    off += (size_t)a.ncol * GB_NGPT;
   }
-  ctx->bscratch_bytes = bytes;
-  return 0;
+  return GB_LW_OK;
 }
 
-}  // namespace
+int gb_ctx_launch_batch(gb_lw_context* ctx, LwBatch& b, cudaStream_t stream) {
+  if (b.col0[b.ngrid] == 0) return GB_LW_OK;
+  cudaSetDevice(ctx->device);
+  const gb_lw_tuning t = tuning_for(ctx, b.nsmax);
+  int rc = ensure_bscratch(ctx, b.nsmax, t.blocks);
+  if (rc) return rc;
+  const size_t nd = gb_ctx_fused_draws(b);
+  if (nd > ctx->fdraws_elems) {
+    cudaFree(ctx->d_fdraws);
+    ctx->d_fdraws = nullptr;
+    ctx->fdraws_elems = 0;
+    if (cudaMalloc(&ctx->d_fdraws, nd * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      ctx->last_error = "device allocation of the McICA draws failed";
+      return GB_LW_E_NOMEM;
+    }
+    ctx->fdraws_elems = nd;
+  }
+  if (nd) {
+    rc = gb_ctx_make_draws(ctx, b, ctx->d_fdraws, stream);
+    if (rc) return rc;
+  }
+  b.scratch = ctx->d_bscratch;
+  cudaError_t e = gb_lw_launch_batch(b, ctx->d_tables, t.variant, t.blocks, stream);
+  if (e != cudaSuccess) return gb_ctx_fail(ctx, e, "batched launch");
+  return GB_LW_OK;
+}
 
 extern "C" {
 
@@ -337,6 +366,9 @@ int gb_rrtmg_lw_free(gb_lw_context* ctx) {
   cudaFree(ctx->d_draws);
   for (auto& p : ctx->d_scratch) cudaFree(p);
   cudaFree(ctx->d_bscratch);
+  cudaFree(ctx->d_sur);
+  cudaFree(ctx->d_sur_flag);
+  cudaFree(ctx->d_fdraws);
   delete ctx;
   return GB_LW_OK;
 }
@@ -685,16 +717,9 @@ int gb_rrtmg_lw_gas_optics_diag(gb_lw_context* ctx, int ncol, int nlay, const do
 int gb_rrtmg_lw_batch_device(gb_lw_context* ctx, void* stream, int ngrid, const gb_lw_grid* grids) {
   if (!ctx) return GB_LW_E_ARGS;
   LwBatch b;
-  int rc = make_batch(ctx, ngrid, grids, 1.0, b);
+  int rc = gb_ctx_make_batch(ctx, ngrid, grids, 1.0, b);
   if (rc) return rc;
-  if (b.col0[ngrid] == 0) return GB_LW_OK;
-  cudaSetDevice(ctx->device);
-  const gb_lw_tuning t = tuning_for(ctx, b.nsmax);
-  rc = ensure_bscratch(ctx, b.nsmax, t.blocks);
-  if (rc) return rc;
-  b.scratch = ctx->d_bscratch;
-  CK(gb_lw_launch_batch(b, ctx->d_tables, t.variant, t.blocks, (cudaStream_t)stream));
-  return GB_LW_OK;
+  return gb_ctx_launch_batch(ctx, b, (cudaStream_t)stream);
 }
 
 int gb_rrtmg_lw_tuning_get(gb_lw_context* ctx, int nlay, gb_lw_tuning* out) {
@@ -736,13 +761,13 @@ int gb_rrtmg_lw_autotune(gb_lw_context* ctx, void* stream, int ngrid, const gb_l
                          int reps, gb_lw_tuning* best) {
   if (!ctx) return GB_LW_E_ARGS;
   LwBatch full;
-  int rc = make_batch(ctx, ngrid, grids, 1.0, full);
+  int rc = gb_ctx_make_batch(ctx, ngrid, grids, 1.0, full);
   if (rc) return rc;
   const long long total = full.col0[ngrid];
   if (total == 0) return GB_LW_E_ARGS;
   const double frac = sample_cols > 0 && sample_cols < total ? (double)sample_cols / (double)total : 1.0;
   LwBatch b;
-  rc = make_batch(ctx, ngrid, grids, frac, b);
+  rc = gb_ctx_make_batch(ctx, ngrid, grids, frac, b);
   if (rc) return rc;
   cudaSetDevice(ctx->device);
   cudaStream_t st = (cudaStream_t)stream;
@@ -762,6 +787,19 @@ int gb_rrtmg_lw_autotune(gb_lw_context* ctx, void* stream, int ngrid, const gb_l
   rc = ensure_bscratch(ctx, b.nsmax, max_blocks);
   if (rc) return rc;
   b.scratch = ctx->d_bscratch;
+  // the fused-cloud draws are made once: every candidate times the column kernel alone
+  const size_t nd = gb_ctx_fused_draws(b);
+  if (nd > ctx->fdraws_elems) {
+    cudaFree(ctx->d_fdraws);
+    ctx->d_fdraws = nullptr;
+    ctx->fdraws_elems = 0;
+    if (cudaMalloc(&ctx->d_fdraws, nd * sizeof(double)) != cudaSuccess) {
+      cudaGetLastError();
+      return GB_LW_E_NOMEM;
+    }
+    ctx->fdraws_elems = nd;
+  }
+  if (nd && (rc = gb_ctx_make_draws(ctx, b, ctx->d_fdraws, st)) != 0) return rc;
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
@@ -809,7 +847,7 @@ int gb_rrtmg_lw_batch_graph_create(gb_lw_context* ctx, int ngrid, const gb_lw_gr
   if (!ctx || !out) return GB_LW_E_ARGS;
   *out = nullptr;
   LwBatch b;
-  int rc = make_batch(ctx, ngrid, grids, 1.0, b);
+  int rc = gb_ctx_make_batch(ctx, ngrid, grids, 1.0, b);
   if (rc) return rc;
   if (b.col0[ngrid] == 0) return GB_LW_E_ARGS;
   cudaSetDevice(ctx->device);
@@ -822,10 +860,18 @@ int gb_rrtmg_lw_batch_graph_create(gb_lw_context* ctx, int ngrid, const gb_lw_gr
     return GB_LW_E_NOMEM;
   }
   b.scratch = g->scratch;
+  const size_t nd = gb_ctx_fused_draws(b);
+  if (nd && cudaMalloc(&g->draws, nd * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    gb_rrtmg_lw_graph_destroy(g);
+    return GB_LW_E_NOMEM;
+  }
   cudaStream_t s = ctx->streams[0];
   cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed);
   if (e == cudaSuccess) {
-    cudaError_t le = gb_lw_launch_batch(b, ctx->d_tables, t.variant, t.blocks, s);
+    cudaError_t le = cudaSuccess;
+    if (nd && gb_ctx_make_draws(ctx, b, g->draws, s) != GB_LW_OK) le = cudaErrorLaunchFailure;
+    if (le == cudaSuccess) le = gb_lw_launch_batch(b, ctx->d_tables, t.variant, t.blocks, s);
     e = cudaStreamEndCapture(s, &g->graph);
     if (le != cudaSuccess) e = le;
   }
@@ -852,6 +898,7 @@ int gb_rrtmg_lw_graph_destroy(gb_lw_graph* g) {
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);
   cudaFree(g->scratch);
+  cudaFree(g->draws);
   delete g;
   return GB_LW_OK;
 }

@@ -1,0 +1,59 @@
+// Library context shared by the C-ABI translation units (lw_capi.cu, lw_mlp_capi.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gb_rrtmg_lw.h"
+#include "lw_common.h"
+#include "lw_solver.h"
+
+struct ChunkBufs {
+  double* in = nullptr;   // all inputs of one chunk, packed
+  double* out = nullptr;  // all outputs of one chunk, packed
+  size_t in_elems = 0, out_elems = 0;
+};
+
+struct gb_lw_context {
+  int device = 0;
+  GbTables tabs;
+  float* d_tables = nullptr;
+  int* d_err = nullptr;      // max status of device calls
+  int* d_err_host = nullptr; // status of the current host call
+  cudaStream_t streams[2] = {nullptr, nullptr};
+  ChunkBufs bufs[2];
+  int chunk_cols = 0, chunk_nlay = 0;
+  double* d_draws = nullptr;
+  size_t draws_elems = 0;
+  float4* d_scratch[2] = {nullptr, nullptr};  // cell-coefficient slots (one set per chunk stream)
+  size_t scratch_bytes = 0;
+  int scratch_slots = 0, scratch_nlay = 0;
+  std::string last_error;
+  size_t max_smem = 0;
+  int num_sms = 0;
+  float4* d_bscratch = nullptr;  // scratch of batched launches
+  size_t bscratch_bytes = 0;
+  std::vector<gb_lw_tuning> tuned;  // autotuned shapes, parallel to tuned_nlay (largest nlay of the batch)
+  std::vector<int> tuned_nlay;
+  // McICA draws of fused-cloud grids in batched calls (grown on demand)
+  double* d_fdraws = nullptr;
+  size_t fdraws_elems = 0;
+  // surrogate outputs of batched calls with a network (grown on demand)
+  float* d_sur = nullptr;
+  unsigned char* d_sur_flag = nullptr;
+  size_t sur_rows = 0;
+};
+
+// records a CUDA error on the context; returns GB_LW_E_CUDA
+int gb_ctx_fail(gb_lw_context* c, cudaError_t e, const char* where);
+// validates a batched call's grids and fills the launch descriptor (frac < 1: sample of each grid)
+int gb_ctx_make_batch(gb_lw_context* ctx, int ngrid, const gb_lw_grid* grids, double frac, LwBatch& b);
+// launches a filled descriptor with the context's shape for its largest nlay
+// (first the McICA draws of its fused-cloud grids, into `draws` when given,
+// else into a context buffer)
+int gb_ctx_launch_batch(gb_lw_context* ctx, LwBatch& b, cudaStream_t stream);
+// doubles of McICA draws a descriptor's fused-cloud grids need
+size_t gb_ctx_fused_draws(const LwBatch& b);
+// launches the draw kernels of a descriptor's fused-cloud grids into buf and sets their draws pointers
+int gb_ctx_make_draws(gb_lw_context* ctx, LwBatch& b, double* buf, cudaStream_t stream);

@@ -41,10 +41,6 @@ __constant__ GbTables c_T;
 
 // most terms any band needs in one layer (band 13, lower atmosphere)
 constexpr int MAXT_ALL = 24;
-// Bands are processed in groups that share one prologue pass and one cell
-// pass; a group's term lists fit TGROUP terms per layer.
-constexpr int NGROUP = 6;
-constexpr int TGROUP = 48;
 // per band: max over lower and upper atmosphere
 __host__ __device__ constexpr int maxt(int b) {
   constexpr int m[17] = {0, 10, 8, 20, 16, 21, 12, 20, 16, 20, 8, 10, 16, 24, 8, 20, 16};

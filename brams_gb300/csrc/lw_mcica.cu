@@ -257,6 +257,12 @@ cudaError_t gb_mcica_launch(const McicaArgs& a, double* d_draws, int* d_err, cud
   return cudaGetLastError();
 }
 
+cudaError_t gb_mcica_percol_mt(int ncol, unsigned seed0, int ndraw, double* d_draws, cudaStream_t stream) {
+  if (ncol <= 0) return cudaSuccess;
+  gbm::mt_percol_kernel<<<(ncol + 127) / 128, 128, 0, stream>>>(ncol, (int)seed0, ndraw, d_draws);
+  return cudaGetLastError();
+}
+
 size_t gb_mcica_draw_count(int ncol, int nlay, int icld) {
   const int per = icld == 3 ? 1 : (icld <= 2 ? nlay : 2 * nlay);
   return (size_t)GB_NGPT * per * (size_t)ncol;

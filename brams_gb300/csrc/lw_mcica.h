@@ -31,3 +31,6 @@ size_t gb_mcica_draw_count(int ncol, int nlay, int icld);
 // seed + c times, reproducing one reference call per column.
 cudaError_t gb_mcica_launch(const McicaArgs& a, double* d_draws, int* d_err, cudaStream_t stream,
                             bool seed_per_column);
+// First ndraw Mersenne-twister reals of seeds seed0 + c for columns c = 0..ncol-1,
+// draws[c * ndraw + k] (the draws of one reference call per column).
+cudaError_t gb_mcica_percol_mt(int ncol, unsigned seed0, int ndraw, double* d_draws, cudaStream_t stream);

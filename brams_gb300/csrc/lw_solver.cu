@@ -40,6 +40,7 @@
 // uflx(icol, k+1) for k = 0..nlay, hr(icol, k+1) for k = 0..nlay-1.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <cmath>
 #include <stdint.h>
 
 #include "lw_common.h"
@@ -52,34 +53,80 @@ namespace gb {
 constexpr int NSW = 5;  // warps of the g-point sweeps (140 lanes)
 constexpr float BPADE = 1.0f / 0.278f;
 
+// ------------------------------------------------------------------ band groups
+// Bands are processed in groups of consecutive bands that share one prologue
+// pass and one cell pass (kGroupFirst: first band of each group, then 17).
+// Term lists of a group's bands sit side by side, TGROUP term slots per layer.
+constexpr int kGroupFirst[] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17};
+constexpr int NGROUP = (int)(sizeof(kGroupFirst) / sizeof(int)) - 1;
+constexpr int group_of(int b) {
+  int gr = 0;
+  while (kGroupFirst[gr + 1] <= b) ++gr;
+  return gr;
+}
+constexpr int term_offset(int b) {  // first term slot of band b in its group
+  int o = 0;
+  for (int k = kGroupFirst[group_of(b)]; k < b; ++k) o += maxt(k);
+  return o;
+}
+constexpr int group_terms(int gr) { return term_offset(kGroupFirst[gr + 1] - 1) + maxt(kGroupFirst[gr + 1] - 1); }
+constexpr int max_group_terms() {
+  int m = 0;
+  for (int gr = 0; gr < NGROUP; ++gr) m = group_terms(gr) > m ? group_terms(gr) : m;
+  return m;
+}
+constexpr int max_group_bands() {
+  int m = 0;
+  for (int gr = 0; gr < NGROUP; ++gr) m = kGroupFirst[gr + 1] - kGroupFirst[gr] > m ? kGroupFirst[gr + 1] - kGroupFirst[gr] : m;
+  return m;
+}
+constexpr int TGROUP = max_group_terms();
+constexpr int GBANDS = max_group_bands();
+__constant__ int c_gfirst[17] = {
+#define GB_G(i) (i <= NGROUP ? kGroupFirst[i] : 0)
+    GB_G(0), GB_G(1), GB_G(2), GB_G(3), GB_G(4), GB_G(5), GB_G(6), GB_G(7), GB_G(8),
+    GB_G(9), GB_G(10), GB_G(11), GB_G(12), GB_G(13), GB_G(14), GB_G(15), GB_G(16)};
+#undef GB_G
+__constant__ int c_toff[17] = {0, term_offset(1), term_offset(2), term_offset(3), term_offset(4), term_offset(5),
+                               term_offset(6), term_offset(7), term_offset(8), term_offset(9), term_offset(10),
+                               term_offset(11), term_offset(12), term_offset(13), term_offset(14), term_offset(15),
+                               term_offset(16)};
+
 // ------------------------------------------------------------------ shared memory layout
 struct Smem {
   float* f;        // [NF][nl]   per-layer coefficients (phases 1-2)
   int* iv;         // [NI][nl]
   float2* terms;   // [TGROUP][nl] gas-optics terms of the current band group, term-major (phase 2)
-  float* part;     // [NSW][nl+1][6] warp partial fluxes (aliases f/iv/terms in phases 3-4)
+  float* part;     // [NSW][nl+1][6] warp partial fluxes (region A, phases 3-4)
   float* taua;     // [16][nl]
   float* plk_lay;  // [16][nl]
   float* plk_lev;  // [16][nl+1]
-  FracRec* frec;   // [3][nl] Planck-fraction records of the current band group
+  FracRec* frec;   // [GBANDS][nl] Planck-fraction records of the current band group
   int* cldlay;     // [nl]
+  int* surok;      // [nl] 1: the layer's gas optics come from the learned model
   unsigned* cbits; // [nl][5] bit g set where cldfmcl == 1
   unsigned* fbits; // [nl][5] bit g set where cldfmcl is neither 0 nor 1
   float* frac1;    // [140] Planck fractions of the bottom layer (surface source)
-  double* fnet;    // [nl+1][2] net fluxes (phase 4)
+  double* fnet;    // [nl+1][2] net fluxes (region A after part, phase 4)
   float* misc;     // [64]: secdiff[16], plankbnd[16], dplankbnd[16], semiss[16]
   float* scal;     // [4]
   int* iscal;      // [4]: laytrop, sum of lower-layer indices, error, column error
-  double* cdf;     // [140] McICA draws of the column (fused cloud mode; compared as bit patterns)
-  uint32_t* mtlo;  // [141] Mersenne-twister state words (fused cloud mode)
+  double* cdf;     // [140] McICA draws of the column (fused cloud mode, phase 1; in the term area)
+  uint32_t* mtlo;  // [141] Mersenne-twister state words (fused cloud mode, phase 1; in the term area)
   float* tcl;      // [nl][16] cloud optical depth per (layer, band) (fused cloud mode)
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
+// Region A holds, by phase: the per-layer coefficients f/iv and the term
+// lists (phases 1-2; the McICA draws of the fused cloud mode borrow the term
+// area during phase 1), then the warp partial sums and net fluxes (3-4).
+__host__ __device__ inline size_t terms_offset(int nl) { return ((size_t)(NF + NI) * nl * 4 + 15) & ~size_t(15); }
 __host__ __device__ inline size_t region_a(int nl) {
-  size_t coef = (((size_t)(NF + NI) * nl * 4 + 15) & ~size_t(15)) + (size_t)nl * TGROUP * 8;
-  size_t part = (size_t)NSW * (nl + 1) * 6 * 4;
+  size_t terms = (size_t)nl * TGROUP * 8;
+  const size_t draws = align16(GB_NGPT * 8) + align16((GB_NGPT + 1) * 4);
+  size_t coef = terms_offset(nl) + (terms > draws ? terms : draws);
+  size_t part = align16((size_t)NSW * (nl + 1) * 6 * 4) + (size_t)(nl + 1) * 2 * 8;
   return align16(coef > part ? coef : part);
 }
 
@@ -88,13 +135,12 @@ __host__ __device__ inline size_t smem_bytes(int nl) {
   a += align16((size_t)nl * 16 * 4);         // taua
   a += align16((size_t)nl * 16 * 4);         // plk_lay
   a += align16((size_t)(nl + 1) * 16 * 4);   // plk_lev
-  a += align16((size_t)3 * nl * sizeof(FracRec));
-  a += align16((size_t)nl * 4);
+  a += align16((size_t)GBANDS * nl * sizeof(FracRec));
+  a += 2 * align16((size_t)nl * 4);
   a += 2 * align16((size_t)nl * 5 * 4);
   a += align16(GB_NGPT * 4);
-  a += align16((size_t)(nl + 1) * 2 * 8);
   a += align16(64 * 4) + align16(4 * 4) + align16(4 * 4);
-  a += align16(GB_NGPT * 8) + align16((GB_NGPT + 1) * 4) + align16((size_t)nl * 16 * 4);
+  a += align16((size_t)nl * 16 * 4);
   return a;
 }
 
@@ -103,23 +149,24 @@ __device__ inline Smem carve(char* base, int nl) {
   char* p = base;
   s.f = (float*)p;
   s.iv = (int*)(p + (size_t)NF * nl * 4);
-  s.terms = (float2*)(p + (((size_t)(NF + NI) * nl * 4 + 15) & ~size_t(15)));
+  s.terms = (float2*)(p + terms_offset(nl));
+  s.cdf = (double*)(p + terms_offset(nl));
+  s.mtlo = (uint32_t*)(p + terms_offset(nl) + align16(GB_NGPT * 8));
   s.part = (float*)p;
+  s.fnet = (double*)(p + align16((size_t)NSW * (nl + 1) * 6 * 4));
   p += region_a(nl);
   s.taua = (float*)p; p += align16((size_t)nl * 16 * 4);
   s.plk_lay = (float*)p; p += align16((size_t)nl * 16 * 4);
   s.plk_lev = (float*)p; p += align16((size_t)(nl + 1) * 16 * 4);
-  s.frec = (FracRec*)p; p += align16((size_t)3 * nl * sizeof(FracRec));
+  s.frec = (FracRec*)p; p += align16((size_t)GBANDS * nl * sizeof(FracRec));
   s.cldlay = (int*)p; p += align16((size_t)nl * 4);
+  s.surok = (int*)p; p += align16((size_t)nl * 4);
   s.cbits = (unsigned*)p; p += align16((size_t)nl * 5 * 4);
   s.fbits = (unsigned*)p; p += align16((size_t)nl * 5 * 4);
   s.frac1 = (float*)p; p += align16(GB_NGPT * 4);
-  s.fnet = (double*)p; p += align16((size_t)(nl + 1) * 2 * 8);
   s.misc = (float*)p; p += align16(64 * 4);
   s.scal = (float*)p; p += align16(4 * 4);
   s.iscal = (int*)p; p += align16(4 * 4);
-  s.cdf = (double*)p; p += align16(GB_NGPT * 8);
-  s.mtlo = (uint32_t*)p; p += align16((GB_NGPT + 1) * 4);
   s.tcl = (float*)p;
   return s;
 }
@@ -301,21 +348,6 @@ __device__ __forceinline__ CellCoef cell_coef(bool cloudy, float odepth, float o
   return r;
 }
 
-// ------------------------------------------------------------------ band groups
-// Groups of consecutive bands whose term lists share the TGROUP slots per
-// layer: {1,2,3} {4,5} {6,7,8} {9,10,11} {12,13} {14,15,16}.  c_toff[b] is the
-// first term slot of band b in its group.
-__constant__ int c_gfirst[NGROUP + 1] = {1, 4, 6, 9, 12, 14, 17};
-__constant__ int c_toff[17] = {0, 0, 10, 18, 0, 16, 0, 12, 32, 0, 20, 28, 0, 16, 0, 8, 28};
-static_assert(maxt(1) + maxt(2) + maxt(3) <= TGROUP && maxt(4) + maxt(5) <= TGROUP &&
-                  maxt(6) + maxt(7) + maxt(8) <= TGROUP && maxt(9) + maxt(10) + maxt(11) <= TGROUP &&
-                  maxt(12) + maxt(13) <= TGROUP && maxt(14) + maxt(15) + maxt(16) <= TGROUP,
-              "band group exceeds its term slots");
-static_assert(maxt(1) == 10 && maxt(1) + maxt(2) == 18 && maxt(4) == 16 && maxt(6) == 12 &&
-                  maxt(6) + maxt(7) == 32 && maxt(9) == 20 && maxt(9) + maxt(10) == 28 && maxt(12) == 16 &&
-                  maxt(14) == 8 && maxt(14) + maxt(15) == 28,
-              "c_toff out of date");
-
 // Prologue of band b for one layer: the band-specific per-layer code
 // (lw_gasoptics.cuh) writing the layer's terms and Planck-fraction record.
 template <int b>
@@ -354,7 +386,7 @@ __device__ __forceinline__ void group_prologues(int gr, const Smem& s, int nl, i
   const int b0 = c_gfirst[gr], nb = c_gfirst[gr + 1] - b0;
   for (int it = threadIdx.x; it < nb * nl; it += NT) {
     const int slot = it / nl, lay = it - slot * nl;
-    prologue_dispatch(b0 + slot, s, nl, lay, lay < laytrop, slot);
+    if (!s.surok[lay]) prologue_dispatch(b0 + slot, s, nl, lay, lay < laytrop, slot);
   }
 }
 
@@ -376,20 +408,27 @@ __device__ __forceinline__ void group_cells(int gr, const LwArgs& a, const Smem&
     }
     const int slot = b - b0;
     const int lay = (int)(((float)c + 0.5f) * __frcp_rn((float)NG)), gi = c - lay * NG, g = c_T.band[b - 1].g0 + gi;
-    const int M = c_maxt[b];
-    const float2* tp = s.terms + (size_t)c_toff[b] * nl + lay;
-    const float* Tg = T + gi;
-    float acc = 0.0f;
-    for (int k = 0; k < M; ++k) {
-      const float2 w = tp[k * nl];
-      acc = fmaf(w.x, __ldg(Tg + __float_as_int(w.y)), acc);
+    float taut, plfrac;
+    if (s.surok[lay]) {  // learned gas optics
+      const long long o = (icol * nl + lay) * GB_NGPT + g;
+      taut = __ldg(a.sur_tau + o) + s.taua[(b - 1) * nl + lay];
+      plfrac = __ldg(a.sur_frac + o);
+    } else {
+      const int M = c_maxt[b];
+      const float2* tp = s.terms + (size_t)c_toff[b] * nl + lay;
+      const float* Tg = T + gi;
+      float acc = 0.0f;
+      for (int k = 0; k < M; ++k) {
+        const float2 w = tp[k * nl];
+        acc = fmaf(w.x, __ldg(Tg + __float_as_int(w.y)), acc);
+      }
+      if ((b == 4 || b == 7) && lay >= laytrop) acc *= gscale(b, gi);
+      taut = acc + s.taua[(b - 1) * nl + lay];
+      const FracRec fr = s.frec[slot * nl + lay];
+      const float* fp = T + fr.off + gi;
+      const float f0 = __ldg(fp);
+      plfrac = f0 + fr.fpl * (__ldg(fp + NG) - f0);
     }
-    if ((b == 4 || b == 7) && lay >= laytrop) acc *= gscale(b, gi);
-    const float taut = acc + s.taua[(b - 1) * nl + lay];
-    const FracRec fr = s.frec[slot * nl + lay];
-    const float* fp = T + fr.off + gi;
-    const float f0 = __ldg(fp);
-    const float plfrac = f0 + fr.fpl * (__ldg(fp + NG) - f0);
     if (lay == 0) s.frac1[g] = plfrac;
     if (a.dbg_taut) {
       a.dbg_taut[(icol * nl + lay) * GB_NGPT + g] = taut;
@@ -422,15 +461,23 @@ __device__ __forceinline__ void solve_column(const LwArgs& a, long long icol, ch
   const int tid = threadIdx.x;
   const bool fused = a.cloud_mode == LW_CLOUD_FUSED;
   {
-    // fused clouds: the column's 140 draws, one thread (the last warp is the
-    // least busy one in phase 1)
-    if (fused && a.icld >= 1 && tid == NT - 1)
-      gbmt::first_reals(a.seed0 + (unsigned)icol, GB_NGPT, s.mtlo, s.cdf, 1);
+    // fused clouds: the column's 140 draws, made beforehand by a parallel
+    // kernel or else here by one thread of the last warp
+    if (fused && a.icld >= 1) {
+      if (a.draws) {
+        for (int g = tid; g < GB_NGPT; g += NT) s.cdf[g] = __ldg(a.draws + icol * GB_NGPT + g);
+      } else if (tid == NT - 1) {
+        gbmt::first_reals(a.seed0 + (unsigned)icol, GB_NGPT, s.mtlo, s.cdf, 1);
+      }
+    }
     if (tid < 4) {
       s.scal[tid] = 0.0f;
       s.iscal[tid] = 0;
     }
-    for (int l = tid; l < nl; l += NT) s.cldlay[l] = 0;
+    for (int l = tid; l < nl; l += NT) {
+      s.cldlay[l] = 0;
+      s.surok[l] = a.sur_flag ? (int)__ldg(a.sur_flag + icol * nl + l) : 0;
+    }
     for (int l = tid; l < nl * 5; l += NT) s.cbits[l] = s.fbits[l] = 0u;
     __syncthreads();
 
@@ -834,7 +881,7 @@ __global__ void __launch_bounds__(NT, MINB) lw_batch_kernel(const __grid_constan
 }
 
 // compiled shapes (threads per column, min blocks per SM); variant 0 is the default
-#define GB_LW_VARIANTS(X) X(0, 160, 6) X(1, 160, 4) X(2, 256, 4) X(3, 256, 3)
+#define GB_LW_VARIANTS(X) X(0, 160, 5) X(1, 160, 6) X(2, 160, 4) X(3, 256, 3)
 
 }  // namespace gb
 
@@ -861,8 +908,24 @@ cudaError_t configure(int nlay, int variant, int* blocks_per_sm) {
   const VariantInfo& v = kVariants[variant];
   const size_t sm = gb::smem_bytes(nlay);
   cudaError_t e = cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(v.fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, v.fn, v.threads, sm);
+}
+
+// Shared-memory carve-out for `per` resident blocks: just what they need, so
+// that the rest of the SM's 256 KB stays L1 for the table gathers (the
+// driver otherwise sizes it for the largest block count shared memory alone
+// would allow, even when registers allow fewer).
+cudaError_t set_carveout(int variant, size_t smem, int per) {
+  int dev = 0, max_sm = 0, reserved = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&max_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  if (max_sm <= 0) return cudaSuccess;
+  int pct = (int)std::ceil(100.0 * (double)per * (double)(smem + reserved) / (double)max_sm);
+  pct = pct < 1 ? 1 : (pct > 100 ? 100 : pct);
+  return cudaFuncSetAttribute(kVariants[variant].fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
 }
 
 }  // namespace
@@ -897,6 +960,12 @@ cudaError_t gb_lw_launch_batch(const LwBatch& b, const float* d_tables, int vari
   cudaError_t e = configure(b.nsmax, variant, &per);
   if (e != cudaSuccess) return e;
   if ((long long)nblocks > b.col0[b.ngrid]) nblocks = (int)b.col0[b.ngrid];
+  int dev = 0, nsm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int resident = (nblocks + nsm - 1) / nsm;
+  e = set_carveout(variant, gb::smem_bytes(b.nsmax), resident < per ? resident : per);
+  if (e != cudaSuccess) return e;
   return kVariants[variant].launch(b, d_tables, nblocks, gb::smem_bytes(b.nsmax), stream);
 }
 

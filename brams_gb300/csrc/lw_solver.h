@@ -33,6 +33,13 @@ struct LwArgs {
   int* err_flag;  // required: max status over the launch
   float* dbg_taut;   // optional diagnostics: taut and Planck fractions per column,
   float* dbg_fracs;  // (ncol, nlay, 140) with g fastest; NULL in production calls
+  // optional learned gas optics: taug and Planck fractions per (column, layer, g)
+  // and a per-layer flag (1: use them, 0: taumol); NULL: taumol everywhere
+  const float *sur_tau, *sur_frac;
+  const unsigned char* sur_flag;
+  // fused cloud mode: the columns' 140 McICA draws [ncol][140] made beforehand
+  // (gb_mcica_percol_mt); NULL: the kernel draws them itself
+  const double* draws;
 };
 
 // Grids of one launch: grid i owns batch columns col0[i] .. col0[i+1]-1.  The

@@ -38,7 +38,13 @@ EXPORTS = [
     "gb_mcica_subcol_lw_noalloc", "gb_rrtmg_lw_batch_device", "gb_rrtmg_lw_autotune",
     "gb_rrtmg_lw_tuning_get", "gb_rrtmg_lw_batch_graph_create", "gb_rrtmg_lw_graph_launch",
     "gb_rrtmg_lw_graph_destroy", "gb_rrtmg_lw_tuning_set", "gb_rrtmg_lw_num_variants",
+    "gb_lw_mlp_create", "gb_lw_mlp_destroy", "gb_lw_mlp_save", "gb_lw_mlp_load", "gb_lw_mlp_get_params",
+    "gb_lw_mlp_set_params", "gb_lw_mlp_set_loss_weights", "gb_lw_mlp_samples", "gb_lw_mlp_fit_norm",
+    "gb_lw_mlp_prepare", "gb_lw_mlp_gradients", "gb_lw_mlp_train_step", "gb_lw_mlp_forward", "gb_lw_mlp_infer",
+    "gb_rrtmg_lw_batch_surrogate",
 ]
+MLP_NPARAM = 72352
+MLP_NNORM = 626
 
 CLOUD_SUBCOL, CLOUD_FUSED = 0, 1
 MAX_GRIDS = 32
@@ -47,7 +53,7 @@ _GRID_PTRS = ["play", "plev", "tlay", "tlev", "tsfc", "h2ovmr", "o3vmr", "co2vmr
               "o2vmr", "cfc11vmr", "cfc12vmr", "cfc22vmr", "ccl4vmr", "emis", "tauaer",
               "cldfmcl", "taucmcl", "ciwpmcl", "clwpmcl", "cldfrac", "ciwp", "clwp", "tauc",
               "reicmcl", "relqmcl", "uflx", "dflx", "hr", "uflxc", "dflxc", "hrc", "duflx_dt", "duflxc_dt",
-              "d_col_status"]
+              "d_col_status", "sur_tau", "sur_frac", "sur_flag"]
 
 
 class GridDesc(C.Structure):
@@ -127,6 +133,22 @@ def load_library(path: str = LIB_PATH):
         L.gb_rrtmg_lw_graph_destroy.argtypes = [P]
         L.gb_rrtmg_lw_tuning_set.argtypes = [P, I, C.POINTER(Tuning)]
         L.gb_rrtmg_lw_num_variants.argtypes = []
+        U64, F = C.c_uint64, C.c_float
+        L.gb_lw_mlp_create.argtypes = [P, U64, C.POINTER(P)]
+        L.gb_lw_mlp_destroy.argtypes = [P]
+        L.gb_lw_mlp_save.argtypes = [P, C.c_char_p]
+        L.gb_lw_mlp_load.argtypes = [P, C.c_char_p, C.POINTER(P)]
+        L.gb_lw_mlp_get_params.argtypes = [P, P, P]
+        L.gb_lw_mlp_set_params.argtypes = [P, P, P]
+        L.gb_lw_mlp_set_loss_weights.argtypes = [P, P]
+        L.gb_lw_mlp_samples.argtypes = [P, P, GP, P, P, P]
+        L.gb_lw_mlp_fit_norm.argtypes = [P, P, LL, P, P, P]
+        L.gb_lw_mlp_prepare.argtypes = [P, P, LL, P, P, P, P, P]
+        L.gb_lw_mlp_gradients.argtypes = [P, P, LL, P, P, P, P]
+        L.gb_lw_mlp_train_step.argtypes = [P, P, LL, P, P, F, P]
+        L.gb_lw_mlp_forward.argtypes = [P, P, LL, P, P]
+        L.gb_lw_mlp_infer.argtypes = [P, P, GP, P, P, P]
+        L.gb_rrtmg_lw_batch_surrogate.argtypes = [P, P, I, GP, P]
         L.gb_rrtmg_lw_strerror.restype = C.c_char_p
         L.gb_rrtmg_lw_strerror.argtypes = [I]
         L.gb_rrtmg_lw_last_error.restype = C.c_char_p
@@ -316,3 +338,78 @@ class BatchGraph:
             self.close()
         except Exception:
             pass
+
+
+class Mlp:
+    """The learned stand-in for taumol (gb_lw_mlp_*): training and inference on device buffers."""
+
+    def __init__(self, ctx: Context, seed: int = 1, path: str | None = None):
+        self.ctx, self.L = ctx, ctx.L
+        h = C.c_void_p()
+        if path is not None:
+            rc = self.L.gb_lw_mlp_load(ctx.h, path.encode(), C.byref(h))
+        else:
+            rc = self.L.gb_lw_mlp_create(ctx.h, seed, C.byref(h))
+        _check(self.L, ctx.h, rc)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gb_lw_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ok(self, rc):
+        _check(self.L, self.ctx.h, rc)
+
+    def save(self, path: str) -> None:
+        self._ok(self.L.gb_lw_mlp_save(self.h, path.encode()))
+
+    def params(self):
+        p = np.zeros(MLP_NPARAM, dtype=np.float32)
+        n = np.zeros(MLP_NNORM, dtype=np.float32)
+        self._ok(self.L.gb_lw_mlp_get_params(self.h, _ptr(p), _ptr(n)))
+        return p, n
+
+    def set_params(self, params=None, norm=None) -> None:
+        p = None if params is None else np.ascontiguousarray(params, dtype=np.float32)
+        n = None if norm is None else np.ascontiguousarray(norm, dtype=np.float32)
+        self._ok(self.L.gb_lw_mlp_set_params(self.h, _ptr(p), _ptr(n)))
+
+    def set_loss_weights(self, w) -> None:
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        self._ok(self.L.gb_lw_mlp_set_loss_weights(self.h, _ptr(w)))
+
+    def samples(self, grid: GridDesc, feat, tau, frac, stream=None) -> None:
+        self._ok(self.L.gb_lw_mlp_samples(self.ctx.h, _ptr(stream or 0), C.byref(grid), _ptr(feat), _ptr(tau),
+                                          _ptr(frac)))
+
+    def fit_norm(self, rows: int, feat, tau, frac, stream=None) -> None:
+        self._ok(self.L.gb_lw_mlp_fit_norm(self.h, _ptr(stream or 0), rows, _ptr(feat), _ptr(tau), _ptr(frac)))
+
+    def prepare(self, rows: int, feat, tau, frac, x, t, stream=None) -> None:
+        self._ok(self.L.gb_lw_mlp_prepare(self.h, _ptr(stream or 0), rows, _ptr(feat), _ptr(tau), _ptr(frac),
+                                          _ptr(x), _ptr(t)))
+
+    def gradients(self, rows: int, x, t, grad, loss, stream=None) -> None:
+        self._ok(self.L.gb_lw_mlp_gradients(self.h, _ptr(stream or 0), rows, _ptr(x), _ptr(t), _ptr(grad),
+                                            _ptr(loss)))
+
+    def train_step(self, rows: int, x, t, lr: float, loss=None, stream=None) -> None:
+        self._ok(self.L.gb_lw_mlp_train_step(self.h, _ptr(stream or 0), rows, _ptr(x), _ptr(t), lr, _ptr(loss)))
+
+    def forward(self, rows: int, x, y, stream=None) -> None:
+        self._ok(self.L.gb_lw_mlp_forward(self.h, _ptr(stream or 0), rows, _ptr(x), _ptr(y)))
+
+    def infer(self, grid: GridDesc, tau, frac, flag, stream=None) -> None:
+        self._ok(self.L.gb_lw_mlp_infer(self.h, _ptr(stream or 0), C.byref(grid), _ptr(tau), _ptr(frac), _ptr(flag)))
+
+    def batch(self, grids, stream=None) -> None:
+        """gb_rrtmg_lw_batch_surrogate: all grids with learned gas optics."""
+        n, arr = Context._grids(grids)
+        self._ok(self.L.gb_rrtmg_lw_batch_surrogate(self.ctx.h, _ptr(stream or 0), n, arr, self.h))

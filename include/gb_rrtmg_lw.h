@@ -204,6 +204,12 @@ typedef struct gb_lw_grid {
   const double *reicmcl, *relqmcl;
   double *uflx, *dflx, *hr, *uflxc, *dflxc, *hrc, *duflx_dt, *duflxc_dt;
   int* d_col_status; /* optional, ncol ints */
+  /* optional learned gas optics (gb_lw_mlp_infer): taug and Planck fractions
+   * [(icol*nlay + lay)*140 + g] and a per-layer flag [icol*nlay + lay]; layers
+   * whose flag is 0 (inputs outside the network's training range) use taumol.
+   * NULL: taumol everywhere. */
+  const float *sur_tau, *sur_frac;
+  const uint8_t* sur_flag;
 } gb_lw_grid;
 
 /* Launch shape of the batched kernel: compiled variant (threads per column
@@ -244,6 +250,72 @@ int gb_rrtmg_lw_batch_graph_create(gb_lw_context* ctx, int ngrid, const gb_lw_gr
                                    gb_lw_graph** graph);
 int gb_rrtmg_lw_graph_launch(gb_lw_graph* graph, void* stream);
 int gb_rrtmg_lw_graph_destroy(gb_lw_graph* graph);
+
+/* ---------------------------------------------------------------------------
+ * Learned gas optics (no counterpart in the reference): a small MLP that maps
+ * per-layer state to the 140 g-point gas optical depths and Planck fractions
+ * that taumol (rrtmg_lw_taumol.f90) computes, used in place of taumol for
+ * layers inside its training range and trained on this library's own taumol.
+ *   features (9 per layer): log p, T, log column H2O, O3, CO2, CH4, N2O
+ *     (molecules cm-2 * 1e-20, as setcoef forms them), log layer pressure
+ *     thickness, temperature of the layer's lower boundary level;
+ *   network: 9 -> 128 -> 128 -> 128 -> 280, SiLU, bf16 weights and
+ *     activations, fp32 accumulation on the tensor cores;
+ *   outputs: standardised log taug (140) and Planck fractions (140).
+ * Device arrays are row-major; "rows" index (column, layer) pairs as
+ * icol*nlay + lay.  Parameters are exchanged as GB_LW_MLP_NPARAM floats
+ * (W1[16][128] b1 W2[128][128] b2 W3[128][128] b3 W4[128][288] b4), the
+ * normalisation as GB_LW_MLP_NNORM floats (in_mu[16] in_sd[16] in_lo[9]
+ * in_hi[9] out_mu[288] out_sd[288]). */
+#define GB_LW_MLP_NPARAM 72352
+#define GB_LW_MLP_NNORM 626
+typedef struct gb_lw_mlp gb_lw_mlp;
+
+/* New network with seeded random weights on the context's device. */
+int gb_lw_mlp_create(gb_lw_context* ctx, uint64_t seed, gb_lw_mlp** mlp);
+int gb_lw_mlp_destroy(gb_lw_mlp* mlp);
+int gb_lw_mlp_save(gb_lw_mlp* mlp, const char* path);
+int gb_lw_mlp_load(gb_lw_context* ctx, const char* path, gb_lw_mlp** mlp);
+/* Host copies of the fp32 parameters / normalisation (either may be NULL). */
+int gb_lw_mlp_get_params(gb_lw_mlp* mlp, float* params, float* norm);
+int gb_lw_mlp_set_params(gb_lw_mlp* mlp, const float* params, const float* norm);
+/* Weight of each of the 280 outputs in the training loss (default 1). */
+int gb_lw_mlp_set_loss_weights(gb_lw_mlp* mlp, const float* w280);
+
+/* Training samples from the plain taumol of one grid (device arrays as in
+ * gb_lw_grid; the grid's flux outputs are overwritten): raw features
+ * d_feat[rows][9], taug d_tau[rows][140] and Planck fractions
+ * d_frac[rows][140], rows = ncol*nlay. */
+int gb_lw_mlp_samples(gb_lw_context* ctx, void* stream, const gb_lw_grid* grid, float* d_feat, float* d_tau,
+                      float* d_frac);
+/* Fits the input/output standardisation and the validity range (min/max of
+ * every feature) on a sample set. */
+int gb_lw_mlp_fit_norm(gb_lw_mlp* mlp, void* stream, int64_t rows, const float* d_feat, const float* d_tau,
+                       const float* d_frac);
+/* Network inputs d_x (bf16 [rows][16]) and targets d_t (fp32 [rows][288],
+ * may be NULL) from samples. */
+int gb_lw_mlp_prepare(gb_lw_mlp* mlp, void* stream, int64_t rows, const float* d_feat, const float* d_tau,
+                      const float* d_frac, void* d_x, float* d_t);
+/* Loss (mean weighted square error of the standardised outputs) and its
+ * gradient w.r.t. every parameter (d_grad: GB_LW_MLP_NPARAM floats, NULL =
+ * internal) for one batch; rows must be a multiple of 8. */
+int gb_lw_mlp_gradients(gb_lw_mlp* mlp, void* stream, int64_t rows, const void* d_x, const float* d_t,
+                        float* d_grad, float* d_loss);
+/* One Adam step (beta 0.9/0.999) on one batch. */
+int gb_lw_mlp_train_step(gb_lw_mlp* mlp, void* stream, int64_t rows, const void* d_x, const float* d_t, float lr,
+                         float* d_loss);
+/* Standardised outputs d_y[rows][288] of the training forward pass. */
+int gb_lw_mlp_forward(gb_lw_mlp* mlp, void* stream, int64_t rows, const void* d_x, float* d_y);
+/* Inference for one grid: taug and Planck fractions [(icol*nlay + lay)*140 + g]
+ * and the per-layer flag (1 inside the training range) for gb_lw_grid's
+ * sur_* fields. */
+int gb_lw_mlp_infer(gb_lw_mlp* mlp, void* stream, const gb_lw_grid* grid, float* d_tau, float* d_frac,
+                    uint8_t* d_flag);
+/* gb_rrtmg_lw_batch_device with learned gas optics: inference for every grid
+ * into context buffers (1121 bytes per column-layer), then the one batched
+ * launch; out-of-range layers use taumol. */
+int gb_rrtmg_lw_batch_surrogate(gb_lw_context* ctx, void* stream, int ngrid, const gb_lw_grid* grids,
+                                gb_lw_mlp* mlp);
 
 /* Human-readable text of a status code (static storage). */
 const char* gb_rrtmg_lw_strerror(int code);

@@ -1,0 +1,140 @@
+"""Learned gas optics on the GPU: the hand-written training kernels against
+the CPU restatement (oracle/mlp_oracle.py), the inference kernel against the
+training forward pass, training on plain-taumol layers, and the per-layer
+fallback to taumol."""
+import numpy as np
+import pytest
+
+import mlp_oracle as M
+from brams_gb300 import rrtmg_lw as R
+from brams_gb300 import surrogate as S
+from brams_gb300.profiles import ProfileSpec, make_state
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def _rand_batch(rows, seed):
+    rs = np.random.default_rng(seed)
+    x = np.zeros((rows, 16), dtype=np.float32)
+    x[:, :9] = rs.normal(size=(rows, 9))
+    x = M.bf16(x)
+    t = np.zeros((rows, 288), dtype=np.float32)
+    t[:, :280] = rs.normal(size=(rows, 280))
+    return x, t
+
+
+def _dev_bf16(x):
+    torch = _torch()
+    return torch.from_numpy(x).cuda().to(torch.bfloat16)
+
+
+def test_gradients_match_cpu_oracle(ctx):
+    torch = _torch()
+    mlp = R.Mlp(ctx, seed=11)
+    p, _ = mlp.params()
+    rows = 256
+    x, t = _rand_batch(rows, 5)
+    grad = torch.zeros(R.MLP_NPARAM, dtype=torch.float32, device="cuda")
+    loss = torch.zeros(1, dtype=torch.float32, device="cuda")
+    mlp.gradients(rows, _dev_bf16(x), torch.from_numpy(t).cuda(), grad, loss)
+    torch.cuda.synchronize()
+    g_gpu = grad.cpu().numpy().astype(np.float64)
+    l_ref, g_ref = M.forward_backward(p, x, t, emulate=True)
+    assert abs(loss.item() - l_ref) <= 1e-4 * l_ref
+    G, Gr = M.unpack(g_gpu), M.unpack(g_ref)
+    for k in G:
+        scale = np.abs(Gr[k]).max()
+        err = np.abs(G[k] - Gr[k]).max()
+        assert err <= 2e-2 * scale + 1e-12, (k, err, scale)
+    # and against the float64 network without bf16 rounding (looser)
+    _, g64 = M.forward_backward(p, x.astype(np.float64), t.astype(np.float64), emulate=False)
+    assert np.abs(g_gpu - g64).max() <= 0.1 * np.abs(g64).max()
+
+
+def test_forward_outputs_match_cpu(ctx):
+    torch = _torch()
+    mlp = R.Mlp(ctx, seed=12)
+    p, _ = mlp.params()
+    rows = 64
+    x, t = _rand_batch(rows, 6)
+    y = torch.zeros((rows, 288), dtype=torch.float32, device="cuda")
+    mlp.forward(rows, _dev_bf16(x), y)
+    P = M.unpack(p)
+    a = x.astype(np.float32)
+    for l in (1, 2, 3):
+        a = M.bf16(M.silu(a @ M.bf16(P[f"W{l}"].astype(np.float32)) + P[f"b{l}"].astype(np.float32)))
+    ref = a @ M.bf16(P["W4"].astype(np.float32)) + P["b4"].astype(np.float32)
+    got = y.cpu().numpy()
+    assert np.abs(got - ref).max() <= 1e-2 * (np.abs(ref).max() + 1.0)
+
+
+@pytest.fixture(scope="module")
+def trained(ctx):
+    """A network trained briefly on plain-taumol layers (small set)."""
+    mlp, info = S.train(ctx, n_layers=120_000, epochs=6, batch=4096, lr=3e-3, seed=3, log=lambda *a: None)
+    return mlp, info
+
+
+def test_training_reduces_loss(trained):
+    _, info = trained
+    h = info["loss"]
+    assert h[-1] < 0.5 * h[0], h
+    assert np.isfinite(h).all()
+
+
+def test_inference_kernel_matches_training_forward(ctx, trained):
+    torch = _torch()
+    mlp, _ = trained
+    spec = ProfileSpec(ncol=40, nlay=45, seed=77, t_noise=4.0, h2o_sigma=0.5)
+    g = S.DeviceGrid(make_state(spec))
+    rows = 40 * 45
+    tau = torch.zeros((rows, 140), dtype=torch.float32, device="cuda")
+    frac = torch.zeros((rows, 140), dtype=torch.float32, device="cuda")
+    flag = torch.zeros(rows, dtype=torch.uint8, device="cuda")
+    mlp.infer(g.desc(), tau, frac, flag)
+    # same layers through the training path
+    feat = torch.zeros((rows, 9), dtype=torch.float32, device="cuda")
+    t0 = torch.zeros((rows, 140), dtype=torch.float32, device="cuda")
+    f0 = torch.zeros((rows, 140), dtype=torch.float32, device="cuda")
+    mlp.samples(g.desc(icld=0), feat, t0, f0)
+    x = torch.zeros((rows, 16), dtype=torch.bfloat16, device="cuda")
+    mlp.prepare(rows, feat, t0, f0, x, None)
+    y = torch.zeros((rows, 288), dtype=torch.float32, device="cuda")
+    mlp.forward(rows, x, y)
+    _, norm = mlp.params()
+    mu, sd = norm[50:338], norm[338:626]
+    yv = y.cpu().numpy() * sd + mu
+    ok = flag.cpu().numpy() == 1
+    assert ok.mean() > 0.9
+    got_tau, got_frac = tau.cpu().numpy(), frac.cpu().numpy()
+    assert np.abs(np.log(got_tau[ok]) - yv[ok, :140]).max() <= 1e-3 * (np.abs(yv[:, :140]).max() + 1)
+    assert np.abs(got_frac[ok] - yv[ok, 140:280]).max() <= 1e-3
+
+
+def test_out_of_range_layers_fall_back_to_taumol(ctx, trained):
+    """A column whose every layer lies outside the training range must give
+    exactly the plain solver's result; in-range columns use the network."""
+    torch = _torch()
+    mlp, _ = trained
+    spec = ProfileSpec(ncol=24, nlay=45, seed=78, t_noise=4.0, h2o_sigma=0.5)
+    st = make_state(spec)
+    st["tlay"][:3] += 200.0  # every layer far outside the training temperatures
+    st["tlev"][:3] += 200.0
+    import pyoracle
+
+    tauc = pyoracle.cldprop_columns(st)
+    g1, g2 = S.DeviceGrid(st, tauc), S.DeviceGrid(st, tauc)
+    ctx.rrtmg_lw_batch_device([g1.desc(seed0=5)])
+    mlp.batch([g2.desc(seed0=5)])
+    torch.cuda.synchronize()
+    a, b = g1.outputs(), g2.outputs()
+    for k in a:
+        assert np.array_equal(a[k][:3], b[k][:3]), k
+    assert not np.array_equal(a["uflx"][3:], b["uflx"][3:])
+    assert ctx.sync_status() == 0
