@@ -1,20 +1,39 @@
 """Benchmark of the GB300 RRTMG_LW column solver.
 
-One step = one pass of rrtmg_lw over the 360x300-column, 45-layer BRAMS-scale
-workload (108,000 columns, McICA sub-columns with seed = base + column index,
-FP32 gas optics and transfer with FP64 flux accumulation and heating rates).
+Headline workload (the metric's own configuration): 2048x1024 columns x 60
+layers (pressure 1000 -> 5 hPa) x 4 ensemble members = 8,388,608 columns in
+all, McICA clouds generated in the kernel (icld 3, seed = base + column), FP32
+transfer with FP64 heating rates.  One step solves every column once by:
 
-  value  -- columns/s of the kernel on device-resident inputs
-            (gb_rrtmg_lw_device, inputs already in HBM; 23 GB of inputs per
-            step, far larger than the 129 MB L2, so no L2 flush is needed)
-  e2e    -- columns/s through the reference-facing C ABI gb_rrtmg_lw with
-            page-locked HOST buffers: host->device copies, kernel and
-            device->host copies inside the timed region
-  roofline -- the kernel's achieved algorithmic bandwidth against the
-            measured HBM copy bandwidth; algorithmic bytes per column are
-            8*(600*nlay + 25) (every rrtmg_lw input and output once)
+  surrogate  -- the learned gas optics (brams_gb300/data/lw_mlp.gbmlp) with
+                per-layer fallback to taumol: per chunk of columns the MLP
+                inference kernel, then one batched launch of the column
+                kernel over the four members;
+  plain      -- taumol: one batched launch of the column kernel over the four
+                members (no learned part).
+
+  value        -- columns/s of the surrogate path, inputs resident in HBM
+                  (~90 GB per step, far larger than the 129 MB L2: no flush)
+  plain_gpu    -- columns/s of the plain path on the same inputs; speedup
+  accuracy     -- heating-rate RMSE of both paths against the FP64 oracle on
+                  a contiguous sample of member 0's columns
+  e2e          -- the surrogate path with every step's inputs copied from
+                  page-locked host memory chunk by chunk and every output read
+                  back (host data: the generator tile, streamed for every chunk)
+  roofline     -- the column kernel (the dominant kernel) against the
+                  measured HBM copy bandwidth, with the algorithmic bytes of
+                  the fused-cloud, learned-gas-optics mode
+  plain_abi    -- the drop-in path on the 360x300x45 BRAMS-scale workload:
+                  gb_rrtmg_lw_device on the reference's (140, ncol, nlay)
+                  McICA arrays, its roofline against 8*(600*nlay + 25) bytes
+                  per column, and gb_rrtmg_lw with page-locked host buffers
   cpu_baseline -- the FP64 oracle (C++ restatement of the reference) on the
-            host cores, on a bounded sample of the same columns
+                  host cores, on a bounded sample of the headline workload
+
+Inputs: a 131,072-column tile from the seeded generator (T noise N(0, 4 K),
+H2O x lognormal(0, 0.5)) is replicated to the 2048x1024 grid with a fresh
+T + N(0, 1 K), H2O x lognormal(0, 0.2) perturbation per replica, and each
+ensemble member perturbs T and H2O again the same way.
 
 ``--impl reference`` times the CPU implementation alone (the reference's
 Fortran cannot be built on this machine; its C++ restatement is timed instead).
@@ -37,8 +56,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "LW columns/s, surrogate vs plain GPU, at <=0.1 K/day heating-rate RMSE"
-NCOL, NLAY, PTOP = 360 * 300, 45, 10.0
+NCOL, NLAY, PTOP = 360 * 300, 45, 10.0          # drop-in block (BRAMS operational scale)
+NX, NY, NMEM, NLAY5, PTOP5 = 2048, 1024, 4, 60, 5.0  # headline workload
+TILE = 131072                                    # generator tile replicated over the grid
+CHUNK = 65536                                    # columns per member per surrogate call
 BASE_SEED = 1
+SAMPLE = 2048                                    # oracle columns for the accuracy check
 
 
 def abi_bytes_per_column(nlay: int) -> int:
@@ -159,45 +182,165 @@ def cpu_baseline(st, mc, max_seconds: float = 12.0):
 
 
 def reference_arm(args, rank, world):
-    """--impl reference: the CPU implementation alone, all host threads."""
+    """--impl reference: the CPU implementation alone (FP64 C++ restatement of
+    the reference, all host threads) on columns of the headline workload."""
     if rank != 0:
         return
-    st, tauc = make_inputs(NCOL, NLAY, BASE_SEED)
+    from brams_gb300.profiles import ProfileSpec, make_state
+    from brams_gb300.tables_io import read_tables
+
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
     pyoracle.build(native=True)
     cores = os.cpu_count() or 1
-    n = min(NCOL, 2048 * cores // 4)
-    s = {k: np.asfortranarray(v[:n]) for k, v in st.items()}
-    mc = pyoracle.mcica_per_column(s, np.asfortranarray(tauc[:, :n]), icld=3, base_seed=BASE_SEED)
+    n = max(256, 256 * cores)
+    st = make_state(ProfileSpec(ncol=n, nlay=NLAY5, seed=BASE_SEED, ptop=PTOP5, t_noise=4.0, h2o_sigma=0.5))
+    tabs = read_tables(os.path.join(ROOT, "brams_gb300", "data", "lw_ref_tables.gblw"))
+    tauc = cldprop_numpy(st, tabs)
+    mc = pyoracle.mcica_per_column(st, tauc, icld=3, base_seed=BASE_SEED)
     for _ in range(args.warmup):
-        pyoracle.rrtmg_lw(s, mc, nthreads=cores, native=True)
+        pyoracle.rrtmg_lw(st, mc, nthreads=cores, native=True)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        pyoracle.rrtmg_lw(s, mc, nthreads=cores, native=True)
+        pyoracle.rrtmg_lw(st, mc, nthreads=cores, native=True)
     dt = (time.perf_counter() - t0) / args.steps
     v = n / dt
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "columns/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "rrtmg_lw 360x300 columns x 45 layers (sample per step)", "columns_per_step": n,
-                       "nlay": NLAY, "icld": 3, "idrv": 1},
+            "config": {"workload": f"rrtmg_lw on {n} columns per step of the {NX}x{NY} x {NLAY5}-layer "
+                                   f"({NMEM}-member) workload", "columns_per_step": n, "nlay": NLAY5, "icld": 3,
+                       "idrv": 1},
             "cpu_baseline": {"value": v, "unit": "columns/s", "cores": cores, "kind": "port",
-                             "sample": f"{n} columns per step of the 360x300x45 workload"},
+                             "sample": f"{n} columns per step, {cores} threads; McICA sub-columns made beforehand"},
             "e2e": {"value": v, "unit": "columns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
 # --------------------------------------------------------------------------- GPU arm
-def traffic_from_profiles():
-    path = os.path.join(ROOT, "profiles", "lw_column_kernel_c2_traffic.txt")
+def traffic_from_profiles(name):
+    path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
         return None
     for line in open(path):
         if line.startswith("dram_bytes_per_launch_full_workload:"):
             return float(line.split(":")[1])
     return None
+
+
+def fused_bytes_per_column(nlay: int, learned: bool) -> int:
+    """Algorithmic bytes of the fused-cloud column kernel: every layer input
+    (12 gas/state + cldfrac, ciwp, clwp, 2 radii, 16 aerosol, 16 tauc = 49 per
+    layer), plev/tlev, tsfc, 16 emis, the 140 McICA draws and every output once;
+    with the learned gas optics also the network's 280 fp32 outputs and flag
+    per layer."""
+    b = 8 * (49 * nlay + 2 * (nlay + 1) + 17) + 8 * GB_NGPT + 8 * (6 * (nlay + 1) + 2 * nlay)
+    if learned:
+        b += nlay * (280 * 4 + 1)
+    return b
+
+
+GB_NGPT = 140
+
+
+class Workload:
+    """Device arrays of the headline workload: a base grid shared by the
+    members (pressure, gases, clouds, emissivity, aerosol, tauc) and per-member
+    T/H2O and outputs, Fortran layout with leading dimension nbase."""
+
+    SHARED = ("play", "plev", "tlev", "tsfc", "o3vmr", "co2vmr", "ch4vmr", "n2ovmr", "o2vmr", "cfc11vmr",
+              "cfc12vmr", "cfc22vmr", "ccl4vmr", "emis", "tauaer", "cldfrac", "ciwp", "clwp", "rei", "rel", "tauc")
+
+    def __init__(self, dev, nbase, nlay, nmem, seed, tile=TILE):
+        import torch
+        from brams_gb300.profiles import ProfileSpec, make_state
+        from brams_gb300.tables_io import read_tables
+
+        self.nbase, self.nlay, self.nmem, self.seed = nbase, nlay, nmem, seed
+        tile = min(tile, nbase)
+        st = make_state(ProfileSpec(ncol=tile, nlay=nlay, seed=seed, ptop=PTOP5, t_noise=4.0, h2o_sigma=0.5))
+        tabs = read_tables(os.path.join(ROOT, "brams_gb300", "data", "lw_ref_tables.gblw"))
+        st["tauc"] = cldprop_numpy(st, tabs)
+        self.tile = st
+        g = torch.Generator(device=dev)
+        g.manual_seed(seed)
+        rep = (nbase + tile - 1) // tile
+
+        def up(a):  # Fortran (tile, ...) -> device tensor with memory order = Fortran (nbase, ...)
+            t = torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=np.float64).T)).to(dev)
+            return torch.cat([t] * rep, dim=-1)[..., :nbase].contiguous()
+
+        d = {k: up(st[k]) for k in self.SHARED if k != "tauc"}
+        tc = torch.from_numpy(np.ascontiguousarray(np.asarray(st["tauc"]).T)).to(dev)  # (nlay, tile, 16)
+        d["tauc"] = torch.cat([tc] * rep, dim=1)[:, :nbase, :].contiguous()
+        tl, hv = up(st["tlay"]), up(st["h2ovmr"])
+        # one perturbation per replica of the tile ...
+        tl += torch.randn(tl.shape, generator=g, device=dev, dtype=torch.float64)
+        hv *= torch.exp(0.2 * torch.randn(hv.shape, generator=g, device=dev, dtype=torch.float64))
+        self.d = d
+        self.mem = []
+        for m in range(nmem):  # ... and one per member
+            t = tl + torch.randn(tl.shape, generator=g, device=dev, dtype=torch.float64)
+            h = (hv * torch.exp(0.2 * torch.randn(hv.shape, generator=g, device=dev, dtype=torch.float64))).clamp_(3.0e-6, 0.05)
+            o = {k: torch.zeros((nlay + 1, nbase), dtype=torch.float64, device=dev)
+                 for k in ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt")}
+            o["hr"] = torch.zeros((nlay, nbase), dtype=torch.float64, device=dev)
+            o["hrc"] = torch.zeros((nlay, nbase), dtype=torch.float64, device=dev)
+            self.mem.append({"tlay": t, "h2ovmr": h, **o})
+        del tl, hv
+
+    def seed0(self, m):
+        return self.seed * 1000003 + m * self.nbase
+
+    def desc(self, m, c0=0, n=None, **extra):
+        """Grid descriptor of member m, columns c0 .. c0+n-1 (pointer offsets, leading dimension nbase)."""
+        from brams_gb300 import rrtmg_lw as R
+
+        n = self.nbase - c0 if n is None else n
+        arrays = {}
+        for k, t in list(self.d.items()) + list(self.mem[m].items()):
+            arrays[k] = t.data_ptr() + 8 * c0 * (16 if k == "tauc" else 1)
+        arrays["reicmcl"], arrays["relqmcl"] = arrays["rei"], arrays["rel"]
+        arrays.update(extra)
+        return R.grid_desc(n, self.nlay, arrays, icld=3, cloud_mode=R.CLOUD_FUSED, seed0=self.seed0(m) + c0,
+                           ld_in=self.nbase, ld_out=self.nbase)
+
+    def host_columns(self, m, c0, n):
+        """Inputs of member m, columns c0 .. c0+n-1, as Fortran numpy arrays (for the oracle)."""
+        out = {}
+        for k, t in list(self.d.items()) + [(k, self.mem[m][k]) for k in ("tlay", "h2ovmr")]:
+            if k == "tauc":
+                out[k] = np.asfortranarray(t[:, c0:c0 + n, :].cpu().numpy().T)
+            else:
+                out[k] = np.asfortranarray(t[..., c0:c0 + n].cpu().numpy().T)
+        return out
+
+    def outputs(self, m, c0, n):
+        return {k: np.asfortranarray(self.mem[m][k][:, c0:c0 + n].cpu().numpy().T) for k in
+                ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt", "hr", "hrc")}
+
+
+def surrogate_step(ctx, mlp, wl, bufs, stream, ev=None):
+    """One step of the learned path: per chunk, inference for the members then one batched column launch."""
+    tau, frac, flag = bufs
+    nch = 0
+    for c0 in range(0, wl.nbase, CHUNK):
+        n = min(CHUNK, wl.nbase - c0)
+        grids = []
+        for m in range(wl.nmem):
+            r0 = m * CHUNK * wl.nlay
+            sur = dict(sur_tau=tau[r0:].data_ptr(), sur_frac=frac[r0:].data_ptr(), sur_flag=flag[r0:].data_ptr())
+            g = wl.desc(m, c0, n)
+            mlp.infer(g, sur["sur_tau"], sur["sur_frac"], sur["sur_flag"], stream=stream)
+            grids.append(wl.desc(m, c0, n, **sur))
+        if ev is not None:
+            ev[nch][0].record()
+        ctx.rrtmg_lw_batch_device(grids, stream=stream)
+        if ev is not None:
+            ev[nch][1].record()
+        nch += 1
+    return nch
 
 
 def gpu_arm(args, rank, world):
@@ -207,19 +350,251 @@ def gpu_arm(args, rank, world):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     from brams_gb300.build import build
-    from brams_gb300.rrtmg_lw import Context, OUT_ORDER, STATE_ORDER
+    from brams_gb300 import rrtmg_lw as R
+    from brams_gb300 import surrogate as S
 
     if rank == 0 or world == 1:
         build()
     if world > 1:
         torch.distributed.barrier()
         build()
-    ctx = Context(device=local)
-    ncol, nlay = args.ncol, NLAY
+    ctx = R.Context(device=local)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        peaks = json.load(open(pk))
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+
+    # ---------------- the learned gas optics
+    wpath = S.DEFAULT_WEIGHTS
+    if os.path.exists(wpath):
+        mlp = R.Mlp(ctx, path=wpath)
+        trained = "loaded " + os.path.relpath(wpath, ROOT)
+    else:
+        mlp, info = S.train(ctx, log=lambda *a: None)
+        trained = f"trained in this run ({info['train_s']:.1f} s on {info['rows']} layers)"
+
+    # ---------------- headline workload
+    nbase = args.nbase
+    seed = BASE_SEED + rank * 7919
+    wl = Workload(dev, nbase, NLAY5, NMEM, seed)
+    ncol = nbase * NMEM
+    rows = CHUNK * NLAY5 * NMEM
+    bufs = (torch.empty((rows, GB_NGPT), dtype=torch.float32, device=dev),
+            torch.empty((rows, GB_NGPT), dtype=torch.float32, device=dev),
+            torch.empty(rows, dtype=torch.uint8, device=dev))
+    plain = lambda: ctx.rrtmg_lw_batch_device([wl.desc(m) for m in range(NMEM)], stream=stream)
+    sur = lambda ev=None: surrogate_step(ctx, mlp, wl, bufs, stream, ev)
+    torch.cuda.synchronize()
+
+    def timed(fn, steps, evs=False):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        return e0.elapsed_time(e1) / 1e3 / steps
+
+    for _ in range(args.warmup):
+        plain()
+    t_plain = timed(plain, args.steps)
+    plain_out = wl.outputs(0, nbase // 2, SAMPLE)
+    for _ in range(args.warmup):
+        sur()
+    if ctx.sync_status(stream) != 0:
+        raise RuntimeError("column status nonzero on the benchmark inputs")
+    nch = (nbase + CHUNK - 1) // CHUNK
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nch * args.steps)]
+    with ClockSampler(local) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        e0.record()
+        for k in range(args.steps):
+            sur(ev[k * nch:(k + 1) * nch])
+        e1.record()
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+    t_sur = e0.elapsed_time(e1) / 1e3 / args.steps
+    t_kernel = sum(a.elapsed_time(b) for a, b in ev) / 1e3 / len(ev)  # one column-kernel launch (with its draws)
+    status = ctx.sync_status(stream)
+    sur_out = wl.outputs(0, nbase // 2, SAMPLE)
+    launches_per_step = nch * (2 * NMEM + 1)  # per chunk: inference and McICA draws per member, one column kernel
+
+    # ---------------- accuracy against the FP64 oracle
+    acc = {}
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+
+        pyoracle.build(native=True)
+        c0 = nbase // 2
+        st = wl.host_columns(0, c0, SAMPLE)
+        mc = pyoracle.mcica_per_column(st, st["tauc"], icld=3, base_seed=wl.seed0(0) + c0)
+        ref = pyoracle.rrtmg_lw(st, mc, nthreads=os.cpu_count() or 1, native=True)
+        for name, o in (("surrogate", sur_out), ("plain", plain_out)):
+            acc[name] = {"hr_rmse_k_per_day": float(np.sqrt(np.mean((o["hr"] - ref["hr"]) ** 2))),
+                         "hr_max_k_per_day": float(np.abs(o["hr"] - ref["hr"]).max()),
+                         "flux_rmse_w_m2": float(np.sqrt(np.mean(np.concatenate(
+                             [(o[k] - ref[k]).ravel() ** 2 for k in ("uflx", "dflx")])))),
+                         "flux_max_w_m2": float(max(np.abs(o[k] - ref[k]).max() for k in ("uflx", "dflx")))}
+        acc["sample"] = f"{SAMPLE} contiguous columns of member 0 from column {c0}; FP64 oracle with the same seeds"
+
+    # ---------------- e2e: every step's inputs from page-locked host memory, outputs back
+    e2e = e2e_headline(ctx, mlp, wl, dev, stream, min(args.steps, 2), world, bufs)
+
+    # ---------------- drop-in block (ABI mode, 360x300x45)
+    abi = None if args.no_abi else abi_block(ctx, dev, stream, args, rank, world, hbm)
+
+    times = torch.tensor([t_sur, t_plain, t_kernel, e2e["t"]], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
+    t_sur, t_plain, t_kernel, t_e2e = (float(x) for x in times)
+    if rank != 0:
+        return
+    alg = fused_bytes_per_column(NLAY5, True) * NMEM * min(CHUNK, nbase)
+    achieved = alg / t_kernel / 1e9
+    line = {
+        "metric": METRIC, "value": world * ncol / t_sur, "unit": "columns/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_sur * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64acc (network bf16/fp32acc)", "data": "synthetic",
+        "config": {"workload": f"surrogate + batched at scale: {NX}x{NY} columns x {NLAY5} layers (1000 -> 5 hPa) "
+                               f"x {NMEM} ensemble members" if nbase == NX * NY else
+                               f"reduced: {nbase} columns x {NLAY5} layers x {NMEM} members",
+                   "columns_per_gpu": ncol, "nlay": NLAY5, "members": NMEM, "icld": 3, "idrv": 1,
+                   "clouds": "McICA generated in the kernel, MT19937 seed = base + column",
+                   "gas_optics": "learned (MLP, " + trained + "), taumol for layers outside the training range",
+                   "chunk_columns_per_member": CHUNK,
+                   "l2": "inputs (~90 GB per step) larger than L2; no flush",
+                   "precision": "fp32 transfer, fp64 flux sums and heating rates; network bf16 with fp32 accumulation"},
+        "plain_gpu": {"value": world * ncol / t_plain, "unit": "columns/s", "ms_per_step": t_plain * 1e3,
+                      "speedup_of_surrogate": t_plain / t_sur},
+        "accuracy": acc,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic_from_profiles("lw_batch_kernel_c5_traffic.txt"),
+                     "kernel": "lw_batch_kernel (learned gas optics, fused clouds), one launch = 4 members x "
+                               f"{min(CHUNK, nbase)} columns; alg bytes/column {fused_bytes_per_column(NLAY5, True)}",
+                     "alg_bytes_per_launch": alg, "launch_ms": t_kernel * 1e3,
+                     "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
+        "e2e": {"value": world * ncol / t_e2e, "unit": "columns/s", "h2d_bytes_per_step": e2e["h2d"],
+                "d2h_bytes_per_step": e2e["d2h"], "host_data": e2e["note"]},
+        "gpu_launches": launches_per_step * args.steps, "clocks": clk.summary(), "column_status": status,
+    }
+    if abi is not None:
+        line["plain_abi"] = abi
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline_headline(wl)
+    print(json.dumps(line), flush=True)
+
+
+def e2e_headline(ctx, mlp, wl, dev, stream, steps, world, bufs):
+    """Surrogate path with host-resident inputs: per chunk, every input array of
+    the four members is copied from page-locked host memory (the generator
+    tile's columns, stored chunk by chunk so that every copy is one contiguous
+    DMA), solved, and every output is copied back to page-locked memory."""
+    import torch
+    from brams_gb300 import rrtmg_lw as R
+
+    nlay, C = wl.nlay, min(CHUNK, wl.nbase)
+    tile = wl.tile
+    T = tile["play"].shape[0]
+    nt = max(1, T // C)
+    names = [k for k in wl.SHARED if k != "tauc"] + ["tlay", "h2ovmr"]
+    host = {}
+    for k in names:
+        a = np.ascontiguousarray(np.asarray(tile[k], dtype=np.float64).T)  # (..., T)
+        host[k] = [torch.from_numpy(np.ascontiguousarray(a[..., j * C:(j + 1) * C])).pin_memory() for j in range(nt)]
+    tc = np.ascontiguousarray(np.asarray(tile["tauc"]).T)  # (nlay, T, 16)
+    host["tauc"] = [torch.from_numpy(np.ascontiguousarray(tc[:, j * C:(j + 1) * C, :])).pin_memory() for j in range(nt)]
+    outs = ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt", "hr", "hrc")
+    stage = []
+    for m in range(wl.nmem):
+        d = {k: torch.empty(host[k][0].shape, dtype=torch.float64, device=dev) for k in host}
+        for k in outs:
+            d[k] = torch.empty((nlay + (0 if k in ("hr", "hrc") else 1), C), dtype=torch.float64, device=dev)
+        stage.append(d)
+    hout = {k: torch.empty((wl.nmem,) + tuple(stage[0][k].shape), dtype=torch.float64).pin_memory() for k in outs}
+    tau, frac, flag = bufs
+    counts = {"h2d": 0, "d2h": 0}
+
+    def step():
+        h2d = d2h = 0
+        for i, c0 in enumerate(range(0, wl.nbase, C)):
+            j = i % nt
+            grids = []
+            for m in range(wl.nmem):
+                d = stage[m]
+                for k in host:
+                    d[k].copy_(host[k][j], non_blocking=True)
+                    h2d += host[k][j].numel() * 8
+                arrays = dict(d)
+                arrays["reicmcl"], arrays["relqmcl"] = d["rei"], d["rel"]
+                r0 = m * C * nlay
+                g = R.grid_desc(C, nlay, arrays, icld=3, cloud_mode=R.CLOUD_FUSED, seed0=wl.seed0(m) + c0)
+                mlp.infer(g, tau[r0:].data_ptr(), frac[r0:].data_ptr(), flag[r0:].data_ptr(), stream=stream)
+                arrays.update(sur_tau=tau[r0:].data_ptr(), sur_frac=frac[r0:].data_ptr(), sur_flag=flag[r0:].data_ptr())
+                grids.append(R.grid_desc(C, nlay, arrays, icld=3, cloud_mode=R.CLOUD_FUSED, seed0=wl.seed0(m) + c0))
+            ctx.rrtmg_lw_batch_device(grids, stream=stream)
+            for m in range(wl.nmem):
+                for k in outs:
+                    hout[k][m].copy_(stage[m][k], non_blocking=True)
+                    d2h += stage[m][k].numel() * 8
+        torch.cuda.current_stream(dev).synchronize()
+        counts["h2d"], counts["d2h"] = h2d, d2h
+
+    step()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    t = (time.perf_counter() - t0) / steps
+    return {"t": t, "h2d": counts["h2d"], "d2h": counts["d2h"],
+            "note": f"every chunk copies all inputs of {wl.nmem} members x {C} columns from page-locked host memory "
+                    f"(the generator tile's columns) and reads all outputs back; {steps} timed steps"}
+
+
+def cpu_baseline_headline(wl):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    pyoracle.build(native=True)
+    cores = os.cpu_count() or 1
+    probe = 32 * cores
+    st = wl.host_columns(0, 0, probe)
+    mc = pyoracle.mcica_per_column(st, st["tauc"], icld=3, base_seed=wl.seed0(0))
+    t0 = time.perf_counter()
+    pyoracle.rrtmg_lw(st, mc, nthreads=cores, native=True)
+    dt = time.perf_counter() - t0
+    n = int(min(wl.nbase, max(probe, probe * 12.0 / max(dt, 1e-6))))
+    st = wl.host_columns(0, 0, n)
+    mc = pyoracle.mcica_per_column(st, st["tauc"], icld=3, base_seed=wl.seed0(0))
+    t0 = time.perf_counter()
+    pyoracle.rrtmg_lw(st, mc, nthreads=cores, native=True)
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "columns/s", "cores": cores, "kind": "port",
+            "sample": f"first {n} columns of member 0 of the {NX}x{NY}x{NLAY5} workload, one pass, {cores} threads, "
+                      "FP64 C++ restatement (-O3 native); McICA sub-columns made beforehand, not timed"}
+
+
+def abi_block(ctx, dev, stream, args, rank, world, hbm):
+    """Drop-in path: gb_rrtmg_lw_device on the reference's McICA arrays (360x300x45) and gb_rrtmg_lw on host buffers."""
+    import torch
+    from brams_gb300.rrtmg_lw import OUT_ORDER, STATE_ORDER
+
+    ncol, nlay = NCOL, NLAY
     seed = BASE_SEED + rank * 7919
     st, tauc = make_inputs(ncol, nlay, seed)
 
-    # device-resident inputs in the reference's Fortran layout
     def dev_f(a):
         return torch.from_numpy(np.ascontiguousarray(np.asarray(a).T)).to(dev)
 
@@ -232,7 +607,6 @@ def gpu_arm(args, rank, world):
         d[k] = torch.empty((nlay, ncol, 140), dtype=torch.float64, device=dev)
     d["reicmcl"] = torch.empty((nlay, ncol), dtype=torch.float64, device=dev)
     d["relqmcl"] = torch.empty((nlay, ncol), dtype=torch.float64, device=dev)
-    stream = torch.cuda.current_stream(dev).cuda_stream
     ctx.mcica_subcol_lw_device(ncol, nlay, d, icld=3, permuteseed=seed, irng=1, seed_per_column=True, stream=stream)
     for k in ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt"):
         d[k] = torch.empty((nlay + 1, ncol), dtype=torch.float64, device=dev)
@@ -245,96 +619,54 @@ def gpu_arm(args, rank, world):
 
     for _ in range(args.warmup):
         step()
-    if ctx.sync_status(stream) != 0:
-        raise RuntimeError("column status nonzero on the benchmark inputs")
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if world > 1:
-        torch.distributed.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        ev0.record()
-        for _ in range(args.steps):
-            step()
-        ev1.record()
-        torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    t_dev = ev0.elapsed_time(ev1) / 1e3 / args.steps
+    e0.record()
+    for _ in range(args.steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    t_dev = e0.elapsed_time(e1) / 1e3 / args.steps
     status = ctx.sync_status(stream)
-
-    # e2e through the host-pointer C ABI with page-locked host buffers
     host = {}
-    for k in list(STATE_ORDER) + ["tauaer", "cldfmcl", "ciwpmcl", "clwpmcl", "taucmcl", "reicmcl", "relqmcl"]:
-        t = d[k]
-        h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
-        h.copy_(t)
+    ins = list(STATE_ORDER) + ["tauaer", "cldfmcl", "ciwpmcl", "clwpmcl", "taucmcl", "reicmcl", "relqmcl"]
+    for k in ins:
+        h = torch.empty(d[k].shape, dtype=d[k].dtype, pin_memory=True)
+        h.copy_(d[k])
         host[k] = h
     for k in OUT_ORDER:
         host[k] = torch.empty(d[k].shape, dtype=torch.float64, pin_memory=True)
-    h2d = sum(host[k].numel() * 8 for k in list(STATE_ORDER) + ["tauaer", "cldfmcl", "ciwpmcl", "clwpmcl", "taucmcl", "reicmcl", "relqmcl"])
+    h2d = sum(host[k].numel() * 8 for k in ins)
     d2h = sum(host[k].numel() * 8 for k in OUT_ORDER)
     hp = {k: v.data_ptr() for k, v in host.items()}
-    rc = ctx.rrtmg_lw_host_ptrs(ncol, nlay, hp)
-    if rc != 0:
-        raise RuntimeError(f"gb_rrtmg_lw status {rc}")
-    e2e_steps = max(1, min(args.steps, 5))
-    if world > 1:
-        torch.distributed.barrier()
+    if ctx.rrtmg_lw_host_ptrs(ncol, nlay, hp) != 0:
+        raise RuntimeError("gb_rrtmg_lw status nonzero")
+    n = max(1, min(args.steps, 3))
     t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        rc = ctx.rrtmg_lw_host_ptrs(ncol, nlay, hp)
-    t_e2e = (time.perf_counter() - t0) / e2e_steps
-    # the host path must reproduce the device path bit for bit
+    for _ in range(n):
+        ctx.rrtmg_lw_host_ptrs(ncol, nlay, hp)
+    t_e2e = (time.perf_counter() - t0) / n
     same = bool(torch.equal(host["hr"].to(dev), d["hr"]) and torch.equal(host["uflx"].to(dev), d["uflx"]))
-
-    # cross-rank max of the per-step times
-    times = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
-    t_dev, t_e2e = float(times[0]), float(times[1])
-    if rank != 0:
-        return
-    peaks = {}
-    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(pk):
-        peaks = json.load(open(pk))
-    hbm = float(peaks.get("hbm_gbs", 6800.0))
     alg = abi_bytes_per_column(nlay) * ncol
     achieved = alg / t_dev / 1e9
-    traffic = traffic_from_profiles()
-    clocks = clk.summary()
-    line = {
-        "metric": METRIC, "value": world * ncol / t_dev, "unit": "columns/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_dev * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64acc", "data": "synthetic",
-        "config": {"workload": "rrtmg_lw plain GPU path, 360x300 columns x 45 layers (BRAMS operational scale)",
-                   "columns_per_gpu": ncol, "nlay": nlay, "icld": 3, "idrv": 1, "inflglw": 2, "iceflglw": 3,
-                   "liqflglw": 1, "mcica": "140 sub-columns, MT19937 seed = base + column",
-                   "l2": "inputs (23 GB per step) larger than L2; no flush", "precision":
-                   "fp32 gas optics and transfer, fp64 flux accumulation and heating rates"},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic, "alg_bytes_per_launch": alg,
-                     "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
-        "e2e": {"value": world * ncol / t_e2e, "unit": "columns/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "host_path_matches_device_path": same},
-        "gpu_launches": args.steps, "clocks": clocks, "column_status": status,
-    }
-    if not args.no_cpu:
-        mc_host = {k: host[k].numpy().T if host[k].dim() == 2 else np.transpose(host[k].numpy(), (2, 1, 0))
-                   for k in ("cldfmcl", "ciwpmcl", "clwpmcl", "taucmcl", "reicmcl", "relqmcl")}
-        mc_host = {k: np.asfortranarray(v) for k, v in mc_host.items()}
-        line["cpu_baseline"] = cpu_baseline(st, mc_host)
-    print(json.dumps(line), flush=True)
+    return {"workload": "rrtmg_lw drop-in (McICA arrays as the reference passes them), 360x300 columns x 45 layers",
+            "value": world * ncol / t_dev, "unit": "columns/s", "ms_per_step": t_dev * 1e3,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                         "traffic": traffic_from_profiles("lw_batch_kernel_c2_traffic.txt"), "alg_bytes_per_launch": alg},
+            "e2e": {"value": world * ncol / t_e2e, "unit": "columns/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "host_path_matches_device_path": same},
+            "column_status": status}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--ncol", type=int, default=NCOL)
-    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--nbase", type=int, default=NX * NY, help="base-grid columns (each of the 4 members)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the oracle accuracy check and the CPU baseline")
+    ap.add_argument("--no-abi", action="store_true", help="skip the 360x300x45 drop-in block")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
