@@ -387,6 +387,19 @@ def gpu_arm(args, rank, world):
     plain = lambda: ctx.rrtmg_lw_batch_device([wl.desc(m) for m in range(NMEM)], stream=stream)
     sur = lambda ev=None: surrogate_step(ctx, mlp, wl, bufs, stream, ev)
     torch.cuda.synchronize()
+    # launch shapes from the autotuner, for both kinds of batch, on a sample of the workload
+    if args.no_tune:
+        tuned = {"plain": ctx.tuning(NLAY5, R.KIND_FUSED), "learned": ctx.tuning(NLAY5, R.KIND_FUSED | R.KIND_LEARNED)}
+    else:
+        tuned = {"plain": ctx.autotune([wl.desc(m) for m in range(NMEM)], sample_cols=65536, reps=2, stream=stream)}
+        n0 = min(CHUNK, nbase)
+        g0 = []
+        for m in range(NMEM):
+            r0 = m * CHUNK * NLAY5
+            ex = dict(sur_tau=bufs[0][r0:].data_ptr(), sur_frac=bufs[1][r0:].data_ptr(), sur_flag=bufs[2][r0:].data_ptr())
+            mlp.infer(wl.desc(m, 0, n0), ex["sur_tau"], ex["sur_frac"], ex["sur_flag"], stream=stream)
+            g0.append(wl.desc(m, 0, n0, **ex))
+        tuned["learned"] = ctx.autotune(g0, sample_cols=65536, reps=2, stream=stream)
 
     def timed(fn, steps, evs=False):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -474,6 +487,9 @@ def gpu_arm(args, rank, world):
                    "clouds": "McICA generated in the kernel, MT19937 seed = base + column",
                    "gas_optics": "learned (MLP, " + trained + "), taumol for layers outside the training range",
                    "chunk_columns_per_member": CHUNK,
+                   "launch_shapes": {k: {f: v[f] for f in ("threads", "min_blocks", "blocks_per_sm")}
+                                     for k, v in tuned.items()},
+                   "inference": "tcgen05 (tensor memory accumulators)",
                    "l2": "inputs (~90 GB per step) larger than L2; no flush",
                    "precision": "fp32 transfer, fp64 flux sums and heating rates; network bf16 with fp32 accumulation"},
         "plain_gpu": {"value": world * ncol / t_plain, "unit": "columns/s", "ms_per_step": t_plain * 1e3,
@@ -667,6 +683,7 @@ def main():
     ap.add_argument("--nbase", type=int, default=NX * NY, help="base-grid columns (each of the 4 members)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the oracle accuracy check and the CPU baseline")
     ap.add_argument("--no-abi", action="store_true", help="skip the 360x300x45 drop-in block")
+    ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

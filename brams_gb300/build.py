@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libgb_rrtmg_lw.so")
-UNITS = ["lw_solver.cu", "lw_mcica.cu", "lw_capi.cu", "lw_tables.cpp", "lw_mlp.cu", "lw_mlp_capi.cu"]
+UNITS = ["lw_solver.cu", "lw_mcica.cu", "lw_capi.cu", "lw_tables.cpp", "lw_mlp.cu", "lw_mlp_capi.cu", "lw_mlp_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

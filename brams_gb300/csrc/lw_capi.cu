@@ -163,21 +163,47 @@ bool flags_ok(int idrv, int inflglw, int iceflglw, int liqflglw) {
          liqflglw >= 0 && liqflglw <= 1;
 }
 
-gb_lw_tuning default_tuning(gb_lw_context* ctx, int nlay) {
+// Kind of a batch for the tuned-shape table: bit 0 fused-cloud grids, bit 1 learned gas optics.
+int batch_kind(const LwBatch& b) {
+  int k = 0;
+  for (int i = 0; i < b.ngrid; ++i) {
+    if (b.g[i].cloud_mode == LW_CLOUD_FUSED && b.g[i].icld >= 1) k |= GB_LW_KIND_FUSED;
+    if (b.g[i].sur_flag) k |= GB_LW_KIND_LEARNED;
+  }
+  return k;
+}
+
+// Default shapes, measured on GB300 at 45 layers (108,000 columns): batches
+// that read the McICA sub-column arrays run best with four blocks per SM
+// (more L1 for the table gathers), fused-cloud batches with six.
+gb_lw_tuning default_tuning(gb_lw_context* ctx, int nlay, int kind) {
   gb_lw_tuning t{};
-  t.variant = 0;
-  t.threads = gb_lw_variant(0).threads;
-  t.min_blocks = gb_lw_variant(0).min_blocks;
-  t.blocks_per_sm = std::max(1, gb_lw_slots(nlay, 0) / std::max(1, ctx->num_sms));
+  t.variant = (kind & GB_LW_KIND_FUSED) ? 1 : 2;
+  t.threads = gb_lw_variant(t.variant).threads;
+  t.min_blocks = gb_lw_variant(t.variant).min_blocks;
+  const int occ = std::max(1, gb_lw_slots(nlay, t.variant) / std::max(1, ctx->num_sms));
+  t.blocks_per_sm = std::min(occ, t.min_blocks);
   t.blocks = t.blocks_per_sm * ctx->num_sms;
   t.ms = 0.0;
   return t;
 }
 
-gb_lw_tuning tuning_for(gb_lw_context* ctx, int nlay) {
+gb_lw_tuning tuning_for(gb_lw_context* ctx, int nlay, int kind) {
+  const int key = nlay * 4 + kind;
   for (size_t i = 0; i < ctx->tuned_nlay.size(); ++i)
-    if (ctx->tuned_nlay[i] == nlay) return ctx->tuned[i];
-  return default_tuning(ctx, nlay);
+    if (ctx->tuned_nlay[i] == key) return ctx->tuned[i];
+  return default_tuning(ctx, nlay, kind);
+}
+
+void store_tuning(gb_lw_context* ctx, int nlay, int kind, const gb_lw_tuning& t) {
+  const int key = nlay * 4 + kind;
+  for (size_t i = 0; i < ctx->tuned_nlay.size(); ++i)
+    if (ctx->tuned_nlay[i] == key) {
+      ctx->tuned[i] = t;
+      return;
+    }
+  ctx->tuned_nlay.push_back(key);
+  ctx->tuned.push_back(t);
 }
 
 int ensure_bscratch(gb_lw_context* ctx, int nlay, int blocks) {
@@ -282,7 +308,7 @@ int gb_ctx_make_draws(gb_lw_context* ctx, LwBatch& b, double* buf, cudaStream_t 
 int gb_ctx_launch_batch(gb_lw_context* ctx, LwBatch& b, cudaStream_t stream) {
   if (b.col0[b.ngrid] == 0) return GB_LW_OK;
   cudaSetDevice(ctx->device);
-  const gb_lw_tuning t = tuning_for(ctx, b.nsmax);
+  const gb_lw_tuning t = tuning_for(ctx, b.nsmax, batch_kind(b));
   int rc = ensure_bscratch(ctx, b.nsmax, t.blocks);
   if (rc) return rc;
   const size_t nd = gb_ctx_fused_draws(b);
@@ -722,17 +748,17 @@ int gb_rrtmg_lw_batch_device(gb_lw_context* ctx, void* stream, int ngrid, const 
   return gb_ctx_launch_batch(ctx, b, (cudaStream_t)stream);
 }
 
-int gb_rrtmg_lw_tuning_get(gb_lw_context* ctx, int nlay, gb_lw_tuning* out) {
-  if (!ctx || !out || nlay < 1 || nlay > GB_MAXLAY) return GB_LW_E_ARGS;
+int gb_rrtmg_lw_tuning_get(gb_lw_context* ctx, int nlay, int kind, gb_lw_tuning* out) {
+  if (!ctx || !out || nlay < 1 || nlay > GB_MAXLAY || kind < 0 || kind > 3) return GB_LW_E_ARGS;
   cudaSetDevice(ctx->device);
-  *out = tuning_for(ctx, nlay);
+  *out = tuning_for(ctx, nlay, kind);
   return GB_LW_OK;
 }
 
 int gb_rrtmg_lw_num_variants(void) { return gb_lw_num_variants(); }
 
-int gb_rrtmg_lw_tuning_set(gb_lw_context* ctx, int nlay, const gb_lw_tuning* shape) {
-  if (!ctx || !shape || nlay < 1 || nlay > GB_MAXLAY) return GB_LW_E_ARGS;
+int gb_rrtmg_lw_tuning_set(gb_lw_context* ctx, int nlay, int kind, const gb_lw_tuning* shape) {
+  if (!ctx || !shape || nlay < 1 || nlay > GB_MAXLAY || kind < 0 || kind > 3) return GB_LW_E_ARGS;
   if (shape->variant < 0 || shape->variant >= gb_lw_num_variants()) return GB_LW_E_ARGS;
   cudaSetDevice(ctx->device);
   const int occ = gb_lw_slots(nlay, shape->variant) / std::max(1, ctx->num_sms);
@@ -747,13 +773,7 @@ int gb_rrtmg_lw_tuning_set(gb_lw_context* ctx, int nlay, const gb_lw_tuning* sha
   t.blocks_per_sm = shape->blocks_per_sm;
   t.blocks = t.blocks_per_sm * ctx->num_sms;
   t.ms = shape->ms;
-  for (size_t i = 0; i < ctx->tuned_nlay.size(); ++i)
-    if (ctx->tuned_nlay[i] == nlay) {
-      ctx->tuned[i] = t;
-      return GB_LW_OK;
-    }
-  ctx->tuned_nlay.push_back(nlay);
-  ctx->tuned.push_back(t);
+  store_tuning(ctx, nlay, kind, t);
   return GB_LW_OK;
 }
 
@@ -829,16 +849,7 @@ int gb_rrtmg_lw_autotune(gb_lw_context* ctx, void* stream, int ngrid, const gb_l
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (err != cudaSuccess) return cuda_fail(ctx, err, "autotune");
-  bool stored = false;
-  for (size_t i = 0; i < ctx->tuned_nlay.size(); ++i)
-    if (ctx->tuned_nlay[i] == b.nsmax) {
-      ctx->tuned[i] = bt;
-      stored = true;
-    }
-  if (!stored) {
-    ctx->tuned_nlay.push_back(b.nsmax);
-    ctx->tuned.push_back(bt);
-  }
+  store_tuning(ctx, b.nsmax, batch_kind(b), bt);
   if (best) *best = bt;
   return GB_LW_OK;
 }
@@ -851,7 +862,7 @@ int gb_rrtmg_lw_batch_graph_create(gb_lw_context* ctx, int ngrid, const gb_lw_gr
   if (rc) return rc;
   if (b.col0[ngrid] == 0) return GB_LW_E_ARGS;
   cudaSetDevice(ctx->device);
-  const gb_lw_tuning t = tuning_for(ctx, b.nsmax);
+  const gb_lw_tuning t = tuning_for(ctx, b.nsmax, batch_kind(b));
   gb_lw_graph* g = new gb_lw_graph();
   g->ctx = ctx;
   if (cudaMalloc(&g->scratch, gb_lw_scratch_bytes(b.nsmax, t.blocks)) != cudaSuccess) {
@@ -915,6 +926,7 @@ const char* gb_rrtmg_lw_strerror(int code) {
     case GB_LW_E_KISS_PMID: return "MCICA_SUBCOL: KISSVEC SEED GENERATOR REQUIRES PMID FROM BOTTOM FOUR LAYERS.";
     case GB_LW_E_LAYTROP: return "pressure must decrease with layer index";
     case GB_LW_E_BADVAL: return "non-positive or non-finite layer pressure or temperature";
+    case GB_LW_E_TCWAIT: return "learned gas optics: a tensor-core wait ran out";
     case GB_LW_E_ARGS: return "invalid arguments";
     case GB_LW_E_CUDA: return "CUDA error";
     case GB_LW_E_TABLES: return "table files missing or malformed";

@@ -57,4 +57,5 @@ enum GbColError {
   GB_COL_LIQ_BOUNDS = 6,  // cldprmc: 'LIQUID EFFECTIVE RADIUS OUT OF BOUNDS'
   GB_COL_LAYTROP = 9,     // lower-atmosphere layers not a prefix of the column
   GB_COL_BADVAL = 11,     // non-finite or non-positive pressure / temperature
+  GB_COL_TCWAIT = 12,     // learned gas optics: a tensor-core wait ran out (kernel stopped early)
 };

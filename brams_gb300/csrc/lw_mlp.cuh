@@ -86,7 +86,7 @@ __device__ __forceinline__ bool in_range(const float* f, const GbMlpNorm& n) {
   return ok;
 }
 
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+__device__ __forceinline__ float silu(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
 __device__ __forceinline__ float dsilu(float z) {
   const float s = 1.0f / (1.0f + __expf(-z));
   return s * (1.0f + z * (1.0f - s));

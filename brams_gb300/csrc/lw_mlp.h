@@ -41,3 +41,11 @@ cudaError_t gb_mlp_sync_bf16(const MlpBuffers& b, cudaStream_t st);
 cudaError_t gb_mlp_infer(const GbMlpGridIn& g, const GbMlpNorm& nm, const __nv_bfloat16* p16, const float* p32,
                          double grav, double avogad, float* d_tau, float* d_frac, unsigned char* d_flag, int nsm,
                          cudaStream_t st);
+
+// tcgen05 inference (lw_mlp_tc.cu): weight images prepared once per parameter change
+size_t gb_mlp_tc_image_bytes();
+cudaError_t gb_mlp_tc_images(const __nv_bfloat16* p16, const float* p32, const GbMlpNorm& nm, void* d_img,
+                             cudaStream_t st);
+cudaError_t gb_mlp_infer_tc(const GbMlpGridIn& g, const GbMlpNorm& nm, const void* d_img, double grav,
+                            double avogad, float* d_tau, float* d_frac, unsigned char* d_flag, int* d_err, int nsm,
+                            cudaStream_t st);

@@ -27,6 +27,9 @@ struct gb_lw_mlp {
   float* d_grad = nullptr;
   float* d_w = nullptr;  // loss weight per output
   int step = 0;
+  int engine = GB_LW_MLP_TCGEN05;
+  void* d_img = nullptr;  // tcgen05 weight images (rebuilt when the parameters change)
+  bool img_dirty = true;
 };
 
 namespace {
@@ -124,6 +127,7 @@ int upload_params(gb_lw_mlp* m, const float* host) {
   if (cudaMemcpy(m->b.p32, host, GB_MLP_NPARAM * 4, cudaMemcpyHostToDevice) != cudaSuccess) return GB_LW_E_CUDA;
   cudaError_t e = gb_mlp_sync_bf16(m->b, 0);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  m->img_dirty = true;
   return e == cudaSuccess ? 0 : fail(m->ctx, e, "parameter upload");
 }
 
@@ -241,6 +245,7 @@ int gb_lw_mlp_destroy(gb_lw_mlp* m) {
   cudaFree(m->b.p16);
   cudaFree(m->d_grad);
   cudaFree(m->d_w);
+  cudaFree(m->d_img);
   delete m;
   return GB_LW_OK;
 }
@@ -257,7 +262,10 @@ int gb_lw_mlp_get_params(gb_lw_mlp* m, float* params, float* norm) {
 int gb_lw_mlp_set_params(gb_lw_mlp* m, const float* params, const float* norm) {
   if (!m) return GB_LW_E_ARGS;
   cudaSetDevice(m->ctx->device);
-  if (norm) std::memcpy(&m->norm, norm, sizeof(GbMlpNorm));
+  if (norm) {
+    std::memcpy(&m->norm, norm, sizeof(GbMlpNorm));
+    m->img_dirty = true;
+  }
   if (params) {
     int rc = upload_params(m, params);
     if (rc) return rc;
@@ -333,6 +341,7 @@ int gb_lw_mlp_fit_norm(gb_lw_mlp* m, void* stream, int64_t rows, const float* d_
     n.out_mu[j] = 0.0f;
     n.out_sd[j] = 1.0f;
   }
+  m->img_dirty = true;
   return GB_LW_OK;
 }
 
@@ -367,6 +376,7 @@ int gb_lw_mlp_train_step(gb_lw_mlp* m, void* stream, int64_t rows, const void* d
   int rc = gb_lw_mlp_gradients(m, stream, rows, d_x, d_t, nullptr, d_loss);
   if (rc) return rc;
   m->step += 1;
+  m->img_dirty = true;
   cudaError_t e = gb_mlp_adam(m->b, m->d_grad, lr, m->step, (cudaStream_t)stream);
   return e == cudaSuccess ? GB_LW_OK : fail(m->ctx, e, "adam");
 }
@@ -392,13 +402,35 @@ int gb_lw_mlp_forward(gb_lw_mlp* m, void* stream, int64_t rows, const void* d_x,
   return e == cudaSuccess ? GB_LW_OK : fail(m->ctx, e, "forward");
 }
 
+int gb_lw_mlp_set_engine(gb_lw_mlp* m, int engine) {
+  if (!m || (engine != GB_LW_MLP_MMA_SYNC && engine != GB_LW_MLP_TCGEN05)) return GB_LW_E_ARGS;
+  m->engine = engine;
+  return GB_LW_OK;
+}
+
 int gb_lw_mlp_infer(gb_lw_mlp* m, void* stream, const gb_lw_grid* grid, float* d_tau, float* d_frac,
                     uint8_t* d_flag) {
   if (!m || !grid || !d_tau || !d_frac || !d_flag) return GB_LW_E_ARGS;
   if (grid->ncol < 0 || grid->nlay < 1 || grid->ld_in < grid->ncol) return GB_LW_E_ARGS;
   cudaSetDevice(m->ctx->device);
-  cudaError_t e = gb_mlp_infer(grid_in(*grid), m->norm, m->b.p16, m->b.p32, m->ctx->tabs.grav, m->ctx->tabs.avogad,
-                               d_tau, d_frac, d_flag, m->ctx->num_sms, (cudaStream_t)stream);
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  if (m->engine == GB_LW_MLP_TCGEN05) {
+    if (!m->d_img && cudaMalloc(&m->d_img, gb_mlp_tc_image_bytes()) != cudaSuccess) {
+      cudaGetLastError();
+      return GB_LW_E_NOMEM;
+    }
+    if (m->img_dirty) {
+      e = gb_mlp_tc_images(m->b.p16, m->b.p32, m->norm, m->d_img, st);
+      if (e != cudaSuccess) return fail(m->ctx, e, "weight images");
+      m->img_dirty = false;
+    }
+    e = gb_mlp_infer_tc(grid_in(*grid), m->norm, m->d_img, m->ctx->tabs.grav, m->ctx->tabs.avogad, d_tau, d_frac,
+                        d_flag, m->ctx->d_err, m->ctx->num_sms, st);
+  } else {
+    e = gb_mlp_infer(grid_in(*grid), m->norm, m->b.p16, m->b.p32, m->ctx->tabs.grav, m->ctx->tabs.avogad, d_tau,
+                     d_frac, d_flag, m->ctx->num_sms, st);
+  }
   return e == cudaSuccess ? GB_LW_OK : fail(m->ctx, e, "inference");
 }
 

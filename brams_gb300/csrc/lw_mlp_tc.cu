@@ -1,0 +1,347 @@
+// Inference of the taumol MLP on the 5th-generation tensor cores (tcgen05).
+//
+// One CTA per SM, persistent over tiles of 128 layers (rows).  The four
+// weight matrices live in shared memory for the whole kernel as K-major,
+// 128-byte-swizzled bf16 images (prepared once by mlp_tc_images_kernel); the
+// 128 x K activation tile is written to shared memory in the same layout by
+// the epilogue of the previous layer.  One thread issues tcgen05.mma
+// (M = 128, kind::f16, bf16 operands, fp32 accumulators in tensor memory) and
+// commits to an mbarrier; sixteen warps then read the accumulators back with
+// tcgen05.ld (warp w: TMEM lanes 32*(w%4).., column quarter w/4), apply bias and
+// SiLU, and write the next layer's operand tile.  The output layer
+// (N = 288 = 2 x 144) is un-standardised and written per (column, layer) in
+// the layout the column kernel reads.
+//
+// Every wait on the mbarrier is bounded; a wait that runs out records an
+// error flag, and the kernel frees its tensor memory and returns.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "lw_mlp.cuh"
+#include "lw_common.h"
+#include "lw_mlp.h"
+
+namespace gbtc {
+
+using bf16 = __nv_bfloat16;
+
+constexpr int M = 128;          // rows per tile (TMEM lanes)
+constexpr int KIN = 64;         // layer-1 K (9 features, zero padded to one 128-byte row)
+constexpr int H = GB_MLP_H;     // 128
+constexpr int NO = GB_MLP_NOUTP;  // 288
+constexpr int NOH = NO / 2;     // 144 per output MMA
+constexpr int NT = 512;         // 16 warps: 4 per TMEM lane quarter
+constexpr int TMEM_COLS = 512;
+
+// shared-memory image offsets (bytes; every operand tile starts on 1024 bytes)
+constexpr int OFF_W1 = 0;                             // [128 n][64 k]          16 KB
+constexpr int OFF_W2 = OFF_W1 + H * 128;              // 2 k-blocks x [128][64] 32 KB
+constexpr int OFF_W3 = OFF_W2 + 2 * H * 128;          // 32 KB
+constexpr int OFF_W4 = OFF_W3 + 2 * H * 128;          // 2 k-blocks x [288][64] 72 KB
+constexpr int IMG_BYTES = OFF_W4 + 2 * NO * 128;      // weight images
+constexpr int OFF_X = IMG_BYTES;                      // [128 m][64 k]          16 KB
+constexpr int OFF_H = OFF_X + M * 128;                // 2 k-blocks x [128][64] 32 KB
+constexpr int OFF_F32 = OFF_H + 2 * M * 128;          // b1 b2 b3 (128 each), b4, omu, osd (288 each)
+constexpr int NF32 = 3 * H + 3 * NO;
+constexpr int OFF_BAR = OFF_F32 + NF32 * 4;           // mbarrier (8 B) + TMEM address (4 B)
+constexpr int SMEM_BYTES = OFF_BAR + 16;
+static_assert(OFF_W2 % 1024 == 0 && OFF_W3 % 1024 == 0 && OFF_W4 % 1024 == 0 && OFF_X % 1024 == 0 &&
+                  OFF_H % 1024 == 0 && (NOH * 128) % 1024 == 0,
+              "operand tiles must start on 1024-byte boundaries (128-byte swizzle atoms)");
+static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
+
+// byte offset of element (r, k) in a K-major, 128-byte-swizzled tile of R rows
+// (k-blocks of 64 elements; 16-byte chunk c of row r sits at chunk c ^ (r & 7))
+__host__ __device__ constexpr uint32_t sw128(int R, int r, int k) {
+  return (uint32_t)((k >> 6) * (R * 128) + r * 128 + ((((k & 63) >> 3) ^ (r & 7)) << 4) + (k & 7) * 2);
+}
+
+// tcgen05 shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row
+// groups 1024 bytes apart (stride byte offset), leading byte offset unused
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);        // start address
+  d |= (uint64_t)1 << 16;                        // leading byte offset (unused with this swizzle)
+  d |= (uint64_t)(1024 >> 4) << 32;              // stride byte offset
+  d |= (uint64_t)1 << 46;                        // descriptor version
+  d |= (uint64_t)2 << 61;                        // 128-byte swizzle
+  return d;
+}
+
+// instruction descriptor, kind::f16: bf16 A and B (K-major), fp32 D, M x N
+__host__ __device__ constexpr uint32_t idesc(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mma(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t id, uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(a), "l"(b), "r"(id), "r"(accumulate));
+}
+
+__device__ __forceinline__ void commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar) : "memory");
+}
+
+// bounded wait for the mbarrier phase with the given parity; false if it ran out
+__device__ __forceinline__ bool wait_parity(uint32_t bar, uint32_t parity) {
+  for (int i = 0; i < (1 << 22); ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+// silu(acc + bias) of 32 consecutive hidden units (from n0) of this thread's
+// row, into the next layer's operand tile
+__device__ __forceinline__ void hidden_epilogue(uint32_t tcol, int row, int n0, const float* bias, char* hbase) {
+#pragma unroll
+  for (int c16 = 0; c16 < 2; ++c16) {
+    float v[16];
+    ld16(tcol + c16 * 16, v);
+    uint32_t p[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int n = n0 + c16 * 16 + 2 * i;
+      p[i] = gbmlp::pack_bf16(gbmlp::silu(v[2 * i] + bias[n]), gbmlp::silu(v[2 * i + 1] + bias[n + 1]));
+    }
+    const int k0 = n0 + c16 * 16;
+    *reinterpret_cast<uint4*>(hbase + sw128(M, row, k0)) = make_uint4(p[0], p[1], p[2], p[3]);
+    *reinterpret_cast<uint4*>(hbase + sw128(M, row, k0 + 8)) = make_uint4(p[4], p[5], p[6], p[7]);
+  }
+}
+
+__global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNorm nm, const uint4* __restrict__ img,
+                                                         const float* __restrict__ f32, double grav, double avogad,
+                                                         float* __restrict__ out_tau, float* __restrict__ out_frac,
+                                                         unsigned char* __restrict__ flag, int* __restrict__ err) {
+  extern __shared__ __align__(1024) char sm[];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const float* sf = reinterpret_cast<const float*>(sm + OFF_F32);
+  const float *b1 = sf, *b2 = sf + H, *b3 = sf + 2 * H, *b4 = sf + 3 * H, *omu = b4 + NO, *osd = omu + NO;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + OFF_BAR);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + OFF_BAR + 8);
+  // weight images and fp32 vectors into shared memory
+  for (int i = tid; i < IMG_BYTES / 16; i += NT) reinterpret_cast<uint4*>(sm)[i] = img[i];
+  for (int i = tid; i < NF32; i += NT) reinterpret_cast<float*>(sm + OFF_F32)[i] = f32[i];
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(tslot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  fence_async_smem();
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *tslot;
+  const uint32_t sbase = smem_addr(sm);
+  // the swizzled operand tiles assume a 1024-byte aligned shared-memory window
+  bool ok = (sbase & 1023u) == 0;
+  const uint32_t bar_a = smem_addr(bar);
+  const int q = warp & 3, part = warp >> 2;  // lane quarter, column quarter
+  const int row = q * 32 + lane;                                // this thread's tile row in the epilogue
+  const uint32_t tlane = tmem + ((uint32_t)(q * 32) << 16);     // TMEM address of the warp's lane quarter
+  const long long rows = (long long)g.ncol * g.nlay;
+  const long long ntile = (rows + M - 1) / M;
+  uint32_t phase = 0;
+  for (long long tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
+    const long long r0 = tile * M;
+    // ---- features of the tile's rows (rows are layer-major: coalesced loads)
+    if (tid < M) {
+      const long long r = r0 + tid;
+      float f[GB_MLP_NF];
+      if (r < rows) {
+        const int lay = (int)(r / g.ncol);
+        const long long icol = r - (long long)lay * g.ncol;
+        gbmlp::layer_features(g.play, g.plev, g.tlay, g.tlev, g.h2ovmr, g.o3vmr, g.co2vmr, g.ch4vmr, g.n2ovmr, g.ld,
+                              icol, lay, grav, avogad, f);
+        flag[icol * g.nlay + lay] = gbmlp::in_range(f, nm) ? 1 : 0;
+      } else {
+#pragma unroll
+        for (int i = 0; i < GB_MLP_NF; ++i) f[i] = nm.in_mu[i];
+      }
+      uint32_t p[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int j0 = 2 * i, j1 = 2 * i + 1;
+        const float x0 = j0 < GB_MLP_NF ? (f[j0] - nm.in_mu[j0]) / nm.in_sd[j0] : 0.0f;
+        const float x1 = j1 < GB_MLP_NF ? (f[j1] - nm.in_mu[j1]) / nm.in_sd[j1] : 0.0f;
+        p[i] = gbmlp::pack_bf16(x0, x1);
+      }
+      char* xb = sm + OFF_X;
+      *reinterpret_cast<uint4*>(xb + sw128(M, tid, 0)) = make_uint4(p[0], p[1], p[2], p[3]);
+      *reinterpret_cast<uint4*>(xb + sw128(M, tid, 8)) = make_uint4(p[4], p[5], p[6], p[7]);
+#pragma unroll
+      for (int c = 2; c < 8; ++c) *reinterpret_cast<uint4*>(xb + sw128(M, tid, 8 * c)) = make_uint4(0, 0, 0, 0);
+    }
+    // ---- four layers
+    for (int l = 0; l < 4; ++l) {
+      fence_async_smem();
+      fence_before();
+      __syncthreads();
+      fence_after();
+      if (tid == 0) {
+        if (l == 0) {
+          for (int s = 0; s < KIN / 16; ++s)
+            mma(tmem, sdesc(sbase + OFF_X + s * 32), sdesc(sbase + OFF_W1 + s * 32), idesc(M, H), s > 0);
+        } else if (l < 3) {
+          const int W = l == 1 ? OFF_W2 : OFF_W3;
+          for (int s = 0; s < H / 16; ++s) {
+            const int kb = s >> 2, ks = (s & 3) * 32;
+            mma(tmem, sdesc(sbase + OFF_H + kb * M * 128 + ks), sdesc(sbase + W + kb * H * 128 + ks), idesc(M, H), s > 0);
+          }
+        } else {
+          for (int hh = 0; hh < 2; ++hh)
+            for (int s = 0; s < H / 16; ++s) {
+              const int kb = s >> 2, ks = (s & 3) * 32;
+              mma(tmem + hh * 256, sdesc(sbase + OFF_H + kb * M * 128 + ks),
+                  sdesc(sbase + OFF_W4 + kb * NO * 128 + hh * NOH * 128 + ks), idesc(M, NOH), s > 0);
+            }
+        }
+        commit(bar_a);
+      }
+      ok = wait_parity(bar_a, phase);
+      phase ^= 1u;
+      fence_after();
+      if (__syncthreads_or(!ok)) {
+        ok = false;
+        break;
+      }
+      if (l < 3) {
+        hidden_epilogue(tlane + part * 32, row, part * 32, l == 0 ? b1 : (l == 1 ? b2 : b3), sm + OFF_H);
+      } else {
+        const long long r = r0 + row;
+        const bool live = r < rows;
+        long long o = 0;
+        if (live) {
+          const int lay = (int)(r / g.ncol);
+          const long long icol = r - (long long)lay * g.ncol;
+          o = (icol * g.nlay + lay) * GB_NGPT_MLP;
+        }
+        // 18 chunks of 16 outputs (two halves of 144); warp quarter `part` takes chunks part, part+4, ...
+#pragma unroll 1
+        for (int c = part; c < 2 * (NOH / 16); c += 4) {
+          const int hh = c / (NOH / 16), c16 = c % (NOH / 16);
+          float v[16];
+          ld16(tlane + hh * 256 + c16 * 16, v);
+          if (!live) continue;
+#pragma unroll
+          for (int i = 0; i < 16; i += 4) {
+            const int j = hh * NOH + c16 * 16 + i;  // output index of v[i]
+            float y[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) y[u] = (v[i + u] + b4[j + u]) * osd[j + u] + omu[j + u];
+            if (j + 3 < GB_NGPT_MLP) {
+              *reinterpret_cast<float4*>(out_tau + o + j) = make_float4(__expf(y[0]), __expf(y[1]), __expf(y[2]), __expf(y[3]));
+            } else if (j >= GB_NGPT_MLP && j + 3 < GB_MLP_NOUT) {
+              *reinterpret_cast<float4*>(out_frac + o + j - GB_NGPT_MLP) = make_float4(y[0], y[1], y[2], y[3]);
+            } else {
+#pragma unroll
+              for (int u = 0; u < 4; ++u) {
+                const int jj = j + u;
+                if (jj < GB_NGPT_MLP) out_tau[o + jj] = __expf(y[u]);
+                else if (jj < GB_MLP_NOUT) out_frac[o + jj - GB_NGPT_MLP] = y[u];
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  if (!ok && tid == 0) atomicMax(err, GB_COL_TCWAIT);
+  fence_before();
+  __syncthreads();
+  fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+}
+
+// K-major 128-byte-swizzled weight images (bf16) from the [in][out] parameter
+// blob, and the fp32 vectors (biases, output scaling) the kernel stages
+__global__ void images_kernel(const bf16* __restrict__ p16, const float* __restrict__ p32, GbMlpNorm nm,
+                              char* __restrict__ img, float* __restrict__ f32) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  // W1: rows n (128), k < 64 (features beyond 16 are zero)
+  for (int i = tid; i < H * KIN; i += nth) {
+    const int n = i / KIN, k = i % KIN;
+    const bf16 v = k < GB_MLP_KIN ? p16[GB_MLP_OFF_W1 + k * H + n] : __float2bfloat16_rn(0.0f);
+    *reinterpret_cast<bf16*>(img + OFF_W1 + sw128(H, n, k)) = v;
+  }
+  for (int i = tid; i < H * H; i += nth) {
+    const int n = i / H, k = i % H;
+    *reinterpret_cast<bf16*>(img + OFF_W2 + sw128(H, n, k)) = p16[GB_MLP_OFF_W2 + k * H + n];
+    *reinterpret_cast<bf16*>(img + OFF_W3 + sw128(H, n, k)) = p16[GB_MLP_OFF_W3 + k * H + n];
+  }
+  for (int i = tid; i < NO * H; i += nth) {
+    const int n = i / H, k = i % H;
+    *reinterpret_cast<bf16*>(img + OFF_W4 + sw128(NO, n, k)) = p16[GB_MLP_OFF_W4 + k * NO + n];
+  }
+  for (int i = tid; i < H; i += nth) {
+    f32[i] = p32[GB_MLP_OFF_B1 + i];
+    f32[H + i] = p32[GB_MLP_OFF_B2 + i];
+    f32[2 * H + i] = p32[GB_MLP_OFF_B3 + i];
+  }
+  for (int i = tid; i < NO; i += nth) {
+    f32[3 * H + i] = p32[GB_MLP_OFF_B4 + i];
+    f32[3 * H + NO + i] = nm.out_mu[i];
+    f32[3 * H + 2 * NO + i] = nm.out_sd[i];
+  }
+}
+
+}  // namespace gbtc
+
+size_t gb_mlp_tc_image_bytes() { return (size_t)gbtc::IMG_BYTES + (size_t)gbtc::NF32 * 4; }
+
+cudaError_t gb_mlp_tc_images(const __nv_bfloat16* p16, const float* p32, const GbMlpNorm& nm, void* d_img,
+                             cudaStream_t st) {
+  char* img = static_cast<char*>(d_img);
+  gbtc::images_kernel<<<256, 256, 0, st>>>(p16, p32, nm, img, reinterpret_cast<float*>(img + gbtc::IMG_BYTES));
+  return cudaGetLastError();
+}
+
+cudaError_t gb_mlp_infer_tc(const GbMlpGridIn& g, const GbMlpNorm& nm, const void* d_img, double grav,
+                            double avogad, float* d_tau, float* d_frac, unsigned char* d_flag, int* d_err, int nsm,
+                            cudaStream_t st) {
+  const long long rows = (long long)g.ncol * g.nlay;
+  if (rows == 0) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(gbtc::infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       gbtc::SMEM_BYTES);
+  if (e != cudaSuccess) return e;
+  const long long tiles = (rows + gbtc::M - 1) / gbtc::M;
+  const int blocks = (int)(tiles < nsm ? tiles : nsm);
+  const char* img = static_cast<const char*>(d_img);
+  gbtc::infer_tc_kernel<<<blocks, gbtc::NT, gbtc::SMEM_BYTES, st>>>(
+      g, nm, reinterpret_cast<const uint4*>(img), reinterpret_cast<const float*>(img + gbtc::IMG_BYTES), grav, avogad,
+      d_tau, d_frac, d_flag, d_err);
+  return cudaGetLastError();
+}

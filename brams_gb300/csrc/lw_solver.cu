@@ -182,6 +182,25 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
+// Warp sums of four values per lane at once (a transposed butterfly, 6
+// shuffles instead of 20): lane i returns the sum over the 32 lanes of v[i & 3].
+__device__ __forceinline__ float reduce4(const float (&v)[4], int lane) {
+  const unsigned F = 0xffffffffu;
+  const bool hi = lane & 2;
+  float k0 = hi ? v[2] : v[0], k1 = hi ? v[3] : v[1];
+  const float s0 = hi ? v[0] : v[2], s1 = hi ? v[1] : v[3];
+  k0 += __shfl_xor_sync(F, s0, 2);
+  k1 += __shfl_xor_sync(F, s1, 2);
+  const bool lo = lane & 1;
+  float k = lo ? k1 : k0;
+  const float sx = lo ? k0 : k1;
+  k += __shfl_xor_sync(F, sx, 1);
+  k += __shfl_xor_sync(F, k, 4);
+  k += __shfl_xor_sync(F, k, 8);
+  k += __shfl_xor_sync(F, k, 16);
+  return k;
+}
+
 // exp_tbl/tfn_tbl/tau_tbl at the index the reference's lookup would pick
 // (rrtmg_lw_rtrnmc.f90:385-388 with rrtmg_lw_init.f90:125-142)
 struct TblEntry {
@@ -771,25 +790,37 @@ __device__ __forceinline__ void solve_column(const LwArgs& a, long long icol, ch
       const bool idrv = a.idrv == 1;
       const bool clouds = a.icld >= 1;
       float* part = s.part + warp * (nl + 1) * 6;  // this warp's [nl+1][6] partial sums
-      auto emit = [&](int lev, int k, float v) {
-        const float sum = warp_sum(v * wgt);
-        if (lane == 0) part[lev * 6 + k] = sum;
-      };
+      // Levels go in blocks of four: the block's scratch loads are issued
+      // together and each stream's four level sums take one reduce4.
       // downward (rtrnmc.f90:347-455): total stream and clear-sky stream
       float radld = 0.0f, radclrd = 0.0f;
-      float4 cnext = scr[(nl - 1) * GB_NGPT + g];
-      for (int L = nl - 1; L >= 0; --L) {
-        const float4 c = cnext;
-        if (L > 0) cnext = scr[(L - 1) * GB_NGPT + g];
-        if (clouds && s.cldlay[L] && cell_is_cloudy(s, L, g)) {
-          const float4 k = scr[(nl + L) * GB_NGPT + g];
-          radld = fmaf(radld, k.x, k.y);
-        } else {
-          radld = fmaf(radld, c.x, c.y);
+      for (int L0 = nl - 1; L0 >= 0; L0 -= 4) {
+        const int nb = L0 + 1 < 4 ? L0 + 1 : 4;  // levels L0, L0-1, .., L0-nb+1
+        float4 c[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) c[j] = j < nb ? scr[(L0 - j) * GB_NGPT + g] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float q0[4], q1[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          q0[j] = q1[j] = 0.0f;
+          if (j < nb) {
+            const int L = L0 - j;
+            if (clouds && s.cldlay[L] && cell_is_cloudy(s, L, g)) {
+              const float4 k = scr[(nl + L) * GB_NGPT + g];
+              radld = fmaf(radld, k.x, k.y);
+            } else {
+              radld = fmaf(radld, c[j].x, c[j].y);
+            }
+            radclrd = fmaf(radclrd, c[j].x, c[j].y);
+            q0[j] = radld * wgt;
+            q1[j] = radclrd * wgt;
+          }
         }
-        radclrd = fmaf(radclrd, c.x, c.y);
-        emit(L, 0, radld);
-        emit(L, 1, radclrd);
+        const float s0 = reduce4(q0, lane), s1 = reduce4(q1, lane);
+        if (lane < nb) {
+          part[(L0 - lane) * 6 + 0] = s0;
+          part[(L0 - lane) * 6 + 1] = s1;
+        }
       }
       // surface emission and reflection (rtrnmc.f90:465-485)
       const float plfrac1 = s.frac1[g];
@@ -798,32 +829,49 @@ __device__ __forceinline__ void solve_column(const LwArgs& a, long long icol, ch
       float radlu = rad0 + reflect * radld;
       float radclru = rad0 + reflect * radclrd;
       float d_radlu = plfrac1 * s.misc[32 + band], d_radclru = d_radlu;
-      emit(0, 2, radlu);
-      emit(0, 3, radclru);
-      if (idrv) {
-        emit(0, 4, d_radlu);
-        emit(0, 5, d_radclru);
-      }
-      // upward (rtrnmc.f90:486-529)
-      cnext = scr[g];
-      for (int L = 0; L < nl; ++L) {
-        const float4 c = cnext;
-        if (L + 1 < nl) cnext = scr[(L + 1) * GB_NGPT + g];
-        if (clouds && s.cldlay[L] && cell_is_cloudy(s, L, g)) {
-          const float4 k = scr[(nl + L) * GB_NGPT + g];
-          radlu = fmaf(radlu, k.x, k.z);
-          d_radlu *= k.w;
-        } else {
-          radlu = fmaf(radlu, c.x, c.z);
-          d_radlu *= c.x;
+      // upward (rtrnmc.f90:486-529): level 0 is the surface, level L+1 follows layer L
+      for (int v0 = 0; v0 <= nl; v0 += 4) {
+        const int nb = nl + 1 - v0 < 4 ? nl + 1 - v0 : 4;  // levels v0 .. v0+nb-1
+        float4 c[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          c[j] = (j < nb && v0 + j >= 1) ? scr[(v0 + j - 1) * GB_NGPT + g] : make_float4(0.f, 0.f, 0.f, 0.f);
+        float u0[4], u1[4], u2[4], u3[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          u0[j] = u1[j] = u2[j] = u3[j] = 0.0f;
+          if (j < nb) {
+            if (v0 + j >= 1) {
+              const int L = v0 + j - 1;
+              if (clouds && s.cldlay[L] && cell_is_cloudy(s, L, g)) {
+                const float4 k = scr[(nl + L) * GB_NGPT + g];
+                radlu = fmaf(radlu, k.x, k.z);
+                d_radlu *= k.w;
+              } else {
+                radlu = fmaf(radlu, c[j].x, c[j].z);
+                d_radlu *= c[j].x;
+              }
+              radclru = fmaf(radclru, c[j].x, c[j].z);
+              d_radclru *= c[j].x;
+            }
+            u0[j] = radlu * wgt;
+            u1[j] = radclru * wgt;
+            u2[j] = d_radlu * wgt;
+            u3[j] = d_radclru * wgt;
+          }
         }
-        radclru = fmaf(radclru, c.x, c.z);
-        d_radclru *= c.x;
-        emit(L + 1, 2, radlu);
-        emit(L + 1, 3, radclru);
+        const float s0 = reduce4(u0, lane), s1 = reduce4(u1, lane);
+        float s2 = 0.0f, s3 = 0.0f;
         if (idrv) {
-          emit(L + 1, 4, d_radlu);
-          emit(L + 1, 5, d_radclru);
+          s2 = reduce4(u2, lane);
+          s3 = reduce4(u3, lane);
+        }
+        if (lane < nb) {
+          float* p = part + (v0 + lane) * 6;
+          p[2] = s0;
+          p[3] = s1;
+          p[4] = s2;
+          p[5] = s3;
         }
       }
     }

@@ -41,12 +41,14 @@ EXPORTS = [
     "gb_lw_mlp_create", "gb_lw_mlp_destroy", "gb_lw_mlp_save", "gb_lw_mlp_load", "gb_lw_mlp_get_params",
     "gb_lw_mlp_set_params", "gb_lw_mlp_set_loss_weights", "gb_lw_mlp_samples", "gb_lw_mlp_fit_norm",
     "gb_lw_mlp_prepare", "gb_lw_mlp_gradients", "gb_lw_mlp_train_step", "gb_lw_mlp_forward", "gb_lw_mlp_infer",
-    "gb_rrtmg_lw_batch_surrogate",
+    "gb_rrtmg_lw_batch_surrogate", "gb_lw_mlp_set_engine",
 ]
+MLP_MMA_SYNC, MLP_TCGEN05 = 0, 1
 MLP_NPARAM = 72352
 MLP_NNORM = 626
 
 CLOUD_SUBCOL, CLOUD_FUSED = 0, 1
+KIND_FUSED, KIND_LEARNED = 1, 2
 MAX_GRIDS = 32
 
 _GRID_PTRS = ["play", "plev", "tlay", "tlev", "tsfc", "h2ovmr", "o3vmr", "co2vmr", "ch4vmr", "n2ovmr",
@@ -127,11 +129,11 @@ def load_library(path: str = LIB_PATH):
         GP = C.POINTER(GridDesc)
         L.gb_rrtmg_lw_batch_device.argtypes = [P, P, I, GP]
         L.gb_rrtmg_lw_autotune.argtypes = [P, P, I, GP, I, I, C.POINTER(Tuning)]
-        L.gb_rrtmg_lw_tuning_get.argtypes = [P, I, C.POINTER(Tuning)]
+        L.gb_rrtmg_lw_tuning_get.argtypes = [P, I, I, C.POINTER(Tuning)]
         L.gb_rrtmg_lw_batch_graph_create.argtypes = [P, I, GP, C.POINTER(P)]
         L.gb_rrtmg_lw_graph_launch.argtypes = [P, P]
         L.gb_rrtmg_lw_graph_destroy.argtypes = [P]
-        L.gb_rrtmg_lw_tuning_set.argtypes = [P, I, C.POINTER(Tuning)]
+        L.gb_rrtmg_lw_tuning_set.argtypes = [P, I, I, C.POINTER(Tuning)]
         L.gb_rrtmg_lw_num_variants.argtypes = []
         U64, F = C.c_uint64, C.c_float
         L.gb_lw_mlp_create.argtypes = [P, U64, C.POINTER(P)]
@@ -149,6 +151,7 @@ def load_library(path: str = LIB_PATH):
         L.gb_lw_mlp_forward.argtypes = [P, P, LL, P, P]
         L.gb_lw_mlp_infer.argtypes = [P, P, GP, P, P, P]
         L.gb_rrtmg_lw_batch_surrogate.argtypes = [P, P, I, GP, P]
+        L.gb_lw_mlp_set_engine.argtypes = [P, I]
         L.gb_rrtmg_lw_strerror.restype = C.c_char_p
         L.gb_rrtmg_lw_strerror.argtypes = [I]
         L.gb_rrtmg_lw_last_error.restype = C.c_char_p
@@ -301,14 +304,15 @@ class Context:
                                                            C.byref(t)))
         return t.as_dict()
 
-    def tuning(self, nlay: int) -> dict:
+    def tuning(self, nlay: int, kind: int = KIND_FUSED) -> dict:
+        """Shape used for batches of this largest nlay and kind (KIND_FUSED | KIND_LEARNED bits)."""
         t = Tuning()
-        _check(self.L, self.h, self.L.gb_rrtmg_lw_tuning_get(self.h, nlay, C.byref(t)))
+        _check(self.L, self.h, self.L.gb_rrtmg_lw_tuning_get(self.h, nlay, kind, C.byref(t)))
         return t.as_dict()
 
-    def set_tuning(self, nlay: int, variant: int, blocks_per_sm: int) -> None:
+    def set_tuning(self, nlay: int, variant: int, blocks_per_sm: int, kind: int = KIND_FUSED) -> None:
         t = Tuning(variant, 0, 0, blocks_per_sm, 0, 0.0)
-        _check(self.L, self.h, self.L.gb_rrtmg_lw_tuning_set(self.h, nlay, C.byref(t)))
+        _check(self.L, self.h, self.L.gb_rrtmg_lw_tuning_set(self.h, nlay, kind, C.byref(t)))
 
     def num_variants(self) -> int:
         return self.L.gb_rrtmg_lw_num_variants()
@@ -369,6 +373,10 @@ class Mlp:
 
     def save(self, path: str) -> None:
         self._ok(self.L.gb_lw_mlp_save(self.h, path.encode()))
+
+    def set_engine(self, engine: int) -> None:
+        """MLP_TCGEN05 (tensor-memory MMAs) or MLP_MMA_SYNC (warp MMAs) for inference."""
+        self._ok(self.L.gb_lw_mlp_set_engine(self.h, engine))
 
     def params(self):
         p = np.zeros(MLP_NPARAM, dtype=np.float32)

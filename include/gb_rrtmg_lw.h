@@ -39,6 +39,7 @@ typedef struct gb_lw_context gb_lw_context;
 #define GB_LW_E_KISS_PMID 8    /* generate_stochastic_clouds: KISS seed needs pmid(1) >= pmid(2) */
 #define GB_LW_E_LAYTROP 9      /* pressure does not decrease with layer index            */
 #define GB_LW_E_BADVAL 11      /* non-positive or non-finite layer pressure/temperature  */
+#define GB_LW_E_TCWAIT 12      /* learned gas optics: a tensor-core wait ran out          */
 #define GB_LW_E_ARGS (-1)      /* invalid sizes, flags or null pointers                  */
 #define GB_LW_E_CUDA (-2)      /* CUDA runtime error (see gb_rrtmg_lw_last_error)        */
 #define GB_LW_E_TABLES (-3)    /* table files missing or malformed                       */
@@ -227,17 +228,21 @@ int gb_rrtmg_lw_batch_device(gb_lw_context* ctx, void* stream, int ngrid, const 
 /* Times every compiled variant and persistent-grid size on a sample of the
  * batch (each grid cut to the same fraction of its columns, about
  * sample_cols columns in all; <= 0 for the whole batch), `reps` launches
- * each after a warm-up, keeps the fastest for batches with this largest
- * nlay and returns it in *best.  Overwrites the outputs of the sampled
- * columns. */
+ * each after a warm-up, keeps the fastest for batches of this largest
+ * nlay and kind (GB_LW_KIND_*) and returns it in *best.  Overwrites the
+ * outputs of the sampled columns. */
 int gb_rrtmg_lw_autotune(gb_lw_context* ctx, void* stream, int ngrid, const gb_lw_grid* grids,
                          int sample_cols, int reps, gb_lw_tuning* best);
 
-/* The shape gb_rrtmg_lw_batch_device would use for a batch whose largest
- * layer count is nlay; _set pins one (e.g. a shape tuned in an earlier run:
- * variant and blocks_per_sm are used, the other fields are derived). */
-int gb_rrtmg_lw_tuning_get(gb_lw_context* ctx, int nlay, gb_lw_tuning* out);
-int gb_rrtmg_lw_tuning_set(gb_lw_context* ctx, int nlay, const gb_lw_tuning* shape);
+/* Shapes are kept per largest layer count and batch kind: GB_LW_KIND_FUSED
+ * if any grid generates its McICA clouds in the kernel, | GB_LW_KIND_LEARNED
+ * if any grid uses learned gas optics.  _get returns the shape
+ * gb_rrtmg_lw_batch_device would use (tuned, pinned or the default); _set
+ * pins one (variant and blocks_per_sm are used, the rest is derived). */
+#define GB_LW_KIND_FUSED 1
+#define GB_LW_KIND_LEARNED 2
+int gb_rrtmg_lw_tuning_get(gb_lw_context* ctx, int nlay, int kind, gb_lw_tuning* out);
+int gb_rrtmg_lw_tuning_set(gb_lw_context* ctx, int nlay, int kind, const gb_lw_tuning* shape);
 /* Number of compiled kernel variants (valid gb_lw_tuning.variant values). */
 int gb_rrtmg_lw_num_variants(void);
 
@@ -279,6 +284,12 @@ int gb_lw_mlp_load(gb_lw_context* ctx, const char* path, gb_lw_mlp** mlp);
 /* Host copies of the fp32 parameters / normalisation (either may be NULL). */
 int gb_lw_mlp_get_params(gb_lw_mlp* mlp, float* params, float* norm);
 int gb_lw_mlp_set_params(gb_lw_mlp* mlp, const float* params, const float* norm);
+/* Inference engine of gb_lw_mlp_infer: GB_LW_MLP_TCGEN05 (default; tcgen05
+ * MMAs with tensor-memory accumulators) or GB_LW_MLP_MMA_SYNC (warp-level
+ * mma.sync, the network's reference GPU implementation). */
+#define GB_LW_MLP_MMA_SYNC 0
+#define GB_LW_MLP_TCGEN05 1
+int gb_lw_mlp_set_engine(gb_lw_mlp* mlp, int engine);
 /* Weight of each of the 280 outputs in the training loss (default 1). */
 int gb_lw_mlp_set_loss_weights(gb_lw_mlp* mlp, const float* w280);
 

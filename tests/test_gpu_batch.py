@@ -136,17 +136,18 @@ def test_every_variant_and_grid_size_identical(ctx, grids, singles):
     import torch
 
     nlay = max(g.nlay for g in grids)
+    saved = ctx.tuning(nlay, R.KIND_FUSED)
     try:
         for v in range(ctx.num_variants()):
             for per in (1, 2):
-                ctx.set_tuning(nlay, v, per)
+                ctx.set_tuning(nlay, v, per, kind=R.KIND_FUSED)
                 outs = [g.new_out() for g in grids]
                 ctx.rrtmg_lw_batch_device([g.desc(R.CLOUD_FUSED, o) for g, o in zip(grids, outs)])
                 torch.cuda.synchronize()
                 for o, ref in zip(outs, singles):
                     _same(_np(o), ref)
     finally:
-        ctx.set_tuning(nlay, 0, 1)
+        ctx.set_tuning(nlay, saved["variant"], saved["blocks_per_sm"], kind=R.KIND_FUSED)
     assert ctx.sync_status() == 0
 
 
@@ -190,7 +191,7 @@ def test_autotune_picks_a_valid_shape(ctx, grids, singles):
     best = ctx.autotune(descs, sample_cols=0, reps=1)
     assert 0 <= best["variant"] < ctx.num_variants()
     assert best["blocks_per_sm"] >= 1 and best["ms"] > 0
-    assert ctx.tuning(max(g.nlay for g in grids))["variant"] == best["variant"]
+    assert ctx.tuning(max(g.nlay for g in grids), R.KIND_FUSED)["variant"] == best["variant"]
     outs = [g.new_out() for g in grids]
     ctx.rrtmg_lw_batch_device([g.desc(R.CLOUD_FUSED, o) for g, o in zip(grids, outs)])
     torch.cuda.synchronize()
@@ -227,3 +228,5 @@ def test_batch_argument_errors(ctx, grids):
         ctx.rrtmg_lw_batch_device([g.desc(R.CLOUD_FUSED)] * (R.MAX_GRIDS + 1))
     with pytest.raises(R.RrtmgLwError):
         ctx.set_tuning(g.nlay, ctx.num_variants(), 1)
+    with pytest.raises(R.RrtmgLwError):
+        ctx.set_tuning(g.nlay, 0, 1, kind=4)

@@ -138,3 +138,31 @@ def test_out_of_range_layers_fall_back_to_taumol(ctx, trained):
         assert np.array_equal(a[k][:3], b[k][:3]), k
     assert not np.array_equal(a["uflx"][3:], b["uflx"][3:])
     assert ctx.sync_status() == 0
+
+
+def test_tcgen05_inference_matches_mma_sync(ctx, trained):
+    """The tensor-memory (tcgen05) inference kernel against the warp-MMA one on
+    the same layers: same flags, outputs equal up to the order of the fp32
+    sums (which can move a bf16 activation by one unit in the last place)."""
+    torch = _torch()
+    mlp, _ = trained
+    spec = ProfileSpec(ncol=203, nlay=45, seed=79, t_noise=4.0, h2o_sigma=0.5)  # 9135 rows: a partial last tile
+    g = S.DeviceGrid(make_state(spec))
+    rows = 203 * 45
+    out = {}
+    for eng in (R.MLP_MMA_SYNC, R.MLP_TCGEN05):
+        mlp.set_engine(eng)
+        tau = torch.full((rows, 140), -1.0, dtype=torch.float32, device="cuda")
+        frac = torch.full((rows, 140), -1.0, dtype=torch.float32, device="cuda")
+        flag = torch.full((rows,), 7, dtype=torch.uint8, device="cuda")
+        mlp.infer(g.desc(), tau, frac, flag)
+        torch.cuda.synchronize()
+        out[eng] = (tau.cpu().numpy(), frac.cpu().numpy(), flag.cpu().numpy())
+    mlp.set_engine(R.MLP_MMA_SYNC)
+    assert ctx.sync_status() == 0
+    (t0, f0, g0), (t1, f1, g1) = out[R.MLP_MMA_SYNC], out[R.MLP_TCGEN05]
+    assert np.array_equal(g0, g1)
+    assert (t1 > 0).all() and np.isfinite(t1).all()
+    assert np.abs(np.log(t1) - np.log(t0)).max() <= 0.05
+    assert np.abs(np.log(t1) - np.log(t0)).mean() <= 2e-3
+    assert np.abs(f1 - f0).max() <= 5e-3
