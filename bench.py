@@ -343,6 +343,10 @@ def surrogate_step(ctx, mlp, wl, bufs, stream, ev=None):
     return nch
 
 
+def log(msg):
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
 def gpu_arm(args, rank, world):
     import torch
 
@@ -376,6 +380,7 @@ def gpu_arm(args, rank, world):
         trained = f"trained in this run ({info['train_s']:.1f} s on {info['rows']} layers)"
 
     # ---------------- headline workload
+    log("network ready; building the workload")
     nbase = args.nbase
     seed = BASE_SEED + rank * 7919
     wl = Workload(dev, nbase, NLAY5, NMEM, seed)
@@ -387,11 +392,13 @@ def gpu_arm(args, rank, world):
     plain = lambda: ctx.rrtmg_lw_batch_device([wl.desc(m) for m in range(NMEM)], stream=stream)
     sur = lambda ev=None: surrogate_step(ctx, mlp, wl, bufs, stream, ev)
     torch.cuda.synchronize()
+    log(f"workload on the device ({torch.cuda.memory_allocated(dev) / 1e9:.1f} GB); tuning")
     # launch shapes from the autotuner, for both kinds of batch, on a sample of the workload
     if args.no_tune:
         tuned = {"plain": ctx.tuning(NLAY5, R.KIND_FUSED), "learned": ctx.tuning(NLAY5, R.KIND_FUSED | R.KIND_LEARNED)}
     else:
-        tuned = {"plain": ctx.autotune([wl.desc(m) for m in range(NMEM)], sample_cols=65536, reps=2, stream=stream)}
+        tuned = {"plain": ctx.autotune([wl.desc(m) for m in range(NMEM)], sample_cols=4 * CHUNK, reps=2, stream=stream)}
+        report = {"plain": ctx.autotune_report()}
         n0 = min(CHUNK, nbase)
         g0 = []
         for m in range(NMEM):
@@ -399,7 +406,10 @@ def gpu_arm(args, rank, world):
             ex = dict(sur_tau=bufs[0][r0:].data_ptr(), sur_frac=bufs[1][r0:].data_ptr(), sur_flag=bufs[2][r0:].data_ptr())
             mlp.infer(wl.desc(m, 0, n0), ex["sur_tau"], ex["sur_frac"], ex["sur_flag"], stream=stream)
             g0.append(wl.desc(m, 0, n0, **ex))
-        tuned["learned"] = ctx.autotune(g0, sample_cols=65536, reps=2, stream=stream)
+        tuned["learned"] = ctx.autotune(g0, sample_cols=0, reps=2, stream=stream)  # a whole chunk
+        report["learned"] = ctx.autotune_report()
+        log("autotuner candidates (variant, blocks/SM, ms): " + json.dumps(
+            {k: [(c["variant"], c["blocks_per_sm"], round(c["ms"], 2)) for c in v] for k, v in report.items()}))
 
     def timed(fn, steps, evs=False):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -415,9 +425,11 @@ def gpu_arm(args, rank, world):
             torch.distributed.barrier()
         return e0.elapsed_time(e1) / 1e3 / steps
 
+    log(f"tuned: {tuned}; timing the plain path")
     for _ in range(args.warmup):
         plain()
     t_plain = timed(plain, args.steps)
+    log("timing the learned path")
     plain_out = wl.outputs(0, nbase // 2, SAMPLE)
     for _ in range(args.warmup):
         sur()
@@ -444,6 +456,7 @@ def gpu_arm(args, rank, world):
     launches_per_step = nch * (2 * NMEM + 1)  # per chunk: inference and McICA draws per member, one column kernel
 
     # ---------------- accuracy against the FP64 oracle
+    log("accuracy against the oracle")
     acc = {}
     if not args.no_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -463,9 +476,11 @@ def gpu_arm(args, rank, world):
         acc["sample"] = f"{SAMPLE} contiguous columns of member 0 from column {c0}; FP64 oracle with the same seeds"
 
     # ---------------- e2e: every step's inputs from page-locked host memory, outputs back
+    log("e2e")
     e2e = e2e_headline(ctx, mlp, wl, dev, stream, min(args.steps, 2), world, bufs)
 
     # ---------------- drop-in block (ABI mode, 360x300x45)
+    log("drop-in block")
     abi = None if args.no_abi else abi_block(ctx, dev, stream, args, rank, world, hbm)
 
     times = torch.tensor([t_sur, t_plain, t_kernel, e2e["t"]], dtype=torch.float64, device=dev)
@@ -579,27 +594,29 @@ def e2e_headline(ctx, mlp, wl, dev, stream, steps, world, bufs):
                     f"(the generator tile's columns) and reads all outputs back; {steps} timed steps"}
 
 
-def cpu_baseline_headline(wl):
+def cpu_baseline_headline(wl, seconds: float = 12.0, max_cols: int = 16384):
+    """The FP64 oracle on all host cores over a bounded sample of member 0's
+    columns (at most max_cols, whose McICA sub-columns take 268 KB each),
+    repeated until about `seconds` of work."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
     pyoracle.build(native=True)
     cores = os.cpu_count() or 1
-    probe = 32 * cores
-    st = wl.host_columns(0, 0, probe)
-    mc = pyoracle.mcica_per_column(st, st["tauc"], icld=3, base_seed=wl.seed0(0))
-    t0 = time.perf_counter()
-    pyoracle.rrtmg_lw(st, mc, nthreads=cores, native=True)
-    dt = time.perf_counter() - t0
-    n = int(min(wl.nbase, max(probe, probe * 12.0 / max(dt, 1e-6))))
+    n = min(wl.nbase, max_cols)
     st = wl.host_columns(0, 0, n)
     mc = pyoracle.mcica_per_column(st, st["tauc"], icld=3, base_seed=wl.seed0(0))
-    t0 = time.perf_counter()
-    pyoracle.rrtmg_lw(st, mc, nthreads=cores, native=True)
-    dt = time.perf_counter() - t0
-    return {"value": n / dt, "unit": "columns/s", "cores": cores, "kind": "port",
-            "sample": f"first {n} columns of member 0 of the {NX}x{NY}x{NLAY5} workload, one pass, {cores} threads, "
-                      "FP64 C++ restatement (-O3 native); McICA sub-columns made beforehand, not timed"}
+    done, t0 = 0, time.perf_counter()
+    while True:
+        pyoracle.rrtmg_lw(st, mc, nthreads=cores, native=True)
+        done += n
+        dt = time.perf_counter() - t0
+        if dt >= seconds:
+            break
+    return {"value": done / dt, "unit": "columns/s", "cores": cores, "kind": "port",
+            "sample": f"the first {n} columns of member 0 of the {NX}x{NY}x{NLAY5} workload, {done // n} passes "
+                      f"({dt:.1f} s), {cores} threads, FP64 C++ restatement (-O3 native); McICA sub-columns made "
+                      "beforehand, not timed"}
 
 
 def abi_block(ctx, dev, stream, args, rank, world, hbm):
@@ -607,7 +624,7 @@ def abi_block(ctx, dev, stream, args, rank, world, hbm):
     import torch
     from brams_gb300.rrtmg_lw import OUT_ORDER, STATE_ORDER
 
-    ncol, nlay = NCOL, NLAY
+    ncol, nlay = args.abi_ncol, NLAY
     seed = BASE_SEED + rank * 7919
     st, tauc = make_inputs(ncol, nlay, seed)
 
@@ -665,7 +682,8 @@ def abi_block(ctx, dev, stream, args, rank, world, hbm):
     same = bool(torch.equal(host["hr"].to(dev), d["hr"]) and torch.equal(host["uflx"].to(dev), d["uflx"]))
     alg = abi_bytes_per_column(nlay) * ncol
     achieved = alg / t_dev / 1e9
-    return {"workload": "rrtmg_lw drop-in (McICA arrays as the reference passes them), 360x300 columns x 45 layers",
+    return {"workload": "rrtmg_lw drop-in (McICA arrays as the reference passes them), "
+                        + ("360x300 columns x 45 layers" if ncol == NCOL else f"{ncol} columns x 45 layers"),
             "value": world * ncol / t_dev, "unit": "columns/s", "ms_per_step": t_dev * 1e3,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                          "traffic": traffic_from_profiles("lw_batch_kernel_c2_traffic.txt"), "alg_bytes_per_launch": alg},
@@ -684,6 +702,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the oracle accuracy check and the CPU baseline")
     ap.add_argument("--no-abi", action="store_true", help="skip the 360x300x45 drop-in block")
     ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's")
+    ap.add_argument("--abi-ncol", type=int, default=NCOL, help="columns of the drop-in block")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -206,6 +206,21 @@ void store_tuning(gb_lw_context* ctx, int nlay, int kind, const gb_lw_tuning& t)
   ctx->tuned.push_back(t);
 }
 
+// One grid through the launch shape tuned (or defaulted) for its layer count and kind,
+// at most nslots persistent blocks (the scratch the caller provides).
+cudaError_t launch_one(gb_lw_context* ctx, const LwArgs& a, float4* scratch, int nslots, cudaStream_t stream) {
+  if (a.ncol <= 0) return cudaSuccess;
+  LwBatch b;
+  b.ngrid = 1;
+  b.nsmax = a.nlay;
+  b.col0[0] = 0;
+  b.col0[1] = a.ncol;
+  b.scratch = scratch;
+  b.g[0] = a;
+  const gb_lw_tuning t = tuning_for(ctx, a.nlay, batch_kind(b));
+  return gb_lw_launch_batch(b, ctx->d_tables, t.variant, std::min(t.blocks, nslots), stream);
+}
+
 int ensure_bscratch(gb_lw_context* ctx, int nlay, int blocks) {
   size_t bytes = gb_lw_scratch_bytes(nlay, blocks);
   if (bytes <= ctx->bscratch_bytes) return 0;
@@ -447,7 +462,7 @@ int gb_rrtmg_lw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int
   cudaSetDevice(ctx->device);
   int rs = ensure_scratch(ctx, nlay);
   if (rs) return rs;
-  CK(gb_lw_launch(a, ctx->d_tables, ctx->d_scratch[0], ctx->scratch_slots, (cudaStream_t)stream));
+  CK(launch_one(ctx, a, ctx->d_scratch[0], ctx->scratch_slots, (cudaStream_t)stream));
   return GB_LW_OK;
 }
 
@@ -543,7 +558,7 @@ int gb_rrtmg_lw(gb_lw_context* ctx, int ncol, int nlay, int* icld, int idrv, con
     a.duflx_dt = O + lo.duflx; a.duflxc_dt = O + lo.duflxc; a.hr = O + lo.hr; a.hrc = O + lo.hrc;
     a.col_err = nullptr;
     a.err_flag = ctx->d_err_host;
-    CK(gb_lw_launch(a, ctx->d_tables, ctx->d_scratch[k & 1], ctx->scratch_slots, s));
+    CK(launch_one(ctx, a, ctx->d_scratch[k & 1], ctx->scratch_slots, s));
     auto D2H = [&](double* dst, size_t soff, size_t rows) {
       return copy2d(dst + c0, (size_t)ld_out, O + soff, P, nc, rows, cudaMemcpyDeviceToHost, s);
     };
@@ -730,7 +745,7 @@ int gb_rrtmg_lw_gas_optics_diag(gb_lw_context* ctx, int ncol, int nlay, const do
     cudaFree(dt);
     return rc;
   }
-  cudaError_t e = gb_lw_launch(a, ctx->d_tables, ctx->d_scratch[0], ctx->scratch_slots, 0);
+  cudaError_t e = launch_one(ctx, a, ctx->d_scratch[0], ctx->scratch_slots, 0);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e == cudaSuccess) e = cudaMemcpy(taut, dt, n2 * GB_NGPT * 4, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(fracs, dt + n2 * GB_NGPT, n2 * GB_NGPT * 4, cudaMemcpyDeviceToHost);
@@ -825,6 +840,7 @@ int gb_rrtmg_lw_autotune(gb_lw_context* ctx, void* stream, int ngrid, const gb_l
   CK(cudaEventCreate(&e1));
   gb_lw_tuning bt{};
   bt.ms = 1e30;
+  ctx->last_tune.clear();
   cudaError_t err = cudaSuccess;
   for (const Cand& c : cands) {
     const int nb = c.per * ctx->num_sms;
@@ -837,6 +853,14 @@ int gb_rrtmg_lw_autotune(gb_lw_context* ctx, void* stream, int ngrid, const gb_l
     if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
     if (err != cudaSuccess) break;
     const double per_launch = ms / reps;
+    gb_lw_tuning rec{};
+    rec.variant = c.v;
+    rec.threads = gb_lw_variant(c.v).threads;
+    rec.min_blocks = gb_lw_variant(c.v).min_blocks;
+    rec.blocks_per_sm = c.per;
+    rec.blocks = nb;
+    rec.ms = per_launch;
+    ctx->last_tune.push_back(rec);
     if (per_launch < bt.ms) {
       bt.variant = c.v;
       bt.threads = gb_lw_variant(c.v).threads;
@@ -852,6 +876,13 @@ int gb_rrtmg_lw_autotune(gb_lw_context* ctx, void* stream, int ngrid, const gb_l
   store_tuning(ctx, b.nsmax, batch_kind(b), bt);
   if (best) *best = bt;
   return GB_LW_OK;
+}
+
+int gb_rrtmg_lw_autotune_report(gb_lw_context* ctx, gb_lw_tuning* out, int max) {
+  if (!ctx || (max > 0 && !out)) return GB_LW_E_ARGS;
+  const int n = (int)ctx->last_tune.size();
+  for (int i = 0; i < n && i < max; ++i) out[i] = ctx->last_tune[i];
+  return n;
 }
 
 int gb_rrtmg_lw_batch_graph_create(gb_lw_context* ctx, int ngrid, const gb_lw_grid* grids, gb_lw_graph** out) {

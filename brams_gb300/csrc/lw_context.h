@@ -36,6 +36,7 @@ struct gb_lw_context {
   size_t bscratch_bytes = 0;
   std::vector<gb_lw_tuning> tuned;  // autotuned shapes, parallel to tuned_nlay (largest nlay of the batch)
   std::vector<int> tuned_nlay;
+  std::vector<gb_lw_tuning> last_tune;  // every candidate of the last autotune call
   // McICA draws of fused-cloud grids in batched calls (grown on demand)
   double* d_fdraws = nullptr;
   size_t fdraws_elems = 0;

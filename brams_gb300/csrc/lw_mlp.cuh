@@ -43,27 +43,48 @@ struct GbMlpNorm {
 
 namespace gbmlp {
 
-// Raw features of one layer from the rrtmg_lw inputs (Fortran layout, leading
-// dimension ld); returns false if the layer is outside the physical domain.
-__device__ __forceinline__ void layer_features(const double* __restrict__ play, const double* __restrict__ plev,
-                                               const double* __restrict__ tlay, const double* __restrict__ tlev,
-                                               const double* __restrict__ h2o, const double* __restrict__ o3,
-                                               const double* __restrict__ co2, const double* __restrict__ ch4,
-                                               const double* __restrict__ n2o, long long ld, long long icol,
-                                               int lay, double grav, double avogad, float* f) {
+// The rrtmg_lw inputs one layer's features are made of.
+struct RawLayer {
+  double play, plev0, plev1, tlay, tlev, h2o, o3, co2, ch4, n2o;
+};
+
+// Loads of one layer's inputs (Fortran layout, leading dimension ld); issued
+// early by the inference kernel so that their latency hides behind the MMAs.
+__device__ __forceinline__ RawLayer load_raw(const double* __restrict__ play, const double* __restrict__ plev,
+                                            const double* __restrict__ tlay, const double* __restrict__ tlev,
+                                            const double* __restrict__ h2o, const double* __restrict__ o3,
+                                            const double* __restrict__ co2, const double* __restrict__ ch4,
+                                            const double* __restrict__ n2o, long long ld, long long icol, int lay) {
   const long long o = icol + ld * lay;
-  const float pavel = (float)__ldg(play + o);
-  const float tavel = (float)__ldg(tlay + o);
-  const double dpz = __ldg(plev + o) - __ldg(plev + o + ld);
-  const float w1 = (float)__ldg(h2o + o);
+  RawLayer r;
+  r.play = __ldg(play + o);
+  r.plev0 = __ldg(plev + o);
+  r.plev1 = __ldg(plev + o + ld);
+  r.tlay = __ldg(tlay + o);
+  r.tlev = __ldg(tlev + o);
+  r.h2o = __ldg(h2o + o);
+  r.o3 = __ldg(o3 + o);
+  r.co2 = __ldg(co2 + o);
+  r.ch4 = __ldg(ch4 + o);
+  r.n2o = __ldg(n2o + o);
+  return r;
+}
+
+// The nine raw features of a layer, formed as inatm/setcoef form the column
+// amounts (coldry, 1e-20 scaling, 1e-32 floors for absent gases).
+__device__ __forceinline__ void raw_features(const RawLayer& r, double grav, double avogad, float* f) {
+  const float pavel = (float)r.play;
+  const float tavel = (float)r.tlay;
+  const double dpz = r.plev0 - r.plev1;
+  const float w1 = (float)r.h2o;
   const float amm = (1.0f - w1) * 28.9660f + w1 * 18.0160f;
   const float coldry = (float)dpz * 1.e3f * (float)avogad / (1.e2f * (float)grav * amm * (1.0f + w1));
   float colh2o = 1.e-20f * coldry * w1;
-  float colo3 = 1.e-20f * coldry * (float)__ldg(o3 + o);
-  float colco2 = 1.e-20f * coldry * (float)__ldg(co2 + o);
-  float colch4 = 1.e-20f * coldry * (float)__ldg(ch4 + o);
-  float coln2o = 1.e-20f * coldry * (float)__ldg(n2o + o);
-  const float floor_ = 1.e-32f * coldry;  // setcoef's floors for absent gases
+  float colo3 = 1.e-20f * coldry * (float)r.o3;
+  float colco2 = 1.e-20f * coldry * (float)r.co2;
+  float colch4 = 1.e-20f * coldry * (float)r.ch4;
+  float coln2o = 1.e-20f * coldry * (float)r.n2o;
+  const float floor_ = 1.e-32f * coldry;
   if (colo3 == 0.0f) colo3 = floor_;
   if (colco2 == 0.0f) colco2 = floor_;
   if (colch4 == 0.0f) colch4 = floor_;
@@ -76,7 +97,17 @@ __device__ __forceinline__ void layer_features(const double* __restrict__ play, 
   f[5] = __logf(fmaxf(colch4, 1.e-30f));
   f[6] = __logf(fmaxf(coln2o, 1.e-30f));
   f[7] = __logf(fmaxf((float)dpz, 1.e-30f));
-  f[8] = (float)__ldg(tlev + o);
+  f[8] = (float)r.tlev;
+}
+
+// Raw features of one layer from the rrtmg_lw inputs.
+__device__ __forceinline__ void layer_features(const double* __restrict__ play, const double* __restrict__ plev,
+                                               const double* __restrict__ tlay, const double* __restrict__ tlev,
+                                               const double* __restrict__ h2o, const double* __restrict__ o3,
+                                               const double* __restrict__ co2, const double* __restrict__ ch4,
+                                               const double* __restrict__ n2o, long long ld, long long icol,
+                                               int lay, double grav, double avogad, float* f) {
+  raw_features(load_raw(play, plev, tlay, tlev, h2o, o3, co2, ch4, n2o, ld, icol, lay), grav, avogad, f);
 }
 
 __device__ __forceinline__ bool in_range(const float* f, const GbMlpNorm& n) {

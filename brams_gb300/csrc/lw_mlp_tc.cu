@@ -44,12 +44,14 @@ constexpr int OFF_X = IMG_BYTES;                      // [128 m][64 k]          
 constexpr int OFF_H = OFF_X + M * 128;                // 2 k-blocks x [128][64] 32 KB
 constexpr int OFF_F32 = OFF_H + 2 * M * 128;          // b1 b2 b3 (128 each), b4, omu, osd (288 each)
 constexpr int NF32 = 3 * H + 3 * NO;
-constexpr int OFF_BAR = OFF_F32 + NF32 * 4;           // mbarrier (8 B) + TMEM address (4 B)
-constexpr int SMEM_BYTES = OFF_BAR + 16;
+constexpr int OFF_BAR = OFF_F32 + NF32 * 4;           // two mbarriers (MMA, weights) + TMEM address
+constexpr int SMEM_BYTES = OFF_BAR + 24;
+constexpr int BULK = 16384;                           // bytes per bulk copy of the weight images
 static_assert(OFF_W2 % 1024 == 0 && OFF_W3 % 1024 == 0 && OFF_W4 % 1024 == 0 && OFF_X % 1024 == 0 &&
                   OFF_H % 1024 == 0 && (NOH * 128) % 1024 == 0,
               "operand tiles must start on 1024-byte boundaries (128-byte swizzle atoms)");
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
+static_assert(IMG_BYTES % 16 == 0 && OFF_BAR % 8 == 0, "bulk copies move multiples of 16 bytes; mbarriers are 8-byte aligned");
 
 // byte offset of element (r, k) in a K-major, 128-byte-swizzled tile of R rows
 // (k-blocks of 64 elements; 16-byte chunk c of row r sits at chunk c ^ (r & 7))
@@ -145,14 +147,26 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
   const float* sf = reinterpret_cast<const float*>(sm + OFF_F32);
   const float *b1 = sf, *b2 = sf + H, *b3 = sf + 2 * H, *b4 = sf + 3 * H, *omu = b4 + NO, *osd = omu + NO;
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + OFF_BAR);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + OFF_BAR + 8);
-  // weight images and fp32 vectors into shared memory
-  for (int i = tid; i < IMG_BYTES / 16; i += NT) reinterpret_cast<uint4*>(sm)[i] = img[i];
-  for (int i = tid; i < NF32; i += NT) reinterpret_cast<float*>(sm + OFF_F32)[i] = f32[i];
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + OFF_BAR + 16);
+  // weight images into shared memory by bulk (TMA) copies completing on an
+  // mbarrier; the fp32 vectors by plain loads
+  uint64_t* wbar = bar + 1;
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(bar)) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(wbar)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_addr(wbar)), "r"(IMG_BYTES)
+                 : "memory");
+    for (int off = 0; off < IMG_BYTES; off += BULK) {
+      const int n = IMG_BYTES - off < BULK ? IMG_BYTES - off : BULK;
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+              smem_addr(sm + off)),
+          "l"(reinterpret_cast<const char*>(img) + off), "r"(n), "r"(smem_addr(wbar))
+          : "memory");
+    }
   }
+  for (int i = tid; i < NF32; i += NT) reinterpret_cast<float*>(sm + OFF_F32)[i] = f32[i];
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(tslot)),
                  "r"(TMEM_COLS)
@@ -167,6 +181,8 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
   const uint32_t sbase = smem_addr(sm);
   // the swizzled operand tiles assume a 1024-byte aligned shared-memory window
   bool ok = (sbase & 1023u) == 0;
+  ok = wait_parity(smem_addr(wbar), 0) && ok;  // weight images in place
+  ok = !__syncthreads_or(!ok);
   const uint32_t bar_a = smem_addr(bar);
   const int q = warp & 3, part = warp >> 2;  // lane quarter, column quarter
   const int row = q * 32 + lane;                                // this thread's tile row in the epilogue
@@ -174,6 +190,19 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
   const long long rows = (long long)g.ncol * g.nlay;
   const long long ntile = (rows + M - 1) / M;
   uint32_t phase = 0;
+  // inputs of this thread's row of the next tile, loaded one tile ahead
+  auto fetch = [&](long long t) {
+    gbmlp::RawLayer rw{};
+    const long long r = t * M + tid;
+    if (tid < M && t < ntile && r < rows) {
+      const int lay = (int)(r / g.ncol);
+      const long long icol = r - (long long)lay * g.ncol;
+      rw = gbmlp::load_raw(g.play, g.plev, g.tlay, g.tlev, g.h2ovmr, g.o3vmr, g.co2vmr, g.ch4vmr, g.n2ovmr, g.ld,
+                           icol, lay);
+    }
+    return rw;
+  };
+  gbmlp::RawLayer raw = fetch(blockIdx.x);
   for (long long tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
     const long long r0 = tile * M;
     // ---- features of the tile's rows (rows are layer-major: coalesced loads)
@@ -183,8 +212,7 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
       if (r < rows) {
         const int lay = (int)(r / g.ncol);
         const long long icol = r - (long long)lay * g.ncol;
-        gbmlp::layer_features(g.play, g.plev, g.tlay, g.tlev, g.h2ovmr, g.o3vmr, g.co2vmr, g.ch4vmr, g.n2ovmr, g.ld,
-                              icol, lay, grav, avogad, f);
+        gbmlp::raw_features(raw, grav, avogad, f);
         flag[icol * g.nlay + lay] = gbmlp::in_range(f, nm) ? 1 : 0;
       } else {
 #pragma unroll
@@ -204,6 +232,7 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
 #pragma unroll
       for (int c = 2; c < 8; ++c) *reinterpret_cast<uint4*>(xb + sw128(M, tid, 8 * c)) = make_uint4(0, 0, 0, 0);
     }
+    raw = fetch(tile + gridDim.x);  // consumed by the next tile; in flight during this one's layers
     // ---- four layers
     for (int l = 0; l < 4; ++l) {
       fence_async_smem();

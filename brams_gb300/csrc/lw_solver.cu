@@ -399,6 +399,16 @@ __device__ __noinline__ void prologue_dispatch(int b, const Smem& s, int nl, int
   }
 }
 
+// Scratch slot of a column: clear-sky coefficients float4 [nl][140] (T, Sd,
+// Su, 0), then the cloudy-layer coefficients float4 [nl][140] (A, Bd, Bu, D),
+// written and read only for cloudy cells.
+__device__ __forceinline__ void put_coef(float4* __restrict__ scr, int nl, int lay, int g, const CellCoef& cc,
+                                         bool cloudy) {
+  const int i = lay * GB_NGPT + g;
+  scr[i] = cc.clr;
+  if (cloudy) scr[nl * GB_NGPT + i] = cc.cld;
+}
+
 // All (band, layer) prologues of group gr, spread over the block's threads.
 template <int NT>
 __device__ __forceinline__ void group_prologues(int gr, const Smem& s, int nl, int laytrop) {
@@ -465,8 +475,41 @@ __device__ __forceinline__ void group_cells(int gr, const LwArgs& a, const Smem&
       cloudy = cell_is_cloudy(s, lay, g);
     }
     CellCoef cc = cell_coef(cloudy, odepth, odcld, efcl, cldf, plfrac, blay, dplankup, dplankdn);
-    scr[lay * GB_NGPT + g] = cc.clr;
-    if (cloudy) scr[(nl + lay) * GB_NGPT + g] = cc.cld;
+    put_coef(scr, nl, lay, g, cc, cloudy);
+  }
+}
+
+// Every layer with learned gas optics: one thread per (layer, g) cell of the
+// whole column, no band passes (cells of group_cells without the gather).
+template <int NT>
+__device__ __forceinline__ void learned_cells(const LwArgs& a, const Smem& s, int nl, const float* __restrict__ T,
+                                              long long icol, float4* __restrict__ scr) {
+  const bool clouds = a.icld >= 1;
+  const float* __restrict__ st = a.sur_tau + icol * nl * GB_NGPT;
+  const float* __restrict__ sf = a.sur_frac + icol * nl * GB_NGPT;
+  for (int cell = threadIdx.x; cell < nl * GB_NGPT; cell += NT) {
+    const int lay = (int)(((float)cell + 0.5f) * (1.0f / GB_NGPT)), g = cell - lay * GB_NGPT;
+    const int b = c_T.ngb[g] - 1;
+    const float taut = __ldg(st + cell) + s.taua[b * nl + lay];
+    const float plfrac = __ldg(sf + cell);
+    if (lay == 0) s.frac1[g] = plfrac;
+    if (a.dbg_taut) {
+      a.dbg_taut[(icol * nl + lay) * GB_NGPT + g] = taut;
+      a.dbg_fracs[(icol * nl + lay) * GB_NGPT + g] = plfrac;
+    }
+    const float secdiff = s.misc[b];
+    const float blay = s.plk_lay[b * nl + lay];
+    const float dplankup = s.plk_lev[b * (nl + 1) + lay + 1] - blay;
+    const float dplankdn = s.plk_lev[b * (nl + 1) + lay] - blay;
+    const float odepth = fmaxf(secdiff * taut, 0.0f);
+    bool cloudy = false;
+    float odcld = 0.0f, efcl = 0.0f, cldf = 0.0f;
+    if (clouds && s.cldlay[lay]) {
+      cldf = cell_cloud(a, s, icol, g, lay, secdiff, b, T, odcld, efcl);
+      cloudy = cell_is_cloudy(s, lay, g);
+    }
+    CellCoef cc = cell_coef(cloudy, odepth, odcld, efcl, cldf, plfrac, blay, dplankup, dplankdn);
+    put_coef(scr, nl, lay, g, cc, cloudy);
   }
 }
 
@@ -510,6 +553,22 @@ __device__ __forceinline__ void solve_column(const LwArgs& a, long long icol, ch
       float tavel = (float)in2(a.tlay, a.ld, icol, lay);
       double dpz = in2(a.plev, a.ld, icol, lay) - in2(a.plev, a.ld, icol, lay + 1);
       float w1 = (float)in2(a.h2ovmr, a.ld, icol, lay);
+      if (s.surok[lay]) {
+        // learned gas optics: only what pwvcm and the checks need (inatm :807-870)
+        const float amm = (1.0f - w1) * amd + w1 * amw;
+        const float coldry = (float)dpz * 1.e3f * (float)c_T.avogad / (1.e2f * (float)c_T.grav * amm * (1.0f + w1));
+        s.f[F_COLDRY * nl + lay] = coldry;
+        s.f[F_COLH2O * nl + lay] = 1.e-20f * (coldry * w1);  // as colh2o = 1e-20 * wk1 below
+        if (!(pavel > 0.0f) || !(tavel > 0.0f) || !isfinite(pavel) || !isfinite(tavel)) my_bad = 1;
+        const float plog = __logf(pavel);
+        bool lower = plog > 4.56f;
+        if (fabsf(plog - 4.56f) < 1.0e-4f) lower = log(pd) > 4.56;
+        if (lower) {
+          atomicAdd(&s.iscal[0], 1);
+          atomicAdd(&s.iscal[1], lay + 1);
+        }
+        continue;
+      }
       float w2 = (float)in2(a.co2vmr, a.ld, icol, lay);
       float w3 = (float)in2(a.o3vmr, a.ld, icol, lay);
       float w4 = (float)in2(a.n2ovmr, a.ld, icol, lay);
@@ -697,7 +756,7 @@ __device__ __forceinline__ void solve_column(const LwArgs& a, long long icol, ch
 #pragma unroll
         for (int w = 0; w < 5; ++w) {
           const int g = w * 32 + lane;
-          cb[w] = g < GB_NGPT ? __double_as_longlong(__ldcs(a.cldfmcl + base + g)) : 0LL;
+          cb[w] = g < GB_NGPT ? __double_as_longlong(__ldg(a.cldfmcl + base + g)) : 0LL;
         }
         unsigned any = 0u;
 #pragma unroll
@@ -732,6 +791,10 @@ __device__ __forceinline__ void solve_column(const LwArgs& a, long long icol, ch
       }
       if (err) atomicMax(&s.iscal[2], err);
     }
+    // learned gas optics for every layer of this column: one pass over all cells
+    int notlearned = 0;
+    for (int l = tid; l < nl; l += NT) notlearned |= !s.surok[l];
+    const bool all_learned = a.sur_flag != nullptr && !__syncthreads_or(notlearned);
     int anybad = __syncthreads_or(my_bad);
     const int laytrop = s.iscal[0];
     if (tid < 32) {
@@ -773,11 +836,16 @@ __device__ __forceinline__ void solve_column(const LwArgs& a, long long icol, ch
     }
     __syncthreads();
     // ---------------- phase 2: gas optics and cell coefficients, band by band
-    for (int gr = 0; gr < NGROUP; ++gr) {
-      group_prologues<NT>(gr, s, nl, laytrop);
+    if (all_learned) {
+      learned_cells<NT>(a, s, nl, T, icol, scr);
       __syncthreads();
-      group_cells<NT>(gr, a, s, nl, laytrop, T, icol, scr);
-      __syncthreads();
+    } else {  // taumol for every layer, or for the layers outside the network's range
+      for (int gr = 0; gr < NGROUP; ++gr) {
+        group_prologues<NT>(gr, s, nl, laytrop);
+        __syncthreads();
+        group_cells<NT>(gr, a, s, nl, laytrop, T, icol, scr);
+        __syncthreads();
+      }
     }
 
     // ---------------- phase 3: sweeps, one thread per g-point
@@ -796,9 +864,12 @@ __device__ __forceinline__ void solve_column(const LwArgs& a, long long icol, ch
       float radld = 0.0f, radclrd = 0.0f;
       for (int L0 = nl - 1; L0 >= 0; L0 -= 4) {
         const int nb = L0 + 1 < 4 ? L0 + 1 : 4;  // levels L0, L0-1, .., L0-nb+1
-        float4 c[4];
+        float2 c[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) c[j] = j < nb ? scr[(L0 - j) * GB_NGPT + g] : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int j = 0; j < 4; ++j) {
+          const float4 v = j < nb ? scr[(L0 - j) * GB_NGPT + g] : make_float4(0.f, 0.f, 0.f, 0.f);
+          c[j] = make_float2(v.x, v.y);  // T, Sd
+        }
         float q0[4], q1[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -832,10 +903,12 @@ __device__ __forceinline__ void solve_column(const LwArgs& a, long long icol, ch
       // upward (rtrnmc.f90:486-529): level 0 is the surface, level L+1 follows layer L
       for (int v0 = 0; v0 <= nl; v0 += 4) {
         const int nb = nl + 1 - v0 < 4 ? nl + 1 - v0 : 4;  // levels v0 .. v0+nb-1
-        float4 c[4];
+        float2 c[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
-          c[j] = (j < nb && v0 + j >= 1) ? scr[(v0 + j - 1) * GB_NGPT + g] : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int j = 0; j < 4; ++j) {
+          const float4 v = (j < nb && v0 + j >= 1) ? scr[(v0 + j - 1) * GB_NGPT + g] : make_float4(0.f, 0.f, 0.f, 0.f);
+          c[j] = make_float2(v.x, v.z);  // T, Su
+        }
         float u0[4], u1[4], u2[4], u3[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
@@ -848,10 +921,10 @@ __device__ __forceinline__ void solve_column(const LwArgs& a, long long icol, ch
                 radlu = fmaf(radlu, k.x, k.z);
                 d_radlu *= k.w;
               } else {
-                radlu = fmaf(radlu, c[j].x, c[j].z);
+                radlu = fmaf(radlu, c[j].x, c[j].y);
                 d_radlu *= c[j].x;
               }
-              radclru = fmaf(radclru, c[j].x, c[j].z);
+              radclru = fmaf(radclru, c[j].x, c[j].y);
               d_radclru *= c[j].x;
             }
             u0[j] = radlu * wgt;

@@ -41,7 +41,7 @@ EXPORTS = [
     "gb_lw_mlp_create", "gb_lw_mlp_destroy", "gb_lw_mlp_save", "gb_lw_mlp_load", "gb_lw_mlp_get_params",
     "gb_lw_mlp_set_params", "gb_lw_mlp_set_loss_weights", "gb_lw_mlp_samples", "gb_lw_mlp_fit_norm",
     "gb_lw_mlp_prepare", "gb_lw_mlp_gradients", "gb_lw_mlp_train_step", "gb_lw_mlp_forward", "gb_lw_mlp_infer",
-    "gb_rrtmg_lw_batch_surrogate", "gb_lw_mlp_set_engine",
+    "gb_rrtmg_lw_batch_surrogate", "gb_lw_mlp_set_engine", "gb_rrtmg_lw_autotune_report",
 ]
 MLP_MMA_SYNC, MLP_TCGEN05 = 0, 1
 MLP_NPARAM = 72352
@@ -152,6 +152,7 @@ def load_library(path: str = LIB_PATH):
         L.gb_lw_mlp_infer.argtypes = [P, P, GP, P, P, P]
         L.gb_rrtmg_lw_batch_surrogate.argtypes = [P, P, I, GP, P]
         L.gb_lw_mlp_set_engine.argtypes = [P, I]
+        L.gb_rrtmg_lw_autotune_report.argtypes = [P, C.POINTER(Tuning), I]
         L.gb_rrtmg_lw_strerror.restype = C.c_char_p
         L.gb_rrtmg_lw_strerror.argtypes = [I]
         L.gb_rrtmg_lw_last_error.restype = C.c_char_p
@@ -303,6 +304,13 @@ class Context:
         _check(self.L, self.h, self.L.gb_rrtmg_lw_autotune(self.h, _ptr(stream or 0), n, arr, sample_cols, reps,
                                                            C.byref(t)))
         return t.as_dict()
+
+    def autotune_report(self) -> list:
+        """Every candidate of the last autotune call: shape and time per launch (ms)."""
+        n = self.L.gb_rrtmg_lw_autotune_report(self.h, None, 0)
+        arr = (Tuning * max(n, 1))()
+        self.L.gb_rrtmg_lw_autotune_report(self.h, arr, n)
+        return [arr[i].as_dict() for i in range(n)]
 
     def tuning(self, nlay: int, kind: int = KIND_FUSED) -> dict:
         """Shape used for batches of this largest nlay and kind (KIND_FUSED | KIND_LEARNED bits)."""

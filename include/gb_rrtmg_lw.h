@@ -234,6 +234,10 @@ int gb_rrtmg_lw_batch_device(gb_lw_context* ctx, void* stream, int ngrid, const 
 int gb_rrtmg_lw_autotune(gb_lw_context* ctx, void* stream, int ngrid, const gb_lw_grid* grids,
                          int sample_cols, int reps, gb_lw_tuning* best);
 
+/* Every candidate of the last gb_rrtmg_lw_autotune call with its time (up to
+ * max into out); returns the number of candidates. */
+int gb_rrtmg_lw_autotune_report(gb_lw_context* ctx, gb_lw_tuning* out, int max);
+
 /* Shapes are kept per largest layer count and batch kind: GB_LW_KIND_FUSED
  * if any grid generates its McICA clouds in the kernel, | GB_LW_KIND_LEARNED
  * if any grid uses learned gas optics.  _get returns the shape

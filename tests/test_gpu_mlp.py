@@ -166,3 +166,52 @@ def test_tcgen05_inference_matches_mma_sync(ctx, trained):
     assert np.abs(np.log(t1) - np.log(t0)).max() <= 0.05
     assert np.abs(np.log(t1) - np.log(t0)).mean() <= 2e-3
     assert np.abs(f1 - f0).max() <= 5e-3
+
+
+def test_what_the_network_gains(ctx):
+    """The trained network (brams_gb300/data/lw_mlp.gbmlp) against the method
+    without it on 32,768 columns x 45 layers: the column kernel with learned
+    gas optics must beat the one running taumol by at least 1.3x at a
+    heating-rate RMSE within 0.1 K/day of the FP64 oracle; the inference cost
+    and the end-to-end ratio are printed (run with -s)."""
+    import pyoracle
+
+    torch = _torch()
+    ncol, nlay = 32768, 45
+    spec = ProfileSpec(ncol=ncol, nlay=nlay, seed=80, t_noise=4.0, h2o_sigma=0.5)
+    st = make_state(spec)
+    tauc = pyoracle.cldprop_columns(st)
+    mlp = S.load(ctx)
+    gp, gl = S.DeviceGrid(st, tauc), S.DeviceGrid(st, tauc)
+    rows = ncol * nlay
+    tau = torch.empty((rows, 140), dtype=torch.float32, device="cuda")
+    frac = torch.empty_like(tau)
+    flag = torch.empty(rows, dtype=torch.uint8, device="cuda")
+
+    def timeit(fn, n=5):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    t_plain = timeit(lambda: ctx.rrtmg_lw_batch_device([gp.desc(seed0=9)]))
+    t_inf = timeit(lambda: mlp.infer(gl.desc(seed0=9), tau, frac, flag))
+    lg = gl.desc(seed0=9, sur_tau=tau, sur_frac=frac, sur_flag=flag)
+    t_col = timeit(lambda: ctx.rrtmg_lw_batch_device([lg]))
+    assert ctx.sync_status() == 0
+    n = 1024
+    sub = {k: np.asfortranarray(v[:n]) for k, v in st.items()}
+    mc = pyoracle.mcica_per_column(sub, np.asfortranarray(tauc[:, :n]), icld=3, base_seed=9)
+    ref = pyoracle.rrtmg_lw(sub, mc, icld=3)
+    hr_l = gl.outputs()["hr"][:n]
+    rmse = float(np.sqrt(np.mean((hr_l - ref["hr"]) ** 2)))
+    print(f"\nplain column kernel {t_plain:.2f} ms; learned: inference {t_inf:.2f} ms + column kernel {t_col:.2f} ms "
+          f"(column kernel {t_plain / t_col:.2f}x, end to end {t_plain / (t_inf + t_col):.2f}x); "
+          f"heating-rate RMSE {rmse:.4f} K/day, layers on the network {flag.float().mean().item():.3f}")
+    assert rmse <= 0.1
+    assert t_plain / t_col >= 1.3
