@@ -17,6 +17,7 @@
 #include <stdint.h>
 
 #define GB_MLP_NF 9
+#define GB_MLP_RANGE_MARGIN 0.02f  // validity range = training range widened by 2% of its width per side
 #define GB_MLP_KIN 16     // input width padded to one mma k-step
 #define GB_MLP_H 128
 #define GB_MLP_NOUT 280

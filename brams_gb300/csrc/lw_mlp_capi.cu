@@ -315,11 +315,17 @@ int gb_lw_mlp_fit_norm(gb_lw_mlp* m, void* stream, int64_t rows, const float* d_
   GbMlpNorm& n = m->norm;
   int rc = colstats(m->ctx, st, rows, GB_MLP_NF, GB_MLP_NF, d_feat, 0, mu, sd, lo, hi);
   if (rc) return rc;
+  // The validity range is the training range widened by GB_MLP_RANGE_MARGIN
+  // of its width on each side: layers at the edge of the training set (the
+  // model-top layer, whose thickness and column amounts are the smallest of
+  // every profile) must not drop out over a rounding or a slightly thinner
+  // top layer.
   for (int i = 0; i < GB_MLP_NF; ++i) {
     n.in_mu[i] = (float)mu[i];
     n.in_sd[i] = (float)std::max(sd[i], 1e-6);
-    n.in_lo[i] = lo[i];
-    n.in_hi[i] = hi[i];
+    const float pad = GB_MLP_RANGE_MARGIN * (hi[i] - lo[i]);
+    n.in_lo[i] = lo[i] - pad;
+    n.in_hi[i] = hi[i] + pad;
   }
   for (int i = GB_MLP_NF; i < GB_MLP_KIN; ++i) {
     n.in_mu[i] = 0.0f;

@@ -303,8 +303,10 @@ int gb_lw_mlp_set_loss_weights(gb_lw_mlp* mlp, const float* w280);
  * d_frac[rows][140], rows = ncol*nlay. */
 int gb_lw_mlp_samples(gb_lw_context* ctx, void* stream, const gb_lw_grid* grid, float* d_feat, float* d_tau,
                       float* d_frac);
-/* Fits the input/output standardisation and the validity range (min/max of
- * every feature) on a sample set. */
+/* Fits the input/output standardisation and the validity range on a sample
+ * set: the min/max of every feature, widened by 2% of that width on each side
+ * so that layers at the edge of the training set (the model-top layer) stay
+ * on the network. */
 int gb_lw_mlp_fit_norm(gb_lw_mlp* mlp, void* stream, int64_t rows, const float* d_feat, const float* d_tau,
                        const float* d_frac);
 /* Network inputs d_x (bf16 [rows][16]) and targets d_t (fp32 [rows][288],
