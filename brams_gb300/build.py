@@ -17,6 +17,11 @@ OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libgb_rrtmg_lw.so")
 UNITS = ["lw_solver.cu", "lw_mcica.cu", "lw_capi.cu", "lw_tables.cpp", "lw_mlp.cu", "lw_mlp_capi.cu", "lw_mlp_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# The column kernel is compiled without multiply-add contraction: every fused
+# multiply-add in it is an explicit fmaf, so that its results are fixed by the
+# source and every launch shape and kernel flavour (full, learned-only,
+# hand-over list) gives the same bits for a column.
+UNIT_FLAGS = {"lw_solver.cu": ["-fmad=false"]}
 
 
 def nvcc() -> str:
@@ -44,7 +49,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
 
     def comp(u):
         obj = os.path.join(OUT, u.rsplit(".", 1)[0] + ".o")
-        cmd = [cc] + common + ["-c", os.path.join(SRC, u), "-o", obj]
+        cmd = [cc] + common + UNIT_FLAGS.get(u, []) + ["-c", os.path.join(SRC, u), "-o", obj]
         if u.endswith(".cpp"):
             cmd = [cc] + common + ["-x", "cu", "-c", os.path.join(SRC, u), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)

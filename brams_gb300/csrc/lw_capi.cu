@@ -32,6 +32,8 @@ struct gb_lw_graph {
   cudaGraphExec_t exec = nullptr;
   float4* scratch = nullptr;
   double* draws = nullptr;  // McICA draws of the fused-cloud grids
+  long long* fall = nullptr;  // hand-over list of a batch with learned gas optics
+  unsigned* nfall = nullptr;
 };
 
 int gb_ctx_fail(gb_lw_context* c, cudaError_t e, const char* where) {
@@ -175,13 +177,16 @@ int batch_kind(const LwBatch& b) {
 
 // Default shapes, measured on GB300 at 45 layers (108,000 columns): batches
 // that read the McICA sub-column arrays run best with four blocks per SM
-// (more L1 for the table gathers), fused-cloud batches with six.
+// (more L1 for the table gathers), fused-cloud batches with six.  Batches
+// with learned gas optics index the learned-only kernel's shapes (its
+// variant 0: 160 threads, six blocks per SM).
 gb_lw_tuning default_tuning(gb_lw_context* ctx, int nlay, int kind) {
   gb_lw_tuning t{};
-  t.variant = (kind & GB_LW_KIND_FUSED) ? 1 : 2;
-  t.threads = gb_lw_variant(t.variant).threads;
-  t.min_blocks = gb_lw_variant(t.variant).min_blocks;
-  const int occ = std::max(1, gb_lw_slots(nlay, t.variant) / std::max(1, ctx->num_sms));
+  const bool lean = kind & GB_LW_KIND_LEARNED;
+  t.variant = lean ? 0 : (kind & GB_LW_KIND_FUSED) ? 1 : 2;
+  t.threads = gb_lw_variant(t.variant, lean).threads;
+  t.min_blocks = gb_lw_variant(t.variant, lean).min_blocks;
+  const int occ = std::max(1, gb_lw_slots(nlay, t.variant, lean) / std::max(1, ctx->num_sms));
   t.blocks_per_sm = std::min(occ, t.min_blocks);
   t.blocks = t.blocks_per_sm * ctx->num_sms;
   t.ms = 0.0;
@@ -233,6 +238,35 @@ int ensure_bscratch(gb_lw_context* ctx, int nlay, int blocks) {
     return GB_LW_E_NOMEM;
   }
   ctx->bscratch_bytes = bytes;
+  return 0;
+}
+
+// A batch with learned gas optics gets the context's hand-over list (room
+// for every column of the batch); other batches run the full kernel alone.
+int attach_fall(gb_lw_context* ctx, LwBatch& b) {
+  b.fall = nullptr;
+  b.nfall = nullptr;
+  if (!(batch_kind(b) & GB_LW_KIND_LEARNED)) return 0;
+  const size_t need = (size_t)b.col0[b.ngrid];
+  if (need > ctx->fall_elems || !ctx->d_nfall) {
+    cudaFree(ctx->d_fall);
+    ctx->d_fall = nullptr;
+    ctx->fall_elems = 0;
+    if (!ctx->d_nfall && cudaMalloc(&ctx->d_nfall, sizeof(unsigned)) != cudaSuccess) {
+      cudaGetLastError();
+      ctx->d_nfall = nullptr;
+      ctx->last_error = "device allocation of the hand-over list failed";
+      return GB_LW_E_NOMEM;
+    }
+    if (cudaMalloc(&ctx->d_fall, need * sizeof(long long)) != cudaSuccess) {
+      cudaGetLastError();
+      ctx->last_error = "device allocation of the hand-over list failed";
+      return GB_LW_E_NOMEM;
+    }
+    ctx->fall_elems = need;
+  }
+  b.fall = ctx->d_fall;
+  b.nfall = ctx->d_nfall;
   return 0;
 }
 
@@ -343,6 +377,7 @@ int gb_ctx_launch_batch(gb_lw_context* ctx, LwBatch& b, cudaStream_t stream) {
     if (rc) return rc;
   }
   b.scratch = ctx->d_bscratch;
+  if ((rc = attach_fall(ctx, b)) != 0) return rc;
   cudaError_t e = gb_lw_launch_batch(b, ctx->d_tables, t.variant, t.blocks, stream);
   if (e != cudaSuccess) return gb_ctx_fail(ctx, e, "batched launch");
   return GB_LW_OK;
@@ -410,6 +445,8 @@ int gb_rrtmg_lw_free(gb_lw_context* ctx) {
   cudaFree(ctx->d_sur);
   cudaFree(ctx->d_sur_flag);
   cudaFree(ctx->d_fdraws);
+  cudaFree(ctx->d_fall);
+  cudaFree(ctx->d_nfall);
   delete ctx;
   return GB_LW_OK;
 }
@@ -776,15 +813,16 @@ int gb_rrtmg_lw_tuning_set(gb_lw_context* ctx, int nlay, int kind, const gb_lw_t
   if (!ctx || !shape || nlay < 1 || nlay > GB_MAXLAY || kind < 0 || kind > 3) return GB_LW_E_ARGS;
   if (shape->variant < 0 || shape->variant >= gb_lw_num_variants()) return GB_LW_E_ARGS;
   cudaSetDevice(ctx->device);
-  const int occ = gb_lw_slots(nlay, shape->variant) / std::max(1, ctx->num_sms);
+  const bool lean = kind & GB_LW_KIND_LEARNED;
+  const int occ = gb_lw_slots(nlay, shape->variant, lean) / std::max(1, ctx->num_sms);
   if (shape->blocks_per_sm < 1 || shape->blocks_per_sm > occ) {
     ctx->last_error = "blocks_per_sm exceeds what fits on an SM for this nlay and variant";
     return GB_LW_E_ARGS;
   }
   gb_lw_tuning t{};
   t.variant = shape->variant;
-  t.threads = gb_lw_variant(t.variant).threads;
-  t.min_blocks = gb_lw_variant(t.variant).min_blocks;
+  t.threads = gb_lw_variant(t.variant, lean).threads;
+  t.min_blocks = gb_lw_variant(t.variant, lean).min_blocks;
   t.blocks_per_sm = shape->blocks_per_sm;
   t.blocks = t.blocks_per_sm * ctx->num_sms;
   t.ms = shape->ms;
@@ -811,8 +849,9 @@ int gb_rrtmg_lw_autotune(gb_lw_context* ctx, void* stream, int ngrid, const gb_l
   struct Cand { int v, per; };
   std::vector<Cand> cands;
   int max_blocks = 1;
+  const bool lean = batch_kind(b) & GB_LW_KIND_LEARNED;
   for (int v = 0; v < gb_lw_num_variants(); ++v) {
-    const int occ = gb_lw_slots(b.nsmax, v) / std::max(1, ctx->num_sms);
+    const int occ = gb_lw_slots(b.nsmax, v, lean) / std::max(1, ctx->num_sms);
     for (int per = 1; per <= occ; ++per) {
       cands.push_back({v, per});
       max_blocks = std::max(max_blocks, per * ctx->num_sms);
@@ -822,6 +861,7 @@ int gb_rrtmg_lw_autotune(gb_lw_context* ctx, void* stream, int ngrid, const gb_l
   rc = ensure_bscratch(ctx, b.nsmax, max_blocks);
   if (rc) return rc;
   b.scratch = ctx->d_bscratch;
+  if ((rc = attach_fall(ctx, b)) != 0) return rc;
   // the fused-cloud draws are made once: every candidate times the column kernel alone
   const size_t nd = gb_ctx_fused_draws(b);
   if (nd > ctx->fdraws_elems) {
@@ -855,16 +895,16 @@ int gb_rrtmg_lw_autotune(gb_lw_context* ctx, void* stream, int ngrid, const gb_l
     const double per_launch = ms / reps;
     gb_lw_tuning rec{};
     rec.variant = c.v;
-    rec.threads = gb_lw_variant(c.v).threads;
-    rec.min_blocks = gb_lw_variant(c.v).min_blocks;
+    rec.threads = gb_lw_variant(c.v, lean).threads;
+    rec.min_blocks = gb_lw_variant(c.v, lean).min_blocks;
     rec.blocks_per_sm = c.per;
     rec.blocks = nb;
     rec.ms = per_launch;
     ctx->last_tune.push_back(rec);
     if (per_launch < bt.ms) {
       bt.variant = c.v;
-      bt.threads = gb_lw_variant(c.v).threads;
-      bt.min_blocks = gb_lw_variant(c.v).min_blocks;
+      bt.threads = gb_lw_variant(c.v, lean).threads;
+      bt.min_blocks = gb_lw_variant(c.v, lean).min_blocks;
       bt.blocks_per_sm = c.per;
       bt.blocks = nb;
       bt.ms = per_launch;
@@ -908,6 +948,16 @@ int gb_rrtmg_lw_batch_graph_create(gb_lw_context* ctx, int ngrid, const gb_lw_gr
     gb_rrtmg_lw_graph_destroy(g);
     return GB_LW_E_NOMEM;
   }
+  if (batch_kind(b) & GB_LW_KIND_LEARNED) {  // the graph owns its hand-over list
+    if (cudaMalloc(&g->fall, (size_t)b.col0[ngrid] * sizeof(long long)) != cudaSuccess ||
+        cudaMalloc(&g->nfall, sizeof(unsigned)) != cudaSuccess) {
+      cudaGetLastError();
+      gb_rrtmg_lw_graph_destroy(g);
+      return GB_LW_E_NOMEM;
+    }
+    b.fall = g->fall;
+    b.nfall = g->nfall;
+  }
   cudaStream_t s = ctx->streams[0];
   cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed);
   if (e == cudaSuccess) {
@@ -941,6 +991,8 @@ int gb_rrtmg_lw_graph_destroy(gb_lw_graph* g) {
   if (g->graph) cudaGraphDestroy(g->graph);
   cudaFree(g->scratch);
   cudaFree(g->draws);
+  cudaFree(g->fall);
+  cudaFree(g->nfall);
   delete g;
   return GB_LW_OK;
 }

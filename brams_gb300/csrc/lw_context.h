@@ -40,6 +40,11 @@ struct gb_lw_context {
   // McICA draws of fused-cloud grids in batched calls (grown on demand)
   double* d_fdraws = nullptr;
   size_t fdraws_elems = 0;
+  // columns the learned-only kernel hands over to the full kernel, and their
+  // count (batches with learned gas optics; grown on demand)
+  long long* d_fall = nullptr;
+  unsigned* d_nfall = nullptr;
+  size_t fall_elems = 0;
   // surrogate outputs of batched calls with a network (grown on demand)
   float* d_sur = nullptr;
   unsigned char* d_sur_flag = nullptr;

@@ -120,18 +120,19 @@ __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(
 
 // Region A holds, by phase: the per-layer coefficients f/iv and the term
 // lists (phases 1-2; the McICA draws of the fused cloud mode borrow the term
-// area during phase 1), then the warp partial sums and net fluxes (3-4).
+// area during phase 1), then the warp partial sums and net fluxes (3-4).  The
+// learned-only kernel (lean) runs no taumol and has no term area.
 __host__ __device__ inline size_t terms_offset(int nl) { return ((size_t)(NF + NI) * nl * 4 + 15) & ~size_t(15); }
-__host__ __device__ inline size_t region_a(int nl) {
-  size_t terms = (size_t)nl * TGROUP * 8;
+__host__ __device__ inline size_t region_a(int nl, bool lean) {
+  size_t terms = lean ? 0 : (size_t)nl * TGROUP * 8;
   const size_t draws = align16(GB_NGPT * 8) + align16((GB_NGPT + 1) * 4);
   size_t coef = terms_offset(nl) + (terms > draws ? terms : draws);
   size_t part = align16((size_t)NSW * (nl + 1) * 6 * 4) + (size_t)(nl + 1) * 2 * 8;
   return align16(coef > part ? coef : part);
 }
 
-__host__ __device__ inline size_t smem_bytes(int nl) {
-  size_t a = region_a(nl);
+__host__ __device__ inline size_t smem_bytes(int nl, bool lean) {
+  size_t a = region_a(nl, lean);
   a += align16((size_t)nl * 16 * 4);         // taua
   a += align16((size_t)nl * 16 * 4);         // plk_lay
   a += align16((size_t)(nl + 1) * 16 * 4);   // plk_lev
@@ -144,7 +145,7 @@ __host__ __device__ inline size_t smem_bytes(int nl) {
   return a;
 }
 
-__device__ inline Smem carve(char* base, int nl) {
+__device__ inline Smem carve(char* base, int nl, bool lean) {
   Smem s;
   char* p = base;
   s.f = (float*)p;
@@ -154,7 +155,7 @@ __device__ inline Smem carve(char* base, int nl) {
   s.mtlo = (uint32_t*)(p + terms_offset(nl) + align16(GB_NGPT * 8));
   s.part = (float*)p;
   s.fnet = (double*)(p + align16((size_t)NSW * (nl + 1) * 6 * 4));
-  p += region_a(nl);
+  p += region_a(nl, lean);
   s.taua = (float*)p; p += align16((size_t)nl * 16 * 4);
   s.plk_lay = (float*)p; p += align16((size_t)nl * 16 * 4);
   s.plk_lev = (float*)p; p += align16((size_t)(nl + 1) * 16 * 4);
@@ -514,12 +515,15 @@ __device__ __forceinline__ void learned_cells(const LwArgs& a, const Smem& s, in
 }
 
 // ------------------------------------------------------------------ one column
-template <int NT>
-__device__ __forceinline__ void solve_column(const LwArgs& a, long long icol, char* smem_raw,
+// LEAN: the learned-only flavour -- a column with any layer off the network
+// is not solved (returns false, the same answer in every thread) and the
+// taumol code is not compiled in.
+template <int NT, bool LEAN>
+__device__ __forceinline__ bool solve_column(const LwArgs& a, long long icol, char* smem_raw,
                                              float4* __restrict__ scr, const float* __restrict__ T) {
   constexpr int NWARP = NT / 32;
   const int nl = a.nlay;
-  const Smem s = carve(smem_raw, nl);
+  const Smem s = carve(smem_raw, nl, LEAN);
   const int tid = threadIdx.x;
   const bool fused = a.cloud_mode == LW_CLOUD_FUSED;
   {
@@ -536,12 +540,18 @@ __device__ __forceinline__ void solve_column(const LwArgs& a, long long icol, ch
       s.scal[tid] = 0.0f;
       s.iscal[tid] = 0;
     }
+    int offnet = 0;
     for (int l = tid; l < nl; l += NT) {
       s.cldlay[l] = 0;
       s.surok[l] = a.sur_flag ? (int)__ldg(a.sur_flag + icol * nl + l) : 0;
+      offnet |= !s.surok[l];
     }
     for (int l = tid; l < nl * 5; l += NT) s.cbits[l] = s.fbits[l] = 0u;
-    __syncthreads();
+    if (LEAN) {
+      if (__syncthreads_or(offnet)) return false;
+    } else {
+      __syncthreads();
+    }
 
     // ---------------- phase 1: inatm + setcoef, one thread per layer
     const float stpfac = 296.0f / 1013.0f;
@@ -553,7 +563,7 @@ __device__ __forceinline__ void solve_column(const LwArgs& a, long long icol, ch
       float tavel = (float)in2(a.tlay, a.ld, icol, lay);
       double dpz = in2(a.plev, a.ld, icol, lay) - in2(a.plev, a.ld, icol, lay + 1);
       float w1 = (float)in2(a.h2ovmr, a.ld, icol, lay);
-      if (s.surok[lay]) {
+      if (LEAN || s.surok[lay]) {
         // learned gas optics: only what pwvcm and the checks need (inatm :807-870)
         const float amm = (1.0f - w1) * amd + w1 * amw;
         const float coldry = (float)dpz * 1.e3f * (float)c_T.avogad / (1.e2f * (float)c_T.grav * amm * (1.0f + w1));
@@ -792,9 +802,7 @@ __device__ __forceinline__ void solve_column(const LwArgs& a, long long icol, ch
       if (err) atomicMax(&s.iscal[2], err);
     }
     // learned gas optics for every layer of this column: one pass over all cells
-    int notlearned = 0;
-    for (int l = tid; l < nl; l += NT) notlearned |= !s.surok[l];
-    const bool all_learned = a.sur_flag != nullptr && !__syncthreads_or(notlearned);
+    const bool all_learned = LEAN || (a.sur_flag != nullptr && !__syncthreads_or(offnet));
     int anybad = __syncthreads_or(my_bad);
     const int laytrop = s.iscal[0];
     if (tid < 32) {
@@ -983,26 +991,37 @@ __device__ __forceinline__ void solve_column(const LwArgs& a, long long icol, ch
       __syncthreads();
     }
   }
+  return true;
 }
 
 // ------------------------------------------------------------------ the kernel
 // Persistent blocks walk the batch columns grid after grid; a block's columns
-// increase, so its grid index only moves forward.
-template <int NT, int MINB>
+// increase, so its grid index only moves forward.  FLAVOR 1 is the
+// learned-only kernel, which appends the columns it does not solve to
+// B.fall; FLAVOR 2 is the full kernel walking that list instead of the batch.
+// The unit is compiled without multiply-add contraction, so a column gives
+// the same bits in every flavour and launch shape.
+template <int NT, int MINB, int FLAVOR>
 __global__ void __launch_bounds__(NT, MINB) lw_batch_kernel(const __grid_constant__ LwBatch B,
                                                              const float* __restrict__ T) {
+  constexpr bool LEAN = FLAVOR == 1, list = FLAVOR == 2;
   extern __shared__ __align__(16) char smem_raw[];
   float4* __restrict__ scr = B.scratch + (size_t)blockIdx.x * ((size_t)2 * B.nsmax * GB_NGPT);
-  const long long total = B.col0[B.ngrid];
+  const long long n = list ? (long long)*B.nfall : B.col0[B.ngrid];
   int gi = 0;
-  for (long long gc = blockIdx.x; gc < total; gc += gridDim.x) {
+  for (long long i = blockIdx.x; i < n; i += gridDim.x) {
+    const long long gc = list ? B.fall[i] : i;
+    if (list) gi = 0;  // the list is in no particular order
     while (gc >= B.col0[gi + 1]) ++gi;
-    solve_column<NT>(B.g[gi], gc - B.col0[gi], smem_raw, scr, T);
+    const bool done = solve_column<NT, LEAN>(B.g[gi], gc - B.col0[gi], smem_raw, scr, T);
+    if (LEAN && !done && threadIdx.x == 0) B.fall[atomicAdd(B.nfall, 1u)] = gc;
   }
 }
 
-// compiled shapes (threads per column, min blocks per SM); variant 0 is the default
+// compiled shapes (threads per column block, min blocks per SM); variant 0 is the default
 #define GB_LW_VARIANTS(X) X(0, 160, 5) X(1, 160, 6) X(2, 160, 4) X(3, 256, 3)
+// the learned-only kernel: less shared memory and fewer registers, so more blocks fit
+#define GB_LW_LEAN_VARIANTS(X) X(0, 160, 6) X(1, 160, 7) X(2, 160, 5) X(3, 256, 4)
 
 }  // namespace gb
 
@@ -1015,19 +1034,25 @@ struct VariantInfo {
   cudaError_t (*launch)(const LwBatch&, const float*, int, size_t, cudaStream_t);
 };
 
-template <int NT, int MINB>
+template <int NT, int MINB, int FLAVOR>
 cudaError_t launch_variant(const LwBatch& b, const float* T, int nblocks, size_t smem, cudaStream_t st) {
-  gb::lw_batch_kernel<NT, MINB><<<nblocks, NT, smem, st>>>(b, T);
+  gb::lw_batch_kernel<NT, MINB, FLAVOR><<<nblocks, NT, smem, st>>>(b, T);
   return cudaGetLastError();
 }
 
-#define GB_LW_VARIANT_ENTRY(i, nt, mb) {nt, mb, (const void*)gb::lw_batch_kernel<nt, mb>, launch_variant<nt, mb>},
+#define GB_LW_VARIANT_ENTRY(i, nt, mb) {nt, mb, (const void*)gb::lw_batch_kernel<nt, mb, 0>, launch_variant<nt, mb, 0>},
+#define GB_LW_LEAN_ENTRY(i, nt, mb) {nt, mb, (const void*)gb::lw_batch_kernel<nt, mb, 1>, launch_variant<nt, mb, 1>},
 const VariantInfo kVariants[] = {GB_LW_VARIANTS(GB_LW_VARIANT_ENTRY)};
+const VariantInfo kLean[] = {GB_LW_LEAN_VARIANTS(GB_LW_LEAN_ENTRY)};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
+static_assert(sizeof(kLean) / sizeof(kLean[0]) == kNumVariants, "one variant index range for both kernels");
+// the full kernel over the columns the learned-only kernel hands over
+const VariantInfo kList = {160, 6, (const void*)gb::lw_batch_kernel<160, 6, 2>, launch_variant<160, 6, 2>};
 
-cudaError_t configure(int nlay, int variant, int* blocks_per_sm) {
-  const VariantInfo& v = kVariants[variant];
-  const size_t sm = gb::smem_bytes(nlay);
+const VariantInfo& info(int variant, bool lean) { return lean ? kLean[variant] : kVariants[variant]; }
+
+cudaError_t configure(int nlay, const VariantInfo& v, bool lean, int* blocks_per_sm) {
+  const size_t sm = gb::smem_bytes(nlay, lean);
   cudaError_t e = cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(v.fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return e;
@@ -1038,7 +1063,7 @@ cudaError_t configure(int nlay, int variant, int* blocks_per_sm) {
 // that the rest of the SM's 256 KB stays L1 for the table gathers (the
 // driver otherwise sizes it for the largest block count shared memory alone
 // would allow, even when registers allow fewer).
-cudaError_t set_carveout(int variant, size_t smem, int per) {
+cudaError_t set_carveout(const VariantInfo& v, size_t smem, int per) {
   int dev = 0, max_sm = 0, reserved = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&max_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
@@ -1046,28 +1071,45 @@ cudaError_t set_carveout(int variant, size_t smem, int per) {
   if (max_sm <= 0) return cudaSuccess;
   int pct = (int)std::ceil(100.0 * (double)per * (double)(smem + reserved) / (double)max_sm);
   pct = pct < 1 ? 1 : (pct > 100 ? 100 : pct);
-  return cudaFuncSetAttribute(kVariants[variant].fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+  return cudaFuncSetAttribute(v.fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+}
+
+// One launch of `variant` of the full (lean false) or learned-only kernel
+// with at most `nblocks` blocks and the carve-out for those resident.
+cudaError_t launch_kernel(const LwBatch& b, const float* d_tables, const VariantInfo& v, bool lean, int nblocks,
+                          cudaStream_t stream) {
+  int per = 0;
+  cudaError_t e = configure(b.nsmax, v, lean, &per);
+  if (e != cudaSuccess) return e;
+  int dev = 0, nsm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int resident = (nblocks + nsm - 1) / nsm;
+  const size_t smem = gb::smem_bytes(b.nsmax, lean);
+  e = set_carveout(v, smem, resident < per ? resident : per);
+  if (e != cudaSuccess) return e;
+  return v.launch(b, d_tables, nblocks, smem, stream);
 }
 
 }  // namespace
 
 int gb_lw_num_variants() { return kNumVariants; }
 
-LwVariant gb_lw_variant(int v) {
+LwVariant gb_lw_variant(int v, bool lean) {
   if (v < 0 || v >= kNumVariants) return LwVariant{0, 0};
-  return LwVariant{kVariants[v].threads, kVariants[v].min_blocks};
+  return LwVariant{info(v, lean).threads, info(v, lean).min_blocks};
 }
 
-size_t gb_lw_smem_bytes(int nlay, int) { return gb::smem_bytes(nlay); }
+size_t gb_lw_smem_bytes(int nlay, bool lean) { return gb::smem_bytes(nlay, lean); }
 
 cudaError_t gb_lw_set_tables(const GbTables& T) { return cudaMemcpyToSymbol(gb::c_T, &T, sizeof(GbTables)); }
 
-int gb_lw_slots(int nlay, int variant) {
+int gb_lw_slots(int nlay, int variant, bool lean) {
   if (variant < 0 || variant >= kNumVariants) variant = 0;
   int dev = 0, nsm = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  if (configure(nlay, variant, &per) != cudaSuccess || per < 1) per = 1;
+  if (configure(nlay, info(variant, lean), lean, &per) != cudaSuccess || per < 1) per = 1;
   return nsm * per;
 }
 
@@ -1077,17 +1119,24 @@ cudaError_t gb_lw_launch_batch(const LwBatch& b, const float* d_tables, int vari
                                cudaStream_t stream) {
   if (variant < 0 || variant >= kNumVariants || b.ngrid < 1 || b.ngrid > GB_LW_MAX_GRIDS) return cudaErrorInvalidValue;
   if (b.col0[b.ngrid] <= 0 || nblocks <= 0) return cudaSuccess;
-  int per = 0;
-  cudaError_t e = configure(b.nsmax, variant, &per);
-  if (e != cudaSuccess) return e;
   if ((long long)nblocks > b.col0[b.ngrid]) nblocks = (int)b.col0[b.ngrid];
+  if (!b.fall || !b.nfall) return launch_kernel(b, d_tables, info(variant, false), false, nblocks, stream);
+  // learned gas optics: the learned-only kernel, then the full kernel over
+  // the columns it handed over (its blocks find an empty list and return
+  // when every column was on the network)
+  cudaError_t e = cudaMemsetAsync(b.nfall, 0, sizeof(unsigned), stream);
+  if (e != cudaSuccess) return e;
+  e = launch_kernel(b, d_tables, info(variant, true), true, nblocks, stream);
+  if (e != cudaSuccess) return e;
+  int per = 0;
+  const VariantInfo& lv = kList;
+  e = configure(b.nsmax, lv, false, &per);
+  if (e != cudaSuccess) return e;
   int dev = 0, nsm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const int resident = (nblocks + nsm - 1) / nsm;
-  e = set_carveout(variant, gb::smem_bytes(b.nsmax), resident < per ? resident : per);
-  if (e != cudaSuccess) return e;
-  return kVariants[variant].launch(b, d_tables, nblocks, gb::smem_bytes(b.nsmax), stream);
+  const int nf = per * nsm < nblocks ? per * nsm : nblocks;  // scratch holds nblocks slots
+  return launch_kernel(b, d_tables, lv, false, nf < 1 ? 1 : nf, stream);
 }
 
 cudaError_t gb_lw_launch(const LwArgs& a, const float* d_tables, float4* scratch, int nslots, cudaStream_t stream) {

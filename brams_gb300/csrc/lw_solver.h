@@ -46,11 +46,18 @@ struct LwArgs {
 // kernel takes this by value (kernel parameter space), so the launch carries
 // no device-side descriptor and can be captured in a CUDA graph as is.
 #define GB_LW_MAX_GRIDS 32
+//
+// Batches with learned gas optics (fall and nfall set) run in two launches:
+// a learned-only kernel solves every column whose layers are all on the
+// network and hands the others (batch numbering) over in fall[0 .. *nfall),
+// then the full kernel solves those.  fall holds at least col0[ngrid] entries.
 struct LwBatch {
   int ngrid;
   int nsmax;                              // largest nlay (scratch-slot stride)
   long long col0[GB_LW_MAX_GRIDS + 1];
   float4* scratch;                        // >= gridDim.x slots of 2*nsmax*140 float4
+  long long* fall = nullptr;              // columns handed over by the learned-only kernel
+  unsigned* nfall = nullptr;              // their count (device)
   LwArgs g[GB_LW_MAX_GRIDS];
 };
 
@@ -59,17 +66,20 @@ struct LwBatch {
 struct LwVariant {
   int threads, min_blocks;
 };
+// The learned-only kernel (lean = true) has its own table of as many shapes.
 int gb_lw_num_variants();
-LwVariant gb_lw_variant(int v);
+LwVariant gb_lw_variant(int v, bool lean = false);
 
-size_t gb_lw_smem_bytes(int nlay, int variant = 0);
+size_t gb_lw_smem_bytes(int nlay, bool lean = false);
 // thread blocks of `variant` that fit on the device at once for this nlay
-int gb_lw_slots(int nlay, int variant = 0);
+int gb_lw_slots(int nlay, int variant = 0, bool lean = false);
 // bytes of scratch for `slots` slots: per slot 2*nlay*140 float4 (clear and cloudy cell coefficients)
 size_t gb_lw_scratch_bytes(int nlay, int slots);
 cudaError_t gb_lw_set_tables(const GbTables& T);
 // One grid, default variant, grid = min(ncol, nslots) blocks.
 cudaError_t gb_lw_launch(const LwArgs& a, const float* d_tables, float4* scratch, int nslots, cudaStream_t stream);
-// All grids of `b` in one launch of `nblocks` persistent blocks of `variant`.
+// All grids of `b` in one launch of `nblocks` persistent blocks of `variant`
+// (with b.fall set: the learned-only kernel's `variant`, then the full kernel
+// over the columns it handed over).
 cudaError_t gb_lw_launch_batch(const LwBatch& b, const float* d_tables, int variant, int nblocks,
                                cudaStream_t stream);

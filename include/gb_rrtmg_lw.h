@@ -242,7 +242,10 @@ int gb_rrtmg_lw_autotune_report(gb_lw_context* ctx, gb_lw_tuning* out, int max);
  * if any grid generates its McICA clouds in the kernel, | GB_LW_KIND_LEARNED
  * if any grid uses learned gas optics.  _get returns the shape
  * gb_rrtmg_lw_batch_device would use (tuned, pinned or the default); _set
- * pins one (variant and blocks_per_sm are used, the rest is derived). */
+ * pins one (variant and blocks_per_sm are used, the rest is derived).  For
+ * the GB_LW_KIND_LEARNED kinds the variant is one of the learned-only
+ * kernel's shapes (that kernel solves the columns wholly on the network; the
+ * full kernel, in a second launch, the rest). */
 #define GB_LW_KIND_FUSED 1
 #define GB_LW_KIND_LEARNED 2
 int gb_rrtmg_lw_tuning_get(gb_lw_context* ctx, int nlay, int kind, gb_lw_tuning* out);

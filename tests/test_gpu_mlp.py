@@ -215,3 +215,45 @@ def test_what_the_network_gains(ctx):
           f"heating-rate RMSE {rmse:.4f} K/day, layers on the network {flag.float().mean().item():.3f}")
     assert rmse <= 0.1
     assert t_plain / t_col >= 1.3
+
+
+def test_hand_over_of_columns_off_the_network(ctx):
+    """A batch with learned gas optics runs the learned-only kernel, which
+    hands every column with a layer off the network to the full kernel.  Two
+    grids -- one with columns wholly or partly off the network, one wholly on
+    it -- must give, column for column, exactly what each grid gives alone;
+    every column must be written; the columns wholly off the network must
+    equal the plain solver's."""
+    import pyoracle
+
+    torch = _torch()
+    mlp = S.load(ctx)
+    sa = make_state(ProfileSpec(ncol=37, nlay=45, seed=91, t_noise=4.0, h2o_sigma=0.5))
+    sb = make_state(ProfileSpec(ncol=53, nlay=45, seed=92, t_noise=4.0, h2o_sigma=0.5))
+    for k in ("tlay", "tlev"):
+        sa[k][:4] += 200.0          # columns 0-3: every layer off the network
+    sa["tlay"][4:11, 20] += 200.0   # columns 4-10: one layer off the network
+    ta, tb = pyoracle.cldprop_columns(sa), pyoracle.cldprop_columns(sb)
+
+    def run(grids):
+        mlp.batch([g.desc(seed0=s) for g, s in grids])
+        torch.cuda.synchronize()
+        assert ctx.sync_status() == 0
+        return [g.outputs() for g, _ in grids]
+
+    both = run([(S.DeviceGrid(sa, ta), 7), (S.DeviceGrid(sb, tb), 8)])
+    alone_a = run([(S.DeviceGrid(sa, ta), 7)])[0]
+    alone_b = run([(S.DeviceGrid(sb, tb), 8)])[0]
+    for got, ref in ((both[0], alone_a), (both[1], alone_b)):
+        for k in ref:
+            assert np.array_equal(got[k], ref[k]), k
+        assert (got["uflx"] > 0).all()
+    gp = S.DeviceGrid(sa, ta)
+    ctx.rrtmg_lw_batch_device([gp.desc(seed0=7)])
+    torch.cuda.synchronize()
+    plain = gp.outputs()
+    for k in plain:
+        assert np.array_equal(both[0][k][:4], plain[k][:4]), k
+    # the partly-off columns: network layers and the taumol layer together, close to the plain solver
+    d = np.abs(both[0]["uflx"][4:11] - plain["uflx"][4:11])
+    assert (d <= 0.01 * np.abs(plain["uflx"][4:11]) + 5.0).all(), float(d.max())
