@@ -209,7 +209,7 @@ struct TblEntry {
 };
 __device__ __forceinline__ TblEntry tbl(float od) {
   float tblind = __fdividef(od, BPADE + od);
-  int itr = (int)(10000.0f * tblind + 0.5f);
+  int itr = (int)fmaf(10000.0f, tblind, 0.5f);
   itr = itr < 0 ? 0 : (itr > 10000 ? 10000 : itr);
   TblEntry e;
   if (itr == 0) {
@@ -223,7 +223,7 @@ __device__ __forceinline__ TblEntry tbl(float od) {
     ex = ex <= 1.0e-20f ? 1.0e-20f : ex;
     e.tau = tau;
     e.trans = ex;
-    e.tfn = tau < 0.06f ? tau * (1.0f / 6.0f) : 1.0f - 2.0f * (__fdividef(1.0f, tau) - __fdividef(ex, 1.0f - ex));
+    e.tfn = tau < 0.06f ? tau * (1.0f / 6.0f) : fmaf(-2.0f, __fdividef(1.0f, tau) - __fdividef(ex, 1.0f - ex), 1.0f);
   }
   return e;
 }
@@ -328,16 +328,16 @@ __device__ __forceinline__ CellCoef cell_coef(bool cloudy, float odepth, float o
   CellCoef r;
   float atrans, bbd, bbu, tau_q;
   if (odepth <= 0.06f) {
-    atrans = odepth - 0.5f * odepth * odepth;
+    atrans = fmaf(-0.5f * odepth, odepth, odepth);
     float o = rec_6 * odepth;
-    bbd = plfrac * (blay + dplankdn * o);
-    bbu = plfrac * (blay + dplankup * o);
+    bbd = plfrac * fmaf(dplankdn, o, blay);
+    bbu = plfrac * fmaf(dplankup, o, blay);
     tau_q = odepth;
   } else {
     TblEntry e = tbl(odepth);
     atrans = 1.0f - e.trans;
-    bbd = plfrac * (blay + e.tfn * dplankdn);
-    bbu = plfrac * (blay + e.tfn * dplankup);
+    bbd = plfrac * fmaf(e.tfn, dplankdn, blay);
+    bbu = plfrac * fmaf(e.tfn, dplankup, blay);
     tau_q = e.tau;
   }
   const float gsd = bbd * atrans, gsu = bbu * atrans;
@@ -346,21 +346,21 @@ __device__ __forceinline__ CellCoef cell_coef(bool cloudy, float odepth, float o
     float atot, bbdtot, bbutot;
     float odtot = odepth + odcld;
     if (odtot < 0.06f) {
-      atot = odtot - 0.5f * odtot * odtot;
+      atot = fmaf(-0.5f * odtot, odtot, odtot);
       float o = rec_6 * odtot;
-      bbdtot = plfrac * (blay + dplankdn * o);
-      bbutot = plfrac * (blay + dplankup * o);
+      bbdtot = plfrac * fmaf(dplankdn, o, blay);
+      bbutot = plfrac * fmaf(dplankup, o, blay);
     } else {
       // odepth <= 0.06: table at odepth + odcld; otherwise at tau_tbl(itgas) + odcld
       TblEntry et = tbl((odepth <= 0.06f ? odepth : tau_q) + odcld);
       atot = 1.0f - et.trans;
-      bbdtot = plfrac * (blay + et.tfn * dplankdn);
-      bbutot = plfrac * (blay + et.tfn * dplankup);
+      bbdtot = plfrac * fmaf(et.tfn, dplankdn, blay);
+      bbutot = plfrac * fmaf(et.tfn, dplankup, blay);
     }
-    float A = 1.0f - (atrans + efcl * (1.0f - atrans));
-    float Bd = gsd + cldf * (bbdtot * atot - gsd);
-    float Bu = gsu + cldf * (bbutot * atot - gsu);
-    float D = cldf * (1.0f - atot) + (1.0f - cldf) * (1.0f - atrans);
+    float A = 1.0f - fmaf(efcl, 1.0f - atrans, atrans);
+    float Bd = fmaf(cldf, fmaf(bbdtot, atot, -gsd), gsd);
+    float Bu = fmaf(cldf, fmaf(bbutot, atot, -gsu), gsu);
+    float D = fmaf(cldf, 1.0f - atot, (1.0f - cldf) * (1.0f - atrans));
     r.cld = make_float4(A, Bd, Bu, D);
   } else {
     r.cld = r.clr;
@@ -457,7 +457,7 @@ __device__ __forceinline__ void group_cells(int gr, const LwArgs& a, const Smem&
       const FracRec fr = s.frec[slot * nl + lay];
       const float* fp = T + fr.off + gi;
       const float f0 = __ldg(fp);
-      plfrac = f0 + fr.fpl * (__ldg(fp + NG) - f0);
+      plfrac = fmaf(fr.fpl, __ldg(fp + NG) - f0, f0);
     }
     if (lay == 0) s.frac1[g] = plfrac;
     if (a.dbg_taut) {
