@@ -42,6 +42,7 @@
 #include <math.h>
 #include <cmath>
 #include <stdint.h>
+#include <climits>
 
 #include "lw_common.h"
 #include "lw_solver.h"
@@ -114,6 +115,13 @@ struct Smem {
   double* cdf;     // [140] McICA draws of the column (fused cloud mode, phase 1; in the term area)
   uint32_t* mtlo;  // [141] Mersenne-twister state words (fused cloud mode, phase 1; in the term area)
   float* tcl;      // [nl][16] cloud optical depth per (layer, band) (fused cloud mode)
+  // fused cloud mode, per layer: the McICA threshold 1 - cldf as double bits
+  // (cdf >= it marks a cloudy cell), the layer's cloud water paths and radii
+  // as floats, and flags: bit 0 ciwp /= 0, bit 1 clwp /= 0, bit 2
+  // ciwp + clwp >= 1e-20, bits 8.. the code cldprmc's radius checks stop with
+  long long* cthr; // [nl]
+  float4* lcw;     // [nl] (ciwp, clwp, radice, radliq)
+  int* lfl;        // [nl]
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -141,7 +149,8 @@ __host__ __device__ inline size_t smem_bytes(int nl, bool lean) {
   a += 2 * align16((size_t)nl * 5 * 4);
   a += align16(GB_NGPT * 4);
   a += align16(64 * 4) + align16(4 * 4) + align16(4 * 4);
-  a += align16((size_t)nl * 16 * 4);
+  a += align16((size_t)nl * 16 * 4);         // tcl
+  a += align16((size_t)nl * 8) + align16((size_t)nl * 16) + align16((size_t)nl * 4);  // cthr, lcw, lfl
   return a;
 }
 
@@ -168,7 +177,10 @@ __device__ inline Smem carve(char* base, int nl, bool lean) {
   s.misc = (float*)p; p += align16(64 * 4);
   s.scal = (float*)p; p += align16(4 * 4);
   s.iscal = (int*)p; p += align16(4 * 4);
-  s.tcl = (float*)p;
+  s.tcl = (float*)p; p += align16((size_t)nl * 16 * 4);
+  s.cthr = (long long*)p; p += align16((size_t)nl * 8);
+  s.lcw = (float4*)p; p += align16((size_t)nl * 16);
+  s.lfl = (int*)p;
   return s;
 }
 
@@ -269,6 +281,42 @@ __device__ __forceinline__ float cloud_tau(const LwArgs& a, long long icol, int 
     }
   }
   return (float)ciwp * abscoice + (float)clwp * abscoliq;
+}
+
+// cloud_tau with the layer's water paths and radii already converted to
+// float (flags bit 0: ciwp /= 0, bit 1: clwp /= 0); the same float
+// operations, so the same result
+__device__ __forceinline__ float cloud_tau_layer(const LwArgs& a, int band, const float* __restrict__ T, float4 w,
+                                                 int flags) {
+  float abscoice = 0.0f, abscoliq = 0.0f;
+  if (flags & 1) {
+    const float radice = w.z;
+    if (a.iceflag == 0) {
+      abscoice = T[c_T.absice0] + T[c_T.absice0 + 1] / radice;
+    } else if (a.iceflag == 1) {
+      int ib = c_icb[band];
+      abscoice = T[c_T.absice1 + 2 * (ib - 1)] + T[c_T.absice1 + 1 + 2 * (ib - 1)] / radice;
+    } else {
+      float factor = (radice - 2.0f) / 3.0f;
+      int nrow = a.iceflag == 2 ? 43 : 46;
+      int index = clampi((int)factor, 1, nrow - 1);
+      float fint = factor - (float)index;
+      const float* t = T + (a.iceflag == 2 ? c_T.absice2 : c_T.absice3) + nrow * band;
+      abscoice = t[index - 1] + fint * (t[index] - t[index - 1]);
+    }
+  }
+  if (flags & 2) {
+    if (a.liqflag == 0) {
+      abscoliq = c_T.absliq0;
+    } else {
+      const float radliq = w.w;
+      int index = clampi((int)(radliq - 1.5f), 1, 57);
+      float fint = radliq - 1.5f - (float)index;
+      const float* t = T + c_T.absliq1 + 58 * band;
+      abscoliq = t[index - 1] + fint * (t[index] - t[index - 1]);
+    }
+  }
+  return w.x * abscoice + w.y * abscoliq;
 }
 
 // McICA cloud optics of one cell: returns cldfmc and sets odcld/efcl
@@ -696,23 +744,42 @@ __device__ __forceinline__ bool solve_column(const LwArgs& a, long long icol, ch
     // "cldfmc == 1" / "cldfmc neither 0 nor 1" bits the later phases use to
     // skip loads, and cldprmc's STOP conditions.
     if (a.icld >= 1 && fused) {
-      __syncthreads();  // draws ready
+      // per layer, once: the McICA threshold and the layer's cloud
+      // quantities (fp64 comparisons here rather than per cell or band)
+      for (int lay = tid; lay < nl; lay += NT) {
+        double cf = in2(a.cldfrac, a.ld, icol, lay);
+        cf = cf < 1.0e-20 ? 0.0 : cf;  // mcica_subcol_gen_lw.f90:463-470
+        // cdf >= 1 - cf, compared on the bit patterns (cdf is in [0, 1], so
+        // for a threshold >= 0 the integer order is the floating-point order);
+        // a negative threshold takes every cell, a NaN none
+        const double thr = 1.0 - cf;
+        s.cthr[lay] = thr < 0.0 ? LLONG_MIN : (thr == thr ? __double_as_longlong(thr) : LLONG_MAX);
+        const double ciwp = in2(a.ciwp, a.ld, icol, lay), clwp = in2(a.clwp, a.ld, icol, lay);
+        const double rice = in2(a.reicmcl, a.ld, icol, lay), rliq = in2(a.relqmcl, a.ld, icol, lay);
+        int fl = (ciwp != 0.0 ? 1 : 0) | (clwp != 0.0 ? 2 : 0) | (ciwp + clwp >= 1.e-20 ? 4 : 0);
+        // the code cldprmc.f90:217-266 stops with for this layer's radii (inflag 2)
+        int e = 0;
+        if (ciwp != 0.0) {
+          if (a.iceflag == 0 && rice < 10.0) e = GB_COL_ICE_SMALL;
+          if (a.iceflag == 1 && (rice < 13.0 || rice > 130.0)) e = GB_COL_ICE_BOUNDS;
+          if (a.iceflag == 2 && (rice < 5.0 || rice > 131.0)) e = GB_COL_ICE_BOUNDS;
+          if (a.iceflag == 3 && (rice < 5.0 || rice > 140.0)) e = GB_COL_DGE_BOUNDS;
+        }
+        if (clwp != 0.0 && a.liqflag == 1 && (rliq < 2.5 || rliq > 60.0)) e = GB_COL_LIQ_BOUNDS;
+        s.lfl[lay] = fl | (e << 8);
+        s.lcw[lay] = make_float4((float)ciwp, (float)clwp, (float)rice, (float)rliq);
+      }
+      __syncthreads();  // draws and layer data ready
       // cloudy cells: cdf(g) >= 1 - cldf(lay) (mcica_subcol_gen_lw.f90:650), one warp per layer
       const int warp = tid >> 5, lane = tid & 31;
       const long long* cdfb = reinterpret_cast<const long long*>(s.cdf);
       for (int lay = warp; lay < nl; lay += NWARP) {
-        double cf = in2(a.cldfrac, a.ld, icol, lay);
-        cf = cf < 1.0e-20 ? 0.0 : cf;  // :463-470
-        // cdf >= 1 - cf, compared on the bit patterns (cdf is in [0, 1], so
-        // for a threshold >= 0 the integer order is the floating-point order)
-        const double thr = 1.0 - cf;
-        const long long tb = __double_as_longlong(thr);
-        const bool all = thr < 0.0, none = !(thr == thr);
+        const long long tb = s.cthr[lay];
         unsigned any = 0u;
 #pragma unroll
         for (int w = 0; w < 5; ++w) {
           const int g = w * 32 + lane;
-          const bool cl = g < GB_NGPT && !none && (all || cdfb[g] >= tb);
+          const bool cl = g < GB_NGPT && cdfb[g] >= tb;
           const unsigned m = __ballot_sync(0xffffffffu, cl);
           if (lane == 0) s.cbits[lay * 5 + w] = m;
           any |= m;
@@ -723,6 +790,7 @@ __device__ __forceinline__ bool solve_column(const LwArgs& a, long long icol, ch
       // cloud optical depth per (layer, band) where the band has a cloudy
       // sub-column (the values cldprmc computes for every such cell), and
       // cldprmc's STOP conditions
+      const long long kMin = __double_as_longlong(1.0e-20), kInf = 0x7FF0000000000000LL;
       int err = 0;
       for (int it = tid; it < nl * 16; it += NT) {
         const int lay = it >> 4, band = it & 15;
@@ -731,25 +799,15 @@ __device__ __forceinline__ bool solve_column(const LwArgs& a, long long icol, ch
         bool any = false;
         for (int g = g0; g < g0 + ng; ++g) any |= (s.cbits[lay * 5 + (g >> 5)] >> (g & 31)) & 1u;
         if (!any) continue;
-        const double ciwp = in2(a.ciwp, a.ld, icol, lay), clwp = in2(a.clwp, a.ld, icol, lay);
         const double tin = __ldg(a.tauc + band + 16 * (icol + a.ld * lay));
-        const double cwp = ciwp + clwp;
-        float tauc;
-        if (a.inflag == 2 && (cwp >= 1.e-20 || tin >= 1.e-20)) tauc = cloud_tau(a, icol, lay, band, T, ciwp, clwp);
-        else tauc = (float)tin;
-        s.tcl[lay * 16 + band] = tauc;
-        if (cwp >= 1.e-20 || tin >= 1.e-20) {
+        const long long tinb = __double_as_longlong(tin);
+        const bool tin_ok = tinb >= kMin && tinb <= kInf;  // tin >= 1e-20
+        const int fl = s.lfl[lay];
+        const bool cond = (fl & 4) || tin_ok;
+        s.tcl[lay * 16 + band] = a.inflag == 2 && cond ? cloud_tau_layer(a, band, T, s.lcw[lay], fl) : (float)tin;
+        if (cond) {
           if (a.inflag == 1) err = GB_COL_INFLAG1;
-          if (a.inflag == 2) {
-            const double rice = in2(a.reicmcl, a.ld, icol, lay), rliq = in2(a.relqmcl, a.ld, icol, lay);
-            if (ciwp != 0.0) {
-              if (a.iceflag == 0 && rice < 10.0) err = GB_COL_ICE_SMALL;
-              if (a.iceflag == 1 && (rice < 13.0 || rice > 130.0)) err = GB_COL_ICE_BOUNDS;
-              if (a.iceflag == 2 && (rice < 5.0 || rice > 131.0)) err = GB_COL_ICE_BOUNDS;
-              if (a.iceflag == 3 && (rice < 5.0 || rice > 140.0)) err = GB_COL_DGE_BOUNDS;
-            }
-            if (clwp != 0.0 && a.liqflag == 1 && (rliq < 2.5 || rliq > 60.0)) err = GB_COL_LIQ_BOUNDS;
-          }
+          if (a.inflag == 2 && (fl >> 8)) err = fl >> 8;
         }
       }
       if (err) atomicMax(&s.iscal[2], err);
@@ -983,10 +1041,11 @@ __device__ __forceinline__ bool solve_column(const LwArgs& a, long long icol, ch
       }
       __syncthreads();
       for (int l = tid; l < nl; l += NT) {
-        double dp = in2(a.plev, a.ld, icol, l) - in2(a.plev, a.ld, icol, l + 1);
+        const double dp = in2(a.plev, a.ld, icol, l) - in2(a.plev, a.ld, icol, l + 1);
+        const double f = c_T.heatfac / dp;  // one division for both heating rates
         long long o = icol + ldo * l;
-        a.hr[o] = c_T.heatfac * (s.fnet[l * 2] - s.fnet[(l + 1) * 2]) / dp;
-        a.hrc[o] = c_T.heatfac * (s.fnet[l * 2 + 1] - s.fnet[(l + 1) * 2 + 1]) / dp;
+        a.hr[o] = f * (s.fnet[l * 2] - s.fnet[(l + 1) * 2]);
+        a.hrc[o] = f * (s.fnet[l * 2 + 1] - s.fnet[(l + 1) * 2 + 1]);
       }
       __syncthreads();
     }
