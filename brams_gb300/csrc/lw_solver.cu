@@ -122,6 +122,7 @@ struct Smem {
   long long* cthr; // [nl]
   float4* lcw;     // [nl] (ciwp, clwp, radice, radliq)
   int* lfl;        // [nl]
+  float4* prow;    // [nl+1] Planck-table row and fraction of tlev and tlay per level (phase 1)
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -151,6 +152,7 @@ __host__ __device__ inline size_t smem_bytes(int nl, bool lean) {
   a += align16(64 * 4) + align16(4 * 4) + align16(4 * 4);
   a += align16((size_t)nl * 16 * 4);         // tcl
   a += align16((size_t)nl * 8) + align16((size_t)nl * 16) + align16((size_t)nl * 4);  // cthr, lcw, lfl
+  a += align16((size_t)(nl + 1) * 16);                                                   // prow
   return a;
 }
 
@@ -180,7 +182,8 @@ __device__ inline Smem carve(char* base, int nl, bool lean) {
   s.tcl = (float*)p; p += align16((size_t)nl * 16 * 4);
   s.cthr = (long long*)p; p += align16((size_t)nl * 8);
   s.lcw = (float4*)p; p += align16((size_t)nl * 16);
-  s.lfl = (int*)p;
+  s.lfl = (int*)p; p += align16((size_t)nl * 4);
+  s.prow = (float4*)p;
   return s;
 }
 
@@ -714,19 +717,31 @@ __device__ __forceinline__ bool solve_column(const LwArgs& a, long long icol, ch
       const int ib = it / nl, lay = it - ib * nl;
       s.taua[it] = (float)__ldg(a.tauaer + icol + (long long)a.ld * (lay + (long long)nl * ib));
     }
-    // Planck interpolation per (level, band) (setcoef.f90:173-269, istart = 1)
+    // Planck interpolation per (level, band) (setcoef.f90:173-269, istart = 1):
+    // table row and fraction once per level (one fp64 conversion each), then
+    // one thread per (level, band)
+    for (int lev = tid; lev <= nl; lev += NT) {
+      const float tz = (float)in2(a.tlev, a.ld, icol, lev);
+      const int ind = clampi((int)(tz - 159.0f), 1, 180);
+      float4 r = make_float4(__int_as_float(ind), tz - 159.0f - (float)ind, 0.0f, 0.0f);
+      if (lev < nl) {
+        const float tl = (float)in2(a.tlay, a.ld, icol, lev);
+        const int il = clampi((int)(tl - 159.0f), 1, 180);
+        r.z = __int_as_float(il);
+        r.w = tl - 159.0f - (float)il;
+      }
+      s.prow[lev] = r;
+    }
+    __syncthreads();
     for (int it = tid; it < (nl + 1) * 16; it += NT) {
       int lev = it >> 4, ib = it & 15;
       const float* tp = T + c_T.totplnk + ib * 181;
-      float tz = (float)in2(a.tlev, a.ld, icol, lev);
-      int ind = clampi((int)(tz - 159.0f), 1, 180);
-      float fr = tz - 159.0f - (float)ind;
-      s.plk_lev[ib * (nl + 1) + lev] = tp[ind - 1] + fr * (tp[ind] - tp[ind - 1]);
+      const float4 r = s.prow[lev];
+      const int ind = __float_as_int(r.x);
+      s.plk_lev[ib * (nl + 1) + lev] = tp[ind - 1] + r.y * (tp[ind] - tp[ind - 1]);
       if (lev < nl) {
-        float tl = (float)in2(a.tlay, a.ld, icol, lev);
-        int il = clampi((int)(tl - 159.0f), 1, 180);
-        float fl = tl - 159.0f - (float)il;
-        s.plk_lay[ib * nl + lev] = tp[il - 1] + fl * (tp[il] - tp[il - 1]);
+        const int il = __float_as_int(r.z);
+        s.plk_lay[ib * nl + lev] = tp[il - 1] + r.w * (tp[il] - tp[il - 1]);
       }
     }
     if (tid < 16) {
@@ -1021,11 +1036,23 @@ __device__ __forceinline__ bool solve_column(const LwArgs& a, long long icol, ch
       const long long ldo = a.ldo;
       const bool idrv = a.idrv == 1;
       for (int lev = tid; lev <= nl; lev += NT) {
-        double acc[6] = {0, 0, 0, 0, 0, 0};
+        // the five warps' fp32 partials summed without rounding error: Knuth's
+        // two-sum keeps each addition's rounding error, and the sum and the
+        // accumulated errors go to fp64 (two conversions instead of five
+        // conversions and four fp64 additions; fp64 is a narrow pipe on GB300)
+        double acc[6];
 #pragma unroll
-        for (int w = 0; w < NSW; ++w)
+        for (int k = 0; k < 6; ++k) {
+          float hi = s.part[lev * 6 + k], lo = 0.0f;
 #pragma unroll
-          for (int k = 0; k < 6; ++k) acc[k] += (double)s.part[(w * (nl + 1) + lev) * 6 + k];
+          for (int w = 1; w < NSW; ++w) {
+            const float b = s.part[(w * (nl + 1) + lev) * 6 + k];
+            const float sum = hi + b, bv = sum - hi;
+            lo += (hi - (sum - bv)) + (b - bv);
+            hi = sum;
+          }
+          acc[k] = (double)hi + (double)lo;
+        }
         if (lev == nl) acc[0] = acc[1] = 0.0;  // no downward radiation at the model top
         long long o = icol + ldo * lev;
         a.uflx[o] = acc[2];
