@@ -36,7 +36,8 @@
 //      heating rates heatfac*dF/dp in fp64 (rtrnmc.f90:566-592).
 //
 // Precision: gas optics and transfer in fp32; flux accumulation across warps
-// and the heating-rate step in fp64.  Outputs follow the reference's layout:
+// error-free (two-sum) into fp64, net fluxes and the heating-rate step in
+// fp64.  Outputs follow the reference's layout:
 // uflx(icol, k+1) for k = 0..nlay, hr(icol, k+1) for k = 0..nlay-1.
 #include <cuda_runtime.h>
 #include <math.h>
