@@ -253,43 +253,9 @@ __constant__ float c_a1[16] = {0.f, 0.25f, 0.22f, 0.f, 0.13f, 0.446f, -0.10f, 0.
 __constant__ float c_a2[16] = {0.f, -12.0f, -11.7f, 0.f, -0.72f, -0.243f, 0.19f, -0.062f, 0.414f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 
 // cldprmc's optical depth ciwp*abscoice + clwp*abscoliq of one cell
-// (cldprmc.f90:194-266; the radius bounds are checked in the pre-pass).
-__device__ __forceinline__ float cloud_tau(const LwArgs& a, long long icol, int lay, int band,
-                                           const float* __restrict__ T, double ciwp, double clwp) {
-  float abscoice = 0.0f, abscoliq = 0.0f;
-  if (ciwp != 0.0) {
-    float radice = (float)in2(a.reicmcl, a.ld, icol, lay);
-    if (a.iceflag == 0) {
-      abscoice = T[c_T.absice0] + T[c_T.absice0 + 1] / radice;
-    } else if (a.iceflag == 1) {
-      int ib = c_icb[band];
-      abscoice = T[c_T.absice1 + 2 * (ib - 1)] + T[c_T.absice1 + 1 + 2 * (ib - 1)] / radice;
-    } else {
-      float factor = (radice - 2.0f) / 3.0f;
-      int nrow = a.iceflag == 2 ? 43 : 46;
-      int index = clampi((int)factor, 1, nrow - 1);
-      float fint = factor - (float)index;
-      const float* t = T + (a.iceflag == 2 ? c_T.absice2 : c_T.absice3) + nrow * band;
-      abscoice = t[index - 1] + fint * (t[index] - t[index - 1]);
-    }
-  }
-  if (clwp != 0.0) {
-    if (a.liqflag == 0) {
-      abscoliq = c_T.absliq0;
-    } else {
-      float radliq = (float)in2(a.relqmcl, a.ld, icol, lay);
-      int index = clampi((int)(radliq - 1.5f), 1, 57);
-      float fint = radliq - 1.5f - (float)index;
-      const float* t = T + c_T.absliq1 + 58 * band;
-      abscoliq = t[index - 1] + fint * (t[index] - t[index - 1]);
-    }
-  }
-  return (float)ciwp * abscoice + (float)clwp * abscoliq;
-}
-
-// cloud_tau with the layer's water paths and radii already converted to
-// float (flags bit 0: ciwp /= 0, bit 1: clwp /= 0); the same float
-// operations, so the same result
+// (cldprmc.f90:194-266; the radius bounds are checked in the pre-pass), from
+// w = (ciwp, clwp, radice, radliq) converted to float and flags bit 0: ciwp
+// /= 0, bit 1: clwp /= 0
 __device__ __forceinline__ float cloud_tau_layer(const LwArgs& a, int band, const float* __restrict__ T, float4 w,
                                                  int flags) {
   float abscoice = 0.0f, abscoliq = 0.0f;
@@ -345,15 +311,21 @@ __device__ __forceinline__ float cell_cloud(const LwArgs& a, const Smem& s, long
     return (float)__ldg(a.cldfmcl + (long long)g + GB_NGPT * (icol + (long long)a.ld * lay));
   }
   long long o = (long long)g + GB_NGPT * (icol + (long long)a.ld * lay);
-  double ciwp = __ldg(a.ciwpmcl + o), clwp = __ldg(a.clwpmcl + o);
+  const double ciwp = __ldg(a.ciwpmcl + o), clwp = __ldg(a.clwpmcl + o);
+  // the optical depth from this cell's water paths and the layer's radii (as
+  // floats in shared memory), or the caller's taucmcl
   float tauc;
-  double cwp = ciwp + clwp;
-  if (a.inflag == 2 && cwp >= 1.e-20) {
-    tauc = cloud_tau(a, icol, lay, band, T, ciwp, clwp);
-  } else {
-    double tin = __ldg(a.taucmcl + o);
-    if (a.inflag == 2 && tin >= 1.e-20) tauc = cloud_tau(a, icol, lay, band, T, ciwp, clwp);
-    else tauc = (float)tin;
+  bool from_paths = a.inflag == 2 && ciwp + clwp >= 1.e-20;
+  if (!from_paths) {
+    const double tin = __ldg(a.taucmcl + o);
+    const long long tb = __double_as_longlong(tin);
+    from_paths = a.inflag == 2 && tb >= __double_as_longlong(1.0e-20) && tb <= 0x7FF0000000000000LL;
+    tauc = (float)tin;
+  }
+  if (from_paths) {
+    const int fl = ((__double_as_longlong(ciwp) << 1) != 0LL ? 1 : 0) | ((__double_as_longlong(clwp) << 1) != 0LL ? 2 : 0);
+    const float4 r = s.lcw[lay];
+    tauc = cloud_tau_layer(a, band, T, make_float4((float)ciwp, (float)clwp, r.z, r.w), fl);
   }
   odcld = secdiff_b * tauc;
   efcl = 1.0f - __expf(-odcld);
@@ -828,6 +800,20 @@ __device__ __forceinline__ bool solve_column(const LwArgs& a, long long icol, ch
       }
       if (err) atomicMax(&s.iscal[2], err);
     } else if (a.icld >= 1) {
+      // per layer, once: the particle radii as floats and the codes cldprmc's
+      // radius checks stop with (cldprmc.f90:217-266): bits 0-7 ice, 8-15 liquid
+      for (int lay = tid; lay < nl; lay += NT) {
+        const double rice = in2(a.reicmcl, a.ld, icol, lay), rliq = in2(a.relqmcl, a.ld, icol, lay);
+        int ei = 0;
+        if (a.iceflag == 0 && rice < 10.0) ei = GB_COL_ICE_SMALL;
+        if (a.iceflag == 1 && (rice < 13.0 || rice > 130.0)) ei = GB_COL_ICE_BOUNDS;
+        if (a.iceflag == 2 && (rice < 5.0 || rice > 131.0)) ei = GB_COL_ICE_BOUNDS;
+        if (a.iceflag == 3 && (rice < 5.0 || rice > 140.0)) ei = GB_COL_DGE_BOUNDS;
+        const int el = a.liqflag == 1 && (rliq < 2.5 || rliq > 60.0) ? GB_COL_LIQ_BOUNDS : 0;
+        s.lfl[lay] = ei | (el << 8);
+        s.lcw[lay] = make_float4(0.0f, 0.0f, (float)rice, (float)rliq);
+      }
+      __syncthreads();
       // one warp per layer: the layer's 140 cldfmcl values tested on their bit
       // patterns (no fp64 pipe): == 1, /= 0, >= 1e-20
       const int warp = tid >> 5, lane = tid & 31;
@@ -856,17 +842,13 @@ __device__ __forceinline__ bool solve_column(const LwArgs& a, long long icol, ch
           if (cb[w] >= kMin && cb[w] <= kInf) {  // cldfmc >= cldmin (cldprmc.f90:178)
             const long long o = base + w * 32 + lane;
             const double ciwp = __ldg(a.ciwpmcl + o), clwp = __ldg(a.clwpmcl + o);
-            if (ciwp + clwp >= 1.e-20 || __ldg(a.taucmcl + o) >= 1.e-20) {
+            const long long tb = __double_as_longlong(__ldg(a.taucmcl + o));
+            if (ciwp + clwp >= 1.e-20 || (tb >= kMin && tb <= kInf)) {
               if (a.inflag == 1) err = GB_COL_INFLAG1;
               if (a.inflag == 2) {
-                const double rice = in2(a.reicmcl, a.ld, icol, lay), rliq = in2(a.relqmcl, a.ld, icol, lay);
-                if (ciwp != 0.0) {
-                  if (a.iceflag == 0 && rice < 10.0) err = GB_COL_ICE_SMALL;
-                  if (a.iceflag == 1 && (rice < 13.0 || rice > 130.0)) err = GB_COL_ICE_BOUNDS;
-                  if (a.iceflag == 2 && (rice < 5.0 || rice > 131.0)) err = GB_COL_ICE_BOUNDS;
-                  if (a.iceflag == 3 && (rice < 5.0 || rice > 140.0)) err = GB_COL_DGE_BOUNDS;
-                }
-                if (clwp != 0.0 && a.liqflag == 1 && (rliq < 2.5 || rliq > 60.0)) err = GB_COL_LIQ_BOUNDS;
+                const int e = s.lfl[lay];
+                if ((__double_as_longlong(ciwp) << 1) != 0LL && (e & 0xff)) err = e & 0xff;  // ciwp /= 0
+                if ((__double_as_longlong(clwp) << 1) != 0LL && (e >> 8)) err = e >> 8;      // clwp /= 0
               }
             }
           }
