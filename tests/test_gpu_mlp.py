@@ -257,3 +257,37 @@ def test_hand_over_of_columns_off_the_network(ctx):
     # the partly-off columns: network layers and the taumol layer together, close to the plain solver
     d = np.abs(both[0]["uflx"][4:11] - plain["uflx"][4:11])
     assert (d <= 0.01 * np.abs(plain["uflx"][4:11]) + 5.0).all(), float(d.max())
+
+
+def test_graph_of_a_learned_batch(ctx):
+    """A captured batch with learned gas optics (the learned-only kernel, the
+    hand-over list the graph owns, the full kernel) replays to exactly what a
+    direct call gives, also when some columns are off the network."""
+    import pyoracle
+
+    torch = _torch()
+    mlp = S.load(ctx)
+    st = make_state(ProfileSpec(ncol=61, nlay=45, seed=93, t_noise=4.0, h2o_sigma=0.5))
+    st["tlay"][5:9, 10] += 200.0  # columns 5-8: one layer off the network
+    tauc = pyoracle.cldprop_columns(st)
+    ga, gb = S.DeviceGrid(st, tauc), S.DeviceGrid(st, tauc)
+    rows = 61 * 45
+    tau = torch.empty((rows, 140), dtype=torch.float32, device="cuda")
+    frac = torch.empty_like(tau)
+    flag = torch.empty(rows, dtype=torch.uint8, device="cuda")
+    mlp.infer(ga.desc(seed0=3), tau, frac, flag)
+    sur = dict(sur_tau=tau.data_ptr(), sur_frac=frac.data_ptr(), sur_flag=flag.data_ptr())
+    ctx.rrtmg_lw_batch_device([ga.desc(seed0=3, **sur)])
+    graph = ctx.batch_graph([gb.desc(seed0=3, **sur)])
+    try:
+        graph.launch()
+        graph.launch()
+        torch.cuda.synchronize()
+    finally:
+        graph.close()
+    assert ctx.sync_status() == 0
+    assert flag.view(61, 45)[5:9, 10].eq(0).all()
+    a, b = ga.outputs(), gb.outputs()
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+    assert (b["uflx"] > 0).all()
