@@ -400,23 +400,28 @@ int gb_rrtmg_lw_ini(double cpdair, const char* table_dir, int device, gb_lw_cont
   std::string dir = table_dir ? table_dir : default_table_dir();
   std::string ref = dir + "/lw_ref_tables.gblw", kt = dir + "/lw_ktables.gblw";
   std::vector<float> blob;
+  std::vector<double> cloud64;
   std::string err;
-  if (!gb_build_tables(ref.c_str(), kt.c_str(), cpdair, ctx->tabs, blob, err)) {
+  if (!gb_build_tables(ref.c_str(), kt.c_str(), cpdair, ctx->tabs, blob, err, &cloud64)) {
     std::fprintf(stderr, "gb_rrtmg_lw_ini: %s\n", err.c_str());
     delete ctx;
     return GB_LW_E_TABLES;
   }
+  ctx->absliq0 = cloud64[ctx->tabs.c64_absliq0];
+  ctx->abscld1 = cloud64[ctx->tabs.c64_abscld1];
   int dev_smem = 0;
   cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
   ctx->max_smem = (size_t)dev_smem;
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
-  if (cudaMalloc(&ctx->d_tables, blob.size() * 4) != cudaSuccess || cudaMalloc(&ctx->d_err, 8) != cudaSuccess) {
+  if (cudaMalloc(&ctx->d_tables, blob.size() * 4) != cudaSuccess || cudaMalloc(&ctx->d_err, 8) != cudaSuccess ||
+      cudaMalloc(&ctx->d_cloud64, cloud64.size() * 8) != cudaSuccess) {
     cudaGetLastError();
     gb_rrtmg_lw_free(ctx);
     return GB_LW_E_NOMEM;
   }
   ctx->d_err_host = ctx->d_err + 1;
   if (cudaMemcpy(ctx->d_tables, blob.data(), blob.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(ctx->d_cloud64, cloud64.data(), cloud64.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemset(ctx->d_err, 0, 8) != cudaSuccess || gb_lw_set_tables(ctx->tabs) != cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->streams[0], cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->streams[1], cudaStreamNonBlocking) != cudaSuccess) {
@@ -447,6 +452,7 @@ int gb_rrtmg_lw_free(gb_lw_context* ctx) {
   cudaFree(ctx->d_fdraws);
   cudaFree(ctx->d_fall);
   cudaFree(ctx->d_nfall);
+  cudaFree(ctx->d_cloud64);
   delete ctx;
   return GB_LW_OK;
 }

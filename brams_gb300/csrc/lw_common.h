@@ -44,6 +44,9 @@ struct GbTables {
   int nspa[GB_NBND], nspb[GB_NBND];
   double heatfac, fluxfac, grav, avogad;
   int total_floats;
+  // the cloud optics tables again in fp64 (for cldprop, which the reference
+  // evaluates in double): offsets into a separate double blob
+  int c64_absice0, c64_absice1, c64_absice2, c64_absice3, c64_absliq1, c64_absliq0, c64_abscld1, c64_total;
 };
 
 // Per-column error codes written by the kernels (0 = ok).  The values match

@@ -19,6 +19,8 @@ struct gb_lw_context {
   int device = 0;
   GbTables tabs;
   float* d_tables = nullptr;
+  double* d_cloud64 = nullptr;  // cloud optics tables in fp64 (cldprop)
+  double absliq0 = 0.0, abscld1 = 0.0;  // cldprop's two scalar cloud constants
   int* d_err = nullptr;      // max status of device calls
   int* d_err_host = nullptr; // status of the current host call
   cudaStream_t streams[2] = {nullptr, nullptr};

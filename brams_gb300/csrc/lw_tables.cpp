@@ -63,7 +63,7 @@ bool read_container(const char* path, std::map<std::string, Entry>& out, std::st
 }  // namespace
 
 bool gb_build_tables(const char* ref_path, const char* k_path, double cpdair, GbTables& T,
-                     std::vector<float>& blob, std::string& err) {
+                     std::vector<float>& blob, std::string& err, std::vector<double>* cloud64) {
   std::map<std::string, Entry> tab;
   if (!read_container(ref_path, tab, err) || !read_container(k_path, tab, err)) return false;
   auto need = [&](const std::string& n) -> const Entry* {
@@ -202,6 +202,24 @@ bool gb_build_tables(const char* ref_path, const char* k_path, double cpdair, Gb
     return false;
   T.absliq0 = (float)aliq0->d[0];
   T.abscld1 = (float)acld1->d[0];
+  if (cloud64) {
+    std::vector<double>& c = *cloud64;
+    c.clear();
+    auto put64 = [&](const char* n) {
+      const Entry* e = need(n);
+      const int off = (int)c.size();
+      c.insert(c.end(), e->d.begin(), e->d.end());
+      return off;
+    };
+    T.c64_absice0 = put64("absice0");
+    T.c64_absice1 = put64("absice1");
+    T.c64_absice2 = put64("absice2");
+    T.c64_absice3 = put64("absice3");
+    T.c64_absliq1 = put64("absliq1");
+    T.c64_absliq0 = put64("absliq0");
+    T.c64_abscld1 = put64("abscld1");
+    T.c64_total = (int)c.size();
+  }
   for (int j = 0; j < 59; ++j) {
     T.pref[j] = (float)pref->d[j];
     T.preflog[j] = (float)preflog->d[j];

@@ -5,5 +5,6 @@
 
 #include "lw_common.h"
 
+// cloud64 (optional): the cloud optics tables in fp64, offsets in T.c64_*
 bool gb_build_tables(const char* ref_path, const char* k_path, double cpdair, GbTables& T,
-                     std::vector<float>& blob, std::string& err);
+                     std::vector<float>& blob, std::string& err, std::vector<double>* cloud64 = nullptr);

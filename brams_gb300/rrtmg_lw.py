@@ -42,6 +42,7 @@ EXPORTS = [
     "gb_lw_mlp_set_params", "gb_lw_mlp_set_loss_weights", "gb_lw_mlp_samples", "gb_lw_mlp_fit_norm",
     "gb_lw_mlp_prepare", "gb_lw_mlp_gradients", "gb_lw_mlp_train_step", "gb_lw_mlp_forward", "gb_lw_mlp_infer",
     "gb_rrtmg_lw_batch_surrogate", "gb_lw_mlp_set_engine", "gb_rrtmg_lw_autotune_report",
+    "gb_cldprop_lw_device",
 ]
 MLP_MMA_SYNC, MLP_TCGEN05 = 0, 1
 MLP_NPARAM = 72352
@@ -125,6 +126,7 @@ def load_library(path: str = LIB_PATH):
         L.gb_mcica_subcol_lw.argtypes = [P, I, I, I, I, IP] + [P] * 8 + [P] * 6 + [LL, I]
         L.gb_mcica_subcol_lw_device.argtypes = [P, P, I, I, I, I, IP] + [P] * 8 + [P] * 6 + [LL, I]
         L.gb_rrtmg_lw_gas_optics_diag.argtypes = [P, I, I] + [P] * 17 + [P, P]
+        L.gb_cldprop_lw_device.argtypes = [P, P, I, I, I, I, I] + [P] * 7 + [LL, P]
         L.gb_mcica_subcol_lw_noalloc.argtypes = [P, I, I, I, I, IP] + [P] * 8 + [P] * 6 + [LL, I, P]
         GP = C.POINTER(GridDesc)
         L.gb_rrtmg_lw_batch_device.argtypes = [P, P, I, GP]
@@ -272,6 +274,16 @@ class Context:
                                        1 if seed_per_column else 0)
         _check(self.L, self.h, rc)
         return o
+
+    def cldprop_lw_device(self, ncol: int, nlay: int, ptrs: dict, inflag: int = 2, iceflag: int = 3,
+                          liqflag: int = 1, ld: int | None = None, stream=None) -> None:
+        """cldprop (rrtmg_lw_cldprop.f90:50) on device arrays: ptrs holds cldfrac, ciwp, clwp, rei,
+        rel ((ld, nlay) memory order), optional tauc (16, ld, nlay), taucloud (16, ld, nlay) out and
+        optional d_col_status (ncol int32)."""
+        g = lambda k: _ptr(ptrs.get(k))
+        _check(self.L, self.h, self.L.gb_cldprop_lw_device(
+            self.h, _ptr(stream or 0), ncol, nlay, inflag, iceflag, liqflag, g("cldfrac"), g("tauc"), g("ciwp"),
+            g("clwp"), g("rei"), g("rel"), g("taucloud"), ld if ld is not None else ncol, g("d_col_status")))
 
     def mcica_subcol_lw_device(self, ncol: int, nlay: int, ptrs: dict, icld: int, permuteseed: int, irng: int = 1,
                                seed_per_column: bool = True, stream=None, ld: int | None = None) -> None:

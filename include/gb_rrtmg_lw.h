@@ -131,6 +131,21 @@ int gb_mcica_subcol_lw_device(gb_lw_context* ctx, void* stream, int ncol, int nl
                               double* clwpmcl, double* reicmcl, double* relqmcl,
                               double* taucmcl, int64_t ld, int seed_per_column);
 
+/* cldprop (rrtmg_lw_cldprop.f90:50-295) on DEVICE arrays for ncol columns, as
+ * BRAMS calls it per column before McICA (rtm_driver.f90:1250-1258):
+ * cldfrac, ciwp, clwp, rei, rel are (ld, nlay); tauc (16, ld, nlay) is the
+ * reference's input tauc (required for inflag 0, may be NULL otherwise);
+ * taucloud (16, ld, nlay) receives the band cloud optical depths in the
+ * layout mcica_subcol_lw and the fused-cloud solver take (bands a layer does
+ * not fill are 0).  fp64 throughout, like the reference.  A radius outside
+ * the bounds the reference STOPs on sets d_col_status (may be NULL) to the
+ * largest such code of the column and the context's status; the offending
+ * layer's output is 0. */
+int gb_cldprop_lw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int inflag, int iceflag,
+                         int liqflag, const double* cldfrac, const double* tauc, const double* ciwp,
+                         const double* clwp, const double* rei, const double* rel, double* taucloud,
+                         int64_t ld, int* d_col_status);
+
 /* Diagnostics (no counterpart in the reference's interface): runs the same
  * column kernel on host arrays (tight layout, ld = ncol) and also returns
  * the gas-plus-aerosol optical depth taut and the Planck fraction of every
