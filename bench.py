@@ -453,7 +453,7 @@ def gpu_arm(args, rank, world):
     t_kernel = sum(a.elapsed_time(b) for a, b in ev) / 1e3 / len(ev)  # one column-kernel launch (with its draws)
     status = ctx.sync_status(stream)
     sur_out = wl.outputs(0, nbase // 2, SAMPLE)
-    launches_per_step = nch * (2 * NMEM + 1)  # per chunk: inference and McICA draws per member, one column kernel
+    launches_per_step = nch * (2 * NMEM + 2)  # per chunk: inference and McICA draws per member, learned-only + hand-over kernels
 
     # ---------------- accuracy against the FP64 oracle
     log("accuracy against the oracle")
@@ -531,10 +531,12 @@ def e2e_headline(ctx, mlp, wl, dev, stream, steps, world, bufs):
     """Surrogate path with host-resident inputs: per chunk, every input array of
     the four members is copied from page-locked host memory (the generator
     tile's columns, stored chunk by chunk so that every copy is one contiguous
-    DMA), solved, and every output is copied back to page-locked memory.
-    Chunks are pipelined over two staging buffers and three streams: the
-    host-to-device copies of chunk i+1 and the device-to-host copies of chunk
-    i-1 run while chunk i is solved (events order every reuse of a buffer)."""
+    DMA), solved, and every output is copied back to page-locked memory.  The
+    band cloud optical depths are not copied: cldprop runs on the device from
+    the layer cloud state, as BRAMS would call it before McICA.  Chunks are
+    pipelined over two staging buffers and three streams: the host-to-device
+    copies of chunk i+1 and the device-to-host copies of chunk i-1 run while
+    chunk i is solved (events order every reuse of a buffer)."""
     import torch
     from brams_gb300 import rrtmg_lw as R
 
@@ -547,8 +549,6 @@ def e2e_headline(ctx, mlp, wl, dev, stream, steps, world, bufs):
     for k in names:
         a = np.ascontiguousarray(np.asarray(tile[k], dtype=np.float64).T)  # (..., T)
         host[k] = [torch.from_numpy(np.ascontiguousarray(a[..., j * C:(j + 1) * C])).pin_memory() for j in range(nt)]
-    tc = np.ascontiguousarray(np.asarray(tile["tauc"]).T)  # (nlay, T, 16)
-    host["tauc"] = [torch.from_numpy(np.ascontiguousarray(tc[:, j * C:(j + 1) * C, :])).pin_memory() for j in range(nt)]
     outs = ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt", "hr", "hrc")
     NBUF = 2
     stage = []
@@ -556,6 +556,7 @@ def e2e_headline(ctx, mlp, wl, dev, stream, steps, world, bufs):
         members = []
         for m in range(wl.nmem):
             d = {k: torch.empty(host[k][0].shape, dtype=torch.float64, device=dev) for k in host}
+            d["tauc"] = torch.empty((nlay, C, 16), dtype=torch.float64, device=dev)  # (16, C, nlay) Fortran
             for k in outs:
                 d[k] = torch.empty((nlay + (0 if k in ("hr", "hrc") else 1), C), dtype=torch.float64, device=dev)
             members.append(d)
@@ -589,6 +590,9 @@ def e2e_headline(ctx, mlp, wl, dev, stream, steps, world, bufs):
             grids = []
             for m in range(wl.nmem):
                 d = stage[b][m]
+                ctx.cldprop_lw_device(C, nlay, {"cldfrac": d["cldfrac"], "ciwp": d["ciwp"], "clwp": d["clwp"],
+                                                "rei": d["rei"], "rel": d["rel"], "taucloud": d["tauc"]},
+                                      inflag=2, iceflag=3, liqflag=1, ld=C, stream=stream)
                 arrays = dict(d)
                 arrays["reicmcl"], arrays["relqmcl"] = d["rei"], d["rel"]
                 r0 = m * C * nlay
@@ -617,8 +621,9 @@ def e2e_headline(ctx, mlp, wl, dev, stream, steps, world, bufs):
     t = (time.perf_counter() - t0) / steps
     return {"t": t, "h2d": counts["h2d"], "d2h": counts["d2h"],
             "note": f"every chunk copies all inputs of {wl.nmem} members x {C} columns from page-locked host memory "
-                    f"(the generator tile's columns) and reads all outputs back, pipelined over two staging buffers "
-                    f"(copies of neighbouring chunks overlap the solve); {steps} timed steps"}
+                    f"(the generator tile's columns; the band cloud optical depths made on the device by cldprop) and "
+                    f"reads all outputs back, pipelined over two staging buffers (copies of neighbouring chunks "
+                    f"overlap the solve); {steps} timed steps"}
 
 
 def cpu_baseline_headline(wl, seconds: float = 12.0, max_cols: int = 16384):
