@@ -51,6 +51,7 @@ static_assert(OFF_W2 % 1024 == 0 && OFF_W3 % 1024 == 0 && OFF_W4 % 1024 == 0 && 
                   OFF_H % 1024 == 0 && (NOH * 128) % 1024 == 0,
               "operand tiles must start on 1024-byte boundaries (128-byte swizzle atoms)");
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
+static_assert(NT / 32 * 32 * 17 * 4 <= OFF_F32 - OFF_X, "the output staging fits in the input and hidden tiles");
 static_assert(IMG_BYTES % 16 == 0 && OFF_BAR % 8 == 0, "bulk copies move multiples of 16 bytes; mbarriers are 8-byte aligned");
 
 // byte offset of element (r, k) in a K-major, 128-byte-swizzled tile of R rows
@@ -205,6 +206,7 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
   gbmlp::RawLayer raw = fetch(blockIdx.x);
   for (long long tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
     const long long r0 = tile * M;
+    __syncthreads();  // the previous tile's output staging (input and hidden tiles) is done
     // ---- features of the tile's rows (rows are layer-major: coalesced loads)
     if (tid < M) {
       const long long r = r0 + tid;
@@ -278,31 +280,44 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
           o = (icol * g.nlay + lay) * GB_NGPT_MLP;
         }
         // 18 chunks of 16 outputs (two halves of 144); warp quarter `part` takes chunks part, part+4, ...
+        // A chunk goes through shared memory (the free input and hidden tiles):
+        // each lane puts its row's 16 values there, then every store writes
+        // 64 contiguous bytes of eight rows instead of 16 bytes of 32 rows.
+        float* stg = reinterpret_cast<float*>(sm + OFF_X) + warp * (32 * 17);
+        long long orow[4];
+        bool lrow[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {  // the rows this lane stores for: k*8 + lane/4 of the warp's 32
+          const int src = k * 8 + (lane >> 2);
+          orow[k] = __shfl_sync(0xffffffffu, o, src);
+          lrow[k] = __shfl_sync(0xffffffffu, live ? 1 : 0, src) != 0;
+        }
 #pragma unroll 1
         for (int c = part; c < 2 * (NOH / 16); c += 4) {
           const int hh = c / (NOH / 16), c16 = c % (NOH / 16);
           float v[16];
           ld16(tlane + hh * 256 + c16 * 16, v);
-          if (!live) continue;
 #pragma unroll
-          for (int i = 0; i < 16; i += 4) {
+          for (int i = 0; i < 16; ++i) {
             const int j = hh * NOH + c16 * 16 + i;  // output index of v[i]
-            float y[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) y[u] = (v[i + u] + b4[j + u]) * osd[j + u] + omu[j + u];
-            if (j + 3 < GB_NGPT_MLP) {
-              *reinterpret_cast<float4*>(out_tau + o + j) = make_float4(__expf(y[0]), __expf(y[1]), __expf(y[2]), __expf(y[3]));
-            } else if (j >= GB_NGPT_MLP && j + 3 < GB_MLP_NOUT) {
-              *reinterpret_cast<float4*>(out_frac + o + j - GB_NGPT_MLP) = make_float4(y[0], y[1], y[2], y[3]);
-            } else {
-#pragma unroll
-              for (int u = 0; u < 4; ++u) {
-                const int jj = j + u;
-                if (jj < GB_NGPT_MLP) out_tau[o + jj] = __expf(y[u]);
-                else if (jj < GB_MLP_NOUT) out_frac[o + jj - GB_NGPT_MLP] = y[u];
-              }
-            }
+            const float y = (v[i] + b4[j]) * osd[j] + omu[j];
+            stg[lane * 17 + i] = j < GB_NGPT_MLP ? __expf(y) : y;
           }
+          __syncwarp();
+          const int q4 = lane & 3, rr = lane >> 2;
+          const int j = hh * NOH + c16 * 16 + 4 * q4;  // first output index of this lane's four
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const float* sp = stg + (k * 8 + rr) * 17 + 4 * q4;
+            const float4 val = make_float4(sp[0], sp[1], sp[2], sp[3]);
+            if (!lrow[k]) continue;
+            if (j + 3 < GB_NGPT_MLP) {
+              *reinterpret_cast<float4*>(out_tau + orow[k] + j) = val;
+            } else if (j >= GB_NGPT_MLP && j + 3 < GB_MLP_NOUT) {
+              *reinterpret_cast<float4*>(out_frac + orow[k] + j - GB_NGPT_MLP) = val;
+            }  // four-output groups never straddle 140 or 280 (both multiples of 4)
+          }
+          __syncwarp();
         }
       }
     }
