@@ -424,13 +424,18 @@ __device__ __noinline__ void prologue_dispatch(int b, const Smem& s, int nl, int
   }
 }
 
-// Scratch slot of a column: clear-sky coefficients float4 [nl][140] (T, Sd,
-// Su, 0), then the cloudy-layer coefficients float4 [nl][140] (A, Bd, Bu, D),
-// written and read only for cloudy cells.
+// Scratch slot of a column (2*nl*140 float4): the clear-sky coefficients as
+// three float planes [nl][140] -- T, Sd, Su -- from the start (the downward
+// sweep reads T and Sd, the upward one T and Su: 8 bytes a cell each), then
+// from float4 offset nl*140 the cloudy-layer coefficients float4 [nl][140]
+// (A, Bd, Bu, D), written and read only for cloudy cells.
 __device__ __forceinline__ void put_coef(float4* __restrict__ scr, int nl, int lay, int g, const CellCoef& cc,
                                          bool cloudy) {
   const int i = lay * GB_NGPT + g;
-  scr[i] = cc.clr;
+  float* pl = reinterpret_cast<float*>(scr);
+  pl[i] = cc.clr.x;
+  pl[nl * GB_NGPT + i] = cc.clr.y;
+  pl[2 * nl * GB_NGPT + i] = cc.clr.z;
   if (cloudy) scr[nl * GB_NGPT + i] = cc.cld;
 }
 
@@ -931,8 +936,9 @@ __device__ __forceinline__ bool solve_column(const LwArgs& a, long long icol, ch
         float2 c[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          const float4 v = j < nb ? scr[(L0 - j) * GB_NGPT + g] : make_float4(0.f, 0.f, 0.f, 0.f);
-          c[j] = make_float2(v.x, v.y);  // T, Sd
+          const int L = j < nb ? L0 - j : 0;  // an address inside the slot even where nothing is loaded
+          const float* pl = reinterpret_cast<const float*>(scr) + L * GB_NGPT + g;
+          c[j] = j < nb ? make_float2(pl[0], pl[nl * GB_NGPT]) : make_float2(0.f, 0.f);  // T, Sd
         }
         float q0[4], q1[4];
 #pragma unroll
@@ -970,8 +976,9 @@ __device__ __forceinline__ bool solve_column(const LwArgs& a, long long icol, ch
         float2 c[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          const float4 v = (j < nb && v0 + j >= 1) ? scr[(v0 + j - 1) * GB_NGPT + g] : make_float4(0.f, 0.f, 0.f, 0.f);
-          c[j] = make_float2(v.x, v.z);  // T, Su
+          const bool in = j < nb && v0 + j >= 1;
+          const float* pl = reinterpret_cast<const float*>(scr) + (in ? v0 + j - 1 : 0) * GB_NGPT + g;
+          c[j] = in ? make_float2(pl[0], pl[2 * nl * GB_NGPT]) : make_float2(0.f, 0.f);  // T, Su
         }
         float u0[4], u1[4], u2[4], u3[4];
 #pragma unroll

@@ -73,7 +73,7 @@ LwVariant gb_lw_variant(int v, bool lean = false);
 size_t gb_lw_smem_bytes(int nlay, bool lean = false);
 // thread blocks of `variant` that fit on the device at once for this nlay
 int gb_lw_slots(int nlay, int variant = 0, bool lean = false);
-// bytes of scratch for `slots` slots: per slot 2*nlay*140 float4 (clear and cloudy cell coefficients)
+// bytes of scratch for `slots` slots: per slot 2*nlay*140 float4 (clear-sky coefficient planes, cloudy cells)
 size_t gb_lw_scratch_bytes(int nlay, int slots);
 cudaError_t gb_lw_set_tables(const GbTables& T);
 // One grid, default variant, grid = min(ncol, nslots) blocks.
