@@ -535,9 +535,10 @@ def e2e_headline(ctx, mlp, wl, dev, stream, steps, world, bufs):
     DMA), solved, and every output is copied back to page-locked memory.  The
     band cloud optical depths are not copied: cldprop runs on the device from
     the layer cloud state, as BRAMS would call it before McICA.  Chunks are
-    pipelined over two staging buffers and three streams: the host-to-device
+    pipelined over three staging buffers and three streams: the host-to-device
     copies of chunk i+1 and the device-to-host copies of chunk i-1 run while
-    chunk i is solved (events order every reuse of a buffer)."""
+    chunk i is solved (events order every reuse of a buffer).  Three staging
+    buffers rather than two let a late copy of one chunk overlap two solves."""
     import torch
     from brams_gb300 import rrtmg_lw as R
 
@@ -551,7 +552,7 @@ def e2e_headline(ctx, mlp, wl, dev, stream, steps, world, bufs):
         a = np.ascontiguousarray(np.asarray(tile[k], dtype=np.float64).T)  # (..., T)
         host[k] = [torch.from_numpy(np.ascontiguousarray(a[..., j * C:(j + 1) * C])).pin_memory() for j in range(nt)]
     outs = ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt", "hr", "hrc")
-    NBUF = 2
+    NBUF = 3
     stage = []
     for _ in range(NBUF):
         members = []
@@ -644,7 +645,7 @@ def e2e_headline(ctx, mlp, wl, dev, stream, steps, world, bufs):
     return {"t": t, "h2d": counts["h2d"], "d2h": counts["d2h"], "matches": matches,
             "note": f"every chunk copies all inputs of {wl.nmem} members x {C} columns from page-locked host memory "
                     f"(the generator tile's columns; the band cloud optical depths made on the device by cldprop) and "
-                    f"reads all outputs back, pipelined over two staging buffers (copies of neighbouring chunks "
+                    f"reads all outputs back, pipelined over three staging buffers (copies of neighbouring chunks "
                     f"overlap the solve); {steps} timed steps"}
 
 
