@@ -233,11 +233,11 @@ def fused_bytes_per_column(nlay: int, learned: bool) -> int:
     """Algorithmic bytes of the fused-cloud column kernel: every layer input
     (12 gas/state + cldfrac, ciwp, clwp, 2 radii, 16 aerosol, 16 tauc = 49 per
     layer), plev/tlev, tsfc, 16 emis, the 140 McICA draws and every output once;
-    with the learned gas optics also the network's 280 fp32 outputs and flag
+    with the learned gas optics also the network's 280 binary16 outputs and flag
     per layer."""
     b = 8 * (49 * nlay + 2 * (nlay + 1) + 17) + 8 * GB_NGPT + 8 * (6 * (nlay + 1) + 2 * nlay)
     if learned:
-        b += nlay * (280 * 4 + 1)
+        b += nlay * (280 * 2 + 1)
     return b
 
 
@@ -386,8 +386,8 @@ def gpu_arm(args, rank, world):
     wl = Workload(dev, nbase, NLAY5, NMEM, seed)
     ncol = nbase * NMEM
     rows = CHUNK * NLAY5 * NMEM
-    bufs = (torch.empty((rows, GB_NGPT), dtype=torch.float32, device=dev),
-            torch.empty((rows, GB_NGPT), dtype=torch.float32, device=dev),
+    bufs = (torch.empty((rows, GB_NGPT), dtype=torch.float16, device=dev),
+            torch.empty((rows, GB_NGPT), dtype=torch.float16, device=dev),
             torch.empty(rows, dtype=torch.uint8, device=dev))
     plain = lambda: ctx.rrtmg_lw_batch_device([wl.desc(m) for m in range(NMEM)], stream=stream)
     sur = lambda ev=None: surrogate_step(ctx, mlp, wl, bufs, stream, ev)

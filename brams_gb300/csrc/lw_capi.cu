@@ -318,8 +318,8 @@ int gb_ctx_make_batch(gb_lw_context* ctx, int ngrid, const gb_lw_grid* grids, do
     a.duflx_dt = g.duflx_dt; a.duflxc_dt = g.duflxc_dt;
     a.col_err = g.d_col_status;
     a.err_flag = ctx->d_err;
-    a.sur_tau = g.sur_tau;
-    a.sur_frac = g.sur_frac;
+    a.sur_tau = reinterpret_cast<const __half*>(g.sur_tau);
+    a.sur_frac = reinterpret_cast<const __half*>(g.sur_frac);
     a.sur_flag = g.sur_flag;
     if ((g.sur_tau != nullptr) != (g.sur_frac != nullptr) || (g.sur_tau != nullptr) != (g.sur_flag != nullptr))
       return GB_LW_E_ARGS;

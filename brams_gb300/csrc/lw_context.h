@@ -48,7 +48,7 @@ struct gb_lw_context {
   unsigned* d_nfall = nullptr;
   size_t fall_elems = 0;
   // surrogate outputs of batched calls with a network (grown on demand)
-  float* d_sur = nullptr;
+  uint16_t* d_sur = nullptr;  // fp16 taug and Planck fractions
   unsigned char* d_sur_flag = nullptr;
   size_t sur_rows = 0;
 };

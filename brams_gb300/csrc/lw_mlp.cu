@@ -309,7 +309,7 @@ __device__ __forceinline__ void hidden_layer(const bf16* w, const float* bias, u
 
 __global__ void __launch_bounds__(IW * 32, 1) infer_kernel(GbMlpGridIn g, GbMlpNorm nm, const bf16* __restrict__ p16,
                                                            const float* __restrict__ p32, double grav, double avogad,
-                                                           float* __restrict__ out_tau, float* __restrict__ out_frac,
+                                                           __half* __restrict__ out_tau, __half* __restrict__ out_frac,
                                                            unsigned char* __restrict__ flag) {
   extern __shared__ __align__(16) char smraw[];
   InferSmem& S = *reinterpret_cast<InferSmem*>(smraw);
@@ -407,8 +407,11 @@ __global__ void __launch_bounds__(IW * 32, 1) infer_kernel(GbMlpGridIn g, GbMlpN
           const long long o = (icol * g.nlay + lay) * GB_NGPT_MLP;
           const float y0 = (acc[ni][2 * h] + S.b4[j]) * S.osd[j] + S.omu[j];
           const float y1 = (acc[ni][2 * h + 1] + S.b4[j + 1]) * S.osd[j + 1] + S.omu[j + 1];
-          if (j < GB_NGPT_MLP) *reinterpret_cast<float2*>(out_tau + o + j) = make_float2(__expf(y0), __expf(y1));
-          else *reinterpret_cast<float2*>(out_frac + o + j - GB_NGPT_MLP) = make_float2(y0, y1);
+          if (j < GB_NGPT_MLP)
+            *reinterpret_cast<__half2*>(out_tau + o + j) =
+                __floats2half2_rn(fminf(__expf(y0), GB_MLP_HALF_MAX), fminf(__expf(y1), GB_MLP_HALF_MAX));
+          else
+            *reinterpret_cast<__half2*>(out_frac + o + j - GB_NGPT_MLP) = __floats2half2_rn(y0, y1);
         }
     }
     __syncwarp();
@@ -519,7 +522,7 @@ cudaError_t gb_mlp_sync_bf16(const MlpBuffers& b, cudaStream_t st) {
 }
 
 cudaError_t gb_mlp_infer(const GbMlpGridIn& g, const GbMlpNorm& nm, const bf16* p16, const float* p32, double grav,
-                         double avogad, float* d_tau, float* d_frac, unsigned char* d_flag, int nsm, cudaStream_t st) {
+                         double avogad, __half* d_tau, __half* d_frac, unsigned char* d_flag, int nsm, cudaStream_t st) {
   const long long rows = (long long)g.ncol * g.nlay;
   if (rows == 0) return cudaSuccess;
   const size_t sm = sizeof(InferSmem);

@@ -1,6 +1,7 @@
 // Host interface of the taumol MLP kernels (lw_mlp.cu).
 #pragma once
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stddef.h>
 
@@ -37,9 +38,11 @@ cudaError_t gb_mlp_forward_backward(const MlpBuffers& b, long long rows, const _
                                     const float* d_w, float* d_grad, float* d_loss, cudaStream_t st);
 cudaError_t gb_mlp_adam(const MlpBuffers& b, const float* d_grad, float lr, int step, cudaStream_t st);
 cudaError_t gb_mlp_sync_bf16(const MlpBuffers& b, cudaStream_t st);
-// surrogate taug [(icol*nlay + lay)*140 + g], Planck fractions (same layout) and the in-range flag per layer
+// surrogate taug [(icol*nlay + lay)*140 + g], Planck fractions (same layout), both fp16 (taug clamped to
+// GB_MLP_HALF_MAX), and the in-range flag per layer
+#define GB_MLP_HALF_MAX 65504.0f
 cudaError_t gb_mlp_infer(const GbMlpGridIn& g, const GbMlpNorm& nm, const __nv_bfloat16* p16, const float* p32,
-                         double grav, double avogad, float* d_tau, float* d_frac, unsigned char* d_flag, int nsm,
+                         double grav, double avogad, __half* d_tau, __half* d_frac, unsigned char* d_flag, int nsm,
                          cudaStream_t st);
 
 // tcgen05 inference (lw_mlp_tc.cu): weight images prepared once per parameter change
@@ -47,5 +50,5 @@ size_t gb_mlp_tc_image_bytes();
 cudaError_t gb_mlp_tc_images(const __nv_bfloat16* p16, const float* p32, const GbMlpNorm& nm, void* d_img,
                              cudaStream_t st);
 cudaError_t gb_mlp_infer_tc(const GbMlpGridIn& g, const GbMlpNorm& nm, const void* d_img, double grav,
-                            double avogad, float* d_tau, float* d_frac, unsigned char* d_flag, int* d_err, int nsm,
+                            double avogad, __half* d_tau, __half* d_frac, unsigned char* d_flag, int* d_err, int nsm,
                             cudaStream_t st);

@@ -414,9 +414,13 @@ int gb_lw_mlp_set_engine(gb_lw_mlp* m, int engine) {
   return GB_LW_OK;
 }
 
-int gb_lw_mlp_infer(gb_lw_mlp* m, void* stream, const gb_lw_grid* grid, float* d_tau, float* d_frac,
+int gb_lw_mlp_infer(gb_lw_mlp* m, void* stream, const gb_lw_grid* grid, uint16_t* d_tau16, uint16_t* d_frac16,
                     uint8_t* d_flag) {
-  if (!m || !grid || !d_tau || !d_frac || !d_flag) return GB_LW_E_ARGS;
+  if (!m || !grid || !d_tau16 || !d_frac16 || !d_flag) return GB_LW_E_ARGS;
+  // the tensor-core engine stores four outputs (8 bytes) at a time
+  if (((uintptr_t)d_tau16 | (uintptr_t)d_frac16) & 7) return GB_LW_E_ARGS;
+  __half* d_tau = reinterpret_cast<__half*>(d_tau16);
+  __half* d_frac = reinterpret_cast<__half*>(d_frac16);
   if (grid->ncol < 0 || grid->nlay < 1 || grid->ld_in < grid->ncol) return GB_LW_E_ARGS;
   cudaSetDevice(m->ctx->device);
   cudaStream_t st = (cudaStream_t)stream;
@@ -451,7 +455,7 @@ int gb_rrtmg_lw_batch_surrogate(gb_lw_context* ctx, void* stream, int ngrid, con
     ctx->d_sur = nullptr;
     ctx->d_sur_flag = nullptr;
     ctx->sur_rows = 0;
-    if (cudaMalloc(&ctx->d_sur, rows * 2 * GB_NGPT_MLP * 4) != cudaSuccess ||
+    if (cudaMalloc(&ctx->d_sur, rows * 2 * GB_NGPT_MLP * sizeof(uint16_t)) != cudaSuccess ||
         cudaMalloc(&ctx->d_sur_flag, rows) != cudaSuccess) {
       cudaGetLastError();
       ctx->last_error = "device allocation of the learned gas-optics buffers failed";
@@ -463,8 +467,8 @@ int gb_rrtmg_lw_batch_surrogate(gb_lw_context* ctx, void* stream, int ngrid, con
   size_t off = 0;
   for (int i = 0; i < ngrid; ++i) {
     const size_t r = (size_t)std::max(g[i].ncol, 0) * std::max(g[i].nlay, 0);
-    float* tau = ctx->d_sur + off * 2 * GB_NGPT_MLP;
-    float* frac = tau + r * GB_NGPT_MLP;
+    uint16_t* tau = ctx->d_sur + off * 2 * GB_NGPT_MLP;
+    uint16_t* frac = tau + r * GB_NGPT_MLP;
     uint8_t* flag = ctx->d_sur_flag + off;
     int rc = gb_lw_mlp_infer(m, stream, &g[i], tau, frac, flag);
     if (rc) return rc;

@@ -141,7 +141,7 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t tcol, int row, int n0, 
 
 __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNorm nm, const uint4* __restrict__ img,
                                                          const float* __restrict__ f32, double grav, double avogad,
-                                                         float* __restrict__ out_tau, float* __restrict__ out_frac,
+                                                         __half* __restrict__ out_tau, __half* __restrict__ out_frac,
                                                          unsigned char* __restrict__ flag, int* __restrict__ err) {
   extern __shared__ __align__(1024) char sm[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -282,7 +282,8 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
         // 18 chunks of 16 outputs (two halves of 144); warp quarter `part` takes chunks part, part+4, ...
         // A chunk goes through shared memory (the free input and hidden tiles):
         // each lane puts its row's 16 values there, then every store writes
-        // 64 contiguous bytes of eight rows instead of 16 bytes of 32 rows.
+        // 32 contiguous bytes (16 fp16 outputs) of eight rows instead of 8
+        // bytes of 32 rows.
         float* stg = reinterpret_cast<float*>(sm + OFF_X) + warp * (32 * 17);
         long long orow[4];
         bool lrow[4];
@@ -301,7 +302,7 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
           for (int i = 0; i < 16; ++i) {
             const int j = hh * NOH + c16 * 16 + i;  // output index of v[i]
             const float y = (v[i] + b4[j]) * osd[j] + omu[j];
-            stg[lane * 17 + i] = j < GB_NGPT_MLP ? __expf(y) : y;
+            stg[lane * 17 + i] = j < GB_NGPT_MLP ? fminf(__expf(y), GB_MLP_HALF_MAX) : y;
           }
           __syncwarp();
           const int q4 = lane & 3, rr = lane >> 2;
@@ -309,12 +310,15 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
             const float* sp = stg + (k * 8 + rr) * 17 + 4 * q4;
-            const float4 val = make_float4(sp[0], sp[1], sp[2], sp[3]);
+            const __half2 h01 = __floats2half2_rn(sp[0], sp[1]), h23 = __floats2half2_rn(sp[2], sp[3]);
+            uint2 val;
+            val.x = *reinterpret_cast<const uint32_t*>(&h01);
+            val.y = *reinterpret_cast<const uint32_t*>(&h23);
             if (!lrow[k]) continue;
             if (j + 3 < GB_NGPT_MLP) {
-              *reinterpret_cast<float4*>(out_tau + orow[k] + j) = val;
+              *reinterpret_cast<uint2*>(out_tau + orow[k] + j) = val;
             } else if (j >= GB_NGPT_MLP && j + 3 < GB_MLP_NOUT) {
-              *reinterpret_cast<float4*>(out_frac + orow[k] + j - GB_NGPT_MLP) = val;
+              *reinterpret_cast<uint2*>(out_frac + orow[k] + j - GB_NGPT_MLP) = val;
             }  // four-output groups never straddle 140 or 280 (both multiples of 4)
           }
           __syncwarp();
@@ -374,7 +378,7 @@ cudaError_t gb_mlp_tc_images(const __nv_bfloat16* p16, const float* p32, const G
 }
 
 cudaError_t gb_mlp_infer_tc(const GbMlpGridIn& g, const GbMlpNorm& nm, const void* d_img, double grav,
-                            double avogad, float* d_tau, float* d_frac, unsigned char* d_flag, int* d_err, int nsm,
+                            double avogad, __half* d_tau, __half* d_frac, unsigned char* d_flag, int* d_err, int nsm,
                             cudaStream_t st) {
   const long long rows = (long long)g.ncol * g.nlay;
   if (rows == 0) return cudaSuccess;

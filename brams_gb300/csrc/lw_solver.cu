@@ -470,8 +470,8 @@ __device__ __forceinline__ void group_cells(int gr, const LwArgs& a, const Smem&
     float taut, plfrac;
     if (s.surok[lay]) {  // learned gas optics
       const long long o = (icol * nl + lay) * GB_NGPT + g;
-      taut = __ldg(a.sur_tau + o) + s.taua[(b - 1) * nl + lay];
-      plfrac = __ldg(a.sur_frac + o);
+      taut = __half2float(__ldg(a.sur_tau + o)) + s.taua[(b - 1) * nl + lay];
+      plfrac = __half2float(__ldg(a.sur_frac + o));
     } else {
       const int M = c_maxt[b];
       const float2* tp = s.terms + (size_t)c_toff[b] * nl + lay;
@@ -515,13 +515,13 @@ template <int NT>
 __device__ __forceinline__ void learned_cells(const LwArgs& a, const Smem& s, int nl, const float* __restrict__ T,
                                               long long icol, float4* __restrict__ scr) {
   const bool clouds = a.icld >= 1;
-  const float* __restrict__ st = a.sur_tau + icol * nl * GB_NGPT;
-  const float* __restrict__ sf = a.sur_frac + icol * nl * GB_NGPT;
+  const __half* __restrict__ st = a.sur_tau + icol * nl * GB_NGPT;
+  const __half* __restrict__ sf = a.sur_frac + icol * nl * GB_NGPT;
   for (int cell = threadIdx.x; cell < nl * GB_NGPT; cell += NT) {
     const int lay = (int)(((float)cell + 0.5f) * (1.0f / GB_NGPT)), g = cell - lay * GB_NGPT;
     const int b = c_T.ngb[g] - 1;
-    const float taut = __ldg(st + cell) + s.taua[b * nl + lay];
-    const float plfrac = __ldg(sf + cell);
+    const float taut = __half2float(__ldg(st + cell)) + s.taua[b * nl + lay];
+    const float plfrac = __half2float(__ldg(sf + cell));
     if (lay == 0) s.frac1[g] = plfrac;
     if (a.dbg_taut) {
       a.dbg_taut[(icol * nl + lay) * GB_NGPT + g] = taut;

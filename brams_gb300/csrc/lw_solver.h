@@ -1,5 +1,6 @@
 // Launch interface of the fused RRTMG_LW column kernel (lw_solver.cu).
 #pragma once
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stddef.h>
 
@@ -34,8 +35,8 @@ struct LwArgs {
   float* dbg_taut;   // optional diagnostics: taut and Planck fractions per column,
   float* dbg_fracs;  // (ncol, nlay, 140) with g fastest; NULL in production calls
   // optional learned gas optics: taug and Planck fractions per (column, layer, g)
-  // and a per-layer flag (1: use them, 0: taumol); NULL: taumol everywhere
-  const float *sur_tau, *sur_frac;
+  // in fp16 and a per-layer flag (1: use them, 0: taumol); NULL: taumol everywhere
+  const __half *sur_tau, *sur_frac;
   const unsigned char* sur_flag;
   // fused cloud mode: the columns' 140 McICA draws [ncol][140] made beforehand
   // (gb_mcica_percol_mt); NULL: the kernel draws them itself

@@ -221,10 +221,10 @@ typedef struct gb_lw_grid {
   double *uflx, *dflx, *hr, *uflxc, *dflxc, *hrc, *duflx_dt, *duflxc_dt;
   int* d_col_status; /* optional, ncol ints */
   /* optional learned gas optics (gb_lw_mlp_infer): taug and Planck fractions
-   * [(icol*nlay + lay)*140 + g] and a per-layer flag [icol*nlay + lay]; layers
-   * whose flag is 0 (inputs outside the network's training range) use taumol.
-   * NULL: taumol everywhere. */
-  const float *sur_tau, *sur_frac;
+   * [(icol*nlay + lay)*140 + g] as IEEE binary16 bit patterns and a per-layer
+   * flag [icol*nlay + lay]; layers whose flag is 0 (inputs outside the
+   * network's training range) use taumol.  NULL: taumol everywhere. */
+  const uint16_t *sur_tau, *sur_frac;
   const uint8_t* sur_flag;
 } gb_lw_grid;
 
@@ -342,12 +342,13 @@ int gb_lw_mlp_train_step(gb_lw_mlp* mlp, void* stream, int64_t rows, const void*
 /* Standardised outputs d_y[rows][288] of the training forward pass. */
 int gb_lw_mlp_forward(gb_lw_mlp* mlp, void* stream, int64_t rows, const void* d_x, float* d_y);
 /* Inference for one grid: taug and Planck fractions [(icol*nlay + lay)*140 + g]
- * and the per-layer flag (1 inside the training range) for gb_lw_grid's
- * sur_* fields. */
-int gb_lw_mlp_infer(gb_lw_mlp* mlp, void* stream, const gb_lw_grid* grid, float* d_tau, float* d_frac,
+ * in binary16 (taug clamped to 65504, the largest finite value; 2 bytes each
+ * instead of 4 halves what the column kernel reads) and the per-layer flag
+ * (1 inside the training range) for gb_lw_grid's sur_* fields. */
+int gb_lw_mlp_infer(gb_lw_mlp* mlp, void* stream, const gb_lw_grid* grid, uint16_t* d_tau, uint16_t* d_frac,
                     uint8_t* d_flag);
 /* gb_rrtmg_lw_batch_device with learned gas optics: inference for every grid
- * into context buffers (1121 bytes per column-layer), then the one batched
+ * into context buffers (561 bytes per column-layer), then the one batched
  * launch; out-of-range layers use taumol. */
 int gb_rrtmg_lw_batch_surrogate(gb_lw_context* ctx, void* stream, int ngrid, const gb_lw_grid* grids,
                                 gb_lw_mlp* mlp);
