@@ -42,8 +42,8 @@ constexpr int OFF_W4 = OFF_W3 + 2 * H * 128;          // 2 k-blocks x [288][64] 
 constexpr int IMG_BYTES = OFF_W4 + 2 * NO * 128;      // weight images
 constexpr int OFF_X = IMG_BYTES;                      // [128 m][64 k]          16 KB
 constexpr int OFF_H = OFF_X + M * 128;                // 2 k-blocks x [128][64] 32 KB
-constexpr int OFF_F32 = OFF_H + 2 * M * 128;          // b1 b2 b3 (128 each), b4, omu, osd (288 each)
-constexpr int NF32 = 3 * H + 3 * NO;
+constexpr int OFF_F32 = OFF_H + 2 * M * 128;          // b1 b2 b3 (128 each), output scale and shift (288 each)
+constexpr int NF32 = 3 * H + 2 * NO;
 constexpr int OFF_BAR = OFF_F32 + NF32 * 4;           // two mbarriers (MMA, weights) + TMEM address
 constexpr int SMEM_BYTES = OFF_BAR + 24;
 constexpr int BULK = 16384;                           // bytes per bulk copy of the weight images
@@ -51,7 +51,7 @@ static_assert(OFF_W2 % 1024 == 0 && OFF_W3 % 1024 == 0 && OFF_W4 % 1024 == 0 && 
                   OFF_H % 1024 == 0 && (NOH * 128) % 1024 == 0,
               "operand tiles must start on 1024-byte boundaries (128-byte swizzle atoms)");
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
-static_assert(NT / 32 * 32 * 17 * 4 <= OFF_F32 - OFF_X, "the output staging fits in the input and hidden tiles");
+static_assert(NT / 32 * 32 * 32 <= OFF_F32 - OFF_X, "the output staging fits in the input and hidden tiles");
 static_assert(IMG_BYTES % 16 == 0 && OFF_BAR % 8 == 0, "bulk copies move multiples of 16 bytes; mbarriers are 8-byte aligned");
 
 // byte offset of element (r, k) in a K-major, 128-byte-swizzled tile of R rows
@@ -120,6 +120,13 @@ __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::be
 __device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 
+// 2^x by the PTX approximate base-2 exponential
+__device__ __forceinline__ float ex2(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;\n" : "=f"(y) : "f"(x));
+  return y;
+}
+
 // silu(acc + bias) of 32 consecutive hidden units (from n0) of this thread's
 // row, into the next layer's operand tile
 __device__ __forceinline__ void hidden_epilogue(uint32_t tcol, int row, int n0, const float* bias, char* hbase) {
@@ -127,12 +134,16 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t tcol, int row, int n0, 
   for (int c16 = 0; c16 < 2; ++c16) {
     float v[16];
     ld16(tcol + c16 * 16, v);
+    float b[16];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {  // n0 is a multiple of 32 and bias 16-byte aligned
+      const float4 q = reinterpret_cast<const float4*>(bias + n0 + c16 * 16)[i];
+      b[4 * i] = q.x, b[4 * i + 1] = q.y, b[4 * i + 2] = q.z, b[4 * i + 3] = q.w;
+    }
     uint32_t p[8];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-      const int n = n0 + c16 * 16 + 2 * i;
-      p[i] = gbmlp::pack_bf16(gbmlp::silu(v[2 * i] + bias[n]), gbmlp::silu(v[2 * i + 1] + bias[n + 1]));
-    }
+    for (int i = 0; i < 8; ++i)
+      p[i] = gbmlp::pack_bf16(gbmlp::silu(v[2 * i] + b[2 * i]), gbmlp::silu(v[2 * i + 1] + b[2 * i + 1]));
     const int k0 = n0 + c16 * 16;
     *reinterpret_cast<uint4*>(hbase + sw128(M, row, k0)) = make_uint4(p[0], p[1], p[2], p[3]);
     *reinterpret_cast<uint4*>(hbase + sw128(M, row, k0 + 8)) = make_uint4(p[4], p[5], p[6], p[7]);
@@ -146,7 +157,9 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
   extern __shared__ __align__(1024) char sm[];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const float* sf = reinterpret_cast<const float*>(sm + OFF_F32);
-  const float *b1 = sf, *b2 = sf + H, *b3 = sf + 2 * H, *b4 = sf + 3 * H, *omu = b4 + NO, *osd = omu + NO;
+  // output j = acc * oscale[j] + oshift[j]: the output bias and un-standardisation
+  // folded together, in base-2 logarithm units for taug (j < 140)
+  const float *b1 = sf, *b2 = sf + H, *b3 = sf + 2 * H, *oscale = sf + 3 * H, *oshift = oscale + NO;
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + OFF_BAR);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + OFF_BAR + 16);
   // weight images into shared memory by bulk (TMA) copies completing on an
@@ -280,11 +293,12 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
           o = (icol * g.nlay + lay) * GB_NGPT_MLP;
         }
         // 18 chunks of 16 outputs (two halves of 144); warp quarter `part` takes chunks part, part+4, ...
-        // A chunk goes through shared memory (the free input and hidden tiles):
-        // each lane puts its row's 16 values there, then every store writes
-        // 32 contiguous bytes (16 fp16 outputs) of eight rows instead of 8
-        // bytes of 32 rows.
-        float* stg = reinterpret_cast<float*>(sm + OFF_X) + warp * (32 * 17);
+        // A chunk goes through shared memory (the free input and hidden tiles)
+        // as binary16: each lane puts its row's 16 values there (four 8-byte
+        // groups, group m of row r at slot m ^ ((r >> 2) & 3), so that neither
+        // the puts nor the gets conflict on banks), then every store writes 32
+        // contiguous bytes (16 outputs) of eight rows instead of 8 bytes of 32.
+        uint2* stg = reinterpret_cast<uint2*>(sm + OFF_X) + warp * (32 * 4);
         long long orow[4];
         bool lrow[4];
 #pragma unroll
@@ -296,24 +310,31 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
 #pragma unroll 1
         for (int c = part; c < 2 * (NOH / 16); c += 4) {
           const int hh = c / (NOH / 16), c16 = c % (NOH / 16);
+          const int j0 = hh * NOH + c16 * 16;  // output index of v[0]
           float v[16];
           ld16(tlane + hh * 256 + c16 * 16, v);
+          const float4* sc = reinterpret_cast<const float4*>(oscale + j0);
+          const float4* sh = reinterpret_cast<const float4*>(oshift + j0);
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            const int j = hh * NOH + c16 * 16 + i;  // output index of v[i]
-            const float y = (v[i] + b4[j]) * osd[j] + omu[j];
-            stg[lane * 17 + i] = j < GB_NGPT_MLP ? fminf(__expf(y), GB_MLP_HALF_MAX) : y;
+          for (int m = 0; m < 4; ++m) {
+            const float4 a = sc[m], b = sh[m];
+            float y0 = fmaf(v[4 * m], a.x, b.x), y1 = fmaf(v[4 * m + 1], a.y, b.y);
+            float y2 = fmaf(v[4 * m + 2], a.z, b.z), y3 = fmaf(v[4 * m + 3], a.w, b.w);
+            if (j0 + 4 * m < GB_NGPT_MLP) {  // groups of four never straddle 140
+              y0 = fminf(ex2(y0), GB_MLP_HALF_MAX), y1 = fminf(ex2(y1), GB_MLP_HALF_MAX);
+              y2 = fminf(ex2(y2), GB_MLP_HALF_MAX), y3 = fminf(ex2(y3), GB_MLP_HALF_MAX);
+            }
+            const __half2 h01 = __floats2half2_rn(y0, y1), h23 = __floats2half2_rn(y2, y3);
+            stg[lane * 4 + (m ^ ((lane >> 2) & 3))] =
+                make_uint2(*reinterpret_cast<const uint32_t*>(&h01), *reinterpret_cast<const uint32_t*>(&h23));
           }
           __syncwarp();
           const int q4 = lane & 3, rr = lane >> 2;
-          const int j = hh * NOH + c16 * 16 + 4 * q4;  // first output index of this lane's four
+          const int j = j0 + 4 * q4;  // first output index of this lane's four
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
-            const float* sp = stg + (k * 8 + rr) * 17 + 4 * q4;
-            const __half2 h01 = __floats2half2_rn(sp[0], sp[1]), h23 = __floats2half2_rn(sp[2], sp[3]);
-            uint2 val;
-            val.x = *reinterpret_cast<const uint32_t*>(&h01);
-            val.y = *reinterpret_cast<const uint32_t*>(&h23);
+            const int r8 = k * 8 + rr;
+            const uint2 val = stg[r8 * 4 + (q4 ^ ((r8 >> 2) & 3))];
             if (!lrow[k]) continue;
             if (j + 3 < GB_NGPT_MLP) {
               *reinterpret_cast<uint2*>(out_tau + orow[k] + j) = val;
@@ -359,10 +380,13 @@ __global__ void images_kernel(const bf16* __restrict__ p16, const float* __restr
     f32[H + i] = p32[GB_MLP_OFF_B2 + i];
     f32[2 * H + i] = p32[GB_MLP_OFF_B3 + i];
   }
+  // output i = (acc + b4) * sd + mu = acc * scale + shift, times log2(e) for
+  // the log-taug outputs so that the kernel takes 2^x
   for (int i = tid; i < NO; i += nth) {
-    f32[3 * H + i] = p32[GB_MLP_OFF_B4 + i];
-    f32[3 * H + NO + i] = nm.out_mu[i];
-    f32[3 * H + 2 * NO + i] = nm.out_sd[i];
+    const double c = i < GB_NGPT_MLP ? 1.4426950408889634 : 1.0;
+    const double sd = nm.out_sd[i];
+    f32[3 * H + i] = (float)(sd * c);
+    f32[3 * H + NO + i] = (float)(((double)p32[GB_MLP_OFF_B4 + i] * sd + (double)nm.out_mu[i]) * c);
   }
 }
 
