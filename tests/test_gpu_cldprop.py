@@ -113,3 +113,25 @@ def test_fused_solver_fed_by_device_cldprop(ctx):
     a, b = ga.outputs(), gb.outputs()
     for k in a:
         assert np.abs(a[k] - b[k]).max() <= 1e-9 * (np.abs(a[k]).max() + 1.0), k
+
+
+@pytest.mark.parametrize("inflag,iceflag,liqflag", [(2, 3, 1), (2, 1, 0), (0, 3, 1)])
+def test_output_off_16_byte_boundary_gives_the_same_bits(ctx, inflag, iceflag, liqflag):
+    """An output array that starts 8 bytes past a 16-byte boundary takes the
+    kernel's one-value-at-a-time stores instead of its pairs: same values."""
+    import torch
+
+    st = _state(61, 45, 300 + 10 * iceflag + liqflag, iceflag)
+    ncol, nlay = st["cldfrac"].shape
+    a, _ = _device(ctx, st, inflag, iceflag, liqflag)
+    d = {k: _dev(st[k]) for k in ("cldfrac", "ciwp", "clwp", "rei", "rel")}
+    d["tauc"] = _dev(st["tauc_in"])
+    flat = torch.full((nlay * ncol * 16 + 1,), -1.0, dtype=torch.float64, device="cuda")
+    d["taucloud"] = flat[1:].view(nlay, ncol, 16)
+    assert d["taucloud"].data_ptr() % 16 == 8
+    ctx.cldprop_lw_device(ncol, nlay, d, inflag, iceflag, liqflag)
+    torch.cuda.synchronize()
+    assert ctx.sync_status() == 0
+    b = d["taucloud"].cpu().numpy().T.copy()
+    assert np.array_equal(a, b)
+    assert flat[0].item() == -1.0  # nothing written before the array
