@@ -9,8 +9,8 @@
 // commits to an mbarrier; sixteen warps then read the accumulators back with
 // tcgen05.ld (warp w: TMEM lanes 32*(w%4).., column quarter w/4), apply bias and
 // SiLU, and write the next layer's operand tile.  The output layer
-// (N = 288 = 2 x 144) is un-standardised and written per (column, layer) in
-// the layout the column kernel reads.
+// (N = 288 = 2 x 144) is un-standardised and written as binary16 per
+// (column, layer) in the layout the column kernel reads.
 //
 // Every wait on the mbarrier is bounded; a wait that runs out records an
 // error flag, and the kernel frees its tensor memory and returns.

@@ -435,6 +435,8 @@ class Mlp:
         self._ok(self.L.gb_lw_mlp_forward(self.h, _ptr(stream or 0), rows, _ptr(x), _ptr(y)))
 
     def infer(self, grid: GridDesc, tau, frac, flag, stream=None) -> None:
+        """gb_lw_mlp_infer: tau and frac are float16 device arrays of
+        ncol*nlay*140 values (8-byte aligned), flag uint8 of ncol*nlay."""
         self._ok(self.L.gb_lw_mlp_infer(self.h, _ptr(stream or 0), C.byref(grid), _ptr(tau), _ptr(frac), _ptr(flag)))
 
     def batch(self, grids, stream=None) -> None:
