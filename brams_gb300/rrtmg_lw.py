@@ -42,7 +42,7 @@ EXPORTS = [
     "gb_lw_mlp_set_params", "gb_lw_mlp_set_loss_weights", "gb_lw_mlp_samples", "gb_lw_mlp_fit_norm",
     "gb_lw_mlp_prepare", "gb_lw_mlp_gradients", "gb_lw_mlp_train_step", "gb_lw_mlp_forward", "gb_lw_mlp_infer",
     "gb_rrtmg_lw_batch_surrogate", "gb_lw_mlp_set_engine", "gb_rrtmg_lw_autotune_report",
-    "gb_cldprop_lw_device",
+    "gb_cldprop_lw_device", "gb_rtm_pack_lw_device", "gb_rtm_unpack_lw_device",
 ]
 MLP_MMA_SYNC, MLP_TCGEN05 = 0, 1
 MLP_NPARAM = 72352
@@ -127,6 +127,8 @@ def load_library(path: str = LIB_PATH):
         L.gb_mcica_subcol_lw_device.argtypes = [P, P, I, I, I, I, IP] + [P] * 8 + [P] * 6 + [LL, I]
         L.gb_rrtmg_lw_gas_optics_diag.argtypes = [P, I, I] + [P] * 17 + [P, P]
         L.gb_cldprop_lw_device.argtypes = [P, P, I, I, I, I, I] + [P] * 7 + [LL, P]
+        L.gb_rtm_pack_lw_device.argtypes = [P, P] + [I] * 9 + [P] * 31 + [LL]
+        L.gb_rtm_unpack_lw_device.argtypes = [P, P] + [I] * 7 + [P] * 3 + [LL, LL, P, P]
         L.gb_mcica_subcol_lw_noalloc.argtypes = [P, I, I, I, I, IP] + [P] * 8 + [P] * 6 + [LL, I, P]
         GP = C.POINTER(GridDesc)
         L.gb_rrtmg_lw_batch_device.argtypes = [P, P, I, GP]
@@ -284,6 +286,33 @@ class Context:
         _check(self.L, self.h, self.L.gb_cldprop_lw_device(
             self.h, _ptr(stream or 0), ncol, nlay, inflag, iceflag, liqflag, g("cldfrac"), g("tauc"), g("ciwp"),
             g("clwp"), g("rei"), g("rel"), g("taucloud"), ld if ld is not None else ncol, g("d_col_status")))
+
+    PACK_IN = ("pi0", "pp", "theta", "rv", "rlongup", "albedt", "cldf", "lwl", "iwl", "rel", "rei")
+    PACK_OUT = ("play", "plev", "tlay", "tlev", "tsfc", "h2ovmr", "co2vmr", "ch4vmr", "n2ovmr", "o2vmr", "cfc11vmr",
+                "cfc12vmr", "cfc22vmr", "ccl4vmr", "emis", "cldfrac", "ciwp", "clwp", "reic", "relq")
+
+    def rtm_pack_lw_device(self, mzp: int, mxp: int, myp: int, box, ptrs: dict, iceflgsw: int = 3,
+                           firsttime: bool = False, ld: int | None = None, stream=None) -> None:
+        """gb_rtm_pack_lw_device: BRAMS fields (PACK_IN, float32 device arrays in
+        Fortran order) of the 1-based box (ia, iz, ja, jz) into the rrtmg_lw
+        inputs (PACK_OUT, float64, leading dimension ld)."""
+        ia, iz, ja, jz = box
+        ncol = (iz - ia + 1) * (jz - ja + 1)
+        args = [_ptr(ptrs[k]) for k in self.PACK_IN] + [_ptr(ptrs[k]) for k in self.PACK_OUT]
+        _check(self.L, self.h, self.L.gb_rtm_pack_lw_device(
+            self.h, _ptr(stream or 0), mzp, mxp, myp, ia, iz, ja, jz, iceflgsw, 1 if firsttime else 0, *args,
+            ld if ld is not None else ncol))
+
+    def rtm_unpack_lw_device(self, mzp: int, mxp: int, myp: int, box, hr, dflx, fthrd, rlong, swhr=None,
+                             ld_hr: int | None = None, ld_flx: int | None = None, stream=None) -> None:
+        """gb_rtm_unpack_lw_device: heating rates into BRAMS's theta tendency
+        fthrd (mzp, mxp, myp) and dflx(:, 1) into rlong (mxp, myp), float32."""
+        ia, iz, ja, jz = box
+        ncol = (iz - ia + 1) * (jz - ja + 1)
+        _check(self.L, self.h, self.L.gb_rtm_unpack_lw_device(
+            self.h, _ptr(stream or 0), mzp, mxp, myp, ia, iz, ja, jz, _ptr(hr), _ptr(swhr), _ptr(dflx),
+            ld_hr if ld_hr is not None else ncol, ld_flx if ld_flx is not None else ncol, _ptr(fthrd),
+            _ptr(rlong)))
 
     def mcica_subcol_lw_device(self, ncol: int, nlay: int, ptrs: dict, icld: int, permuteseed: int, irng: int = 1,
                                seed_per_column: bool = True, stream=None, ld: int | None = None) -> None:

@@ -146,6 +146,38 @@ int gb_cldprop_lw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, i
                          const double* clwp, const double* rei, const double* rel, double* taucloud,
                          int64_t ld, int* d_col_status);
 
+/* BRAMS's column packing for rrtmg_lw on DEVICE arrays: the statements of
+ * radrrtmdrv (rtm_driver.f90:978-1076, 1176-1231) that turn the model state
+ * of the subdomain i = ia..iz, j = ja..jz (1-based, columns j outer and i
+ * inner) into the solver's inputs.  Model fields are BRAMS's default-real
+ * (float) arrays: pi0, pp, theta, rv, cldf, lwl, iwl, rel, rei are
+ * (mzp, mxp, myp); rlongup, albedt are (mxp, myp).  Outputs are the
+ * rrtmg_lw arrays with leading dimension ld >= ncol and nlay = mzp - 1
+ * layers: play, tlay, h2ovmr, the fixed gases, cldfrac, ciwp, clwp, reic
+ * (clamped as the driver does for iceflgsw 1-3), relq (ld, nlay); plev,
+ * tlev (ld, nlay+1); tsfc (ld); emis (ld, 16), 0 when firsttime is nonzero
+ * as on the driver's first call.  Float operations round as the driver's
+ * default-real statements do before they meet real(8) values.  o3vmr and
+ * tauaer are not written (ozone climatology and CARMA stay with the
+ * caller). */
+int gb_rtm_pack_lw_device(gb_lw_context* ctx, void* stream, int mzp, int mxp, int myp, int ia, int iz, int ja, int jz,
+                          int iceflgsw, int firsttime, const float* pi0, const float* pp, const float* theta,
+                          const float* rv, const float* rlongup, const float* albedt, const float* cldf,
+                          const float* lwl, const float* iwl, const float* rel, const float* rei, double* play,
+                          double* plev, double* tlay, double* tlev, double* tsfc, double* h2ovmr, double* co2vmr,
+                          double* ch4vmr, double* n2ovmr, double* o2vmr, double* cfc11vmr, double* cfc12vmr,
+                          double* cfc22vmr, double* ccl4vmr, double* emis, double* cldfrac, double* ciwp,
+                          double* clwp, double* reic, double* relq, int64_t ld);
+
+/* The driver's write-back (rtm_driver.f90:1443-1456) on DEVICE arrays:
+ * fthrd(k, i, j) = (swhr + hr)(column, k-1) / 86400 for k = 2..mzp-1, copied
+ * to k = 1 and k = mzp, and rlong(i, j) = dflx(column, 1), into BRAMS's float
+ * fields fthrd (mzp, mxp, myp) and rlong (mxp, myp).  hr (and swhr, NULL for
+ * none) have leading dimension ld_hr, dflx ld_flx. */
+int gb_rtm_unpack_lw_device(gb_lw_context* ctx, void* stream, int mzp, int mxp, int myp, int ia, int iz, int ja,
+                            int jz, const double* hr, const double* swhr, const double* dflx, int64_t ld_hr,
+                            int64_t ld_flx, float* fthrd, float* rlong);
+
 /* Diagnostics (no counterpart in the reference's interface): runs the same
  * column kernel on host arrays (tight layout, ld = ncol) and also returns
  * the gas-plus-aerosol optical depth taut and the Planck fraction of every
