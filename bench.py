@@ -491,6 +491,7 @@ def gpu_arm(args, rank, world):
         return
     alg = fused_bytes_per_column(NLAY5, True) * NMEM * min(CHUNK, nbase)
     achieved = alg / t_kernel / 1e9
+    traffic = traffic_from_profiles("lw_batch_kernel_c5_traffic.txt")
     line = {
         "metric": METRIC, "value": world * ncol / t_sur, "unit": "columns/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_sur * 1e3, "higher_is_better": True,
@@ -511,7 +512,11 @@ def gpu_arm(args, rank, world):
                       "speedup_of_surrogate": t_plain / t_sur},
         "accuracy": acc,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": traffic_from_profiles("lw_batch_kernel_c5_traffic.txt"),
+                     "traffic": traffic,
+                     # what DRAM actually moved (ncu bytes per launch over this run's launch time): the
+                     # kernel is latency-bound, not bandwidth-bound, at either count
+                     "dram_gbs": traffic / t_kernel / 1e9 if traffic else None,
+                     "dram_frac": traffic / t_kernel / 1e9 / hbm if traffic else None,
                      "kernel": "lw_batch_kernel (learned gas optics, fused clouds), one launch = 4 members x "
                                f"{min(CHUNK, nbase)} columns; alg bytes/column {fused_bytes_per_column(NLAY5, True)}",
                      "alg_bytes_per_launch": alg, "launch_ms": t_kernel * 1e3,
