@@ -491,7 +491,7 @@ def gpu_arm(args, rank, world):
         return
     alg = fused_bytes_per_column(NLAY5, True) * NMEM * min(CHUNK, nbase)
     achieved = alg / t_kernel / 1e9
-    traffic = traffic_from_profiles("lw_batch_kernel_c5_traffic.txt")
+    traffic = traffic_from_profiles("lw_batch_kernel_learned_traffic.txt")
     line = {
         "metric": METRIC, "value": world * ncol / t_sur, "unit": "columns/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_sur * 1e3, "higher_is_better": True,
@@ -755,7 +755,7 @@ def abi_block(ctx, dev, stream, args, rank, world, hbm):
                         + ("360x300 columns x 45 layers" if ncol == NCOL else f"{ncol} columns x 45 layers"),
             "value": world * ncol / t_dev, "unit": "columns/s", "ms_per_step": t_dev * 1e3,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": traffic_from_profiles("lw_batch_kernel_c2_traffic.txt"), "alg_bytes_per_launch": alg},
+                         "traffic": traffic_from_profiles("lw_batch_kernel_drop_in_traffic.txt"), "alg_bytes_per_launch": alg},
             "e2e": {"value": world * ncol / t_e2e, "unit": "columns/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "host_path_matches_device_path": same},
             "column_status": status}

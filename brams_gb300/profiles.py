@@ -152,17 +152,17 @@ def make_state(spec: ProfileSpec) -> dict:
     return out
 
 
-CONFIGS = {
+WORKLOADS = {
     # name: (ncol, nlay, ptop, t_noise, h2o_sigma)
-    "c1_oracle_64x64x38": dict(ncol=64 * 64, nlay=38, ptop=10.0, t_noise=2.0, h2o_sigma=0.3),
-    "c2_brams_360x300x45": dict(ncol=360 * 300, nlay=45, ptop=10.0, t_noise=4.0, h2o_sigma=0.5),
-    "c4_eval_512x512x45": dict(ncol=512 * 512, nlay=45, ptop=10.0, t_noise=4.0, h2o_sigma=0.5),
-    "c5_scale_2048x1024x4x60": dict(ncol=2048 * 1024 * 4, nlay=60, ptop=5.0, t_noise=4.0, h2o_sigma=0.5),
+    "oracle_64x64x38": dict(ncol=64 * 64, nlay=38, ptop=10.0, t_noise=2.0, h2o_sigma=0.3),
+    "drop_in_360x300x45": dict(ncol=360 * 300, nlay=45, ptop=10.0, t_noise=4.0, h2o_sigma=0.5),
+    "eval_512x512x45": dict(ncol=512 * 512, nlay=45, ptop=10.0, t_noise=4.0, h2o_sigma=0.5),
+    "scale_2048x1024x4x60": dict(ncol=2048 * 1024 * 4, nlay=60, ptop=5.0, t_noise=4.0, h2o_sigma=0.5),
 }
 
 
-def config_spec(name: str, ncol: int | None = None, seed: int = 20240601) -> ProfileSpec:
-    c = dict(CONFIGS[name])
+def workload_spec(name: str, ncol: int | None = None, seed: int = 20240601) -> ProfileSpec:
+    c = dict(WORKLOADS[name])
     if ncol is not None:
         c["ncol"] = ncol
     return ProfileSpec(seed=seed, **c)

@@ -33,8 +33,8 @@ def case(name, ncol, nlay, seed, ptop=10.0, t_noise=2.0, h2o_sigma=0.3):
 
 
 def main():
-    case("lw_c1_16x38", 16, 38, seed=20240601)
-    case("lw_c5_8x60", 8, 60, seed=77, ptop=5.0, t_noise=4.0, h2o_sigma=0.5)
+    case("lw_16x38", 16, 38, seed=20240601)
+    case("lw_8x60_top5hpa", 8, 60, seed=77, ptop=5.0, t_noise=4.0, h2o_sigma=0.5)
     seeds = np.array([1, 5489, 12345, 2**31 - 1], dtype=np.int64)
     ints = np.stack([pyoracle.mt_draws(int(s), 700)[0] for s in seeds])
     np.savez_compressed(os.path.join(HERE, "mt19937_draws.npz"), seeds=seeds, ints=ints)

@@ -8,7 +8,7 @@ import pytest
 import pyoracle
 
 G = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["lw_c1_16x38", "lw_c5_8x60"]
+CASES = ["lw_16x38", "lw_8x60_top5hpa"]
 OUTS = ["uflx", "dflx", "uflxc", "dflxc", "hr", "hrc", "duflx_dt", "duflxc_dt"]
 
 
