@@ -25,7 +25,8 @@ makes, so :func:`build` reduces them to 140 g-points with the reference's
 reference's own reader can load the tables this project generates.
 netCDF classic files (CDF-1/CDF-2) only: scipy reads no HDF5-based netCDF-4.
 
-Usage:  python -m brams_gb300.data.nc_ktables rrtmg_lw.nc [out.gblw]
+Usage:  python -m brams_gb300.data.nc_ktables rrtmg_lw.nc <table dir>
+        (then gb_rrtmg_lw_ini(cpdair, "<table dir>", ...))
 """
 from __future__ import annotations
 
@@ -138,17 +139,26 @@ def write_original(path: str, orig: dict) -> None:
             f.createVariable(v, "d", dims)[:] = data[v]
 
 
-def build(nc_path: str, dst: str | None = None) -> str:
+def build(nc_path: str, out_dir: str) -> str:
     """Reduce the file's tables to the solver's 140 g-points (the reference's
-    cmbgb1..16) and write them as the solver's k-distribution table file."""
-    ref = read_tables(os.path.join(HERE, "lw_ref_tables.gblw"))
-    red = reduce_tables(read_original(nc_path), ref)
-    dst = dst or os.path.join(HERE, "lw_ktables.gblw")
+    cmbgb1..16) into out_dir/lw_ktables.gblw, beside a copy of the constant
+    tables, so that out_dir is a table directory for gb_rrtmg_lw_ini.  The
+    shipped synthetic tables are left as they are."""
+    import shutil
+
+    os.makedirs(out_dir, exist_ok=True)
+    ref_path = os.path.join(HERE, "lw_ref_tables.gblw")
+    red = reduce_tables(read_original(nc_path), read_tables(ref_path))
+    dst = os.path.join(out_dir, "lw_ktables.gblw")
+    if os.path.abspath(dst) == os.path.abspath(os.path.join(HERE, "lw_ktables.gblw")):
+        raise ValueError("out_dir must not be the directory of the shipped tables")
     write_tables(dst, red)
+    if os.path.abspath(out_dir) != HERE:
+        shutil.copyfile(ref_path, os.path.join(out_dir, "lw_ref_tables.gblw"))
     return dst
 
 
 if __name__ == "__main__":
-    if len(sys.argv) < 2:
+    if len(sys.argv) != 3:
         sys.exit(__doc__)
-    print(build(sys.argv[1], sys.argv[2] if len(sys.argv) > 2 else None))
+    print(build(sys.argv[1], sys.argv[2]))

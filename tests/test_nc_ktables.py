@@ -68,7 +68,8 @@ def test_round_trip_and_reduced_tables_equal_the_shipped_ones(tmp_path):
     for k in orig:
         assert back[k].shape == np.asarray(orig[k]).shape, k
         assert np.array_equal(back[k], orig[k]), k
-    dst = N.build(p, str(tmp_path / "k.gblw"))
+    dst = N.build(p, str(tmp_path / "tables"))
+    assert os.path.exists(str(tmp_path / "tables" / "lw_ref_tables.gblw"))
     built, shipped = read_tables(dst), read_tables(os.path.join(DATA, "lw_ktables.gblw"))
     assert list(built) == list(shipped)
     for k in shipped:
