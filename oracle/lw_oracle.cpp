@@ -103,6 +103,10 @@ struct Col {
   double semiss[NBND];
   std::vector<double> cldfmc, taucmc, ciwpmc, clwpmc, relqmc, reicmc, taua /*(l,16)*/;
   int inflag = 0, iceflag = 0, liqflag = 0;
+  // non-McICA random overlap (rtrn): layer cloud fraction and cldprop's
+  // band cloud optical depths taucloud(l, ib), ib < ncbands
+  int rtrn = 0, ncbands = 0;
+  std::vector<double> cldfr_lay, taucloud;
   // setcoef
   int laytrop = 0;
   std::vector<int> jp, jt, jt1, indself, indfor, indminor;
@@ -153,6 +157,7 @@ struct Col {
   double& FRACS(int l, int ig) { return fracs[l + (nlayers + 1) * (ig - 1)]; }
   double& TAUT(int l, int ig) { return taut[l + (nlayers + 1) * (ig - 1)]; }
   double& TAUA(int l, int b) { return taua[l + (nlayers + 1) * (b - 1)]; }
+  double& TAUCL(int l, int b) { return taucloud[(l - 1) + nlayers * (b - 1)]; }  // (nlayers, 16)
 };
 
 enum { ERR_OK = 0, ERR_NOT_INIT = 1, ERR_INFLAG1 = 2, ERR_ICE_SMALL = 3, ERR_ICE_BOUNDS = 4,
@@ -1159,20 +1164,56 @@ void rtrnmc(Col& c, int idrv) {
     c.totuflux[lev] = c.totdflux[lev] = c.totuclfl[lev] = c.totdclfl[lev] = 0.0;
     if (idrv == 1) c.dtotuflux_dt[lev] = c.dtotuclfl_dt[lev] = 0.0;
   }
-  for (int lay = 1; lay <= nlayers; ++lay) {
-    icldlyr[lay] = 0;
-    for (int ig = 1; ig <= NGPT; ++ig) {
-      if (c.CF(c.cldfmc, ig, lay) == 1.0) {
-        int ib = ngb[ig - 1];
-        L(odcld, lay, ig) = secdiff[ib - 1] * c.CF(c.taucmc, ig, lay);
-        double transcld = std::exp(-L(odcld, lay, ig));
-        L(abscld, lay, ig) = 1.0 - transcld;
-        L(efclfrac, lay, ig) = L(abscld, lay, ig) * c.CF(c.cldfmc, ig, lay);
-        icldlyr[lay] = 1;
-      } else {
-        L(odcld, lay, ig) = 0.0;
-        L(abscld, lay, ig) = 0.0;
-        L(efclfrac, lay, ig) = 0.0;
+  if (c.rtrn) {
+    // rrtmg_lw_rtrn.f90:319-336: cloud prep per layer and cloud band; the
+    // sweeps below are rtrn's (:361-603 match rtrnmc's statement for
+    // statement with the cloud band ib of :343-349 for the g-point index of
+    // odcld/efclfrac and cldfrac(lev) for cldfmc(igc, lev)), so the band
+    // values are spread over the g-points of the spectral bands that read them
+    static const int ipat[3][16] = {{1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1},
+                                    {1, 2, 3, 3, 3, 4, 4, 4, 5, 5, 5, 5, 5, 5, 5, 5},
+                                    {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16}};
+    const int row = c.ncbands == 1 ? 0 : (c.ncbands == 5 ? 1 : 2);
+    std::vector<double> bod(16), bab(16), bef(16);
+    for (int lay = 1; lay <= nlayers; ++lay) {
+      icldlyr[lay] = 0;
+      const double cf = c.cldfr_lay[lay];
+      for (int ib = 1; ib <= c.ncbands; ++ib) {
+        if (cf >= 1.e-6) {
+          bod[ib - 1] = secdiff[ib - 1] * c.TAUCL(lay, ib);
+          const double transcld = std::exp(-bod[ib - 1]);
+          bab[ib - 1] = 1.0 - transcld;
+          bef[ib - 1] = bab[ib - 1] * cf;
+          icldlyr[lay] = 1;
+        } else {
+          bod[ib - 1] = bab[ib - 1] = bef[ib - 1] = 0.0;
+          icldlyr[lay] = 0;
+        }
+      }
+      for (int ig = 1; ig <= NGPT; ++ig) {
+        const int ib = ipat[row][ngb[ig - 1] - 1];
+        L(odcld, lay, ig) = bod[ib - 1];
+        L(abscld, lay, ig) = bab[ib - 1];
+        L(efclfrac, lay, ig) = bef[ib - 1];
+        c.CF(c.cldfmc, ig, lay) = cf;
+      }
+    }
+  } else {
+    for (int lay = 1; lay <= nlayers; ++lay) {
+      icldlyr[lay] = 0;
+      for (int ig = 1; ig <= NGPT; ++ig) {
+        if (c.CF(c.cldfmc, ig, lay) == 1.0) {
+          int ib = ngb[ig - 1];
+          L(odcld, lay, ig) = secdiff[ib - 1] * c.CF(c.taucmc, ig, lay);
+          double transcld = std::exp(-L(odcld, lay, ig));
+          L(abscld, lay, ig) = 1.0 - transcld;
+          L(efclfrac, lay, ig) = L(abscld, lay, ig) * c.CF(c.cldfmc, ig, lay);
+          icldlyr[lay] = 1;
+        } else {
+          L(odcld, lay, ig) = 0.0;
+          L(abscld, lay, ig) = 0.0;
+          L(efclfrac, lay, ig) = 0.0;
+        }
       }
     }
   }
@@ -1364,6 +1405,12 @@ void rtrnmc(Col& c, int idrv) {
   c.htrc[nlayers] = 0.0;
 }
 
+}  // namespace
+extern "C" int ora_cldprop(int nlayers, int inflag, int iceflag, int liqflag, const double* cldfrac,
+                           const double* tauc, const double* ciwp, const double* clwp, const double* rei,
+                           const double* rel, int* ncbands_out, double* taucloud);
+namespace {
+
 // one column through inatm..rtrnmc (rrtmg_lw_rad.f90:486-570)
 struct Args {
   int ncol, nlay, icld, idrv;
@@ -1387,6 +1434,51 @@ int run_column(const Args& a, int iplon, Col& c) {
   for (int k = 1; k <= c.nlayers; ++k)
     for (int ig = 1; ig <= NGPT; ++ig) c.TAUT(k, ig) = c.TAUG(k, ig) + c.TAUA(k, ngb[ig - 1]);
   rtrnmc(c, a.idrv);
+  return 0;
+}
+
+// Band-level clouds of the non-McICA driver (rrtmg_lw_rad.nomcica.f90):
+// cldfr (ncol, nlay), taucld (16, ncol, nlay), cicewp, cliqwp, reice, reliq
+// (ncol, nlay).
+struct CloudsR {
+  const double *cldfr, *taucld, *cicewp, *cliqwp, *reice, *reliq;
+};
+
+// one column of the non-McICA driver with random overlap, icld = 1
+// (rrtmg_lw_rad.nomcica.f90:470-553: inatm, cldprop, setcoef, taumol, rtrn;
+// the state part of inatm is the McICA driver's, its cloud part :886-920
+// copies the band-level clouds below)
+int run_column_rtrn(const Args& a, const CloudsR& cl, int iplon, Col& c) {
+  const int iaer = 10;
+  inatm(iplon, a.ncol, a.nlay, 0, iaer, a.play, a.plev, a.tlay, a.tlev, a.tsfc, a.h2ovmr, a.o3vmr,
+        a.co2vmr, a.ch4vmr, a.n2ovmr, a.o2vmr, a.cfc11vmr, a.cfc12vmr, a.cfc22vmr, a.ccl4vmr, a.emis,
+        a.inflglw, a.iceflglw, a.liqflglw, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+        a.tauaer, c);
+  const int nl = c.nlayers;
+  std::vector<double> cf(nl), ci(nl), cw(nl), ri(nl), rl(nl), tc(16 * nl);
+  for (int l = 1; l <= nl; ++l) {
+    const size_t o = (iplon - 1) + (size_t)a.ncol * (l - 1);
+    cf[l - 1] = cl.cldfr[o];
+    ci[l - 1] = cl.cicewp[o];
+    cw[l - 1] = cl.cliqwp[o];
+    ri[l - 1] = cl.reice[o];
+    rl[l - 1] = cl.reliq[o];
+    for (int n = 1; n <= 16; ++n) tc[(n - 1) + 16 * (l - 1)] = cl.taucld[(n - 1) + 16 * o];
+  }
+  c.rtrn = 1;
+  c.cldfr_lay.assign(nl + 1, 0.0);
+  for (int l = 1; l <= nl; ++l) c.cldfr_lay[l] = cf[l - 1];
+  c.taucloud.assign((size_t)nl * 16, 0.0);
+  int err = ora_cldprop(nl, a.inflglw, a.iceflglw, a.liqflglw, cf.data(), tc.data(), ci.data(), cw.data(),
+                        ri.data(), rl.data(), &c.ncbands, c.taucloud.data());
+  if (err) return err;
+  err = setcoef(c, a.idrv);
+  if (err) return err;
+  taumol(c);
+  for (int k = 1; k <= c.nlayers; ++k)
+    for (int ig = 1; ig <= NGPT; ++ig) c.TAUT(k, ig) = c.TAUG(k, ig) + c.TAUA(k, ngb[ig - 1]);
+  rtrnmc(c, a.idrv);
+  c.rtrn = 0;
   return 0;
 }
 
@@ -1489,6 +1581,43 @@ int ora_rrtmg_lw(int ncol, int nlay, int* icld, int idrv, const double* play, co
   for (auto& t : th) t.join();
   for (int e : errs)
     if (e) return e;
+  return 0;
+}
+
+// rrtmg_lw of the non-McICA driver (rrtmg_lw_rad.nomcica.f90:99-560) for
+// icld = 1, random cloud overlap through rtrn; other icld values (rtrnmr)
+// are not restated here and return ERR_ICLD.
+int ora_rrtmg_lw_rtrn(int ncol, int nlay, int icld, int idrv, const double* play, const double* plev,
+                      const double* tlay, const double* tlev, const double* tsfc, const double* h2ovmr,
+                      const double* o3vmr, const double* co2vmr, const double* ch4vmr, const double* n2ovmr,
+                      const double* o2vmr, const double* cfc11vmr, const double* cfc12vmr,
+                      const double* cfc22vmr, const double* ccl4vmr, const double* emis, int inflglw,
+                      int iceflglw, int liqflglw, const double* cldfr, const double* taucld,
+                      const double* cicewp, const double* cliqwp, const double* reice, const double* reliq,
+                      const double* tauaer, double* uflx, double* dflx, double* hr, double* uflxc,
+                      double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt) {
+  if (!g_ready) return ERR_NOT_INIT;
+  if (ncol < 0 || nlay < 1) return ERR_ARGS;
+  if (icld != 1) return ERR_ICLD;
+  Args a{ncol, nlay, icld, idrv, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr,
+         n2ovmr, o2vmr, cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis, inflglw, iceflglw,
+         liqflglw, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, tauaer};
+  CloudsR cl{cldfr, taucld, cicewp, cliqwp, reice, reliq};
+  Col c;
+  for (int iplon = 1; iplon <= ncol; ++iplon) {
+    const int e = run_column_rtrn(a, cl, iplon, c);
+    if (e) return e;
+    for (int k = 0; k <= nlay; ++k) {
+      const size_t o = (iplon - 1) + (size_t)ncol * k;
+      uflx[o] = c.totuflux[k]; dflx[o] = c.totdflux[k];
+      uflxc[o] = c.totuclfl[k]; dflxc[o] = c.totdclfl[k];
+      if (idrv == 1) { duflx_dt[o] = c.dtotuflux_dt[k]; duflxc_dt[o] = c.dtotuclfl_dt[k]; }
+    }
+    for (int k = 0; k <= nlay - 1; ++k) {
+      const size_t o = (iplon - 1) + (size_t)ncol * k;
+      hr[o] = c.htr[k]; hrc[o] = c.htrc[k];
+    }
+  }
   return 0;
 }
 
