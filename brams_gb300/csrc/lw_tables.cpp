@@ -62,6 +62,18 @@ bool read_container(const char* path, std::map<std::string, Entry>& out, std::st
 
 }  // namespace
 
+bool gb_read_table_f64(const char* path, const char* name, std::vector<double>& out, std::string& err) {
+  std::map<std::string, Entry> tab;
+  if (!read_container(path, tab, err)) return false;
+  auto it = tab.find(name);
+  if (it == tab.end() || it->second.is_int) {
+    err = std::string("table file ") + path + " has no float64 array " + name;
+    return false;
+  }
+  out = it->second.d;
+  return true;
+}
+
 bool gb_build_tables(const char* ref_path, const char* k_path, double cpdair, GbTables& T,
                      std::vector<float>& blob, std::string& err, std::vector<double>* cloud64) {
   std::map<std::string, Entry> tab;

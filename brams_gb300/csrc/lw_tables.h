@@ -8,3 +8,6 @@
 // cloud64 (optional): the cloud optics tables in fp64, offsets in T.c64_*
 bool gb_build_tables(const char* ref_path, const char* k_path, double cpdair, GbTables& T,
                      std::vector<float>& blob, std::string& err, std::vector<double>* cloud64 = nullptr);
+
+// one float64 array of a table container (Fortran element order)
+bool gb_read_table_f64(const char* path, const char* name, std::vector<double>& out, std::string& err);

@@ -43,6 +43,7 @@ EXPORTS = [
     "gb_lw_mlp_prepare", "gb_lw_mlp_gradients", "gb_lw_mlp_train_step", "gb_lw_mlp_forward", "gb_lw_mlp_infer",
     "gb_rrtmg_lw_batch_surrogate", "gb_lw_mlp_set_engine", "gb_rrtmg_lw_autotune_report",
     "gb_cldprop_lw_device", "gb_rtm_pack_lw_device", "gb_rtm_unpack_lw_device",
+    "gb_rtm_ozone_load", "gb_rtm_ozone_free", "gb_rtm_ozone_lw",
 ]
 MLP_MMA_SYNC, MLP_TCGEN05 = 0, 1
 MLP_NPARAM = 72352
@@ -129,6 +130,9 @@ def load_library(path: str = LIB_PATH):
         L.gb_cldprop_lw_device.argtypes = [P, P, I, I, I, I, I] + [P] * 7 + [LL, P]
         L.gb_rtm_pack_lw_device.argtypes = [P, P] + [I] * 9 + [P] * 31 + [LL]
         L.gb_rtm_unpack_lw_device.argtypes = [P, P] + [I] * 7 + [P] * 3 + [LL, LL, P, P]
+        L.gb_rtm_ozone_load.argtypes = [C.c_char_p, C.POINTER(P)]
+        L.gb_rtm_ozone_free.argtypes = [P]
+        L.gb_rtm_ozone_lw.argtypes = [P, I, I, P, LL, P, I, P, LL]
         L.gb_mcica_subcol_lw_noalloc.argtypes = [P, I, I, I, I, IP] + [P] * 8 + [P] * 6 + [LL, I, P]
         GP = C.POINTER(GridDesc)
         L.gb_rrtmg_lw_batch_device.argtypes = [P, P, I, GP]
@@ -472,3 +476,40 @@ class Mlp:
         """gb_rrtmg_lw_batch_surrogate: all grids with learned gas optics."""
         n, arr = Context._grids(grids)
         self._ok(self.L.gb_rrtmg_lw_batch_surrogate(self.ctx.h, _ptr(stream or 0), n, arr, self.h))
+
+
+class Ozone:
+    """gb_rtm_ozone_*: BRAMS's zonal ozone climatology for packed columns, on
+    host arrays (no GPU needed)."""
+
+    def __init__(self, table_dir: str | None = None):
+        self.L = load_library()
+        h = C.c_void_p()
+        rc = self.L.gb_rtm_ozone_load((table_dir or DATA_DIR).encode(), C.byref(h))
+        if rc != 0:
+            raise RrtmgLwError(rc, self.L.gb_rrtmg_lw_strerror(rc).decode())
+        self.h = h
+
+    def o3vmr(self, plev: np.ndarray, glat: np.ndarray, doy: int) -> np.ndarray:
+        """plev (ncol, mzp) interface pressures, glat (ncol,) degrees ->
+        o3vmr (ncol, mzp - 1)."""
+        plev = np.asfortranarray(plev, dtype=np.float64)
+        glat = np.ascontiguousarray(glat, dtype=np.float32)
+        ncol, mzp = plev.shape
+        out = np.zeros((ncol, mzp - 1), order="F")
+        rc = self.L.gb_rtm_ozone_lw(self.h, ncol, mzp, plev.ctypes.data, ncol, glat.ctypes.data, int(doy),
+                                    out.ctypes.data, ncol)
+        if rc != 0:
+            raise RrtmgLwError(rc, self.L.gb_rrtmg_lw_strerror(rc).decode())
+        return out
+
+    def close(self) -> None:
+        if self.h:
+            self.L.gb_rtm_ozone_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -169,6 +169,20 @@ int gb_rtm_pack_lw_device(gb_lw_context* ctx, void* stream, int mzp, int mxp, in
                           double* cfc22vmr, double* ccl4vmr, double* emis, double* cldfrac, double* ciwp,
                           double* clwp, double* reic, double* relq, int64_t ld);
 
+/* BRAMS's zonal ozone climatology for the packed columns, on HOST arrays
+ * (rtm_driver.f90:1120-1173 with InitGetoz_rrtm :2062-2636 and getoz_rrtm
+ * :2638-2823): from each column's interface pressures plev (ld, mzp) (the
+ * rrtmg_lw plev, mzp = nlay + 1 levels), its grid latitude glat (degrees,
+ * BRAMS's float field) and the day of the year, o3vmr (ld_out, mzp - 1) in
+ * the driver's layer order, as the driver forms it without chemistry ozone.
+ * gb_rtm_ozone_load reads the climatology (brams_ozone.gblw) from
+ * table_dir. */
+typedef struct gb_rtm_ozone gb_rtm_ozone;
+int gb_rtm_ozone_load(const char* table_dir, gb_rtm_ozone** out);
+int gb_rtm_ozone_free(gb_rtm_ozone* oz);
+int gb_rtm_ozone_lw(const gb_rtm_ozone* oz, int ncol, int mzp, const double* plev, int64_t ld, const float* glat,
+                    int doy, double* o3vmr, int64_t ld_out);
+
 /* The driver's write-back (rtm_driver.f90:1443-1456) on DEVICE arrays:
  * fthrd(k, i, j) = (swhr + hr)(column, k-1) / 86400 for k = 2..mzp-1, copied
  * to k = 1 and k = mzp, and rlong(i, j) = dflx(column, 1), into BRAMS's float
