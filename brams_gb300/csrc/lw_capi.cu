@@ -30,7 +30,7 @@ struct gb_lw_graph {
   gb_lw_context* ctx = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  float4* scratch = nullptr;
+  float* gas = nullptr;      // taumol hand-over planes
   double* draws = nullptr;  // McICA draws of the fused-cloud grids
   long long* fall = nullptr;  // hand-over list of a batch with learned gas optics
   unsigned* nfall = nullptr;
@@ -137,28 +137,32 @@ cudaError_t copy2d(double* dst, size_t dpitch, const double* src, size_t spitch,
   return cudaMemcpy2DAsync(dst, dpitch * 8, src, spitch * 8, width * 8, rows, kind, s);
 }
 
-// scratch slots for the column kernel at this nlay (grown on demand)
-int ensure_scratch(gb_lw_context* ctx, int nlay) {
-  if (ctx->d_scratch[0] && ctx->scratch_nlay >= nlay) return 0;
-  int slots = gb_lw_slots(nlay);
-  size_t bytes = gb_lw_scratch_bytes(nlay, slots);
-  for (auto& p : ctx->d_scratch) {
-    cudaFree(p);
-    p = nullptr;
+// a taumol hand-over buffer of at least `bytes` (grown on demand)
+int ensure_buffer(gb_lw_context* ctx, float** buf, size_t* have, size_t bytes) {
+  if (*buf && *have >= bytes) return 0;
+  cudaFree(*buf);
+  *buf = nullptr;
+  *have = 0;
+  if (cudaMalloc(buf, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    *buf = nullptr;
+    ctx->last_error = "device allocation of the gas-optics hand-over planes failed";
+    return GB_LW_E_NOMEM;
   }
-  ctx->scratch_bytes = 0;
-  for (auto& p : ctx->d_scratch) {
-    if (cudaMalloc(&p, bytes) != cudaSuccess) {
-      cudaGetLastError();
-      ctx->last_error = "device allocation of the cell-coefficient scratch failed";
-      return GB_LW_E_NOMEM;
-    }
-  }
-  ctx->scratch_bytes = bytes;
-  ctx->scratch_slots = slots;
-  ctx->scratch_nlay = nlay;
+  *have = bytes;
   return 0;
 }
+
+// points a descriptor at a hand-over buffer of `bytes` (slots of nsmax layers)
+void attach_gas(LwBatch& b, float* buf, size_t bytes) {
+  b.gstride = (long long)b.nsmax * GB_NGPT;
+  b.gslots = (long long)(bytes / (2 * sizeof(float) * (size_t)b.gstride));
+  b.gtau = buf;
+  b.gfrac = buf + (size_t)b.gslots * b.gstride;
+}
+
+// hand-over bytes a batch of `ncols` columns at `nlay` layers is solved with
+size_t gas_need(int nlay, long long ncols) { return gb_lw_gas_bytes(nlay, gb_lw_gas_slots(nlay, ncols)); }
 
 bool flags_ok(int idrv, int inflglw, int iceflglw, int liqflglw) {
   return (idrv == 0 || idrv == 1) && inflglw >= 0 && inflglw <= 2 && iceflglw >= 0 && iceflglw <= 3 &&
@@ -175,15 +179,13 @@ int batch_kind(const LwBatch& b) {
   return k;
 }
 
-// Default shapes, measured on GB300 at 45 layers (108,000 columns): batches
-// that read the McICA sub-column arrays run best with four blocks per SM
-// (more L1 for the table gathers), fused-cloud batches with six.  Batches
-// with learned gas optics index the learned-only kernel's shapes (its
-// variant 0: 160 threads, six blocks per SM).
+// Default shape: variant 0 at as many resident blocks as fit.  Batches with
+// learned gas optics index the shapes of the transfer kernel on the
+// network's outputs.
 gb_lw_tuning default_tuning(gb_lw_context* ctx, int nlay, int kind) {
   gb_lw_tuning t{};
   const bool lean = kind & GB_LW_KIND_LEARNED;
-  t.variant = lean ? 0 : (kind & GB_LW_KIND_FUSED) ? 1 : 2;
+  t.variant = 0;
   t.threads = gb_lw_variant(t.variant, lean).threads;
   t.min_blocks = gb_lw_variant(t.variant, lean).min_blocks;
   const int occ = std::max(1, gb_lw_slots(nlay, t.variant, lean) / std::max(1, ctx->num_sms));
@@ -211,34 +213,22 @@ void store_tuning(gb_lw_context* ctx, int nlay, int kind, const gb_lw_tuning& t)
   ctx->tuned.push_back(t);
 }
 
-// One grid through the launch shape tuned (or defaulted) for its layer count and kind,
-// at most nslots persistent blocks (the scratch the caller provides).
-cudaError_t launch_one(gb_lw_context* ctx, const LwArgs& a, float4* scratch, int nslots, cudaStream_t stream) {
-  if (a.ncol <= 0) return cudaSuccess;
+// One grid through the launch shape tuned (or defaulted) for its layer count
+// and kind, with the hand-over buffer `k` of the context (grown on demand).
+int launch_one(gb_lw_context* ctx, const LwArgs& a, int k, cudaStream_t stream) {
+  if (a.ncol <= 0) return GB_LW_OK;
   LwBatch b;
   b.ngrid = 1;
   b.nsmax = a.nlay;
   b.col0[0] = 0;
   b.col0[1] = a.ncol;
-  b.scratch = scratch;
   b.g[0] = a;
+  int rc = ensure_buffer(ctx, &ctx->d_gas[k], &ctx->gas_bytes[k], gas_need(a.nlay, a.ncol));
+  if (rc) return rc;
+  attach_gas(b, ctx->d_gas[k], ctx->gas_bytes[k]);
   const gb_lw_tuning t = tuning_for(ctx, a.nlay, batch_kind(b));
-  return gb_lw_launch_batch(b, ctx->d_tables, t.variant, std::min(t.blocks, nslots), stream);
-}
-
-int ensure_bscratch(gb_lw_context* ctx, int nlay, int blocks) {
-  size_t bytes = gb_lw_scratch_bytes(nlay, blocks);
-  if (bytes <= ctx->bscratch_bytes) return 0;
-  cudaFree(ctx->d_bscratch);
-  ctx->d_bscratch = nullptr;
-  ctx->bscratch_bytes = 0;
-  if (cudaMalloc(&ctx->d_bscratch, bytes) != cudaSuccess) {
-    cudaGetLastError();
-    ctx->last_error = "device allocation of the batch scratch failed";
-    return GB_LW_E_NOMEM;
-  }
-  ctx->bscratch_bytes = bytes;
-  return 0;
+  cudaError_t e = gb_lw_launch_batch(b, ctx->d_tables, t.variant, t.blocks, stream);
+  return e == cudaSuccess ? GB_LW_OK : gb_ctx_fail(ctx, e, "column kernels");
 }
 
 // A batch with learned gas optics gets the context's hand-over list (room
@@ -333,6 +323,14 @@ int gb_ctx_make_batch(gb_lw_context* ctx, int ngrid, const gb_lw_grid* grids, do
   return 0;
 }
 
+// hand-over planes for a descriptor's columns from the context's batch buffer
+static int attach_batch_gas(gb_lw_context* ctx, LwBatch& b) {
+  int rc = ensure_buffer(ctx, &ctx->d_bgas, &ctx->bgas_bytes, gas_need(b.nsmax, b.col0[b.ngrid]));
+  if (rc) return rc;
+  attach_gas(b, ctx->d_bgas, ctx->bgas_bytes);
+  return 0;
+}
+
 
 size_t gb_ctx_fused_draws(const LwBatch& b) {
   size_t n = 0;
@@ -358,7 +356,7 @@ int gb_ctx_launch_batch(gb_lw_context* ctx, LwBatch& b, cudaStream_t stream) {
   if (b.col0[b.ngrid] == 0) return GB_LW_OK;
   cudaSetDevice(ctx->device);
   const gb_lw_tuning t = tuning_for(ctx, b.nsmax, batch_kind(b));
-  int rc = ensure_bscratch(ctx, b.nsmax, t.blocks);
+  int rc = attach_batch_gas(ctx, b);
   if (rc) return rc;
   const size_t nd = gb_ctx_fused_draws(b);
   if (nd > ctx->fdraws_elems) {
@@ -376,7 +374,6 @@ int gb_ctx_launch_batch(gb_lw_context* ctx, LwBatch& b, cudaStream_t stream) {
     rc = gb_ctx_make_draws(ctx, b, ctx->d_fdraws, stream);
     if (rc) return rc;
   }
-  b.scratch = ctx->d_bscratch;
   if ((rc = attach_fall(ctx, b)) != 0) return rc;
   cudaError_t e = gb_lw_launch_batch(b, ctx->d_tables, t.variant, t.blocks, stream);
   if (e != cudaSuccess) return gb_ctx_fail(ctx, e, "batched launch");
@@ -445,8 +442,8 @@ int gb_rrtmg_lw_free(gb_lw_context* ctx) {
   cudaFree(ctx->d_tables);
   cudaFree(ctx->d_err);
   cudaFree(ctx->d_draws);
-  for (auto& p : ctx->d_scratch) cudaFree(p);
-  cudaFree(ctx->d_bscratch);
+  for (auto& p : ctx->d_gas) cudaFree(p);
+  cudaFree(ctx->d_bgas);
   cudaFree(ctx->d_sur);
   cudaFree(ctx->d_sur_flag);
   cudaFree(ctx->d_fdraws);
@@ -503,10 +500,7 @@ int gb_rrtmg_lw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int
   a.col_err = d_col_status;
   a.err_flag = ctx->d_err;
   cudaSetDevice(ctx->device);
-  int rs = ensure_scratch(ctx, nlay);
-  if (rs) return rs;
-  CK(launch_one(ctx, a, ctx->d_scratch[0], ctx->scratch_slots, (cudaStream_t)stream));
-  return GB_LW_OK;
+  return launch_one(ctx, a, 0, (cudaStream_t)stream);
 }
 
 int gb_rrtmg_lw_sync_status(gb_lw_context* ctx, void* stream) {
@@ -543,8 +537,6 @@ int gb_rrtmg_lw(gb_lw_context* ctx, int ncol, int nlay, int* icld, int idrv, con
   const size_t per_col = (size_t)(600 * nlay + 64) * 8;
   int C = (int)std::max<size_t>(1, std::min<size_t>((size_t)ncol, (size_t)(2ull << 30) / per_col));
   int rc = ensure_chunks(ctx, C, nlay);
-  if (rc) return rc;
-  rc = ensure_scratch(ctx, nlay);
   if (rc) return rc;
   const InLayout li = in_layout(C, nlay);
   const OutLayout lo = out_layout(C, nlay);
@@ -601,7 +593,8 @@ int gb_rrtmg_lw(gb_lw_context* ctx, int ncol, int nlay, int* icld, int idrv, con
     a.duflx_dt = O + lo.duflx; a.duflxc_dt = O + lo.duflxc; a.hr = O + lo.hr; a.hrc = O + lo.hrc;
     a.col_err = nullptr;
     a.err_flag = ctx->d_err_host;
-    CK(launch_one(ctx, a, ctx->d_scratch[k & 1], ctx->scratch_slots, s));
+    rc = launch_one(ctx, a, k & 1, s);
+    if (rc) return rc;
     auto D2H = [&](double* dst, size_t soff, size_t rows) {
       return copy2d(dst + c0, (size_t)ld_out, O + soff, P, nc, rows, cudaMemcpyDeviceToHost, s);
     };
@@ -746,53 +739,58 @@ int gb_rrtmg_lw_gas_optics_diag(gb_lw_context* ctx, int ncol, int nlay, const do
                                 const double* cfc12vmr, const double* cfc22vmr, const double* ccl4vmr,
                                 const double* emis, const double* tauaer, float* taut, float* fracs) {
   if (!ctx || ncol <= 0 || nlay < 1 || nlay > GB_MAXLAY || !taut || !fracs) return GB_LW_E_ARGS;
+  (void)tlev;
+  (void)tsfc;
+  (void)emis;
   cudaSetDevice(ctx->device);
   const size_t n2 = (size_t)ncol * nlay, n3 = (size_t)ncol * (nlay + 1);
   const double* src2[] = {play, tlay, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr, cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr};
-  size_t total = 12 * n2 + 2 * n3 + ncol + 16 * (size_t)ncol + 16 * n2 + 6 * n3 + 2 * n2;
   double* d = nullptr;
   float* dt = nullptr;
-  if (cudaMalloc(&d, total * 8) != cudaSuccess || cudaMalloc(&dt, 2 * n2 * GB_NGPT * 4) != cudaSuccess) {
+  if (cudaMalloc(&d, (12 * n2 + n3) * 8) != cudaSuccess || cudaMalloc(&dt, 2 * n2 * GB_NGPT * 4) != cudaSuccess) {
     cudaFree(d);
     cudaGetLastError();
     return GB_LW_E_NOMEM;
   }
-  double* p = d;
   double* dev2[12];
   for (int k = 0; k < 12; ++k) {
-    dev2[k] = p;
-    cudaMemcpy(p, src2[k], n2 * 8, cudaMemcpyHostToDevice);
-    p += n2;
+    dev2[k] = d + k * n2;
+    cudaMemcpy(dev2[k], src2[k], n2 * 8, cudaMemcpyHostToDevice);
   }
-  double* dplev = p; cudaMemcpy(p, plev, n3 * 8, cudaMemcpyHostToDevice); p += n3;
-  double* dtlev = p; cudaMemcpy(p, tlev, n3 * 8, cudaMemcpyHostToDevice); p += n3;
-  double* dtsfc = p; cudaMemcpy(p, tsfc, ncol * 8, cudaMemcpyHostToDevice); p += ncol;
-  double* demis = p; cudaMemcpy(p, emis, 16 * (size_t)ncol * 8, cudaMemcpyHostToDevice); p += 16 * (size_t)ncol;
-  double* dtau = p; cudaMemcpy(p, tauaer, 16 * n2 * 8, cudaMemcpyHostToDevice); p += 16 * n2;
-  double* o = p;
-  LwArgs a{};
+  double* dplev = d + 12 * n2;
+  cudaMemcpy(dplev, plev, n3 * 8, cudaMemcpyHostToDevice);
+  LwBatch b;
+  b.ngrid = 1;
+  b.nsmax = nlay;
+  b.col0[0] = 0;
+  b.col0[1] = ncol;
+  LwArgs& a = b.g[0];
+  a = LwArgs{};
   a.ncol = ncol; a.nlay = nlay; a.ld = ncol; a.ldo = ncol;
-  a.icld = 0; a.idrv = 1; a.inflag = 2; a.iceflag = 3; a.liqflag = 1;
   a.play = dev2[0]; a.tlay = dev2[1]; a.h2ovmr = dev2[2]; a.o3vmr = dev2[3]; a.co2vmr = dev2[4];
   a.ch4vmr = dev2[5]; a.n2ovmr = dev2[6]; a.o2vmr = dev2[7]; a.cfc11vmr = dev2[8]; a.cfc12vmr = dev2[9];
-  a.cfc22vmr = dev2[10]; a.ccl4vmr = dev2[11];
-  a.plev = dplev; a.tlev = dtlev; a.tsfc = dtsfc; a.emis = demis; a.tauaer = dtau;
-  a.uflx = o; a.dflx = o + n3; a.uflxc = o + 2 * n3; a.dflxc = o + 3 * n3; a.duflx_dt = o + 4 * n3;
-  a.duflxc_dt = o + 5 * n3; a.hr = o + 6 * n3; a.hrc = o + 6 * n3 + n2;
+  a.cfc22vmr = dev2[10]; a.ccl4vmr = dev2[11]; a.plev = dplev;
   a.err_flag = ctx->d_err_host;
-  a.dbg_taut = dt;
-  a.dbg_fracs = dt + n2 * GB_NGPT;
-  int rc = ensure_scratch(ctx, nlay);
-  if (rc) {
-    cudaFree(d);
-    cudaFree(dt);
-    return rc;
-  }
-  cudaError_t e = launch_one(ctx, a, ctx->d_scratch[0], ctx->scratch_slots, 0);
+  // the taumol kernel writes column i, layer l at row i * nlay + l
+  b.gstride = (long long)nlay * GB_NGPT;
+  b.gslots = ncol;
+  b.gtau = dt;
+  b.gfrac = dt + n2 * GB_NGPT;
+  int rc = GB_LW_OK;
+  cudaError_t e = gb_lw_launch_gas(b, ctx->d_tables, 0, ncol, 0);
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   if (e == cudaSuccess) e = cudaMemcpy(taut, dt, n2 * GB_NGPT * 4, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(fracs, dt + n2 * GB_NGPT, n2 * GB_NGPT * 4, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) rc = cuda_fail(ctx, e, "gas optics diagnostics");
+  if (rc == GB_LW_OK) {
+    // taut = taug + the aerosol optical depth of the g-point's band (rrtmg_lw_rad.f90:548-553), in fp32
+    for (int i = 0; i < ncol; ++i)
+      for (int l = 0; l < nlay; ++l)
+        for (int g = 0; g < GB_NGPT; ++g) {
+          const int ib = ctx->tabs.ngb[g] - 1;
+          taut[((size_t)i * nlay + l) * GB_NGPT + g] += (float)tauaer[i + (size_t)ncol * (l + (size_t)nlay * ib)];
+        }
+  }
   cudaFree(d);
   cudaFree(dt);
   return rc;
@@ -864,9 +862,8 @@ int gb_rrtmg_lw_autotune(gb_lw_context* ctx, void* stream, int ngrid, const gb_l
     }
   }
   if (cands.empty()) return GB_LW_E_ARGS;
-  rc = ensure_bscratch(ctx, b.nsmax, max_blocks);
-  if (rc) return rc;
-  b.scratch = ctx->d_bscratch;
+  (void)max_blocks;
+  if ((rc = attach_batch_gas(ctx, b)) != 0) return rc;
   if ((rc = attach_fall(ctx, b)) != 0) return rc;
   // the fused-cloud draws are made once: every candidate times the column kernel alone
   const size_t nd = gb_ctx_fused_draws(b);
@@ -942,12 +939,13 @@ int gb_rrtmg_lw_batch_graph_create(gb_lw_context* ctx, int ngrid, const gb_lw_gr
   const gb_lw_tuning t = tuning_for(ctx, b.nsmax, batch_kind(b));
   gb_lw_graph* g = new gb_lw_graph();
   g->ctx = ctx;
-  if (cudaMalloc(&g->scratch, gb_lw_scratch_bytes(b.nsmax, t.blocks)) != cudaSuccess) {
+  const size_t gbytes = gas_need(b.nsmax, b.col0[ngrid]);
+  if (cudaMalloc(&g->gas, gbytes) != cudaSuccess) {
     cudaGetLastError();
     delete g;
     return GB_LW_E_NOMEM;
   }
-  b.scratch = g->scratch;
+  attach_gas(b, g->gas, gbytes);
   const size_t nd = gb_ctx_fused_draws(b);
   if (nd && cudaMalloc(&g->draws, nd * sizeof(double)) != cudaSuccess) {
     cudaGetLastError();
@@ -995,7 +993,7 @@ int gb_rrtmg_lw_graph_destroy(gb_lw_graph* g) {
   cudaSetDevice(g->ctx->device);
   if (g->exec) cudaGraphExecDestroy(g->exec);
   if (g->graph) cudaGraphDestroy(g->graph);
-  cudaFree(g->scratch);
+  cudaFree(g->gas);
   cudaFree(g->draws);
   cudaFree(g->fall);
   cudaFree(g->nfall);

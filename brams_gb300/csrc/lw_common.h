@@ -40,6 +40,12 @@ struct GbTables {
   // 0 h2o/co2, 1 h2o/o3, 2 h2o/n2o, 3 h2o/ch4, 4 n2o/co2, 5 o3/co2
   float rat[6][59];
   float delwave[GB_NBND];
+  // the same reference-atmosphere values in the float blob, for lookups whose
+  // index differs from thread to thread: preflog[59], tref[59], chi[7][59], rat[6][59]
+  int ref_preflog, ref_tref, ref_chi, ref_rat;
+  // rtrnmc's lookup tables (rrtmg_lw_init.f90:120-142) in the float blob:
+  // tbl_tt (exp_tbl, tfn_tbl) pairs [10001] (8-byte aligned), tbl_tau [10001]
+  int tbl_tt, tbl_tau;
   int ngb[GB_NGPT];
   int nspa[GB_NBND], nspb[GB_NBND];
   double heatfac, fluxfac, grav, avogad;

@@ -28,14 +28,14 @@ struct gb_lw_context {
   int chunk_cols = 0, chunk_nlay = 0;
   double* d_draws = nullptr;
   size_t draws_elems = 0;
-  float4* d_scratch[2] = {nullptr, nullptr};  // cell-coefficient slots (one set per chunk stream)
-  size_t scratch_bytes = 0;
-  int scratch_slots = 0, scratch_nlay = 0;
+  // taumol hand-over planes of the single-grid calls (one buffer per chunk stream)
+  float* d_gas[2] = {nullptr, nullptr};
+  size_t gas_bytes[2] = {0, 0};
   std::string last_error;
   size_t max_smem = 0;
   int num_sms = 0;
-  float4* d_bscratch = nullptr;  // scratch of batched launches
-  size_t bscratch_bytes = 0;
+  float* d_bgas = nullptr;  // taumol hand-over planes of batched launches
+  size_t bgas_bytes = 0;
   std::vector<gb_lw_tuning> tuned;  // autotuned shapes, parallel to tuned_nlay (largest nlay of the batch)
   std::vector<int> tuned_nlay;
   std::vector<gb_lw_tuning> last_tune;  // every candidate of the last autotune call

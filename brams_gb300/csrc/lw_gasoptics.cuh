@@ -59,6 +59,7 @@ struct Cell {
   const float* f;  // [NF][nl] shared memory
   const int* iv;   // [NI][nl] shared memory
   int nl, lay;
+  const float* T;  // device table blob
   __device__ __forceinline__ float F(int k) const { return f[k * nl + lay]; }
   __device__ __forceinline__ int I(int k) const { return iv[k * nl + lay]; }
 };
@@ -90,8 +91,11 @@ struct Terms {
   }
 };
 
-__device__ __forceinline__ float chi(int m, int jp) { return c_T.chi[m - 1][jp - 1]; }
-__device__ __forceinline__ float rat(int k, int jp) { return c_T.rat[k][jp - 1]; }
+// chi_mls and its ratios at reference level jp: a per-layer index, so they are
+// read from the table blob (global memory) rather than the constant bank,
+// which serialises loads whose address differs between threads
+__device__ __forceinline__ float chi(const Cell& c, int m, int jp) { return __ldg(c.T + c_T.ref_chi + (m - 1) * 59 + jp - 1); }
+__device__ __forceinline__ float rat(const Cell& c, int k, int jp) { return __ldg(c.T + c_T.ref_rat + k * 59 + jp - 1); }
 
 struct Spec {
   float comb, parm, f;
@@ -218,7 +222,7 @@ __device__ __forceinline__ float adj_col(float col, float coldry, float chiref, 
   return col;
 }
 __device__ __forceinline__ float adj_n2o(const Cell& c) {
-  return adj_col(c.F(F_COLN2O), c.F(F_COLDRY), chi(4, clampi(c.I(I_JP), 1, 58) + 1), 1.5f, 0.5f, 0.65f);
+  return adj_col(c.F(F_COLN2O), c.F(F_COLDRY), chi(c, 4, clampi(c.I(I_JP), 1, 58) + 1), 1.5f, 0.5f, 0.65f);
 }
 
 // -------------------------------------------------------------------------
@@ -277,17 +281,17 @@ __device__ FracRec prologue<3>(const Cell& c, bool lower, Terms& t) {
   float h2o = c.F(F_COLH2O), co2 = c.F(F_COLCO2);
   float adjcoln2o = adj_n2o(c);
   if (lower) {
-    Spec s = spec(h2o, rat(0, jp), co2, 8.0f, 9), s1 = spec(h2o, rat(0, jp + 1), co2, 8.0f, 9);
-    Spec sm = spec(h2o, chi(1, 3) / chi(2, 3), co2, 8.0f, 9);
-    Spec sp = spec(h2o, chi(1, 9) / chi(2, 9), co2, 8.0f, 9);
+    Spec s = spec(h2o, rat(c, 0, jp), co2, 8.0f, 9), s1 = spec(h2o, rat(c, 0, jp + 1), co2, 8.0f, 9);
+    Spec sm = spec(h2o, chi(c, 1, 3) / chi(c, 2, 3), co2, 8.0f, 9);
+    Spec sp = spec(h2o, chi(c, 1, 9) / chi(c, 2, 9), co2, 8.0f, 9);
     binary_lower_terms(t, c, s, s1, BT.ka, NGB);
     self_terms(t, c, BT.sr, NGB);
     for_terms(t, c, BT.fo, NGB);
     minor_et_terms(t, c, adjcoln2o, BT.ma0, 9, NGB, sm.j, sm.f);
     return {BT.fa + (sp.j - 1) * NGB, sp.f};
   }
-  Spec s = spec(h2o, rat(0, jp), co2, 4.0f, 5), s1 = spec(h2o, rat(0, jp + 1), co2, 4.0f, 5);
-  Spec sm = spec(h2o, chi(1, 13) / chi(2, 13), co2, 4.0f, 5);
+  Spec s = spec(h2o, rat(c, 0, jp), co2, 4.0f, 5), s1 = spec(h2o, rat(c, 0, jp + 1), co2, 4.0f, 5);
+  Spec sm = spec(h2o, chi(c, 1, 13) / chi(c, 2, 13), co2, 4.0f, 5);
   binary_upper_terms(t, c, s, s1, BT.kb, NGB);
   for_terms(t, c, BT.fo, NGB);
   minor_et_terms(t, c, adjcoln2o, BT.mb0, 5, NGB, sm.j, sm.f);
@@ -301,16 +305,16 @@ __device__ FracRec prologue<4>(const Cell& c, bool lower, Terms& t) {
   int jp = clampi(c.I(I_JP), 1, 58);
   if (lower) {
     float h2o = c.F(F_COLH2O), co2 = c.F(F_COLCO2);
-    Spec s = spec(h2o, rat(0, jp), co2, 8.0f, 9), s1 = spec(h2o, rat(0, jp + 1), co2, 8.0f, 9);
-    Spec sp = spec(h2o, chi(1, 11) / chi(2, 11), co2, 8.0f, 9);
+    Spec s = spec(h2o, rat(c, 0, jp), co2, 8.0f, 9), s1 = spec(h2o, rat(c, 0, jp + 1), co2, 8.0f, 9);
+    Spec sp = spec(h2o, chi(c, 1, 11) / chi(c, 2, 11), co2, 8.0f, 9);
     binary_lower_terms(t, c, s, s1, BT.ka, NGB);
     self_terms(t, c, BT.sr, NGB);
     for_terms(t, c, BT.fo, NGB);
     return {BT.fa + (sp.j - 1) * NGB, sp.f};
   }
   float o3 = c.F(F_COLO3), co2 = c.F(F_COLCO2);
-  Spec s = spec(o3, rat(5, jp), co2, 4.0f, 5), s1 = spec(o3, rat(5, jp + 1), co2, 4.0f, 5);
-  Spec sp = spec(o3, chi(3, 13) / chi(2, 13), co2, 4.0f, 5);
+  Spec s = spec(o3, rat(c, 5, jp), co2, 4.0f, 5), s1 = spec(o3, rat(c, 5, jp + 1), co2, 4.0f, 5);
+  Spec sp = spec(o3, chi(c, 3, 13) / chi(c, 2, 13), co2, 4.0f, 5);
   binary_upper_terms(t, c, s, s1, BT.kb, NGB);
   return {BT.fb + (clampi(sp.j, 1, 4) - 1) * NGB, sp.f};
 }
@@ -322,9 +326,9 @@ __device__ FracRec prologue<5>(const Cell& c, bool lower, Terms& t) {
   int jp = clampi(c.I(I_JP), 1, 58);
   if (lower) {
     float h2o = c.F(F_COLH2O), co2 = c.F(F_COLCO2);
-    Spec s = spec(h2o, rat(0, jp), co2, 8.0f, 9), s1 = spec(h2o, rat(0, jp + 1), co2, 8.0f, 9);
-    Spec sm = spec(h2o, chi(1, 7) / chi(2, 7), co2, 8.0f, 9);
-    Spec sp = spec(h2o, chi(1, 5) / chi(2, 5), co2, 8.0f, 9);
+    Spec s = spec(h2o, rat(c, 0, jp), co2, 8.0f, 9), s1 = spec(h2o, rat(c, 0, jp + 1), co2, 8.0f, 9);
+    Spec sm = spec(h2o, chi(c, 1, 7) / chi(c, 2, 7), co2, 8.0f, 9);
+    Spec sp = spec(h2o, chi(c, 1, 5) / chi(c, 2, 5), co2, 8.0f, 9);
     binary_lower_terms(t, c, s, s1, BT.ka, NGB);
     self_terms(t, c, BT.sr, NGB);
     for_terms(t, c, BT.fo, NGB);
@@ -333,8 +337,8 @@ __device__ FracRec prologue<5>(const Cell& c, bool lower, Terms& t) {
     return {BT.fa + (sp.j - 1) * NGB, sp.f};
   }
   float o3 = c.F(F_COLO3), co2 = c.F(F_COLCO2);
-  Spec s = spec(o3, rat(5, jp), co2, 4.0f, 5), s1 = spec(o3, rat(5, jp + 1), co2, 4.0f, 5);
-  Spec sp = spec(o3, chi(3, 43) / chi(2, 43), co2, 4.0f, 5);
+  Spec s = spec(o3, rat(c, 5, jp), co2, 4.0f, 5), s1 = spec(o3, rat(c, 5, jp + 1), co2, 4.0f, 5);
+  Spec sp = spec(o3, chi(c, 3, 43) / chi(c, 2, 43), co2, 4.0f, 5);
   binary_upper_terms(t, c, s, s1, BT.kb, NGB);
   t.add(c.F(F_WX1), BT.x0);
   return {BT.fb + (clampi(sp.j, 1, 4) - 1) * NGB, sp.f};
@@ -346,7 +350,7 @@ __device__ FracRec prologue<6>(const Cell& c, bool lower, Terms& t) {
   constexpr int b = 6;
   if (lower) {
     int jp = clampi(c.I(I_JP), 1, 58);
-    float adjcolco2 = adj_col(c.F(F_COLCO2), c.F(F_COLDRY), chi(2, jp + 1), 3.0f, 2.0f, 0.77f);
+    float adjcolco2 = adj_col(c.F(F_COLCO2), c.F(F_COLDRY), chi(c, 2, jp + 1), 3.0f, 2.0f, 0.77f);
     single_lower_terms(t, c, c.F(F_COLH2O), BT.ka, NGB);
     self_terms(t, c, BT.sr, NGB);
     for_terms(t, c, BT.fo, NGB);
@@ -364,18 +368,18 @@ __device__ FracRec prologue<7>(const Cell& c, bool lower, Terms& t) {
   int jp = clampi(c.I(I_JP), 1, 58);
   if (lower) {
     float h2o = c.F(F_COLH2O), o3 = c.F(F_COLO3);
-    Spec s = spec(h2o, rat(1, jp), o3, 8.0f, 9), s1 = spec(h2o, rat(1, jp + 1), o3, 8.0f, 9);
-    Spec sm = spec(h2o, chi(1, 3) / chi(3, 3), o3, 8.0f, 9);  // minor and planck use the same ratio
-    float adjcolco2 = adj_col(c.F(F_COLCO2), c.F(F_COLDRY), chi(2, jp + 1), 3.0f, 3.0f, 0.79f);
+    Spec s = spec(h2o, rat(c, 1, jp), o3, 8.0f, 9), s1 = spec(h2o, rat(c, 1, jp + 1), o3, 8.0f, 9);
+    Spec sm = spec(h2o, chi(c, 1, 3) / chi(c, 3, 3), o3, 8.0f, 9);  // minor and planck use the same ratio
+    float adjcolco2 = adj_col(c.F(F_COLCO2), c.F(F_COLDRY), chi(c, 2, jp + 1), 3.0f, 3.0f, 0.79f);
     binary_lower_terms(t, c, s, s1, BT.ka, NGB);
     self_terms(t, c, BT.sr, NGB);
     for_terms(t, c, BT.fo, NGB);
     minor_et_terms(t, c, adjcolco2, BT.ma0, 9, NGB, sm.j, sm.f);
     return {BT.fa + (sm.j - 1) * NGB, sm.f};
   }
-  float ratio = 1.e20f * __fdividef(__fdividef(c.F(F_COLCO2), c.F(F_COLDRY)), chi(2, jp + 1));
+  float ratio = 1.e20f * __fdividef(__fdividef(c.F(F_COLCO2), c.F(F_COLDRY)), chi(c, 2, jp + 1));
   float adjcolco2 = c.F(F_COLCO2);
-  if (ratio > 3.0f) adjcolco2 = (2.0f + powf(ratio - 2.0f, 0.79f)) * chi(2, jp + 1) * c.F(F_COLDRY) * 1.e-20f;
+  if (ratio > 3.0f) adjcolco2 = (2.0f + powf(ratio - 2.0f, 0.79f)) * chi(c, 2, jp + 1) * c.F(F_COLDRY) * 1.e-20f;
   single_upper_terms(t, c, c.F(F_COLO3), BT.kb, 1, NGB);
   minor_t_terms(t, c, adjcolco2, BT.mb0, NGB);
   return {BT.fb, 0.0f};
@@ -386,7 +390,7 @@ template <>
 __device__ FracRec prologue<8>(const Cell& c, bool lower, Terms& t) {
   constexpr int b = 8;
   int jp = clampi(c.I(I_JP), 1, 58);
-  float adjcolco2 = adj_col(c.F(F_COLCO2), c.F(F_COLDRY), chi(2, jp + 1), 3.0f, 2.0f, 0.65f);
+  float adjcolco2 = adj_col(c.F(F_COLCO2), c.F(F_COLDRY), chi(c, 2, jp + 1), 3.0f, 2.0f, 0.65f);
   if (lower) {
     single_lower_terms(t, c, c.F(F_COLH2O), BT.ka, NGB);
     self_terms(t, c, BT.sr, NGB);
@@ -412,9 +416,9 @@ __device__ FracRec prologue<9>(const Cell& c, bool lower, Terms& t) {
   float adjcoln2o = adj_n2o(c);
   if (lower) {
     float h2o = c.F(F_COLH2O), ch4 = c.F(F_COLCH4);
-    Spec s = spec(h2o, rat(3, jp), ch4, 8.0f, 9), s1 = spec(h2o, rat(3, jp + 1), ch4, 8.0f, 9);
-    Spec sm = spec(h2o, chi(1, 3) / chi(6, 3), ch4, 8.0f, 9);
-    Spec sp = spec(h2o, chi(1, 9) / chi(6, 9), ch4, 8.0f, 9);
+    Spec s = spec(h2o, rat(c, 3, jp), ch4, 8.0f, 9), s1 = spec(h2o, rat(c, 3, jp + 1), ch4, 8.0f, 9);
+    Spec sm = spec(h2o, chi(c, 1, 3) / chi(c, 6, 3), ch4, 8.0f, 9);
+    Spec sp = spec(h2o, chi(c, 1, 9) / chi(c, 6, 9), ch4, 8.0f, 9);
     binary_lower_terms(t, c, s, s1, BT.ka, NGB);
     self_terms(t, c, BT.sr, NGB);
     for_terms(t, c, BT.fo, NGB);
@@ -466,8 +470,8 @@ __device__ FracRec prologue<12>(const Cell& c, bool lower, Terms& t) {
   if (!lower) return {c_T.zero_row, 0.0f};
   int jp = clampi(c.I(I_JP), 1, 58);
   float h2o = c.F(F_COLH2O), co2 = c.F(F_COLCO2);
-  Spec s = spec(h2o, rat(0, jp), co2, 8.0f, 9), s1 = spec(h2o, rat(0, jp + 1), co2, 8.0f, 9);
-  Spec sp = spec(h2o, chi(1, 10) / chi(2, 10), co2, 8.0f, 9);
+  Spec s = spec(h2o, rat(c, 0, jp), co2, 8.0f, 9), s1 = spec(h2o, rat(c, 0, jp + 1), co2, 8.0f, 9);
+  Spec sp = spec(h2o, chi(c, 1, 10) / chi(c, 2, 10), co2, 8.0f, 9);
   binary_lower_terms(t, c, s, s1, BT.ka, NGB);
   self_terms(t, c, BT.sr, NGB);
   for_terms(t, c, BT.fo, NGB);
@@ -484,10 +488,10 @@ __device__ FracRec prologue<13>(const Cell& c, bool lower, Terms& t) {
   }
   int jp = clampi(c.I(I_JP), 1, 58);
   float h2o = c.F(F_COLH2O), n2o = c.F(F_COLN2O);
-  Spec s = spec(h2o, rat(2, jp), n2o, 8.0f, 9), s1 = spec(h2o, rat(2, jp + 1), n2o, 8.0f, 9);
-  Spec sm = spec(h2o, chi(1, 1) / chi(4, 1), n2o, 8.0f, 9);
-  Spec sm3 = spec(h2o, chi(1, 3) / chi(4, 3), n2o, 8.0f, 9);
-  Spec sp = spec(h2o, chi(1, 5) / chi(4, 5), n2o, 8.0f, 9);
+  Spec s = spec(h2o, rat(c, 2, jp), n2o, 8.0f, 9), s1 = spec(h2o, rat(c, 2, jp + 1), n2o, 8.0f, 9);
+  Spec sm = spec(h2o, chi(c, 1, 1) / chi(c, 4, 1), n2o, 8.0f, 9);
+  Spec sm3 = spec(h2o, chi(c, 1, 3) / chi(c, 4, 3), n2o, 8.0f, 9);
+  Spec sp = spec(h2o, chi(c, 1, 5) / chi(c, 4, 5), n2o, 8.0f, 9);
   // CO2 adjustment against the fixed 3.55e-4 reference (taumol.f90:2532-2540)
   float co2 = c.F(F_COLCO2), coldry = c.F(F_COLDRY);
   float ratio = 1.e20f * __fdividef(__fdividef(co2, coldry), 3.55e-4f);
@@ -522,8 +526,8 @@ __device__ FracRec prologue<15>(const Cell& c, bool lower, Terms& t) {
   if (!lower) return {c_T.zero_row, 0.0f};
   int jp = clampi(c.I(I_JP), 1, 58);
   float n2o = c.F(F_COLN2O), co2 = c.F(F_COLCO2);
-  Spec s = spec(n2o, rat(4, jp), co2, 8.0f, 9), s1 = spec(n2o, rat(4, jp + 1), co2, 8.0f, 9);
-  Spec sm = spec(n2o, chi(4, 1) / chi(2, 1), co2, 8.0f, 9);  // minor and planck share the ratio
+  Spec s = spec(n2o, rat(c, 4, jp), co2, 8.0f, 9), s1 = spec(n2o, rat(c, 4, jp + 1), co2, 8.0f, 9);
+  Spec sm = spec(n2o, chi(c, 4, 1) / chi(c, 2, 1), co2, 8.0f, 9);  // minor and planck share the ratio
   binary_lower_terms(t, c, s, s1, BT.ka, NGB);
   self_terms(t, c, BT.sr, NGB);
   for_terms(t, c, BT.fo, NGB);
@@ -538,8 +542,8 @@ __device__ FracRec prologue<16>(const Cell& c, bool lower, Terms& t) {
   if (lower) {
     int jp = clampi(c.I(I_JP), 1, 58);
     float h2o = c.F(F_COLH2O), ch4 = c.F(F_COLCH4);
-    Spec s = spec(h2o, rat(3, jp), ch4, 8.0f, 9), s1 = spec(h2o, rat(3, jp + 1), ch4, 8.0f, 9);
-    Spec sp = spec(h2o, chi(1, 6) / chi(6, 6), ch4, 8.0f, 9);
+    Spec s = spec(h2o, rat(c, 3, jp), ch4, 8.0f, 9), s1 = spec(h2o, rat(c, 3, jp + 1), ch4, 8.0f, 9);
+    Spec sp = spec(h2o, chi(c, 1, 6) / chi(c, 6, 6), ch4, 8.0f, 9);
     binary_lower_terms(t, c, s, s1, BT.ka, NGB);
     self_terms(t, c, BT.sr, NGB);
     for_terms(t, c, BT.fo, NGB);

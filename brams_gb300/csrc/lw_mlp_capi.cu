@@ -296,13 +296,18 @@ int gb_lw_mlp_samples(gb_lw_context* ctx, void* stream, const gb_lw_grid* grid, 
   LwBatch b;
   int rc = gb_ctx_make_batch(ctx, 1, &g, 1.0, b);
   if (rc) return rc;
-  b.g[0].dbg_taut = d_tau;
-  b.g[0].dbg_fracs = d_frac;
+  // the taumol kernel writes taug and the Planck fractions of column i,
+  // layer l at row i * nlay + l of the caller's (rows, 140) arrays
+  b.gstride = (long long)g.nlay * GB_NGPT;
+  b.gslots = g.ncol;
+  b.gtau = d_tau;
+  b.gfrac = d_frac;
   cudaStream_t st = (cudaStream_t)stream;
   cudaSetDevice(ctx->device);
   cudaError_t e = gb_mlp_features(grid_in(g), ctx->tabs.grav, ctx->tabs.avogad, d_feat, st);
   if (e != cudaSuccess) return fail(ctx, e, "features");
-  return gb_ctx_launch_batch(ctx, b, st);
+  e = gb_lw_launch_gas(b, ctx->d_tables, 0, g.ncol, st);
+  return e == cudaSuccess ? GB_LW_OK : fail(ctx, e, "taumol samples");
 }
 
 int gb_lw_mlp_fit_norm(gb_lw_mlp* m, void* stream, int64_t rows, const float* d_feat, const float* d_tau,

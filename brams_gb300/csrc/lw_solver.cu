@@ -1,46 +1,51 @@
-// Fused RRTMG_LW column kernel for GB300 (sm_103a).
+// RRTMG_LW column kernels for GB300 (sm_103a).
 //
-// A persistent grid of thread blocks; each block solves one column at a time
-// (the reference's column loop, rrtmg_lw_rad.f90:486-593) and owns one slot
-// of an L2-resident scratch area.  One launch covers a batch of grids (nested
-// grids, ensemble members) with their own column and layer counts: the batch
-// columns are numbered grid after grid and each block walks them with stride
-// gridDim.x.  Phases per column, separated by barriers:
-//   1. inatm + setcoef (rrtmg_lw_rad.f90:598-924, rrtmg_lw_setcoef.f90:50-434):
-//      one thread per layer, coefficients into shared memory; Planck
-//      interpolation with one thread per (level, band); column sums for
-//      pwvcm.  All threads also scan the McICA cloud fractions to mark cloudy
-//      layers and cells (rtrnmc.f90:292-331) and to check the particle sizes
-//      where cldprmc would stop (cldprmc.f90:178-266).  In the fused cloud
-//      mode the block instead draws the column's 140 McICA random numbers
-//      (mcica_subcol_gen_lw.f90:484-512 with icld 3, Mersenne twister seeded
-//      seed0 + column) and marks cell (lay, g) cloudy iff cdf(g) >= 1 -
-//      cldf(lay) (:650), with the cloud optical depth of each (layer, band)
-//      computed once -- the values mcica_subcol_lw would have copied into
-//      every sub-column of that band.
-//   2. gas optics and cell transfer coefficients, band by band: a prologue
-//      per (layer, band) builds the taumol term list (lw_gasoptics.cuh), then
-//      one thread per (layer, g) cell evaluates taug, adds the aerosol depth
-//      (rrtmg_lw_rad.f90:548-553), takes the Planck fraction and computes the
-//      cell's layer transmittance and down/up sources exactly as rtrnmc's
-//      down sweep does (rtrnmc.f90:350-455): clear-sky coefficients for every
-//      cell and cloudy-layer coefficients where cldfmc /= 0.  They go to the
-//      block's scratch slot.  Lookup-table entries exp_tbl/tfn_tbl/tau_tbl
-//      (rrtmg_lw_init.f90:125-142) are evaluated at the quantised index.
-//   3. rtrnmc sweeps, one thread per g-point: each layer is then an affine
-//      update radiance*A + B (rtrnmc.f90:347-529); the clear-sky stream and
-//      the surface-temperature derivatives follow with their own
-//      coefficients.  Per-level g-point sums are weighted by
-//      0.5*delwave*fluxfac and reduced across each warp in fp32.
-//   4. fp64 epilogue: per-warp partial sums added in fp64, net fluxes and
-//      heating rates heatfac*dF/dp in fp64 (rtrnmc.f90:566-592).
+// The reference solves one column at a time (rrtmg_lw_rad.f90:486-593):
+// inatm, cldprmc, setcoef, taumol, the aerosol add and rtrnmc.  Here one
+// thread block of 160 threads solves a column, thread t standing for g-point
+// t (the last warp has 12 live lanes), and persistent blocks walk the columns
+// of a batch of grids.  Nothing per cell goes to global scratch:
 //
-// Precision: gas optics and transfer in fp32; flux accumulation across warps
-// error-free (two-sum) into fp64, net fluxes and the heating-rate step in
-// fp64.  Outputs follow the reference's layout:
-// uflx(icol, k+1) for k = 0..nlay, hr(icol, k+1) for k = 0..nlay-1.
+//   taumol (gas_column) -- setcoef (rrtmg_lw_setcoef.f90:275-430) with one
+//     thread per layer, then band by band a prologue per layer builds the
+//     layer's term list (lw_gasoptics.cuh) and one thread per (layer, g) cell
+//     gathers taug = sum w * table[row + g] and interpolates the Planck
+//     fraction.  taug (without aerosol) and the fractions go to fp32 planes in
+//     a slot owned by the block, which stays in L2 until the transfer of the
+//     same column reads it.
+//
+//   transfer (rt_column) -- inatm's column amounts, the laytrop and value
+//     checks, Planck interpolation per (layer, band) and the surface source,
+//     the McICA cloud bits and cldprmc's optical depths, then rtrnmc: a
+//     downward pass from the model top and an upward pass from the surface.
+//     Each pass evaluates a cell's transmittance and sources in registers from
+//     taug, the Planck fraction, the layer's Planck values and rtrnmc's
+//     exp_tbl/tfn_tbl/tau_tbl (rrtmg_lw_init.f90:120-142, built in double
+//     precision at set-up) at the reference's quantised index
+//     (rtrnmc.f90:350-455 down, 486-529 up); the up pass recomputes what the
+//     down pass computed instead of storing it.  The passes are software
+//     pipelined: while layer l is finished, the gas optics of the layer two
+//     ahead are loaded and the table entry of the next layer is looked up.
+//     Per level the 32 lanes' weighted radiances are summed with a transposed
+//     butterfly (two streams down, four up); the five warps' fp32 partials
+//     are added error-free (two-sum) into fp64, and the net fluxes and heating
+//     rates heatfac*dF/dp are fp64 (rtrnmc.f90:566-592).
+//
+// Kernels: lw_full_kernel (taumol then the transfer; for batches without a
+// network, and for the columns a network batch hands over), lw_rt_kernel (the
+// transfer on the network's fp16 taug and Planck fractions; columns with a
+// layer off the network are handed over), lw_gas_kernel (taumol alone, for
+// the network's training samples and the gas-optics diagnostics).
+//
+// Precision: gas optics and transfer in fp32, flux sums across warps
+// error-free into fp64, net fluxes and the heating-rate step in fp64.
+// Outputs follow the reference's layout: uflx(icol, k+1) for k = 0..nlay,
+// hr(icol, k+1) for k = 0..nlay-1.  The unit is compiled without multiply-add
+// contraction (every fused multiply-add is an explicit fmaf), so a column
+// gives the same bits in every kernel flavour and launch shape.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <algorithm>
 #include <cmath>
 #include <stdint.h>
 #include <climits>
@@ -48,164 +53,58 @@
 #include "lw_common.h"
 #include "lw_solver.h"
 #include "lw_gasoptics.cuh"
-#include "lw_mt.cuh"
 
 namespace gb {
 
-constexpr int NSW = 5;  // warps of the g-point sweeps (140 lanes)
 constexpr float BPADE = 1.0f / 0.278f;
+constexpr float REC_6 = 0.166667f;
+constexpr int TGROUP = MAXT_ALL;  // term slots per layer of a band's term list
+constexpr int RT_NT = 160;        // threads per column block: one per g-point
+constexpr int RT_NW = RT_NT / 32;
 
-// ------------------------------------------------------------------ band groups
-// Bands are processed in groups of consecutive bands that share one prologue
-// pass and one cell pass (kGroupFirst: first band of each group, then 17).
-// Term lists of a group's bands sit side by side, TGROUP term slots per layer.
-constexpr int kGroupFirst[] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17};
-constexpr int NGROUP = (int)(sizeof(kGroupFirst) / sizeof(int)) - 1;
-constexpr int group_of(int b) {
-  int gr = 0;
-  while (kGroupFirst[gr + 1] <= b) ++gr;
-  return gr;
-}
-constexpr int term_offset(int b) {  // first term slot of band b in its group
-  int o = 0;
-  for (int k = kGroupFirst[group_of(b)]; k < b; ++k) o += maxt(k);
-  return o;
-}
-constexpr int group_terms(int gr) { return term_offset(kGroupFirst[gr + 1] - 1) + maxt(kGroupFirst[gr + 1] - 1); }
-constexpr int max_group_terms() {
-  int m = 0;
-  for (int gr = 0; gr < NGROUP; ++gr) m = group_terms(gr) > m ? group_terms(gr) : m;
-  return m;
-}
-constexpr int max_group_bands() {
-  int m = 0;
-  for (int gr = 0; gr < NGROUP; ++gr) m = kGroupFirst[gr + 1] - kGroupFirst[gr] > m ? kGroupFirst[gr + 1] - kGroupFirst[gr] : m;
-  return m;
-}
-constexpr int TGROUP = max_group_terms();
-constexpr int GBANDS = max_group_bands();
-__constant__ int c_gfirst[17] = {
-#define GB_G(i) (i <= NGROUP ? kGroupFirst[i] : 0)
-    GB_G(0), GB_G(1), GB_G(2), GB_G(3), GB_G(4), GB_G(5), GB_G(6), GB_G(7), GB_G(8),
-    GB_G(9), GB_G(10), GB_G(11), GB_G(12), GB_G(13), GB_G(14), GB_G(15), GB_G(16)};
-#undef GB_G
-__constant__ int c_toff[17] = {0, term_offset(1), term_offset(2), term_offset(3), term_offset(4), term_offset(5),
-                               term_offset(6), term_offset(7), term_offset(8), term_offset(9), term_offset(10),
-                               term_offset(11), term_offset(12), term_offset(13), term_offset(14), term_offset(15),
-                               term_offset(16)};
-
-// ------------------------------------------------------------------ shared memory layout
-struct Smem {
-  float* f;        // [NF][nl]   per-layer coefficients (phases 1-2)
-  int* iv;         // [NI][nl]
-  float2* terms;   // [TGROUP][nl] gas-optics terms of the current band group, term-major (phase 2)
-  float* part;     // [NSW][nl+1][6] warp partial fluxes (region A, phases 3-4)
-  float* taua;     // [16][nl]
-  float* plk_lay;  // [16][nl]
-  float* plk_lev;  // [16][nl+1]
-  FracRec* frec;   // [GBANDS][nl] Planck-fraction records of the current band group
-  int* cldlay;     // [nl]
-  int* surok;      // [nl] 1: the layer's gas optics come from the learned model
-  unsigned* cbits; // [nl][5] bit g set where cldfmcl == 1
-  unsigned* fbits; // [nl][5] bit g set where cldfmcl is neither 0 nor 1
-  float* frac1;    // [140] Planck fractions of the bottom layer (surface source)
-  double* fnet;    // [nl+1][2] net fluxes (region A after part, phase 4)
-  float* misc;     // [64]: secdiff[16], plankbnd[16], dplankbnd[16], semiss[16]
-  float* scal;     // [4]
-  int* iscal;      // [4]: laytrop, sum of lower-layer indices, error, column error
-  double* cdf;     // [140] McICA draws of the column (fused cloud mode, phase 1; in the term area)
-  uint32_t* mtlo;  // [141] Mersenne-twister state words (fused cloud mode, phase 1; in the term area)
-  float* tcl;      // [nl][16] cloud optical depth per (layer, band) (fused cloud mode)
-  // fused cloud mode, per layer: the McICA threshold 1 - cldf as double bits
-  // (cdf >= it marks a cloudy cell), the layer's cloud water paths and radii
-  // as floats, and flags: bit 0 ciwp /= 0, bit 1 clwp /= 0, bit 2
-  // ciwp + clwp >= 1e-20, bits 8.. the code cldprmc's radius checks stop with
-  long long* cthr; // [nl]
-  float4* lcw;     // [nl] (ciwp, clwp, radice, radliq)
-  int* lfl;        // [nl]
-  float4* prow;    // [nl+1] Planck-table row and fraction of tlev and tlay per level (phase 1)
-};
+__constant__ int c_icb[16] = {1, 2, 3, 3, 3, 4, 4, 4, 5, 5, 5, 5, 5, 5, 5, 5};  // cldprmc.f90:133
+// diffusivity-angle coefficients (rtrnmc.f90:236-247)
+__constant__ float c_a0[16] = {1.66f, 1.55f, 1.58f, 1.66f, 1.54f, 1.454f, 1.89f, 1.33f, 1.668f, 1.66f, 1.66f, 1.66f, 1.66f, 1.66f, 1.66f, 1.66f};
+__constant__ float c_a1[16] = {0.f, 0.25f, 0.22f, 0.f, 0.13f, 0.446f, -0.10f, 0.40f, -0.006f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+__constant__ float c_a2[16] = {0.f, -12.0f, -11.7f, 0.f, -0.72f, -0.243f, 0.19f, -0.062f, 0.414f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
-
-// Region A holds, by phase: the per-layer coefficients f/iv and the term
-// lists (phases 1-2; the McICA draws of the fused cloud mode borrow the term
-// area during phase 1), then the warp partial sums and net fluxes (3-4).  The
-// learned-only kernel (lean) runs no taumol and has no term area.
-__host__ __device__ inline size_t terms_offset(int nl) { return ((size_t)(NF + NI) * nl * 4 + 15) & ~size_t(15); }
-__host__ __device__ inline size_t region_a(int nl, bool lean) {
-  size_t terms = lean ? 0 : (size_t)nl * TGROUP * 8;
-  const size_t draws = align16(GB_NGPT * 8) + align16((GB_NGPT + 1) * 4);
-  size_t coef = terms_offset(nl) + (terms > draws ? terms : draws);
-  size_t part = align16((size_t)NSW * (nl + 1) * 6 * 4) + (size_t)(nl + 1) * 2 * 8;
-  return align16(coef > part ? coef : part);
-}
-
-__host__ __device__ inline size_t smem_bytes(int nl, bool lean) {
-  size_t a = region_a(nl, lean);
-  a += align16((size_t)nl * 16 * 4);         // taua
-  a += align16((size_t)nl * 16 * 4);         // plk_lay
-  a += align16((size_t)(nl + 1) * 16 * 4);   // plk_lev
-  a += align16((size_t)GBANDS * nl * sizeof(FracRec));
-  a += 2 * align16((size_t)nl * 4);
-  a += 2 * align16((size_t)nl * 5 * 4);
-  a += align16(GB_NGPT * 4);
-  a += align16(64 * 4) + align16(4 * 4) + align16(4 * 4);
-  a += align16((size_t)nl * 16 * 4);         // tcl
-  a += align16((size_t)nl * 8) + align16((size_t)nl * 16) + align16((size_t)nl * 4);  // cthr, lcw, lfl
-  a += align16((size_t)(nl + 1) * 16);                                                   // prow
-  return a;
-}
-
-__device__ inline Smem carve(char* base, int nl, bool lean) {
-  Smem s;
-  char* p = base;
-  s.f = (float*)p;
-  s.iv = (int*)(p + (size_t)NF * nl * 4);
-  s.terms = (float2*)(p + terms_offset(nl));
-  s.cdf = (double*)(p + terms_offset(nl));
-  s.mtlo = (uint32_t*)(p + terms_offset(nl) + align16(GB_NGPT * 8));
-  s.part = (float*)p;
-  s.fnet = (double*)(p + align16((size_t)NSW * (nl + 1) * 6 * 4));
-  p += region_a(nl, lean);
-  s.taua = (float*)p; p += align16((size_t)nl * 16 * 4);
-  s.plk_lay = (float*)p; p += align16((size_t)nl * 16 * 4);
-  s.plk_lev = (float*)p; p += align16((size_t)(nl + 1) * 16 * 4);
-  s.frec = (FracRec*)p; p += align16((size_t)GBANDS * nl * sizeof(FracRec));
-  s.cldlay = (int*)p; p += align16((size_t)nl * 4);
-  s.surok = (int*)p; p += align16((size_t)nl * 4);
-  s.cbits = (unsigned*)p; p += align16((size_t)nl * 5 * 4);
-  s.fbits = (unsigned*)p; p += align16((size_t)nl * 5 * 4);
-  s.frac1 = (float*)p; p += align16(GB_NGPT * 4);
-  s.misc = (float*)p; p += align16(64 * 4);
-  s.scal = (float*)p; p += align16(4 * 4);
-  s.iscal = (int*)p; p += align16(4 * 4);
-  s.tcl = (float*)p; p += align16((size_t)nl * 16 * 4);
-  s.cthr = (long long*)p; p += align16((size_t)nl * 8);
-  s.lcw = (float4*)p; p += align16((size_t)nl * 16);
-  s.lfl = (int*)p; p += align16((size_t)nl * 4);
-  s.prow = (float4*)p;
-  return s;
-}
 
 // ------------------------------------------------------------------ helpers
 __device__ __forceinline__ double in2(const double* __restrict__ a, long long ld, long long icol, int k) {
   return __ldg(a + icol + ld * k);
 }
 
-__device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
+// setcoef's regime switch (plog <= 4.56 is the upper atmosphere,
+// rrtmg_lw_setcoef.f90:312), decided in fp64 near the switch
+__device__ __forceinline__ bool lower_atmosphere(double pd, float plog) {
+  bool lower = plog > 4.56f;
+  if (fabsf(plog - 4.56f) < 1.0e-4f) lower = log(pd) > 4.56;
+  return lower;
+}
+
+// Warp sums of two values per lane at once: lane i returns the sum over the
+// 32 lanes of v(i & 1) (one exchange, then four xor steps).
+__device__ __forceinline__ float reduce2(float v0, float v1, int lane) {
+  const unsigned F = 0xffffffffu;
+  const bool lo = lane & 1;
+  float k = lo ? v1 : v0;
+  const float s = lo ? v0 : v1;
+  k += __shfl_xor_sync(F, s, 1);
+  k += __shfl_xor_sync(F, k, 2);
+  k += __shfl_xor_sync(F, k, 4);
+  k += __shfl_xor_sync(F, k, 8);
+  k += __shfl_xor_sync(F, k, 16);
+  return k;
 }
 
 // Warp sums of four values per lane at once (a transposed butterfly, 6
 // shuffles instead of 20): lane i returns the sum over the 32 lanes of v[i & 3].
-__device__ __forceinline__ float reduce4(const float (&v)[4], int lane) {
+__device__ __forceinline__ float reduce4(float v0, float v1, float v2, float v3, int lane) {
   const unsigned F = 0xffffffffu;
   const bool hi = lane & 2;
-  float k0 = hi ? v[2] : v[0], k1 = hi ? v[3] : v[1];
-  const float s0 = hi ? v[0] : v[2], s1 = hi ? v[1] : v[3];
+  float k0 = hi ? v2 : v0, k1 = hi ? v3 : v1;
+  const float s0 = hi ? v0 : v2, s1 = hi ? v1 : v3;
   k0 += __shfl_xor_sync(F, s0, 2);
   k1 += __shfl_xor_sync(F, s1, 2);
   const bool lo = lane & 1;
@@ -218,42 +117,22 @@ __device__ __forceinline__ float reduce4(const float (&v)[4], int lane) {
   return k;
 }
 
-// exp_tbl/tfn_tbl/tau_tbl at the index the reference's lookup would pick
-// (rrtmg_lw_rtrnmc.f90:385-388 with rrtmg_lw_init.f90:125-142)
-struct TblEntry {
-  float tau, trans, tfn;
-};
-__device__ __forceinline__ TblEntry tbl(float od) {
-  float tblind = __fdividef(od, BPADE + od);
-  int itr = (int)fmaf(10000.0f, tblind, 0.5f);
-  itr = itr < 0 ? 0 : (itr > 10000 ? 10000 : itr);
-  TblEntry e;
-  if (itr == 0) {
-    e.tau = 0.0f; e.trans = 1.0f; e.tfn = 0.0f;
-  } else if (itr == 10000) {
-    e.tau = 1.0e10f; e.trans = 1.0e-20f; e.tfn = 1.0f;
-  } else {
-    float t = (float)itr * 1.0e-4f;
-    float tau = BPADE * __fdividef(t, 1.0f - t);
-    float ex = __expf(-tau);
-    ex = ex <= 1.0e-20f ? 1.0e-20f : ex;
-    e.tau = tau;
-    e.trans = ex;
-    e.tfn = tau < 0.06f ? tau * (1.0f / 6.0f) : fmaf(-2.0f, __fdividef(1.0f, tau) - __fdividef(ex, 1.0f - ex), 1.0f);
-  }
-  return e;
+// rtrnmc's table index of an optical depth (rrtmg_lw_rtrnmc.f90:385-388):
+// itr = int(tblint * od / (bpade + od) + 0.5), within 0 .. ntbl
+__device__ __forceinline__ int tbl_index(float od) {
+  const float tblind = __fdividef(od, BPADE + od);
+  const int itr = (int)fmaf(10000.0f, tblind, 0.5f);
+  return itr < 0 ? 0 : (itr > 10000 ? 10000 : itr);
 }
-
-__constant__ int c_maxt[17] = {0, maxt(1), maxt(2), maxt(3), maxt(4), maxt(5), maxt(6), maxt(7), maxt(8),
-                               maxt(9), maxt(10), maxt(11), maxt(12), maxt(13), maxt(14), maxt(15), maxt(16)};
-__constant__ int c_icb[16] = {1, 2, 3, 3, 3, 4, 4, 4, 5, 5, 5, 5, 5, 5, 5, 5};  // cldprmc.f90:133
-// diffusivity-angle coefficients (rtrnmc.f90:236-247)
-__constant__ float c_a0[16] = {1.66f, 1.55f, 1.58f, 1.66f, 1.54f, 1.454f, 1.89f, 1.33f, 1.668f, 1.66f, 1.66f, 1.66f, 1.66f, 1.66f, 1.66f, 1.66f};
-__constant__ float c_a1[16] = {0.f, 0.25f, 0.22f, 0.f, 0.13f, 0.446f, -0.10f, 0.40f, -0.006f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-__constant__ float c_a2[16] = {0.f, -12.0f, -11.7f, 0.f, -0.72f, -0.243f, 0.19f, -0.062f, 0.414f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+// (exp_tbl, tfn_tbl) and tau_tbl at an index (rrtmg_lw_init.f90:120-142,
+// computed in double precision at set-up and stored as float)
+__device__ __forceinline__ float2 tbl_tt(const float* __restrict__ T, int itr) {
+  return __ldg(reinterpret_cast<const float2*>(T + c_T.tbl_tt) + itr);
+}
+__device__ __forceinline__ float tbl_tau(const float* __restrict__ T, int itr) { return __ldg(T + c_T.tbl_tau + itr); }
 
 // cldprmc's optical depth ciwp*abscoice + clwp*abscoliq of one cell
-// (cldprmc.f90:194-266; the radius bounds are checked in the pre-pass), from
+// (cldprmc.f90:194-266; the radius bounds are checked beforehand), from
 // w = (ciwp, clwp, radice, radliq) converted to float and flags bit 0: ciwp
 // /= 0, bit 1: clwp /= 0
 __device__ __forceinline__ float cloud_tau_layer(const LwArgs& a, int band, const float* __restrict__ T, float4 w,
@@ -289,32 +168,348 @@ __device__ __forceinline__ float cloud_tau_layer(const LwArgs& a, int band, cons
   return w.x * abscoice + w.y * abscoliq;
 }
 
-// McICA cloud optics of one cell: returns cldfmc and sets odcld/efcl
-// (cldprmc.f90:178-266 then rtrnmc.f90:300-312; computed only where
-// cldfmc == 1, the only cells whose optical depth rtrnmc reads).
-__device__ __forceinline__ float cell_cloud(const LwArgs& a, const Smem& s, long long icol, int g, int lay,
-                                            float secdiff_b, int band, const float* __restrict__ T, float& odcld,
-                                            float& efcl) {
-  const unsigned bit = 1u << (g & 31);
-  const bool one = s.cbits[lay * 5 + (g >> 5)] & bit;
+// ================================================================== taumol
+struct GasSmem {
+  float* f;        // [NF][nl]   per-layer setcoef quantities
+  int* iv;         // [NI][nl]
+  float2* terms;   // [TGROUP][nl] gas-optics terms of the current band, term-major
+  FracRec* frec;   // [nl] Planck-fraction records of the current band
+  int* iscal;      // [4]: laytrop
+};
+
+__host__ __device__ inline size_t gas_smem_bytes(int nl) {
+  return align16((size_t)(NF + NI) * nl * 4) + align16((size_t)nl * TGROUP * 8) + align16((size_t)nl * sizeof(FracRec)) + 16;
+}
+
+__device__ inline GasSmem gas_carve(char* p, int nl) {
+  GasSmem s;
+  s.f = (float*)p;
+  s.iv = (int*)(p + (size_t)NF * nl * 4);
+  p += align16((size_t)(NF + NI) * nl * 4);
+  s.terms = (float2*)p;
+  p += align16((size_t)nl * TGROUP * 8);
+  s.frec = (FracRec*)p;
+  p += align16((size_t)nl * sizeof(FracRec));
+  s.iscal = (int*)p;
+  return s;
+}
+
+// Prologue of band b for one layer: the band-specific per-layer code
+// (lw_gasoptics.cuh) writing the layer's terms and Planck-fraction record.
+template <int b>
+__device__ __forceinline__ void band_prologue(const GasSmem& s, int nl, int lay, bool lower, const float* T) {
+  Cell c{s.f, s.iv, nl, lay, T};
+  Terms t{s.terms + lay, nl, 0};
+  FracRec r = prologue<b>(c, lower, t);
+  t.pad(maxt(b), c_T.band[b - 1].sr);
+  s.frec[lay] = r;
+}
+
+// taumol of band b for every layer of a column: the prologue of each layer,
+// then one thread per (layer, g) cell gathering taug = sum w * table[row + g]
+// (the band's term count and g-points are compile-time constants, so the
+// gather loop is unrolled) and interpolating the Planck fraction.  Ends with
+// a barrier.
+template <int b, int NT>
+__device__ __forceinline__ void gas_band(const GasSmem& s, int nl, int laytrop, const float* __restrict__ T,
+                                         float* gt, float* gf) {
+  constexpr int NG = ngb_const(b), G0 = g0_const(b), M = maxt(b);
+  for (int lay = threadIdx.x; lay < nl; lay += NT) band_prologue<b>(s, nl, lay, lay < laytrop, T);
+  __syncthreads();
+  for (int cell = threadIdx.x; cell < nl * NG; cell += NT) {
+    const int lay = cell / NG, gi = cell - lay * NG;
+    const float2* tp = s.terms + lay;
+    const float* Tg = T + gi;
+    float acc = 0.0f;
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      const float2 w = tp[k * nl];
+      acc = fmaf(w.x, __ldg(Tg + __float_as_int(w.y)), acc);
+    }
+    if ((b == 4 || b == 7) && lay >= laytrop) acc *= gscale(b, gi);
+    const FracRec fr = s.frec[lay];
+    const float* fp = T + fr.off + gi;
+    const float f0 = __ldg(fp);
+    gt[lay * GB_NGPT + G0 + gi] = acc;
+    gf[lay * GB_NGPT + G0 + gi] = fmaf(fr.fpl, __ldg(fp + NG) - f0, f0);
+  }
+  __syncthreads();
+}
+
+// taumol of one column by the whole block: taug and Planck fractions of every
+// (layer, g) cell into the planes gt/gf ([nl][140] each).  Ends with a barrier.
+template <int NT>
+__device__ void gas_column(const LwArgs& a, long long icol, const GasSmem& s, float* gt, float* gf,
+                           const float* __restrict__ T) {
+  const int nl = a.nlay, tid = threadIdx.x;
+  if (tid == 0) s.iscal[0] = 0;
+  __syncthreads();
+  // setcoef (rrtmg_lw_setcoef.f90:275-430) after inatm's column amounts
+  // (rrtmg_lw_rad.f90:807-867), one thread per layer
+  const float stpfac = 296.0f / 1013.0f;
+  const float amd = 28.9660f, amw = 18.0160f;
+  for (int lay = tid; lay < nl; lay += NT) {
+    const double pd = in2(a.play, a.ld, icol, lay);
+    const float pavel = (float)pd;
+    const float tavel = (float)in2(a.tlay, a.ld, icol, lay);
+    const double dpz = in2(a.plev, a.ld, icol, lay) - in2(a.plev, a.ld, icol, lay + 1);
+    const float w1 = (float)in2(a.h2ovmr, a.ld, icol, lay);
+    const float w2 = (float)in2(a.co2vmr, a.ld, icol, lay);
+    const float w3 = (float)in2(a.o3vmr, a.ld, icol, lay);
+    const float w4 = (float)in2(a.n2ovmr, a.ld, icol, lay);
+    const float w6 = (float)in2(a.ch4vmr, a.ld, icol, lay);
+    const float w7 = (float)in2(a.o2vmr, a.ld, icol, lay);
+    const float amm = (1.0f - w1) * amd + w1 * amw;
+    const float coldry = (float)dpz * 1.e3f * (float)c_T.avogad / (1.e2f * (float)c_T.grav * amm * (1.0f + w1));
+    const float summol = w2 + w3 + w4 + 0.0f + w6 + w7;
+    const float wbrodl = coldry * (1.0f - summol);
+    const float wk1 = coldry * w1, wk2 = coldry * w2, wk3 = coldry * w3, wk4 = coldry * w4, wk6 = coldry * w6,
+                wk7 = coldry * w7;
+    float* F = s.f;
+    auto put = [&](int k, float v) { F[k * nl + lay] = v; };
+    put(F_COLDRY, coldry);
+    put(F_PAVEL, pavel);
+    put(F_WX1, coldry * (float)in2(a.ccl4vmr, a.ld, icol, lay) * 1.e-20f);
+    put(F_WX2, coldry * (float)in2(a.cfc11vmr, a.ld, icol, lay) * 1.e-20f);
+    put(F_WX3, coldry * (float)in2(a.cfc12vmr, a.ld, icol, lay) * 1.e-20f);
+    put(F_WX4, coldry * (float)in2(a.cfc22vmr, a.ld, icol, lay) * 1.e-20f);
+    const float plog = __logf(pavel);
+    const bool lower = lower_atmosphere(pd, plog);
+    int jp = clampi((int)(36.0f - 5.0f * (plog + 0.04f)), 1, 58);
+    jp = lower ? (jp > 12 ? 12 : jp) : (jp < 13 ? 13 : jp);
+    const float fp = 5.0f * (__ldg(T + c_T.ref_preflog + jp - 1) - plog);
+    const float dt0 = (tavel - __ldg(T + c_T.ref_tref + jp - 1)) / 15.0f;
+    const int jt = clampi((int)(3.0f + dt0), 1, 4);
+    const float ft = dt0 - (float)(jt - 3);
+    const float dt1 = (tavel - __ldg(T + c_T.ref_tref + jp)) / 15.0f;
+    const int jt1 = clampi((int)(3.0f + dt1), 1, 4);
+    const float ft1 = dt1 - (float)(jt1 - 3);
+    const float water = wk1 / coldry;
+    const float scalefac = pavel * stpfac / tavel;
+    const float forfac = scalefac / (1.0f + water);
+    float forfrac, selffrac = 0.0f;
+    int indfor, indself = 1;
+    if (lower) {
+      float factor = (332.0f - tavel) / 36.0f;
+      indfor = min(2, max(1, (int)factor));
+      forfrac = factor - (float)indfor;
+      factor = (tavel - 188.0f) / 7.2f;
+      indself = min(9, max(1, (int)factor - 7));
+      selffrac = factor - (float)(indself + 7);
+    } else {
+      const float factor = (tavel - 188.0f) / 36.0f;
+      indfor = 3;
+      forfrac = factor - 1.0f;
+    }
+    const float selffac = water * forfac;
+    const float scaleminor = pavel / tavel;
+    const float scaleminorn2 = scaleminor * (wbrodl / (coldry + wk1));
+    const float factor = (tavel - 180.8f) / 7.2f;
+    const int indminor = min(18, max(1, (int)factor));
+    const float minorfrac = factor - (float)indminor;
+    const float colh2o = 1.e-20f * wk1;
+    float colco2 = 1.e-20f * wk2, colo3 = 1.e-20f * wk3, coln2o = 1.e-20f * wk4, colco = 0.0f;
+    float colch4 = 1.e-20f * wk6;
+    const float colo2 = 1.e-20f * wk7;
+    if (colco2 == 0.0f) colco2 = 1.e-32f * coldry;
+    if (colo3 == 0.0f) colo3 = 1.e-32f * coldry;
+    if (coln2o == 0.0f) coln2o = 1.e-32f * coldry;
+    if (colco == 0.0f) colco = 1.e-32f * coldry;
+    if (colch4 == 0.0f) colch4 = 1.e-32f * coldry;
+    const float compfp = 1.0f - fp;
+    put(F_FAC10, compfp * ft);
+    put(F_FAC00, compfp * (1.0f - ft));
+    put(F_FAC11, fp * ft1);
+    put(F_FAC01, fp * (1.0f - ft1));
+    put(F_COLH2O, colh2o); put(F_COLCO2, colco2); put(F_COLO3, colo3); put(F_COLN2O, coln2o);
+    put(F_COLCO, colco); put(F_COLCH4, colch4); put(F_COLO2, colo2); put(F_COLBRD, 1.e-20f * wbrodl);
+    put(F_SELFFAC, colh2o * selffac); put(F_SELFFRAC, selffrac);
+    put(F_FORFAC, colh2o * forfac); put(F_FORFRAC, forfrac);
+    put(F_MINORFRAC, minorfrac); put(F_SCALEMINOR, scaleminor); put(F_SCALEMINORN2, scaleminorn2);
+    int* IV = s.iv;
+    IV[I_JP * nl + lay] = jp; IV[I_JT * nl + lay] = jt; IV[I_JT1 * nl + lay] = jt1;
+    IV[I_INDSELF * nl + lay] = indself; IV[I_INDFOR * nl + lay] = indfor; IV[I_INDMINOR * nl + lay] = indminor;
+    if (lower) atomicAdd(&s.iscal[0], 1);  // laytrop (the transfer checks that these form a prefix)
+  }
+  __syncthreads();
+  const int laytrop = s.iscal[0];
+  gas_band<1, NT>(s, nl, laytrop, T, gt, gf);
+  gas_band<2, NT>(s, nl, laytrop, T, gt, gf);
+  gas_band<3, NT>(s, nl, laytrop, T, gt, gf);
+  gas_band<4, NT>(s, nl, laytrop, T, gt, gf);
+  gas_band<5, NT>(s, nl, laytrop, T, gt, gf);
+  gas_band<6, NT>(s, nl, laytrop, T, gt, gf);
+  gas_band<7, NT>(s, nl, laytrop, T, gt, gf);
+  gas_band<8, NT>(s, nl, laytrop, T, gt, gf);
+  gas_band<9, NT>(s, nl, laytrop, T, gt, gf);
+  gas_band<10, NT>(s, nl, laytrop, T, gt, gf);
+  gas_band<11, NT>(s, nl, laytrop, T, gt, gf);
+  gas_band<12, NT>(s, nl, laytrop, T, gt, gf);
+  gas_band<13, NT>(s, nl, laytrop, T, gt, gf);
+  gas_band<14, NT>(s, nl, laytrop, T, gt, gf);
+  gas_band<15, NT>(s, nl, laytrop, T, gt, gf);
+  gas_band<16, NT>(s, nl, laytrop, T, gt, gf);
+}
+
+// ================================================================== transfer
+// Shared memory of one column: a fixed header, one 384-byte record per
+// layer (so that every per-layer access in the loops is base + layer * 384
+// + a constant), then the per-warp level sums.
+struct RtHead {
+  float misc[64];         // secdiff[16], plankbnd[16], dplankbnd[16], semiss[16]
+  float red[2 * RT_NW];   // per-warp column sums for pwvcm
+  int iscal[4];           // stop code, lower-layer count
+  int pad[2];
+};
+struct RtLayer {
+  float4 rec[16];     // per band: Planck value of the layer, level-minus-layer Planck below and
+                      // above (dplankdn, dplankup), aerosol optical depth
+  float tcl[16];      // fused clouds: cloud optical depth per band; caller sub-columns: the
+                      // first five words are fbits (bit g: cldfmcl neither 0 nor 1)
+  unsigned cbits[5];  // bit g set where the cell is cloudy (cldfmc == 1)
+  int cldlay;         // 1: a cell of the layer has cldfmc == 1 (rtrnmc's icldlyr); in the first
+                      // phase: 1 where the layer is in the lower atmosphere
+  int lfl;            // cloud flags of the layer (bits 0-2) and cldprmc's stop code (bits 8..)
+  int pad0;
+  long long cthr;     // fused clouds: McICA threshold 1 - cldf as double bits
+  long long pad1;
+  float4 lcw;         // (ciwp, clwp, radice, radliq) as floats
+};
+static_assert(sizeof(RtHead) == 320 && sizeof(RtLayer) == 384, "transfer shared-memory records");
+
+struct RtSmem {
+  RtHead* h;
+  RtLayer* L;   // [nl]; in the last phase: fp64 net fluxes [nl+1][2]
+  float* part;  // [RT_NW][nl+1][6] per-warp level sums: dn, dn clear, up, up clear, dup/dT,
+                // dup clear/dT; in the first phase: float4 per level, the Planck-table row and
+                // fraction of tlev and tlay
+  __device__ __forceinline__ unsigned* fbits(int lay) const { return reinterpret_cast<unsigned*>(L[lay].tcl); }
+};
+
+__host__ __device__ inline size_t rt_layers_bytes(int nl) {
+  const size_t layers = (size_t)(nl < 1 ? 1 : nl) * sizeof(RtLayer);
+  return layers > (size_t)(nl + 1) * 16 ? layers : (size_t)(nl + 1) * 16;
+}
+__host__ __device__ inline size_t rt_smem_bytes(int nl) {
+  return sizeof(RtHead) + rt_layers_bytes(nl) + align16((size_t)RT_NW * (nl + 1) * 6 * 4);
+}
+
+__device__ inline RtSmem rt_carve(char* p, int nl) {
+  RtSmem s;
+  s.h = (RtHead*)p;
+  p += sizeof(RtHead);
+  s.L = (RtLayer*)p;
+  p += rt_layers_bytes(nl);
+  s.part = (float*)p;
+  return s;
+}
+
+// Where taug and the Planck fractions of a column come from.
+struct GasSrc {
+  const float* gt;            // fp32 planes [nl][140] (taumol), or NULL
+  const float* gf;
+  const __half* nt;           // fp16 rows [nl][140] (network), or NULL
+  const __half* nf;
+  const unsigned char* flag;  // per layer: 1 -> network, 0 -> fp32 planes
+};
+enum RtMode { RT_GAS = 0, RT_NET = 1, RT_MIX = 2 };
+
+template <int MODE>
+__device__ __forceinline__ bool layer_on_net(const GasSrc& src, int lay) {
+  if (MODE == RT_GAS) return false;
+  if (MODE == RT_NET) return true;
+  return src.flag[lay] != 0;
+}
+
+template <int MODE>
+__device__ __forceinline__ void gas_at(const GasSrc& src, bool net, int lay, int g, float& tg, float& pf) {
+  const int o = lay * GB_NGPT + g;
+  if (MODE != RT_GAS && net) {
+    tg = __half2float(__ldg(src.nt + o));
+    pf = __half2float(__ldg(src.nf + o));
+  } else {
+    tg = src.gt[o];  // plain loads: taumol wrote these planes in the same launch
+    pf = src.gf[o];
+  }
+}
+
+// Clear-sky layer transmittance and source factor of a cell: rtrnmc's
+// odepth <= 0.06 expansion or its table lookup (rtrnmc.f90:380-413).  x is
+// odepth/6 or tfn; the source from level Planck values is
+// plfrac * (blay + x * dplank).  itr is the table index (used above 0.06).
+struct Clr {
+  float atrans, x;
+  int itr;
+  bool thin;
+};
+__device__ __forceinline__ Clr clear_cell(float od, int itr, float2 e) {
+  Clr c;
+  c.thin = od <= 0.06f;
+  c.itr = itr;
+  c.atrans = c.thin ? fmaf(-0.5f * od, od, od) : 1.0f - e.x;
+  c.x = c.thin ? REC_6 * od : e.y;
+  return c;
+}
+
+// One layer of a g-point as the passes consume it: the Planck fraction, the
+// layer's Planck values and aerosol depth, the clear-sky optical depth along
+// the diffusivity angle, its table index and the table entry (looked up for
+// every cell, used above 0.06).  The passes set up the next layer's stage
+// while they finish the current one, so the table load is in flight meanwhile.
+struct Stage {
+  float pf, od;
+  float4 r;
+  int itr;
+  float2 tt;
+};
+__device__ __forceinline__ Stage stage_of(const RtSmem& S, const float* __restrict__ T, int lay, int band, float sd,
+                                          float tg, float pf) {
+  Stage st;
+  st.pf = pf;
+  st.r = S.L[lay].rec[band];
+  st.od = fmaxf(sd * (tg + st.r.w), 0.0f);
+  st.itr = tbl_index(st.od);
+  st.tt = tbl_tt(T, st.itr);
+  return st;
+}
+
+// Total (gas + cloud) absorptance and source factor of a cloudy cell
+// (rtrnmc.f90:356-379): the expansion below 0.06, else the table at the
+// clear cell's optical depth (odepth itself below 0.06, else tau_tbl at its
+// index) plus the cloud's.
+__device__ __forceinline__ void cloud_total(const float* __restrict__ T, const Clr& c, float od, float odcld,
+                                            float& atot, float& x) {
+  const float odtot = od + odcld;
+  if (odtot < 0.06f) {
+    atot = fmaf(-0.5f * odtot, odtot, odtot);
+    x = REC_6 * odtot;
+  } else {
+    const float tauq = c.thin ? od : tbl_tau(T, c.itr);
+    const float2 et = tbl_tt(T, tbl_index(tauq + odcld));
+    atot = 1.0f - et.x;
+    x = et.y;
+  }
+}
+
+// McICA cloud of a cell flagged cloudy in the layer bits: returns cldfmc and
+// sets the cloud optical depth along the diffusivity angle and its
+// absorptance (cldprmc.f90:178-266, rtrnmc.f90:300-312); a fractional
+// cldfmc (caller sub-columns only) enters with zero cloud optical depth.
+__device__ __forceinline__ float cell_cloud(const LwArgs& a, const RtSmem& S, long long icol, int g, int lay,
+                                            int band, float secdiff, bool one, const float* __restrict__ T,
+                                            float& odcld, float& efcl) {
   odcld = 0.0f;
   efcl = 0.0f;
-  if (a.cloud_mode == LW_CLOUD_FUSED) {  // sub-column clouds are 0 or 1; optical depth per (layer, band)
-    if (!one) return 0.0f;
-    odcld = secdiff_b * s.tcl[lay * 16 + band];
+  if (a.cloud_mode == LW_CLOUD_FUSED) {
+    odcld = secdiff * S.L[lay].tcl[band];
     efcl = 1.0f - __expf(-odcld);
     return 1.0f;
   }
-  if (!one) {
-    if (!(s.fbits[lay * 5 + (g >> 5)] & bit)) return 0.0f;
-    // fractional cldfmc: enters the cloudy-layer formulas with zero cloud optical depth
-    return (float)__ldg(a.cldfmcl + (long long)g + GB_NGPT * (icol + (long long)a.ld * lay));
-  }
-  long long o = (long long)g + GB_NGPT * (icol + (long long)a.ld * lay);
+  const long long o = (long long)g + GB_NGPT * (icol + (long long)a.ld * lay);
+  if (!one) return (float)__ldg(a.cldfmcl + o);
   const double ciwp = __ldg(a.ciwpmcl + o), clwp = __ldg(a.clwpmcl + o);
-  // the optical depth from this cell's water paths and the layer's radii (as
-  // floats in shared memory), or the caller's taucmcl
-  float tauc;
+  // the optical depth from this cell's water paths and the layer's radii, or the caller's taucmcl
+  float tauc = 0.0f;
   bool from_paths = a.inflag == 2 && ciwp + clwp >= 1.e-20;
   if (!from_paths) {
     const double tin = __ldg(a.taucmcl + o);
@@ -324,780 +519,528 @@ __device__ __forceinline__ float cell_cloud(const LwArgs& a, const Smem& s, long
   }
   if (from_paths) {
     const int fl = ((__double_as_longlong(ciwp) << 1) != 0LL ? 1 : 0) | ((__double_as_longlong(clwp) << 1) != 0LL ? 2 : 0);
-    const float4 r = s.lcw[lay];
+    const float4 r = S.L[lay].lcw;
     tauc = cloud_tau_layer(a, band, T, make_float4((float)ciwp, (float)clwp, r.z, r.w), fl);
   }
-  odcld = secdiff_b * tauc;
+  odcld = secdiff * tauc;
   efcl = 1.0f - __expf(-odcld);
   return 1.0f;
 }
 
-
-__device__ __forceinline__ bool cell_is_cloudy(const Smem& s, int lay, int g) {
-  const unsigned bit = 1u << (g & 31);
-  return ((s.cbits[lay * 5 + (g >> 5)] | s.fbits[lay * 5 + (g >> 5)]) & bit) != 0u;
+// radius checks of cldprmc (cldprmc.f90:217-266): the code it stops with for
+// ice radius `rice` (iceflag) and liquid radius `rliq` (liqflag)
+__device__ __forceinline__ int ice_code(int iceflag, double rice) {
+  if (iceflag == 0 && rice < 10.0) return GB_COL_ICE_SMALL;
+  if (iceflag == 1 && (rice < 13.0 || rice > 130.0)) return GB_COL_ICE_BOUNDS;
+  if (iceflag == 2 && (rice < 5.0 || rice > 131.0)) return GB_COL_ICE_BOUNDS;
+  if (iceflag == 3 && (rice < 5.0 || rice > 140.0)) return GB_COL_DGE_BOUNDS;
+  return 0;
+}
+__device__ __forceinline__ int liq_code(int liqflag, double rliq) {
+  return liqflag == 1 && (rliq < 2.5 || rliq > 60.0) ? GB_COL_LIQ_BOUNDS : 0;
 }
 
-// Transfer coefficients of one cell (rtrnmc.f90:350-455 rearranged): the
-// clear-sky stream uses radiance*T + S (S = bbd*atrans down, bbugas*atrans
-// up); a cloudy cell uses radiance*A + Bd (down) / + Bu (up) and scales the
-// surface-temperature derivative by D.
-struct CellCoef {
-  float4 clr;  // T, Sd, Su, 0
-  float4 cld;  // A, Bd, Bu, D
-};
-__device__ __forceinline__ CellCoef cell_coef(bool cloudy, float odepth, float odcld, float efcl, float cldf,
-                                              float plfrac, float blay, float dplankup, float dplankdn) {
-  const float rec_6 = 0.166667f;
-  CellCoef r;
-  float atrans, bbd, bbu, tau_q;
-  if (odepth <= 0.06f) {
-    atrans = fmaf(-0.5f * odepth, odepth, odepth);
-    float o = rec_6 * odepth;
-    bbd = plfrac * fmaf(dplankdn, o, blay);
-    bbu = plfrac * fmaf(dplankup, o, blay);
-    tau_q = odepth;
-  } else {
-    TblEntry e = tbl(odepth);
-    atrans = 1.0f - e.trans;
-    bbd = plfrac * fmaf(e.tfn, dplankdn, blay);
-    bbu = plfrac * fmaf(e.tfn, dplankup, blay);
-    tau_q = e.tau;
-  }
-  const float gsd = bbd * atrans, gsu = bbu * atrans;
-  r.clr = make_float4(1.0f - atrans, gsd, gsu, 0.0f);
-  if (cloudy) {
-    float atot, bbdtot, bbutot;
-    float odtot = odepth + odcld;
-    if (odtot < 0.06f) {
-      atot = fmaf(-0.5f * odtot, odtot, odtot);
-      float o = rec_6 * odtot;
-      bbdtot = plfrac * fmaf(dplankdn, o, blay);
-      bbutot = plfrac * fmaf(dplankup, o, blay);
-    } else {
-      // odepth <= 0.06: table at odepth + odcld; otherwise at tau_tbl(itgas) + odcld
-      TblEntry et = tbl((odepth <= 0.06f ? odepth : tau_q) + odcld);
-      atot = 1.0f - et.trans;
-      bbdtot = plfrac * fmaf(et.tfn, dplankdn, blay);
-      bbutot = plfrac * fmaf(et.tfn, dplankup, blay);
-    }
-    float A = 1.0f - fmaf(efcl, 1.0f - atrans, atrans);
-    float Bd = fmaf(cldf, fmaf(bbdtot, atot, -gsd), gsd);
-    float Bu = fmaf(cldf, fmaf(bbutot, atot, -gsu), gsu);
-    float D = fmaf(cldf, 1.0f - atot, (1.0f - cldf) * (1.0f - atrans));
-    r.cld = make_float4(A, Bd, Bu, D);
-  } else {
-    r.cld = r.clr;
-  }
-  return r;
-}
-
-// Prologue of band b for one layer: the band-specific per-layer code
-// (lw_gasoptics.cuh) writing the layer's terms and Planck-fraction record.
-template <int b>
-__device__ __forceinline__ void band_prologue(const Smem& s, int nl, int lay, bool lower, int slot) {
-  Cell c{s.f, s.iv, nl, lay};
-  Terms t{s.terms + (size_t)c_toff[b] * nl + lay, nl, 0};
-  FracRec r = prologue<b>(c, lower, t);
-  t.pad(maxt(b), c_T.band[b - 1].sr);
-  s.frec[slot * nl + lay] = r;
-}
-
-__device__ __noinline__ void prologue_dispatch(int b, const Smem& s, int nl, int lay, bool lower, int slot) {
-  switch (b) {
-    case 1: band_prologue<1>(s, nl, lay, lower, slot); break;
-    case 2: band_prologue<2>(s, nl, lay, lower, slot); break;
-    case 3: band_prologue<3>(s, nl, lay, lower, slot); break;
-    case 4: band_prologue<4>(s, nl, lay, lower, slot); break;
-    case 5: band_prologue<5>(s, nl, lay, lower, slot); break;
-    case 6: band_prologue<6>(s, nl, lay, lower, slot); break;
-    case 7: band_prologue<7>(s, nl, lay, lower, slot); break;
-    case 8: band_prologue<8>(s, nl, lay, lower, slot); break;
-    case 9: band_prologue<9>(s, nl, lay, lower, slot); break;
-    case 10: band_prologue<10>(s, nl, lay, lower, slot); break;
-    case 11: band_prologue<11>(s, nl, lay, lower, slot); break;
-    case 12: band_prologue<12>(s, nl, lay, lower, slot); break;
-    case 13: band_prologue<13>(s, nl, lay, lower, slot); break;
-    case 14: band_prologue<14>(s, nl, lay, lower, slot); break;
-    case 15: band_prologue<15>(s, nl, lay, lower, slot); break;
-    default: band_prologue<16>(s, nl, lay, lower, slot); break;
-  }
-}
-
-// Scratch slot of a column (2*nl*140 float4): the clear-sky coefficients as
-// three float planes [nl][140] -- T, Sd, Su -- from the start (the downward
-// sweep reads T and Sd, the upward one T and Su: 8 bytes a cell each), then
-// from float4 offset nl*140 the cloudy-layer coefficients float4 [nl][140]
-// (A, Bd, Bu, D), written and read only for cloudy cells.
-__device__ __forceinline__ void put_coef(float4* __restrict__ scr, int nl, int lay, int g, const CellCoef& cc,
-                                         bool cloudy) {
-  const int i = lay * GB_NGPT + g;
-  float* pl = reinterpret_cast<float*>(scr);
-  pl[i] = cc.clr.x;
-  pl[nl * GB_NGPT + i] = cc.clr.y;
-  pl[2 * nl * GB_NGPT + i] = cc.clr.z;
-  if (cloudy) scr[nl * GB_NGPT + i] = cc.cld;
-}
-
-// All (band, layer) prologues of group gr, spread over the block's threads.
-template <int NT>
-__device__ __forceinline__ void group_prologues(int gr, const Smem& s, int nl, int laytrop) {
-  const int b0 = c_gfirst[gr], nb = c_gfirst[gr + 1] - b0;
-  for (int it = threadIdx.x; it < nb * nl; it += NT) {
-    const int slot = it / nl, lay = it - slot * nl;
-    if (!s.surok[lay]) prologue_dispatch(b0 + slot, s, nl, lay, lay < laytrop, slot);
-  }
-}
-
-// One thread per (band, layer, g) cell of group gr: optical depth, Planck
-// fraction and transfer coefficients into the scratch slot.
-template <int NT>
-__device__ __forceinline__ void group_cells(int gr, const LwArgs& a, const Smem& s, int nl, int laytrop,
-                                            const float* __restrict__ T, long long icol, float4* __restrict__ scr) {
-  const int b0 = c_gfirst[gr], b1 = c_gfirst[gr + 1];
-  int ncell = 0;
-  for (int b = b0; b < b1; ++b) ncell += nl * c_T.band[b - 1].ng;
-  const bool clouds = a.icld >= 1;
-  for (int cell = threadIdx.x; cell < ncell; cell += NT) {
-    int b = b0, c = cell, NG = c_T.band[b0 - 1].ng;
-    while (c >= nl * NG) {
-      c -= nl * NG;
-      ++b;
-      NG = c_T.band[b - 1].ng;
-    }
-    const int slot = b - b0;
-    const int lay = (int)(((float)c + 0.5f) * __frcp_rn((float)NG)), gi = c - lay * NG, g = c_T.band[b - 1].g0 + gi;
-    float taut, plfrac;
-    if (s.surok[lay]) {  // learned gas optics
-      const long long o = (icol * nl + lay) * GB_NGPT + g;
-      taut = __half2float(__ldg(a.sur_tau + o)) + s.taua[(b - 1) * nl + lay];
-      plfrac = __half2float(__ldg(a.sur_frac + o));
-    } else {
-      const int M = c_maxt[b];
-      const float2* tp = s.terms + (size_t)c_toff[b] * nl + lay;
-      const float* Tg = T + gi;
-      float acc = 0.0f;
-      for (int k = 0; k < M; ++k) {
-        const float2 w = tp[k * nl];
-        acc = fmaf(w.x, __ldg(Tg + __float_as_int(w.y)), acc);
-      }
-      if ((b == 4 || b == 7) && lay >= laytrop) acc *= gscale(b, gi);
-      taut = acc + s.taua[(b - 1) * nl + lay];
-      const FracRec fr = s.frec[slot * nl + lay];
-      const float* fp = T + fr.off + gi;
-      const float f0 = __ldg(fp);
-      plfrac = fmaf(fr.fpl, __ldg(fp + NG) - f0, f0);
-    }
-    if (lay == 0) s.frac1[g] = plfrac;
-    if (a.dbg_taut) {
-      a.dbg_taut[(icol * nl + lay) * GB_NGPT + g] = taut;
-      a.dbg_fracs[(icol * nl + lay) * GB_NGPT + g] = plfrac;
-    }
-    const float secdiff = s.misc[b - 1];
-    const float blay = s.plk_lay[(b - 1) * nl + lay];
-    const float dplankup = s.plk_lev[(b - 1) * (nl + 1) + lay + 1] - blay;
-    const float dplankdn = s.plk_lev[(b - 1) * (nl + 1) + lay] - blay;
-    const float odepth = fmaxf(secdiff * taut, 0.0f);
-    bool cloudy = false;
-    float odcld = 0.0f, efcl = 0.0f, cldf = 0.0f;
-    if (clouds && s.cldlay[lay]) {
-      cldf = cell_cloud(a, s, icol, g, lay, secdiff, b - 1, T, odcld, efcl);
-      cloudy = cell_is_cloudy(s, lay, g);
-    }
-    CellCoef cc = cell_coef(cloudy, odepth, odcld, efcl, cldf, plfrac, blay, dplankup, dplankdn);
-    put_coef(scr, nl, lay, g, cc, cloudy);
-  }
-}
-
-// Every layer with learned gas optics: one thread per (layer, g) cell of the
-// whole column, no band passes (cells of group_cells without the gather).
-template <int NT>
-__device__ __forceinline__ void learned_cells(const LwArgs& a, const Smem& s, int nl, const float* __restrict__ T,
-                                              long long icol, float4* __restrict__ scr) {
-  const bool clouds = a.icld >= 1;
-  const __half* __restrict__ st = a.sur_tau + icol * nl * GB_NGPT;
-  const __half* __restrict__ sf = a.sur_frac + icol * nl * GB_NGPT;
-  for (int cell = threadIdx.x; cell < nl * GB_NGPT; cell += NT) {
-    const int lay = (int)(((float)cell + 0.5f) * (1.0f / GB_NGPT)), g = cell - lay * GB_NGPT;
-    const int b = c_T.ngb[g] - 1;
-    const float taut = __half2float(__ldg(st + cell)) + s.taua[b * nl + lay];
-    const float plfrac = __half2float(__ldg(sf + cell));
-    if (lay == 0) s.frac1[g] = plfrac;
-    if (a.dbg_taut) {
-      a.dbg_taut[(icol * nl + lay) * GB_NGPT + g] = taut;
-      a.dbg_fracs[(icol * nl + lay) * GB_NGPT + g] = plfrac;
-    }
-    const float secdiff = s.misc[b];
-    const float blay = s.plk_lay[b * nl + lay];
-    const float dplankup = s.plk_lev[b * (nl + 1) + lay + 1] - blay;
-    const float dplankdn = s.plk_lev[b * (nl + 1) + lay] - blay;
-    const float odepth = fmaxf(secdiff * taut, 0.0f);
-    bool cloudy = false;
-    float odcld = 0.0f, efcl = 0.0f, cldf = 0.0f;
-    if (clouds && s.cldlay[lay]) {
-      cldf = cell_cloud(a, s, icol, g, lay, secdiff, b, T, odcld, efcl);
-      cloudy = cell_is_cloudy(s, lay, g);
-    }
-    CellCoef cc = cell_coef(cloudy, odepth, odcld, efcl, cldf, plfrac, blay, dplankup, dplankdn);
-    put_coef(scr, nl, lay, g, cc, cloudy);
-  }
-}
-
-// ------------------------------------------------------------------ one column
-// LEAN: the learned-only flavour -- a column with any layer off the network
-// is not solved (returns false, the same answer in every thread) and the
-// taumol code is not compiled in.
-template <int NT, bool LEAN>
-__device__ __forceinline__ bool solve_column(const LwArgs& a, long long icol, char* smem_raw,
-                                             float4* __restrict__ scr, const float* __restrict__ T) {
-  constexpr int NWARP = NT / 32;
+// The transfer of one column by the block (see the file header).  RT_NET: a
+// column with any layer off the network is not solved (returns false in
+// every thread).  Ends with a barrier.
+template <int MODE>
+__device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, const GasSrc& src,
+                          const float* __restrict__ T) {
+  const unsigned FULL = 0xffffffffu;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nl = a.nlay;
-  const Smem s = carve(smem_raw, nl, LEAN);
-  const int tid = threadIdx.x;
   const bool fused = a.cloud_mode == LW_CLOUD_FUSED;
-  {
-    // fused clouds: the column's 140 draws, made beforehand by a parallel
-    // kernel or else here by one thread of the last warp
-    if (fused && a.icld >= 1) {
-      if (a.draws) {
-        for (int g = tid; g < GB_NGPT; g += NT) s.cdf[g] = __ldg(a.draws + icol * GB_NGPT + g);
-      } else if (tid == NT - 1) {
-        gbmt::first_reals(a.seed0 + (unsigned)icol, GB_NGPT, s.mtlo, s.cdf, 1);
-      }
-    }
-    if (tid < 4) {
-      s.scal[tid] = 0.0f;
-      s.iscal[tid] = 0;
-    }
-    int offnet = 0;
-    for (int l = tid; l < nl; l += NT) {
-      s.cldlay[l] = 0;
-      s.surok[l] = a.sur_flag ? (int)__ldg(a.sur_flag + icol * nl + l) : 0;
-      offnet |= !s.surok[l];
-    }
-    for (int l = tid; l < nl * 5; l += NT) s.cbits[l] = s.fbits[l] = 0u;
-    if (LEAN) {
-      if (__syncthreads_or(offnet)) return false;
-    } else {
-      __syncthreads();
-    }
+  const bool clouds = a.icld >= 1;
+  if (MODE == RT_NET) {
+    int off = src.flag == nullptr;
+    for (int l = tid; l < nl && !off; l += RT_NT) off = src.flag[l] == 0;
+    if (__syncthreads_or(off)) return false;
+  }
+  if (tid < 4) S.h->iscal[tid] = 0;
+  // this thread's g-point
+  const bool live = tid < GB_NGPT;
+  const int g = live ? tid : GB_NGPT - 1;
+  const int band = c_T.ngb[g] - 1;
+  const float wgt = live ? (float)(0.5 * (double)c_T.delwave[band] * c_T.fluxfac) : 0.0f;
+  __syncthreads();
 
-    // ---------------- phase 1: inatm + setcoef, one thread per layer
-    const float stpfac = 296.0f / 1013.0f;
-    const float amd = 28.9660f, amw = 18.0160f;
-    int my_bad = 0;
-    for (int lay = tid; lay < nl; lay += NT) {
-      double pd = in2(a.play, a.ld, icol, lay);
-      float pavel = (float)pd;
-      float tavel = (float)in2(a.tlay, a.ld, icol, lay);
-      double dpz = in2(a.plev, a.ld, icol, lay) - in2(a.plev, a.ld, icol, lay + 1);
-      float w1 = (float)in2(a.h2ovmr, a.ld, icol, lay);
-      if (LEAN || s.surok[lay]) {
-        // learned gas optics: only what pwvcm and the checks need (inatm :807-870)
-        const float amm = (1.0f - w1) * amd + w1 * amw;
-        const float coldry = (float)dpz * 1.e3f * (float)c_T.avogad / (1.e2f * (float)c_T.grav * amm * (1.0f + w1));
-        s.f[F_COLDRY * nl + lay] = coldry;
-        s.f[F_COLH2O * nl + lay] = 1.e-20f * (coldry * w1);  // as colh2o = 1e-20 * wk1 below
-        if (!(pavel > 0.0f) || !(tavel > 0.0f) || !isfinite(pavel) || !isfinite(tavel)) my_bad = 1;
-        const float plog = __logf(pavel);
-        bool lower = plog > 4.56f;
-        if (fabsf(plog - 4.56f) < 1.0e-4f) lower = log(pd) > 4.56;
-        if (lower) {
-          atomicAdd(&s.iscal[0], 1);
-          atomicAdd(&s.iscal[1], lay + 1);
-        }
-        continue;
-      }
-      float w2 = (float)in2(a.co2vmr, a.ld, icol, lay);
-      float w3 = (float)in2(a.o3vmr, a.ld, icol, lay);
-      float w4 = (float)in2(a.n2ovmr, a.ld, icol, lay);
-      float w6 = (float)in2(a.ch4vmr, a.ld, icol, lay);
-      float w7 = (float)in2(a.o2vmr, a.ld, icol, lay);
-      float amm = (1.0f - w1) * amd + w1 * amw;
-      float coldry = (float)dpz * 1.e3f * (float)c_T.avogad / (1.e2f * (float)c_T.grav * amm * (1.0f + w1));
-      float summol = w2 + w3 + w4 + 0.0f + w6 + w7;
-      float wbrodl = coldry * (1.0f - summol);
-      float wk1 = coldry * w1, wk2 = coldry * w2, wk3 = coldry * w3, wk4 = coldry * w4, wk6 = coldry * w6,
-            wk7 = coldry * w7;
-      float* F = s.f;
-      auto put = [&](int k, float v) { F[k * nl + lay] = v; };
-      put(F_COLDRY, coldry);
-      put(F_PAVEL, pavel);
-      put(F_WX1, coldry * (float)in2(a.ccl4vmr, a.ld, icol, lay) * 1.e-20f);
-      put(F_WX2, coldry * (float)in2(a.cfc11vmr, a.ld, icol, lay) * 1.e-20f);
-      put(F_WX3, coldry * (float)in2(a.cfc12vmr, a.ld, icol, lay) * 1.e-20f);
-      put(F_WX4, coldry * (float)in2(a.cfc22vmr, a.ld, icol, lay) * 1.e-20f);
-      if (!(pavel > 0.0f) || !(tavel > 0.0f) || !isfinite(pavel) || !isfinite(tavel)) my_bad = 1;
-      // setcoef (rrtmg_lw_setcoef.f90:275-430)
-      float plog = __logf(pavel);
-      bool lower = plog > 4.56f;
-      if (fabsf(plog - 4.56f) < 1.0e-4f) lower = log(pd) > 4.56;  // decide the regime in fp64 near the switch
-      int jp = clampi((int)(36.0f - 5.0f * (plog + 0.04f)), 1, 58);
-      jp = lower ? (jp > 12 ? 12 : jp) : (jp < 13 ? 13 : jp);
-      float fp = 5.0f * (c_T.preflog[jp - 1] - plog);
-      float dt0 = (tavel - c_T.tref[jp - 1]) / 15.0f;
-      int jt = clampi((int)(3.0f + dt0), 1, 4);
-      float ft = dt0 - (float)(jt - 3);
-      float dt1 = (tavel - c_T.tref[jp]) / 15.0f;
-      int jt1 = clampi((int)(3.0f + dt1), 1, 4);
-      float ft1 = dt1 - (float)(jt1 - 3);
-      float water = wk1 / coldry;
-      float scalefac = pavel * stpfac / tavel;
-      float forfac = scalefac / (1.0f + water), forfrac, selffrac = 0.0f;
-      int indfor, indself = 1;
-      if (lower) {
-        float factor = (332.0f - tavel) / 36.0f;
-        indfor = min(2, max(1, (int)factor));
-        forfrac = factor - (float)indfor;
-        factor = (tavel - 188.0f) / 7.2f;
-        indself = min(9, max(1, (int)factor - 7));
-        selffrac = factor - (float)(indself + 7);
-      } else {
-        float factor = (tavel - 188.0f) / 36.0f;
-        indfor = 3;
-        forfrac = factor - 1.0f;
-      }
-      float selffac = water * forfac;
-      float scaleminor = pavel / tavel;
-      float scaleminorn2 = scaleminor * (wbrodl / (coldry + wk1));
-      float factor = (tavel - 180.8f) / 7.2f;
-      int indminor = min(18, max(1, (int)factor));
-      float minorfrac = factor - (float)indminor;
-      float colh2o = 1.e-20f * wk1;
-      float colco2 = 1.e-20f * wk2, colo3 = 1.e-20f * wk3, coln2o = 1.e-20f * wk4, colco = 0.0f;
-      float colch4 = 1.e-20f * wk6, colo2 = 1.e-20f * wk7;
-      if (colco2 == 0.0f) colco2 = 1.e-32f * coldry;
-      if (colo3 == 0.0f) colo3 = 1.e-32f * coldry;
-      if (coln2o == 0.0f) coln2o = 1.e-32f * coldry;
-      if (colco == 0.0f) colco = 1.e-32f * coldry;
-      if (colch4 == 0.0f) colch4 = 1.e-32f * coldry;
-      float compfp = 1.0f - fp;
-      put(F_FAC10, compfp * ft);
-      put(F_FAC00, compfp * (1.0f - ft));
-      put(F_FAC11, fp * ft1);
-      put(F_FAC01, fp * (1.0f - ft1));
-      put(F_COLH2O, colh2o); put(F_COLCO2, colco2); put(F_COLO3, colo3); put(F_COLN2O, coln2o);
-      put(F_COLCO, colco); put(F_COLCH4, colch4); put(F_COLO2, colo2); put(F_COLBRD, 1.e-20f * wbrodl);
-      put(F_SELFFAC, colh2o * selffac); put(F_SELFFRAC, selffrac);
-      put(F_FORFAC, colh2o * forfac); put(F_FORFRAC, forfrac);
-      put(F_MINORFRAC, minorfrac); put(F_SCALEMINOR, scaleminor); put(F_SCALEMINORN2, scaleminorn2);
-      int* IV = s.iv;
-      IV[I_JP * nl + lay] = jp; IV[I_JT * nl + lay] = jt; IV[I_JT1 * nl + lay] = jt1;
-      IV[I_INDSELF * nl + lay] = indself; IV[I_INDFOR * nl + lay] = indfor; IV[I_INDMINOR * nl + lay] = indminor;
-      // lower layers must form the prefix 0..laytrop-1
-      if (lower) {
-        atomicAdd(&s.iscal[0], 1);        // laytrop
-        atomicAdd(&s.iscal[1], lay + 1);  // sum of 1-based indices of lower layers
-      }
-    }
-    // aerosol optical depths (rrtmg_lw_rad.f90:548-553), all threads
-    for (int it = tid; it < 16 * nl; it += NT) {
-      const int ib = it / nl, lay = it - ib * nl;
-      s.taua[it] = (float)__ldg(a.tauaer + icol + (long long)a.ld * (lay + (long long)nl * ib));
-    }
-    // Planck interpolation per (level, band) (setcoef.f90:173-269, istart = 1):
-    // table row and fraction once per level (one fp64 conversion each), then
-    // one thread per (level, band)
-    for (int lev = tid; lev <= nl; lev += NT) {
-      const float tz = (float)in2(a.tlev, a.ld, icol, lev);
-      const int ind = clampi((int)(tz - 159.0f), 1, 180);
-      float4 r = make_float4(__int_as_float(ind), tz - 159.0f - (float)ind, 0.0f, 0.0f);
-      if (lev < nl) {
-        const float tl = (float)in2(a.tlay, a.ld, icol, lev);
-        const int il = clampi((int)(tl - 159.0f), 1, 180);
-        r.z = __int_as_float(il);
-        r.w = tl - 159.0f - (float)il;
-      }
-      s.prow[lev] = r;
-    }
-    __syncthreads();
-    for (int it = tid; it < (nl + 1) * 16; it += NT) {
-      int lev = it >> 4, ib = it & 15;
-      const float* tp = T + c_T.totplnk + ib * 181;
-      const float4 r = s.prow[lev];
-      const int ind = __float_as_int(r.x);
-      s.plk_lev[ib * (nl + 1) + lev] = tp[ind - 1] + r.y * (tp[ind] - tp[ind - 1]);
-      if (lev < nl) {
-        const int il = __float_as_int(r.z);
-        s.plk_lay[ib * nl + lev] = tp[il - 1] + r.w * (tp[il] - tp[il - 1]);
-      }
-    }
-    if (tid < 16) {
-      float tb = (float)__ldg(a.tsfc + icol);
-      int ind = clampi((int)(tb - 159.0f), 1, 180);
-      float fr = tb - 159.0f - (float)ind;
-      float se = (float)__ldg(a.emis + icol + (long long)a.ld * tid);
-      const float* tp = T + c_T.totplnk + tid * 181;
-      const float* td = T + c_T.totplnkderiv + tid * 181;
-      s.misc[16 + tid] = se * (tp[ind - 1] + fr * (tp[ind] - tp[ind - 1]));
-      s.misc[32 + tid] = se * (td[ind - 1] + fr * (td[ind] - td[ind - 1]));
-      s.misc[48 + tid] = se;
-    }
-    // McICA pre-pass over every (layer, g) cell: cloudy layers, the per-cell
-    // "cldfmc == 1" / "cldfmc neither 0 nor 1" bits the later phases use to
-    // skip loads, and cldprmc's STOP conditions.
-    if (a.icld >= 1 && fused) {
-      // per layer, once: the McICA threshold and the layer's cloud
-      // quantities (fp64 comparisons here rather than per cell or band)
-      for (int lay = tid; lay < nl; lay += NT) {
-        double cf = in2(a.cldfrac, a.ld, icol, lay);
-        cf = cf < 1.0e-20 ? 0.0 : cf;  // mcica_subcol_gen_lw.f90:463-470
-        // cdf >= 1 - cf, compared on the bit patterns (cdf is in [0, 1], so
-        // for a threshold >= 0 the integer order is the floating-point order);
-        // a negative threshold takes every cell, a NaN none
-        const double thr = 1.0 - cf;
-        s.cthr[lay] = thr < 0.0 ? LLONG_MIN : (thr == thr ? __double_as_longlong(thr) : LLONG_MAX);
-        const double ciwp = in2(a.ciwp, a.ld, icol, lay), clwp = in2(a.clwp, a.ld, icol, lay);
-        const double rice = in2(a.reicmcl, a.ld, icol, lay), rliq = in2(a.relqmcl, a.ld, icol, lay);
-        int fl = (ciwp != 0.0 ? 1 : 0) | (clwp != 0.0 ? 2 : 0) | (ciwp + clwp >= 1.e-20 ? 4 : 0);
-        // the code cldprmc.f90:217-266 stops with for this layer's radii (inflag 2)
-        int e = 0;
-        if (ciwp != 0.0) {
-          if (a.iceflag == 0 && rice < 10.0) e = GB_COL_ICE_SMALL;
-          if (a.iceflag == 1 && (rice < 13.0 || rice > 130.0)) e = GB_COL_ICE_BOUNDS;
-          if (a.iceflag == 2 && (rice < 5.0 || rice > 131.0)) e = GB_COL_ICE_BOUNDS;
-          if (a.iceflag == 3 && (rice < 5.0 || rice > 140.0)) e = GB_COL_DGE_BOUNDS;
-        }
-        if (clwp != 0.0 && a.liqflag == 1 && (rliq < 2.5 || rliq > 60.0)) e = GB_COL_LIQ_BOUNDS;
-        s.lfl[lay] = fl | (e << 8);
-        s.lcw[lay] = make_float4((float)ciwp, (float)clwp, (float)rice, (float)rliq);
-      }
-      __syncthreads();  // draws and layer data ready
-      // cloudy cells: cdf(g) >= 1 - cldf(lay) (mcica_subcol_gen_lw.f90:650), one warp per layer
-      const int warp = tid >> 5, lane = tid & 31;
-      const long long* cdfb = reinterpret_cast<const long long*>(s.cdf);
-      for (int lay = warp; lay < nl; lay += NWARP) {
-        const long long tb = s.cthr[lay];
-        unsigned any = 0u;
-#pragma unroll
-        for (int w = 0; w < 5; ++w) {
-          const int g = w * 32 + lane;
-          const bool cl = g < GB_NGPT && cdfb[g] >= tb;
-          const unsigned m = __ballot_sync(0xffffffffu, cl);
-          if (lane == 0) s.cbits[lay * 5 + w] = m;
-          any |= m;
-        }
-        if (lane == 0) s.cldlay[lay] = any != 0u;
-      }
-      __syncthreads();
-      // cloud optical depth per (layer, band) where the band has a cloudy
-      // sub-column (the values cldprmc computes for every such cell), and
-      // cldprmc's STOP conditions
-      const long long kMin = __double_as_longlong(1.0e-20), kInf = 0x7FF0000000000000LL;
-      int err = 0;
-      for (int it = tid; it < nl * 16; it += NT) {
-        const int lay = it >> 4, band = it & 15;
-        if (!s.cldlay[lay]) continue;
-        const int g0 = c_T.band[band].g0, ng = c_T.band[band].ng;
-        bool any = false;
-        for (int g = g0; g < g0 + ng; ++g) any |= (s.cbits[lay * 5 + (g >> 5)] >> (g & 31)) & 1u;
-        if (!any) continue;
-        const double tin = __ldg(a.tauc + band + 16 * (icol + a.ld * lay));
-        const long long tinb = __double_as_longlong(tin);
-        const bool tin_ok = tinb >= kMin && tinb <= kInf;  // tin >= 1e-20
-        const int fl = s.lfl[lay];
-        const bool cond = (fl & 4) || tin_ok;
-        s.tcl[lay * 16 + band] = a.inflag == 2 && cond ? cloud_tau_layer(a, band, T, s.lcw[lay], fl) : (float)tin;
-        if (cond) {
-          if (a.inflag == 1) err = GB_COL_INFLAG1;
-          if (a.inflag == 2 && (fl >> 8)) err = fl >> 8;
-        }
-      }
-      if (err) atomicMax(&s.iscal[2], err);
-    } else if (a.icld >= 1) {
-      // per layer, once: the particle radii as floats and the codes cldprmc's
-      // radius checks stop with (cldprmc.f90:217-266): bits 0-7 ice, 8-15 liquid
-      for (int lay = tid; lay < nl; lay += NT) {
-        const double rice = in2(a.reicmcl, a.ld, icol, lay), rliq = in2(a.relqmcl, a.ld, icol, lay);
-        int ei = 0;
-        if (a.iceflag == 0 && rice < 10.0) ei = GB_COL_ICE_SMALL;
-        if (a.iceflag == 1 && (rice < 13.0 || rice > 130.0)) ei = GB_COL_ICE_BOUNDS;
-        if (a.iceflag == 2 && (rice < 5.0 || rice > 131.0)) ei = GB_COL_ICE_BOUNDS;
-        if (a.iceflag == 3 && (rice < 5.0 || rice > 140.0)) ei = GB_COL_DGE_BOUNDS;
-        const int el = a.liqflag == 1 && (rliq < 2.5 || rliq > 60.0) ? GB_COL_LIQ_BOUNDS : 0;
-        s.lfl[lay] = ei | (el << 8);
-        s.lcw[lay] = make_float4(0.0f, 0.0f, (float)rice, (float)rliq);
-      }
-      __syncthreads();
-      // one warp per layer: the layer's 140 cldfmcl values tested on their bit
-      // patterns (no fp64 pipe): == 1, /= 0, >= 1e-20
-      const int warp = tid >> 5, lane = tid & 31;
-      const long long kOne = 0x3FF0000000000000LL, kInf = 0x7FF0000000000000LL;
-      const long long kMin = __double_as_longlong(1.0e-20);
-      int err = 0;
-      for (int lay = warp; lay < nl; lay += NWARP) {
-        const long long base = GB_NGPT * (icol + (long long)a.ld * lay);
-        long long cb[5];
-#pragma unroll
-        for (int w = 0; w < 5; ++w) {
-          const int g = w * 32 + lane;
-          cb[w] = g < GB_NGPT ? __double_as_longlong(__ldg(a.cldfmcl + base + g)) : 0LL;
-        }
-        unsigned any = 0u;
-#pragma unroll
-        for (int w = 0; w < 5; ++w) {
-          const bool one = cb[w] == kOne;
-          const bool frac = !one && (cb[w] << 1) != 0LL;  // neither +-0 nor 1 (NaN included, as /= 0 is)
-          const unsigned m1 = __ballot_sync(0xffffffffu, one), mf = __ballot_sync(0xffffffffu, frac);
-          if (lane == 0) {
-            s.cbits[lay * 5 + w] = m1;
-            s.fbits[lay * 5 + w] = mf;
-          }
-          any |= m1;
-          if (cb[w] >= kMin && cb[w] <= kInf) {  // cldfmc >= cldmin (cldprmc.f90:178)
-            const long long o = base + w * 32 + lane;
-            const double ciwp = __ldg(a.ciwpmcl + o), clwp = __ldg(a.clwpmcl + o);
-            const long long tb = __double_as_longlong(__ldg(a.taucmcl + o));
-            if (ciwp + clwp >= 1.e-20 || (tb >= kMin && tb <= kInf)) {
-              if (a.inflag == 1) err = GB_COL_INFLAG1;
-              if (a.inflag == 2) {
-                const int e = s.lfl[lay];
-                if ((__double_as_longlong(ciwp) << 1) != 0LL && (e & 0xff)) err = e & 0xff;  // ciwp /= 0
-                if ((__double_as_longlong(clwp) << 1) != 0LL && (e >> 8)) err = e >> 8;      // clwp /= 0
-              }
-            }
-          }
-        }
-        if (lane == 0) s.cldlay[lay] = any != 0u;
-      }
-      if (err) atomicMax(&s.iscal[2], err);
-    }
-    // learned gas optics for every layer of this column: one pass over all cells
-    const bool all_learned = LEAN || (a.sur_flag != nullptr && !__syncthreads_or(offnet));
-    int anybad = __syncthreads_or(my_bad);
-    const int laytrop = s.iscal[0];
-    if (tid < 32) {
-      if (tid == 0) {
-        int err = s.iscal[2];
-        // sum of 1-based indices of lower layers equals laytrop*(laytrop+1)/2 iff they form a prefix
-        if (s.iscal[1] != laytrop * (laytrop + 1) / 2) err = GB_COL_LAYTROP;
-        if (anybad) err = GB_COL_BADVAL;
-        s.iscal[3] = err;
-        if (err) {
-          if (a.col_err) a.col_err[icol] = err;
-          atomicMax(a.err_flag, err);
-        } else if (a.col_err) {
-          a.col_err[icol] = 0;
-        }
-      }
-      // pwvcm (inatm :859-870; a fixed-order warp sum over layers) and
-      // secdiff (rtrnmc.f90:258-266), one band per lane
-      float amttl = 0.0f, wvttl = 0.0f;
-      for (int l = tid; l < nl; l += 32) {
-        const float wk1 = s.f[F_COLH2O * nl + l] * 1.e20f;
-        amttl += s.f[F_COLDRY * nl + l] + wk1;
-        wvttl += wk1;
-      }
-      amttl = __shfl_sync(0xffffffffu, warp_sum(amttl), 0);
-      wvttl = __shfl_sync(0xffffffffu, warp_sum(wvttl), 0);
-      if (tid < 16) {
-        const int ib = tid;
-        const float wvsh = (amw * wvttl) / (amd * amttl);
-        const float pz0 = (float)in2(a.plev, a.ld, icol, 0);
-        const float pwvcm = wvsh * (1.e3f * pz0) / (1.e2f * (float)c_T.grav);
-        float sd = 1.66f;
-        if (!(ib == 0 || ib == 3 || ib >= 9)) {
-          sd = c_a0[ib] + c_a1[ib] * __expf(c_a2[ib] * pwvcm);
-          sd = fminf(fmaxf(sd, 1.50f), 1.80f);
-        }
-        s.misc[ib] = sd;
-      }
-    }
-    __syncthreads();
-    // ---------------- phase 2: gas optics and cell coefficients, band by band
-    if (all_learned) {
-      learned_cells<NT>(a, s, nl, T, icol, scr);
-      __syncthreads();
-    } else {  // taumol for every layer, or for the layers outside the network's range
-      for (int gr = 0; gr < NGROUP; ++gr) {
-        group_prologues<NT>(gr, s, nl, laytrop);
-        __syncthreads();
-        group_cells<NT>(gr, a, s, nl, laytrop, T, icol, scr);
-        __syncthreads();
-      }
-    }
-
-    // ---------------- phase 3: sweeps, one thread per g-point
-    if (tid < NSW * 32) {
-      const int warp = tid >> 5, lane = tid & 31;
-      const bool active = tid < GB_NGPT;
-      const int g = active ? tid : GB_NGPT - 1;
-      const int band = c_T.ngb[g] - 1;
-      const float wgt = active ? (float)(0.5 * (double)c_T.delwave[band] * c_T.fluxfac) : 0.0f;
-      const bool idrv = a.idrv == 1;
-      const bool clouds = a.icld >= 1;
-      float* part = s.part + warp * (nl + 1) * 6;  // this warp's [nl+1][6] partial sums
-      // Levels go in blocks of four: the block's scratch loads are issued
-      // together and each stream's four level sums take one reduce4.
-      // downward (rtrnmc.f90:347-455): total stream and clear-sky stream
-      float radld = 0.0f, radclrd = 0.0f;
-      for (int L0 = nl - 1; L0 >= 0; L0 -= 4) {
-        const int nb = L0 + 1 < 4 ? L0 + 1 : 4;  // levels L0, L0-1, .., L0-nb+1
-        float2 c[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int L = j < nb ? L0 - j : 0;  // an address inside the slot even where nothing is loaded
-          const float* pl = reinterpret_cast<const float*>(scr) + L * GB_NGPT + g;
-          c[j] = j < nb ? make_float2(pl[0], pl[nl * GB_NGPT]) : make_float2(0.f, 0.f);  // T, Sd
-        }
-        float q0[4], q1[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          q0[j] = q1[j] = 0.0f;
-          if (j < nb) {
-            const int L = L0 - j;
-            if (clouds && s.cldlay[L] && cell_is_cloudy(s, L, g)) {
-              const float4 k = scr[(nl + L) * GB_NGPT + g];
-              radld = fmaf(radld, k.x, k.y);
-            } else {
-              radld = fmaf(radld, c[j].x, c[j].y);
-            }
-            radclrd = fmaf(radclrd, c[j].x, c[j].y);
-            q0[j] = radld * wgt;
-            q1[j] = radclrd * wgt;
-          }
-        }
-        const float s0 = reduce4(q0, lane), s1 = reduce4(q1, lane);
-        if (lane < nb) {
-          part[(L0 - lane) * 6 + 0] = s0;
-          part[(L0 - lane) * 6 + 1] = s1;
-        }
-      }
-      // surface emission and reflection (rtrnmc.f90:465-485)
-      const float plfrac1 = s.frac1[g];
-      const float rad0 = plfrac1 * s.misc[16 + band];
-      const float reflect = 1.0f - s.misc[48 + band];
-      float radlu = rad0 + reflect * radld;
-      float radclru = rad0 + reflect * radclrd;
-      float d_radlu = plfrac1 * s.misc[32 + band], d_radclru = d_radlu;
-      // upward (rtrnmc.f90:486-529): level 0 is the surface, level L+1 follows layer L
-      for (int v0 = 0; v0 <= nl; v0 += 4) {
-        const int nb = nl + 1 - v0 < 4 ? nl + 1 - v0 : 4;  // levels v0 .. v0+nb-1
-        float2 c[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const bool in = j < nb && v0 + j >= 1;
-          const float* pl = reinterpret_cast<const float*>(scr) + (in ? v0 + j - 1 : 0) * GB_NGPT + g;
-          c[j] = in ? make_float2(pl[0], pl[2 * nl * GB_NGPT]) : make_float2(0.f, 0.f);  // T, Su
-        }
-        float u0[4], u1[4], u2[4], u3[4];
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          u0[j] = u1[j] = u2[j] = u3[j] = 0.0f;
-          if (j < nb) {
-            if (v0 + j >= 1) {
-              const int L = v0 + j - 1;
-              if (clouds && s.cldlay[L] && cell_is_cloudy(s, L, g)) {
-                const float4 k = scr[(nl + L) * GB_NGPT + g];
-                radlu = fmaf(radlu, k.x, k.z);
-                d_radlu *= k.w;
-              } else {
-                radlu = fmaf(radlu, c[j].x, c[j].y);
-                d_radlu *= c[j].x;
-              }
-              radclru = fmaf(radclru, c[j].x, c[j].y);
-              d_radclru *= c[j].x;
-            }
-            u0[j] = radlu * wgt;
-            u1[j] = radclru * wgt;
-            u2[j] = d_radlu * wgt;
-            u3[j] = d_radclru * wgt;
-          }
-        }
-        const float s0 = reduce4(u0, lane), s1 = reduce4(u1, lane);
-        float s2 = 0.0f, s3 = 0.0f;
-        if (idrv) {
-          s2 = reduce4(u2, lane);
-          s3 = reduce4(u3, lane);
-        }
-        if (lane < nb) {
-          float* p = part + (v0 + lane) * 6;
-          p[2] = s0;
-          p[3] = s1;
-          p[4] = s2;
-          p[5] = s3;
-        }
-      }
-    }
-    __syncthreads();
-
-    // ---------------- phase 4: fp64 sums, net fluxes, heating rates, stores
-    {
-      const long long ldo = a.ldo;
-      const bool idrv = a.idrv == 1;
-      for (int lev = tid; lev <= nl; lev += NT) {
-        // the five warps' fp32 partials summed without rounding error: Knuth's
-        // two-sum keeps each addition's rounding error, and the sum and the
-        // accumulated errors go to fp64 (two conversions instead of five
-        // conversions and four fp64 additions; fp64 is a narrow pipe on GB300)
-        double acc[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-          float hi = s.part[lev * 6 + k], lo = 0.0f;
-#pragma unroll
-          for (int w = 1; w < NSW; ++w) {
-            const float b = s.part[(w * (nl + 1) + lev) * 6 + k];
-            const float sum = hi + b, bv = sum - hi;
-            lo += (hi - (sum - bv)) + (b - bv);
-            hi = sum;
-          }
-          acc[k] = (double)hi + (double)lo;
-        }
-        if (lev == nl) acc[0] = acc[1] = 0.0;  // no downward radiation at the model top
-        long long o = icol + ldo * lev;
-        a.uflx[o] = acc[2];
-        a.dflx[o] = acc[0];
-        a.uflxc[o] = acc[3];
-        a.dflxc[o] = acc[1];
-        if (idrv) {
-          a.duflx_dt[o] = acc[4];
-          a.duflxc_dt[o] = acc[5];
-        }
-        s.fnet[lev * 2 + 0] = acc[2] - acc[0];
-        s.fnet[lev * 2 + 1] = acc[3] - acc[1];
-      }
-      __syncthreads();
-      for (int l = tid; l < nl; l += NT) {
-        const double dp = in2(a.plev, a.ld, icol, l) - in2(a.plev, a.ld, icol, l + 1);
-        const double f = c_T.heatfac / dp;  // one division for both heating rates
-        long long o = icol + ldo * l;
-        a.hr[o] = f * (s.fnet[l * 2] - s.fnet[(l + 1) * 2]);
-        a.hrc[o] = f * (s.fnet[l * 2 + 1] - s.fnet[(l + 1) * 2 + 1]);
-      }
-      __syncthreads();
+  // ---------------- per layer: inatm's column amounts (pwvcm), value checks, laytrop, Planck rows
+  const float amd = 28.9660f, amw = 18.0160f;
+  float amttl = 0.0f, wvttl = 0.0f;
+  int bad = 0;
+  float4* prow = reinterpret_cast<float4*>(S.part);
+  for (int lay = tid; lay < nl; lay += RT_NT) {
+    const double pd = in2(a.play, a.ld, icol, lay);
+    const float pavel = (float)pd;
+    const float tavel = (float)in2(a.tlay, a.ld, icol, lay);
+    const double dpz = in2(a.plev, a.ld, icol, lay) - in2(a.plev, a.ld, icol, lay + 1);
+    const float w1 = (float)in2(a.h2ovmr, a.ld, icol, lay);
+    const float tz = (float)in2(a.tlev, a.ld, icol, lay);
+    const float amm = (1.0f - w1) * amd + w1 * amw;
+    const float coldry = (float)dpz * 1.e3f * (float)c_T.avogad / (1.e2f * (float)c_T.grav * amm * (1.0f + w1));
+    const float wk1 = coldry * w1;
+    amttl += coldry + wk1;
+    wvttl += wk1;
+    if (!(pavel > 0.0f) || !(tavel > 0.0f) || !isfinite(pavel) || !isfinite(tavel)) bad = 1;
+    const bool lower = lower_atmosphere(pd, __logf(pavel));
+    S.L[lay].cldlay = lower;
+    if (lower) atomicAdd(&S.h->iscal[1], 1);
+    // Planck-table rows of the level below and of the layer (setcoef.f90:173-269)
+    const int ind = clampi((int)(tz - 159.0f), 1, 180);
+    const int il = clampi((int)(tavel - 159.0f), 1, 180);
+    prow[lay] = make_float4(__int_as_float(ind), tz - 159.0f - (float)ind, __int_as_float(il), tavel - 159.0f - (float)il);
+    if (lay == nl - 1) {
+      const float tt = (float)in2(a.tlev, a.ld, icol, nl);
+      const int it = clampi((int)(tt - 159.0f), 1, 180);
+      prow[nl] = make_float4(__int_as_float(it), tt - 159.0f - (float)it, 0.0f, 0.0f);
     }
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {  // fixed-order sums: within the warp, then over the warps in order
+    amttl += __shfl_xor_sync(FULL, amttl, o);
+    wvttl += __shfl_xor_sync(FULL, wvttl, o);
+  }
+  if (lane == 0) {
+    S.h->red[2 * warp] = amttl;
+    S.h->red[2 * warp + 1] = wvttl;
+  }
+  bad = __syncthreads_or(bad);
+  // lower-atmosphere layers must form the prefix 0 .. laytrop-1
+  const int laytrop = S.h->iscal[1];
+  int notpre = 0;
+  for (int lay = tid; lay < nl; lay += RT_NT) notpre |= S.L[lay].cldlay != (lay < laytrop ? 1 : 0);
+  if (tid < 16) {
+    // pwvcm (inatm :869-870) and secdiff (rtrnmc.f90:258-266), one band per thread
+    const int ib = tid;
+    float at = S.h->red[0], wt = S.h->red[1];
+    for (int w = 1; w < RT_NW; ++w) {
+      at += S.h->red[2 * w];
+      wt += S.h->red[2 * w + 1];
+    }
+    const float wvsh = (amw * wt) / (amd * at);
+    const float pz0 = (float)in2(a.plev, a.ld, icol, 0);
+    const float pwvcm = wvsh * (1.e3f * pz0) / (1.e2f * (float)c_T.grav);
+    float sd = 1.66f;
+    if (!(ib == 0 || ib == 3 || ib >= 9)) {
+      sd = c_a0[ib] + c_a1[ib] * __expf(c_a2[ib] * pwvcm);
+      sd = fminf(fmaxf(sd, 1.50f), 1.80f);
+    }
+    S.h->misc[ib] = sd;
+    // surface source and its temperature derivative (setcoef.f90:270-282)
+    const float tb = (float)__ldg(a.tsfc + icol);
+    const int ind = clampi((int)(tb - 159.0f), 1, 180);
+    const float fr = tb - 159.0f - (float)ind;
+    const float se = (float)__ldg(a.emis + icol + a.ld * ib);
+    const float* tp = T + c_T.totplnk + ib * 181;
+    const float* td = T + c_T.totplnkderiv + ib * 181;
+    S.h->misc[16 + ib] = se * (tp[ind - 1] + fr * (tp[ind] - tp[ind - 1]));
+    S.h->misc[32 + ib] = se * (td[ind - 1] + fr * (td[ind] - td[ind - 1]));
+    S.h->misc[48 + ib] = se;
+  }
+  notpre = __syncthreads_or(notpre);
+  // ---------------- per (layer, band): Planck values and the aerosol optical depth (rrtmg_lw_rad.f90:548-553)
+#pragma unroll 2
+  for (int it = tid; it < nl * 16; it += RT_NT) {
+    const int lay = it >> 4, ib = it & 15;
+    const float* tp = T + c_T.totplnk + ib * 181;
+    const float4 r0 = prow[lay], r1 = prow[lay + 1];
+    const int i0 = __float_as_int(r0.x), il = __float_as_int(r0.z), i1 = __float_as_int(r1.x);
+    const float pdn = tp[i0 - 1] + r0.y * (tp[i0] - tp[i0 - 1]);
+    const float pup = tp[i1 - 1] + r1.y * (tp[i1] - tp[i1 - 1]);
+    const float blay = tp[il - 1] + r0.w * (tp[il] - tp[il - 1]);
+    const float taua = (float)__ldg(a.tauaer + icol + a.ld * (lay + (long long)nl * ib));
+    S.L[lay].rec[ib] = make_float4(blay, pdn - blay, pup - blay, taua);
+  }
+  // ---------------- clouds: the cells' McICA bits, cldprmc's optical depths and stop conditions
+  int err = 0;
+  for (int i = tid; i < nl * 5; i += RT_NT) {
+    const int l = i / 5, w = i - 5 * l;
+    S.L[l].cbits[w] = 0u;
+    S.fbits(l)[w] = 0u;  // caller sub-columns
+  }
+  if (clouds && fused) {
+    // per layer, once: the McICA threshold and the layer's cloud quantities
+    for (int lay = tid; lay < nl; lay += RT_NT) {
+      double cf = in2(a.cldfrac, a.ld, icol, lay);
+      cf = cf < 1.0e-20 ? 0.0 : cf;  // mcica_subcol_gen_lw.f90:463-470
+      // cdf >= 1 - cf, compared on the bit patterns (cdf is in [0, 1], so
+      // for a threshold >= 0 the integer order is the floating-point order);
+      // a negative threshold takes every cell, a NaN none
+      const double thr = 1.0 - cf;
+      S.L[lay].cthr = thr < 0.0 ? LLONG_MIN : (thr == thr ? __double_as_longlong(thr) : LLONG_MAX);
+      const double ciwp = in2(a.ciwp, a.ld, icol, lay), clwp = in2(a.clwp, a.ld, icol, lay);
+      const double rice = in2(a.reicmcl, a.ld, icol, lay), rliq = in2(a.relqmcl, a.ld, icol, lay);
+      const int fl = (ciwp != 0.0 ? 1 : 0) | (clwp != 0.0 ? 2 : 0) | (ciwp + clwp >= 1.e-20 ? 4 : 0);
+      int e = 0;
+      if (ciwp != 0.0) e = ice_code(a.iceflag, rice);
+      if (clwp != 0.0 && liq_code(a.liqflag, rliq)) e = GB_COL_LIQ_BOUNDS;
+      S.L[lay].lfl = fl | (e << 8);
+      S.L[lay].lcw = make_float4((float)ciwp, (float)clwp, (float)rice, (float)rliq);
+    }
+    // this g-point's draw (mcica_subcol_gen_lw.f90:484-512, icld 3) as a bit
+    // pattern, and the warp's largest
+    const long long cdb = __double_as_longlong(__ldg(a.draws + icol * GB_NGPT + g));
+    long long mx = live ? cdb : LLONG_MIN;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const long long v = __shfl_xor_sync(FULL, mx, o);
+      mx = v > mx ? v : mx;
+    }
+    __syncthreads();
+    // cloudy cells: cdf(g) >= 1 - cldf(lay) (mcica_subcol_gen_lw.f90:650); a
+    // layer whose threshold is above every draw of the warp has none there
+    for (int lay = 0; lay < nl; ++lay) {
+      const long long tb = S.L[lay].cthr;
+      if (tb > mx) continue;
+      const unsigned m = __ballot_sync(FULL, live && cdb >= tb);
+      if (lane == 0) S.L[lay].cbits[warp] = m;
+    }
+    __syncthreads();
+    for (int lay = tid; lay < nl; lay += RT_NT) {
+      const unsigned* c = S.L[lay].cbits;
+      S.L[lay].cldlay = (c[0] | c[1] | c[2] | c[3] | c[4]) != 0u;
+    }
+    __syncthreads();
+    // cloud optical depth per (layer, band) where the band has a cloudy
+    // sub-column (the values cldprmc computes for every such cell), and
+    // cldprmc's stop conditions
+    const long long kMin = __double_as_longlong(1.0e-20), kInf = 0x7FF0000000000000LL;
+    for (int it = tid; it < nl * 16; it += RT_NT) {
+      const int lay = it >> 4, ib = it & 15;
+      if (!S.L[lay].cldlay) continue;
+      const int g0 = c_T.band[ib].g0, ng = c_T.band[ib].ng;
+      bool any = false;
+      for (int k = g0; k < g0 + ng; ++k) any |= (S.L[lay].cbits[k >> 5] >> (k & 31)) & 1u;
+      if (!any) continue;
+      const double tin = __ldg(a.tauc + ib + 16 * (icol + a.ld * lay));
+      const long long tinb = __double_as_longlong(tin);
+      const bool tin_ok = tinb >= kMin && tinb <= kInf;  // tin >= 1e-20
+      const int fl = S.L[lay].lfl;
+      const bool cond = (fl & 4) || tin_ok;
+      S.L[lay].tcl[ib] = a.inflag == 2 && cond ? cloud_tau_layer(a, ib, T, S.L[lay].lcw, fl) : (float)tin;
+      if (cond) {
+        if (a.inflag == 1) err = GB_COL_INFLAG1;
+        if (a.inflag == 2 && (fl >> 8)) err = fl >> 8;
+      }
+    }
+  } else if (clouds) {
+    // caller sub-columns: the layer radii as floats and the codes cldprmc's
+    // radius checks stop with: bits 0-7 ice, 8-15 liquid
+    for (int lay = tid; lay < nl; lay += RT_NT) {
+      const double rice = in2(a.reicmcl, a.ld, icol, lay), rliq = in2(a.relqmcl, a.ld, icol, lay);
+      S.L[lay].lfl = ice_code(a.iceflag, rice) | (liq_code(a.liqflag, rliq) << 8);
+      S.L[lay].lcw = make_float4(0.0f, 0.0f, (float)rice, (float)rliq);
+    }
+    __syncthreads();
+    // per layer, each warp: its 32 cldfmcl values tested on their bit
+    // patterns: == 1, /= 0, >= 1e-20
+    const long long kOne = 0x3FF0000000000000LL, kInf = 0x7FF0000000000000LL;
+    const long long kMin = __double_as_longlong(1.0e-20);
+#pragma unroll 4
+    for (int lay = 0; lay < nl; ++lay) {
+      const long long o = g + GB_NGPT * (icol + a.ld * lay);
+      const long long cb = live ? __double_as_longlong(__ldg(a.cldfmcl + o)) : 0LL;
+      const bool one = cb == kOne;
+      const bool frac = !one && (cb << 1) != 0LL;  // neither +-0 nor 1 (NaN included, as /= 0 is)
+      const unsigned m1 = __ballot_sync(FULL, one), mf = __ballot_sync(FULL, frac);
+      if (lane == 0) {
+        S.L[lay].cbits[warp] = m1;
+        S.fbits(lay)[warp] = mf;
+      }
+      if (cb >= kMin && cb <= kInf) {  // cldfmc >= cldmin (cldprmc.f90:178)
+        const double ciwp = __ldg(a.ciwpmcl + o), clwp = __ldg(a.clwpmcl + o);
+        const long long tb = __double_as_longlong(__ldg(a.taucmcl + o));
+        if (ciwp + clwp >= 1.e-20 || (tb >= kMin && tb <= kInf)) {
+          const int e = S.L[lay].lfl;
+          if (a.inflag == 1) err = GB_COL_INFLAG1;
+          if (a.inflag == 2) {
+            if ((__double_as_longlong(ciwp) << 1) != 0LL && (e & 0xff)) err = e & 0xff;  // ciwp /= 0
+            if ((__double_as_longlong(clwp) << 1) != 0LL && (e >> 8)) err = e >> 8;      // clwp /= 0
+          }
+        }
+      }
+    }
+    __syncthreads();
+    for (int lay = tid; lay < nl; lay += RT_NT) {
+      const unsigned* c = S.L[lay].cbits;
+      S.L[lay].cldlay = (c[0] | c[1] | c[2] | c[3] | c[4]) != 0u;
+    }
+  } else {
+    for (int lay = tid; lay < nl; lay += RT_NT) S.L[lay].cldlay = 0;
+  }
+  if (err) atomicMax(&S.h->iscal[0], err);
+  __syncthreads();
+  if (tid == 0) {
+    err = S.h->iscal[0];
+    if (notpre) err = GB_COL_LAYTROP;
+    if (bad) err = GB_COL_BADVAL;
+    if (err) {
+      if (a.col_err) a.col_err[icol] = err;
+      atomicMax(a.err_flag, err);
+    } else if (a.col_err) {
+      a.col_err[icol] = 0;
+    }
+  }
+
+  const float sd = S.h->misc[band];
+  const unsigned bit = 1u << lane;
+  float* part = S.part + warp * (nl + 1) * 6;  // this warp's level sums
+
+  // ---------------- downward pass (rtrnmc.f90:347-455): total and clear-sky streams
+  // Software pipeline: in the step for layer lay, the gas optics of lay-2 are
+  // loaded and the stage (table lookup) of lay-1 is set up.
+  float rd = 0.0f, rc = 0.0f, f1 = 0.0f, tga = 0.0f, pfa = 0.0f;
+  Stage cur;
+  {
+    float tg, pf;
+    gas_at<MODE>(src, layer_on_net<MODE>(src, nl - 1), nl - 1, g, tg, pf);
+    cur = stage_of(S, T, nl - 1, band, sd, tg, pf);
+    if (nl >= 2) gas_at<MODE>(src, layer_on_net<MODE>(src, nl - 2), nl - 2, g, tga, pfa);
+  }
+  for (int lay = nl - 1; lay >= 0; --lay) {
+    Stage nxt = cur;
+    if (lay >= 1) {
+      float tgb = 0.0f, pfb = 0.0f;
+      if (lay >= 2) gas_at<MODE>(src, layer_on_net<MODE>(src, lay - 2), lay - 2, g, tgb, pfb);
+      nxt = stage_of(S, T, lay - 1, band, sd, tga, pfa);
+      tga = tgb;
+      pfa = pfb;
+    }
+    const float pf = cur.pf, od = cur.od;
+    const float4 r = cur.r;
+    const Clr c = clear_cell(od, cur.itr, cur.tt);
+    const float gsd = pf * fmaf(c.x, r.y, r.x) * c.atrans;
+    const float tr = 1.0f - c.atrans;
+    rc = fmaf(rc, tr, gsd);
+    float A = tr, B = gsd;
+    if (clouds && S.L[lay].cldlay) {
+      const bool one = S.L[lay].cbits[warp] & bit;
+      if (one || (!fused && (S.fbits(lay)[warp] & bit))) {
+        float odcld, efcl, atot, x;
+        const float cldf = cell_cloud(a, S, icol, g, lay, band, sd, one, T, odcld, efcl);
+        cloud_total(T, c, od, odcld, atot, x);
+        A = 1.0f - fmaf(efcl, 1.0f - c.atrans, c.atrans);
+        B = fmaf(cldf, fmaf(pf * fmaf(x, r.y, r.x), atot, -gsd), gsd);
+      }
+    }
+    rd = fmaf(rd, A, B);
+    if (lay == 0) f1 = pf;
+    const float s = reduce2(rd * wgt, rc * wgt, lane);
+    if (lane < 2) part[lay * 6 + lane] = s;
+    cur = nxt;
+  }
+
+  // ---------------- surface emission and reflection (rtrnmc.f90:465-485)
+  const bool idrv = a.idrv == 1;
+  const float rad0 = f1 * S.h->misc[16 + band];
+  const float reflect = 1.0f - S.h->misc[48 + band];
+  float ru = rad0 + reflect * rd;
+  float rcu = rad0 + reflect * rc;
+  float du = f1 * S.h->misc[32 + band];
+  float dcu = du;
+  if (idrv) {
+    const float s = reduce4(ru * wgt, rcu * wgt, du * wgt, dcu * wgt, lane);
+    if (lane < 4) part[2 + lane] = s;
+  } else {
+    const float s = reduce2(ru * wgt, rcu * wgt, lane);
+    if (lane < 2) part[2 + lane] = s;
+  }
+  // ---------------- upward pass (rtrnmc.f90:486-529): level lay+1 above layer lay
+  {
+    float tg, pf;
+    gas_at<MODE>(src, layer_on_net<MODE>(src, 0), 0, g, tg, pf);
+    cur = stage_of(S, T, 0, band, sd, tg, pf);
+    if (nl >= 2) gas_at<MODE>(src, layer_on_net<MODE>(src, 1), 1, g, tga, pfa);
+  }
+  for (int lay = 0; lay < nl; ++lay) {
+    Stage nxt = cur;
+    if (lay + 1 < nl) {
+      float tgb = 0.0f, pfb = 0.0f;
+      if (lay + 2 < nl) gas_at<MODE>(src, layer_on_net<MODE>(src, lay + 2), lay + 2, g, tgb, pfb);
+      nxt = stage_of(S, T, lay + 1, band, sd, tga, pfa);
+      tga = tgb;
+      pfa = pfb;
+    }
+    const float pf = cur.pf, od = cur.od;
+    const float4 r = cur.r;
+    const Clr c = clear_cell(od, cur.itr, cur.tt);
+    const float gsu = pf * fmaf(c.x, r.z, r.x) * c.atrans;
+    const float tr = 1.0f - c.atrans;
+    rcu = fmaf(rcu, tr, gsu);
+    dcu *= tr;
+    float A = tr, B = gsu, D = tr;
+    if (clouds && S.L[lay].cldlay) {
+      const bool one = S.L[lay].cbits[warp] & bit;
+      if (one || (!fused && (S.fbits(lay)[warp] & bit))) {
+        float odcld, efcl, atot, x;
+        const float cldf = cell_cloud(a, S, icol, g, lay, band, sd, one, T, odcld, efcl);
+        cloud_total(T, c, od, odcld, atot, x);
+        A = 1.0f - fmaf(efcl, 1.0f - c.atrans, c.atrans);
+        B = fmaf(cldf, fmaf(pf * fmaf(x, r.z, r.x), atot, -gsu), gsu);
+        D = fmaf(cldf, 1.0f - atot, (1.0f - cldf) * (1.0f - c.atrans));
+      }
+    }
+    ru = fmaf(ru, A, B);
+    du *= D;
+    float* p = part + (lay + 1) * 6 + 2;
+    if (idrv) {
+      const float s = reduce4(ru * wgt, rcu * wgt, du * wgt, dcu * wgt, lane);
+      if (lane < 4) p[lane] = s;
+    } else {
+      const float s = reduce2(ru * wgt, rcu * wgt, lane);
+      if (lane < 2) p[lane] = s;
+    }
+    cur = nxt;
+  }
+  __syncthreads();
+
+  // ---------------- fp64 outputs: fluxes, net fluxes, heating rates (rtrnmc.f90:566-592)
+  const long long ldo = a.ldo;
+  double* fnet = reinterpret_cast<double*>(S.L);  // [nl+1][2]
+  for (int lev = tid; lev <= nl; lev += RT_NT) {
+    // the five warps' fp32 partials summed without rounding error: Knuth's
+    // two-sum keeps each addition's rounding error, and the sum and the
+    // accumulated errors go to fp64 together
+    double acc[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      float hi = S.part[lev * 6 + k], lo = 0.0f;
+#pragma unroll
+      for (int w = 1; w < RT_NW; ++w) {
+        const float b = S.part[(w * (nl + 1) + lev) * 6 + k];
+        const float sum = hi + b, bv = sum - hi;
+        lo += (hi - (sum - bv)) + (b - bv);
+        hi = sum;
+      }
+      acc[k] = (double)hi + (double)lo;
+    }
+    if (lev == nl) acc[0] = acc[1] = 0.0;  // no downward radiation at the model top
+    const long long o = icol + ldo * lev;
+    a.uflx[o] = acc[2];
+    a.dflx[o] = acc[0];
+    a.uflxc[o] = acc[3];
+    a.dflxc[o] = acc[1];
+    if (idrv) {
+      a.duflx_dt[o] = acc[4];
+      a.duflxc_dt[o] = acc[5];
+    }
+    fnet[lev * 2 + 0] = acc[2] - acc[0];
+    fnet[lev * 2 + 1] = acc[3] - acc[1];
+  }
+  __syncthreads();
+  for (int l = tid; l < nl; l += RT_NT) {
+    const double dp = in2(a.plev, a.ld, icol, l) - in2(a.plev, a.ld, icol, l + 1);
+    const double f = c_T.heatfac / dp;  // one division for both heating rates
+    const long long o = icol + ldo * l;
+    a.hr[o] = f * (fnet[l * 2] - fnet[(l + 1) * 2]);
+    a.hrc[o] = f * (fnet[l * 2 + 1] - fnet[(l + 1) * 2 + 1]);
+  }
+  __syncthreads();
   return true;
 }
 
-// ------------------------------------------------------------------ the kernel
-// Persistent blocks walk the batch columns grid after grid; a block's columns
-// increase, so its grid index only moves forward.  FLAVOR 1 is the
-// learned-only kernel, which appends the columns it does not solve to
-// B.fall; FLAVOR 2 is the full kernel walking that list instead of the batch.
-// The unit is compiled without multiply-add contraction, so a column gives
-// the same bits in every flavour and launch shape.
-template <int NT, int MINB, int FLAVOR>
-__global__ void __launch_bounds__(NT, MINB) lw_batch_kernel(const __grid_constant__ LwBatch B,
-                                                             const float* __restrict__ T) {
-  constexpr bool LEAN = FLAVOR == 1, list = FLAVOR == 2;
+// ------------------------------------------------------------------ kernels
+__device__ __forceinline__ int grid_of(const LwBatch& B, long long gc, int gi) {
+  while (gc >= B.col0[gi + 1]) ++gi;
+  return gi;
+}
+
+// The column's grid arguments are copied into shared memory (the first
+// ARGS_BYTES of every kernel's dynamic shared memory): the loops then read
+// them as shared-memory broadcasts instead of constant-bank loads indexed by
+// the grid number, which the compiler re-issues wherever it does not keep a
+// field in a register.
+constexpr size_t ARGS_BYTES = (sizeof(LwArgs) + 15) & ~size_t(15);
+static_assert(sizeof(LwArgs) % 4 == 0, "LwArgs copied as 32-bit words");
+__device__ __forceinline__ const LwArgs& stage_args(const LwArgs& a, char* smem) {
+  __syncthreads();  // every thread is done with the previous column's copy
+  int* dst = reinterpret_cast<int*>(smem);
+  const int* src = reinterpret_cast<const int*>(&a);
+  for (int k = threadIdx.x; k < (int)(sizeof(LwArgs) / 4); k += blockDim.x) dst[k] = src[k];
+  __syncthreads();
+  return *reinterpret_cast<const LwArgs*>(smem);
+}
+
+// taumol over batch columns [c0, c1): column c0 + k into slot k.
+template <int NT>
+__global__ void __launch_bounds__(NT) lw_gas_kernel(const __grid_constant__ LwBatch B, const float* __restrict__ T,
+                                                    long long c0, long long c1) {
   extern __shared__ __align__(16) char smem_raw[];
-  float4* __restrict__ scr = B.scratch + (size_t)blockIdx.x * ((size_t)2 * B.nsmax * GB_NGPT);
-  const long long n = list ? (long long)*B.nfall : B.col0[B.ngrid];
+  const GasSmem s = gas_carve(smem_raw + ARGS_BYTES, B.nsmax);
   int gi = 0;
-  for (long long i = blockIdx.x; i < n; i += gridDim.x) {
-    const long long gc = list ? B.fall[i] : i;
-    if (list) gi = 0;  // the list is in no particular order
-    while (gc >= B.col0[gi + 1]) ++gi;
-    const bool done = solve_column<NT, LEAN>(B.g[gi], gc - B.col0[gi], smem_raw, scr, T);
-    if (LEAN && !done && threadIdx.x == 0) B.fall[atomicAdd(B.nfall, 1u)] = gc;
+  for (long long i = c0 + blockIdx.x; i < c1; i += gridDim.x) {
+    gi = grid_of(B, i, gi);
+    const LwArgs& a = stage_args(B.g[gi], smem_raw);
+    const long long slot = i - c0;
+    gas_column<NT>(a, i - B.col0[gi], s, B.gtau + slot * B.gstride, B.gfrac + slot * B.gstride, T);
   }
 }
 
-// compiled shapes (threads per column block, min blocks per SM); variant 0 is the default
-#define GB_LW_VARIANTS(X) X(0, 160, 5) X(1, 160, 6) X(2, 160, 4) X(3, 256, 3)
-// the learned-only kernel: less shared memory and fewer registers, so more blocks fit
-#define GB_LW_LEAN_VARIANTS(X) X(0, 160, 6) X(1, 160, 7) X(2, 160, 5) X(3, 256, 4)
+// The transfer on the network's gas optics over batch columns [c0, c1), one
+// block per column; a column with a layer off the network is appended to
+// B.fall instead.
+template <int MINB>
+__global__ void __launch_bounds__(RT_NT, MINB) lw_rt_kernel(const __grid_constant__ LwBatch B,
+                                                             const float* __restrict__ T, long long c0, long long c1) {
+  extern __shared__ __align__(16) char smem_raw[];
+  const RtSmem S = rt_carve(smem_raw + ARGS_BYTES, B.nsmax);
+  int gi = 0;
+  for (long long i = c0 + blockIdx.x; i < c1; i += gridDim.x) {
+    gi = grid_of(B, i, gi);
+    const LwArgs& a = stage_args(B.g[gi], smem_raw);
+    const long long icol = i - B.col0[gi];
+    GasSrc src{};
+    const long long row = icol * a.nlay * GB_NGPT;
+    src.nt = a.sur_tau ? a.sur_tau + row : nullptr;
+    src.nf = a.sur_frac ? a.sur_frac + row : nullptr;
+    src.flag = a.sur_flag ? a.sur_flag + icol * a.nlay : nullptr;
+    const bool done = rt_column<RT_NET>(a, icol, S, src, T);
+    if (!done && threadIdx.x == 0) B.fall[atomicAdd(B.nfall, 1u)] = i;
+  }
+}
+
+// taumol and the transfer of a column in one block, taumol's planes in the
+// block's own slot (which stays in L2).  LIST: the columns handed over by the
+// network's transfer kernel (B.fall), each layer's gas optics from the
+// network or from taumol; else batch columns [c0, c1).
+template <int MINB, bool LIST>
+__global__ void __launch_bounds__(RT_NT, MINB) lw_full_kernel(const __grid_constant__ LwBatch B,
+                                                               const float* __restrict__ T, long long c0, long long c1) {
+  extern __shared__ __align__(16) char smem_raw[];
+  const GasSmem gs = gas_carve(smem_raw + ARGS_BYTES, B.nsmax);
+  const RtSmem S = rt_carve(smem_raw + ARGS_BYTES, B.nsmax);  // used after taumol is done with the same memory
+  float* gt = B.gtau + (long long)blockIdx.x * B.gstride;
+  float* gf = B.gfrac + (long long)blockIdx.x * B.gstride;
+  const long long n = LIST ? (long long)*B.nfall : c1;
+  int gi = 0;
+  for (long long i = (LIST ? 0 : c0) + blockIdx.x; i < n; i += gridDim.x) {
+    const long long gc = LIST ? B.fall[i] : i;
+    gi = grid_of(B, gc, LIST ? 0 : gi);  // the list is in no particular order
+    const LwArgs& a = stage_args(B.g[gi], smem_raw);
+    const long long icol = gc - B.col0[gi];
+    gas_column<RT_NT>(a, icol, gs, gt, gf, T);
+    GasSrc src{};
+    src.gt = gt;
+    src.gf = gf;
+    if (LIST && a.sur_flag) {
+      const long long row = icol * a.nlay * GB_NGPT;
+      src.nt = a.sur_tau + row;
+      src.nf = a.sur_frac + row;
+      src.flag = a.sur_flag + icol * a.nlay;
+      rt_column<RT_MIX>(a, icol, S, src, T);
+    } else {
+      rt_column<RT_GAS>(a, icol, S, src, T);
+    }
+  }
+}
+
+constexpr int GAS_NT = 128;      // threads of the taumol kernel
+constexpr int LIST_PER_SM = 2;   // hand-over kernel blocks per SM
+constexpr int LIST_MINB = 6;
+
+// compiled shapes (min blocks per SM for the register allocation, 160
+// threads each); variant 0 is the default
+#define GB_LW_VARIANTS(X) X(0, 6) X(1, 7) X(2, 5) X(3, 4)
 
 }  // namespace gb
 
@@ -1105,41 +1048,52 @@ __global__ void __launch_bounds__(NT, MINB) lw_batch_kernel(const __grid_constan
 namespace {
 
 struct VariantInfo {
-  int threads, min_blocks;
-  const void* fn;
-  cudaError_t (*launch)(const LwBatch&, const float*, int, size_t, cudaStream_t);
+  int min_blocks;
+  const void* fn;  // the kernel this shape launches
+  cudaError_t (*launch)(const LwBatch&, const float*, long long, long long, int, size_t, cudaStream_t);
 };
 
-template <int NT, int MINB, int FLAVOR>
-cudaError_t launch_variant(const LwBatch& b, const float* T, int nblocks, size_t smem, cudaStream_t st) {
-  gb::lw_batch_kernel<NT, MINB, FLAVOR><<<nblocks, NT, smem, st>>>(b, T);
+template <int MINB>
+cudaError_t launch_full(const LwBatch& b, const float* T, long long c0, long long c1, int nblocks, size_t smem,
+                        cudaStream_t st) {
+  gb::lw_full_kernel<MINB, false><<<nblocks, gb::RT_NT, smem, st>>>(b, T, c0, c1);
+  return cudaGetLastError();
+}
+template <int MINB>
+cudaError_t launch_net(const LwBatch& b, const float* T, long long c0, long long c1, int nblocks, size_t smem,
+                       cudaStream_t st) {
+  gb::lw_rt_kernel<MINB><<<nblocks, gb::RT_NT, smem, st>>>(b, T, c0, c1);
   return cudaGetLastError();
 }
 
-#define GB_LW_VARIANT_ENTRY(i, nt, mb) {nt, mb, (const void*)gb::lw_batch_kernel<nt, mb, 0>, launch_variant<nt, mb, 0>},
-#define GB_LW_LEAN_ENTRY(i, nt, mb) {nt, mb, (const void*)gb::lw_batch_kernel<nt, mb, 1>, launch_variant<nt, mb, 1>},
-const VariantInfo kVariants[] = {GB_LW_VARIANTS(GB_LW_VARIANT_ENTRY)};
-const VariantInfo kLean[] = {GB_LW_LEAN_VARIANTS(GB_LW_LEAN_ENTRY)};
+// batches without a network: the fused taumol + transfer kernel; with a
+// network: the transfer kernel on the network's outputs
+#define GB_LW_FULL_ENTRY(i, mb) {mb, (const void*)gb::lw_full_kernel<mb, false>, launch_full<mb>},
+#define GB_LW_NET_ENTRY(i, mb) {mb, (const void*)gb::lw_rt_kernel<mb>, launch_net<mb>},
+const VariantInfo kVariants[] = {GB_LW_VARIANTS(GB_LW_FULL_ENTRY)};
+const VariantInfo kLean[] = {GB_LW_VARIANTS(GB_LW_NET_ENTRY)};
 constexpr int kNumVariants = sizeof(kVariants) / sizeof(kVariants[0]);
-static_assert(sizeof(kLean) / sizeof(kLean[0]) == kNumVariants, "one variant index range for both kernels");
-// the full kernel over the columns the learned-only kernel hands over
-const VariantInfo kList = {160, 6, (const void*)gb::lw_batch_kernel<160, 6, 2>, launch_variant<160, 6, 2>};
+constexpr int kMaxPerSm = 16;  // most resident column blocks per SM any shape launches
 
 const VariantInfo& info(int variant, bool lean) { return lean ? kLean[variant] : kVariants[variant]; }
 
-cudaError_t configure(int nlay, const VariantInfo& v, bool lean, int* blocks_per_sm) {
-  const size_t sm = gb::smem_bytes(nlay, lean);
-  cudaError_t e = cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(v.fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
-  if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, v.fn, v.threads, sm);
+int device_sms() {
+  int dev = 0, nsm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  return nsm;
 }
 
-// Shared-memory carve-out for `per` resident blocks: just what they need, so
-// that the rest of the SM's 256 KB stays L1 for the table gathers (the
-// driver otherwise sizes it for the largest block count shared memory alone
-// would allow, even when registers allow fewer).
-cudaError_t set_carveout(const VariantInfo& v, size_t smem, int per) {
+// shared memory of a block of the fused kernel (taumol or transfer area) or of the transfer kernel
+size_t block_smem(int nlay, bool lean) {
+  return gb::ARGS_BYTES +
+         (lean ? gb::rt_smem_bytes(nlay) : std::max(gb::rt_smem_bytes(nlay), gb::gas_smem_bytes(nlay)));
+}
+
+// Shared-memory carve-out for `per` resident blocks of `smem` bytes: just what
+// they need, so that the rest of the SM's memory stays L1 for the table
+// gathers and input loads.
+cudaError_t set_carveout(const void* fn, size_t smem, int per) {
   int dev = 0, max_sm = 0, reserved = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&max_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
@@ -1147,24 +1101,44 @@ cudaError_t set_carveout(const VariantInfo& v, size_t smem, int per) {
   if (max_sm <= 0) return cudaSuccess;
   int pct = (int)std::ceil(100.0 * (double)per * (double)(smem + reserved) / (double)max_sm);
   pct = pct < 1 ? 1 : (pct > 100 ? 100 : pct);
-  return cudaFuncSetAttribute(v.fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+  return cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
 }
 
-// One launch of `variant` of the full (lean false) or learned-only kernel
-// with at most `nblocks` blocks and the carve-out for those resident.
-cudaError_t launch_kernel(const LwBatch& b, const float* d_tables, const VariantInfo& v, bool lean, int nblocks,
-                          cudaStream_t stream) {
+// resident blocks per SM of `fn` with `threads` and `smem` (after allowing that much shared memory)
+cudaError_t occupancy(const void* fn, int threads, size_t smem, int* per) {
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per, fn, threads, smem);
+}
+
+// One launch of a kernel with `nblocks` blocks and the carve-out for those resident.
+template <class F>
+cudaError_t launch_resident(const void* fn, int threads, size_t smem, int nblocks, F&& go) {
   int per = 0;
-  cudaError_t e = configure(b.nsmax, v, lean, &per);
+  cudaError_t e = occupancy(fn, threads, smem, &per);
   if (e != cudaSuccess) return e;
-  int dev = 0, nsm = 1;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (per < 1) return cudaErrorInvalidConfiguration;
+  const int nsm = device_sms();
   const int resident = (nblocks + nsm - 1) / nsm;
-  const size_t smem = gb::smem_bytes(b.nsmax, lean);
-  e = set_carveout(v, smem, resident < per ? resident : per);
+  e = set_carveout(fn, smem, resident < per ? resident : per);
   if (e != cudaSuccess) return e;
-  return v.launch(b, d_tables, nblocks, smem, stream);
+  return go(nblocks);
+}
+
+cudaError_t launch_gas_range(const LwBatch& b, const float* T, long long c0, long long c1, cudaStream_t st) {
+  const void* fn = (const void*)gb::lw_gas_kernel<gb::GAS_NT>;
+  const size_t smem = gb::ARGS_BYTES + gb::gas_smem_bytes(b.nsmax);
+  int per = 0;
+  cudaError_t e = occupancy(fn, gb::GAS_NT, smem, &per);
+  if (e != cudaSuccess) return e;
+  long long nb = (long long)device_sms() * (per < 1 ? 1 : per);
+  if (nb > c1 - c0) nb = c1 - c0;
+  if (nb < 1) return cudaSuccess;
+  return launch_resident(fn, gb::GAS_NT, smem, (int)nb, [&](int n) {
+    gb::lw_gas_kernel<gb::GAS_NT><<<n, gb::GAS_NT, smem, st>>>(b, T, c0, c1);
+    return cudaGetLastError();
+  });
 }
 
 }  // namespace
@@ -1173,56 +1147,70 @@ int gb_lw_num_variants() { return kNumVariants; }
 
 LwVariant gb_lw_variant(int v, bool lean) {
   if (v < 0 || v >= kNumVariants) return LwVariant{0, 0};
-  return LwVariant{info(v, lean).threads, info(v, lean).min_blocks};
+  return LwVariant{gb::RT_NT, info(v, lean).min_blocks};
 }
 
-size_t gb_lw_smem_bytes(int nlay, bool lean) { return gb::smem_bytes(nlay, lean); }
+size_t gb_lw_smem_bytes(int nlay) { return block_smem(nlay, false); }
 
 cudaError_t gb_lw_set_tables(const GbTables& T) { return cudaMemcpyToSymbol(gb::c_T, &T, sizeof(GbTables)); }
 
 int gb_lw_slots(int nlay, int variant, bool lean) {
   if (variant < 0 || variant >= kNumVariants) variant = 0;
-  int dev = 0, nsm = 0, per = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  if (configure(nlay, info(variant, lean), lean, &per) != cudaSuccess || per < 1) per = 1;
-  return nsm * per;
+  const VariantInfo& v = info(variant, lean);
+  int per = 0;
+  if (occupancy(v.fn, gb::RT_NT, block_smem(nlay, lean), &per) != cudaSuccess || per < 1) per = 1;
+  return device_sms() * std::min(per, kMaxPerSm);
 }
 
-size_t gb_lw_scratch_bytes(int nlay, int slots) { return (size_t)slots * 2 * nlay * GB_NGPT * sizeof(float4); }
+long long gb_lw_gas_slots(int nlay, long long ncols) {
+  (void)nlay;
+  (void)ncols;
+  return (long long)device_sms() * kMaxPerSm;  // one per resident block of the fused or hand-over kernel
+}
+
+size_t gb_lw_gas_bytes(int nlay, long long slots) { return (size_t)slots * 2 * nlay * GB_NGPT * sizeof(float); }
+
+long long gb_lw_list_slots() { return (long long)device_sms() * gb::LIST_PER_SM; }
+
+cudaError_t gb_lw_launch_gas(const LwBatch& b, const float* d_tables, long long c0, long long c1,
+                             cudaStream_t stream) {
+  if (c1 <= c0) return cudaSuccess;
+  if (c1 - c0 > b.gslots || !b.gtau || !b.gfrac) return cudaErrorInvalidValue;
+  return launch_gas_range(b, d_tables, c0, c1, stream);
+}
 
 cudaError_t gb_lw_launch_batch(const LwBatch& b, const float* d_tables, int variant, int nblocks,
                                cudaStream_t stream) {
   if (variant < 0 || variant >= kNumVariants || b.ngrid < 1 || b.ngrid > GB_LW_MAX_GRIDS) return cudaErrorInvalidValue;
-  if (b.col0[b.ngrid] <= 0 || nblocks <= 0) return cudaSuccess;
-  if ((long long)nblocks > b.col0[b.ngrid]) nblocks = (int)b.col0[b.ngrid];
-  if (!b.fall || !b.nfall) return launch_kernel(b, d_tables, info(variant, false), false, nblocks, stream);
-  // learned gas optics: the learned-only kernel, then the full kernel over
-  // the columns it handed over (its blocks find an empty list and return
-  // when every column was on the network)
+  const long long n = b.col0[b.ngrid];
+  if (n <= 0 || nblocks <= 0) return cudaSuccess;
+  if (!b.gtau || !b.gfrac || b.gslots < 1 || b.gstride < (long long)b.nsmax * GB_NGPT) return cudaErrorInvalidValue;
+  for (int i = 0; i < b.ngrid; ++i)  // fused-cloud grids come with their McICA draws
+    if (b.g[i].cloud_mode == LW_CLOUD_FUSED && b.g[i].icld >= 1 && b.g[i].ncol > 0 && !b.g[i].draws)
+      return cudaErrorInvalidValue;
+  if ((long long)nblocks > n) nblocks = (int)n;
+  if (!b.fall || !b.nfall) {
+    // taumol and the transfer, one block per column, taumol's planes in the block's slot
+    if ((long long)nblocks > b.gslots) nblocks = (int)b.gslots;
+    const VariantInfo& v = info(variant, false);
+    const size_t smem = block_smem(b.nsmax, false);
+    return launch_resident(v.fn, gb::RT_NT, smem, nblocks,
+                           [&](int nb) { return v.launch(b, d_tables, 0, n, nb, smem, stream); });
+  }
+  // learned gas optics: the transfer kernel on the network's outputs, then the
+  // hand-over kernel over the columns it passed on (its blocks find an empty
+  // list and return when every column was on the network)
+  if (b.gslots < gb_lw_list_slots()) return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(b.nfall, 0, sizeof(unsigned), stream);
   if (e != cudaSuccess) return e;
-  e = launch_kernel(b, d_tables, info(variant, true), true, nblocks, stream);
+  const VariantInfo& v = info(variant, true);
+  const size_t smem = block_smem(b.nsmax, true);
+  e = launch_resident(v.fn, gb::RT_NT, smem, nblocks, [&](int nb) { return v.launch(b, d_tables, 0, n, nb, smem, stream); });
   if (e != cudaSuccess) return e;
-  int per = 0;
-  const VariantInfo& lv = kList;
-  e = configure(b.nsmax, lv, false, &per);
-  if (e != cudaSuccess) return e;
-  int dev = 0, nsm = 1;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const int nf = per * nsm < nblocks ? per * nsm : nblocks;  // scratch holds nblocks slots
-  return launch_kernel(b, d_tables, lv, false, nf < 1 ? 1 : nf, stream);
-}
-
-cudaError_t gb_lw_launch(const LwArgs& a, const float* d_tables, float4* scratch, int nslots, cudaStream_t stream) {
-  if (a.ncol <= 0) return cudaSuccess;
-  LwBatch b;
-  b.ngrid = 1;
-  b.nsmax = a.nlay;
-  b.col0[0] = 0;
-  b.col0[1] = a.ncol;
-  b.scratch = scratch;
-  b.g[0] = a;
-  return gb_lw_launch_batch(b, d_tables, 0, a.ncol < nslots ? a.ncol : nslots, stream);
+  const void* fn = (const void*)gb::lw_full_kernel<gb::LIST_MINB, true>;
+  const size_t lsmem = block_smem(b.nsmax, false);
+  return launch_resident(fn, gb::RT_NT, lsmem, (int)gb_lw_list_slots(), [&](int nb) {
+    gb::lw_full_kernel<gb::LIST_MINB, true><<<nb, gb::RT_NT, lsmem, stream>>>(b, d_tables, 0, 0);
+    return cudaGetLastError();
+  });
 }

@@ -1,4 +1,4 @@
-// Launch interface of the fused RRTMG_LW column kernel (lw_solver.cu).
+// Launch interface of the RRTMG_LW column kernels (lw_solver.cu).
 #pragma once
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -9,7 +9,7 @@
 // Where a grid's McICA sub-column clouds come from.
 enum LwCloudMode {
   LW_CLOUD_SUBCOL = 0,  // caller-supplied (140, ld, nlay) arrays cldfmcl/ciwpmcl/clwpmcl/taucmcl
-  LW_CLOUD_FUSED = 1,   // generated inside the kernel from layer clouds (icld 3, Mersenne twister,
+  LW_CLOUD_FUSED = 1,   // generated from layer clouds (icld 3, Mersenne twister,
                         // column c seeded with seed0 + c), as mcica_subcol_lw would for one column
 };
 
@@ -32,55 +32,71 @@ struct LwArgs {
   double *uflx, *dflx, *hr, *uflxc, *dflxc, *hrc, *duflx_dt, *duflxc_dt;
   int* col_err;   // optional per-column status (ncol)
   int* err_flag;  // required: max status over the launch
-  float* dbg_taut;   // optional diagnostics: taut and Planck fractions per column,
-  float* dbg_fracs;  // (ncol, nlay, 140) with g fastest; NULL in production calls
   // optional learned gas optics: taug and Planck fractions per (column, layer, g)
   // in fp16 and a per-layer flag (1: use them, 0: taumol); NULL: taumol everywhere
   const __half *sur_tau, *sur_frac;
   const unsigned char* sur_flag;
-  // fused cloud mode: the columns' 140 McICA draws [ncol][140] made beforehand
-  // (gb_mcica_percol_mt); NULL: the kernel draws them itself
+  // fused cloud mode: the columns' 140 McICA draws [ncol][140] (gb_mcica_percol_mt);
+  // required when cloud_mode is LW_CLOUD_FUSED and icld >= 1
   const double* draws;
 };
 
 // Grids of one launch: grid i owns batch columns col0[i] .. col0[i+1]-1.  The
-// kernel takes this by value (kernel parameter space), so the launch carries
+// kernels take this by value (kernel parameter space), so a launch carries
 // no device-side descriptor and can be captured in a CUDA graph as is.
 #define GB_LW_MAX_GRIDS 32
 //
+// Gas optics hand-over: taumol writes, per slot, taug (without aerosol) and
+// the Planck fractions as fp32 [nlay][140] planes at gtau + slot * gstride and
+// gfrac + slot * gstride; the transfer reads them.  The fused taumol and
+// transfer kernel uses one slot per block (so that the planes stay in L2).
+//
 // Batches with learned gas optics (fall and nfall set) run in two launches:
-// a learned-only kernel solves every column whose layers are all on the
-// network and hands the others (batch numbering) over in fall[0 .. *nfall),
-// then the full kernel solves those.  fall holds at least col0[ngrid] entries.
+// the transfer kernel solves every column whose layers are all on the network
+// and hands the others (batch numbering) over in fall[0 .. *nfall), then the
+// hand-over kernel runs taumol and the transfer for those, mixing per layer
+// the network's values and taumol's.  fall holds at least col0[ngrid] entries.
 struct LwBatch {
   int ngrid;
-  int nsmax;                              // largest nlay (scratch-slot stride)
+  int nsmax;                              // largest nlay (stride of the shared-memory areas)
   long long col0[GB_LW_MAX_GRIDS + 1];
-  float4* scratch;                        // >= gridDim.x slots of 2*nsmax*140 float4
-  long long* fall = nullptr;              // columns handed over by the learned-only kernel
+  float* gtau = nullptr;                  // gas-optics hand-over (see above)
+  float* gfrac = nullptr;
+  long long gstride = 0;                  // floats per slot (>= nsmax * 140)
+  long long gslots = 0;                   // slots available
+  long long* fall = nullptr;              // columns handed over off the network
   unsigned* nfall = nullptr;              // their count (device)
   LwArgs g[GB_LW_MAX_GRIDS];
 };
 
-// Compiled shapes of the column kernel: threads per column block and the
-// minimum resident blocks per SM the register allocation is sized for.
+// Compiled shapes of the column kernels: threads per block (one column per
+// block, one g-point per thread) and the minimum resident blocks per SM the
+// register allocation is sized for.
 struct LwVariant {
   int threads, min_blocks;
 };
-// The learned-only kernel (lean = true) has its own table of as many shapes.
+// The learned-gas-optics transfer kernel (lean = true) has its own table of as many shapes.
 int gb_lw_num_variants();
 LwVariant gb_lw_variant(int v, bool lean = false);
 
-size_t gb_lw_smem_bytes(int nlay, bool lean = false);
-// thread blocks of `variant` that fit on the device at once for this nlay
+// shared memory one block needs at this nlay (one column's taumol or
+// transfer area); a launch is possible iff this fits in one block
+size_t gb_lw_smem_bytes(int nlay);
+// column blocks of `variant` resident on the device at once for this nlay
 int gb_lw_slots(int nlay, int variant = 0, bool lean = false);
-// bytes of scratch for `slots` slots: per slot 2*nlay*140 float4 (clear-sky coefficient planes, cloudy cells)
-size_t gb_lw_scratch_bytes(int nlay, int slots);
+// hand-over slots a batch is solved with (one per resident block)
+long long gb_lw_gas_slots(int nlay, long long ncols);
+// bytes of a hand-over buffer of `slots` slots (taug and fractions, fp32)
+size_t gb_lw_gas_bytes(int nlay, long long slots);
+// hand-over slots the hand-over kernel of a learned batch uses (one per block)
+long long gb_lw_list_slots();
 cudaError_t gb_lw_set_tables(const GbTables& T);
-// One grid, default variant, grid = min(ncol, nslots) blocks.
-cudaError_t gb_lw_launch(const LwArgs& a, const float* d_tables, float4* scratch, int nslots, cudaStream_t stream);
-// All grids of `b` in one launch of `nblocks` persistent blocks of `variant`
-// (with b.fall set: the learned-only kernel's `variant`, then the full kernel
-// over the columns it handed over).
+// All grids of `b` with `variant` at `nblocks` persistent blocks: taumol
+// batches through the fused taumol + transfer kernel (block k in slot k);
+// with b.fall set the learned-gas-optics transfer kernel, then the hand-over
+// kernel.
 cudaError_t gb_lw_launch_batch(const LwBatch& b, const float* d_tables, int variant, int nblocks,
                                cudaStream_t stream);
+// The taumol kernel alone over batch columns [c0, c1) into slots 0 .. c1-c0-1.
+cudaError_t gb_lw_launch_gas(const LwBatch& b, const float* d_tables, long long c0, long long c1,
+                             cudaStream_t stream);

@@ -245,6 +245,43 @@ bool gb_build_tables(const char* ref_path, const char* k_path, double cpdair, Gb
     T.rat[4][j] = (float)(c(4) / c(2));
     T.rat[5][j] = (float)(c(3) / c(2));
   }
+  // the reference atmosphere again in the blob (read with per-thread indices)
+  T.ref_preflog = push(59);
+  T.ref_tref = push(59);
+  T.ref_chi = push(7 * 59);
+  T.ref_rat = push(6 * 59);
+  for (int j = 0; j < 59; ++j) {
+    blob[T.ref_preflog + j] = T.preflog[j];
+    blob[T.ref_tref + j] = T.tref[j];
+    for (int m = 0; m < 7; ++m) blob[T.ref_chi + m * 59 + j] = T.chi[m][j];
+    for (int k = 0; k < 6; ++k) blob[T.ref_rat + k * 59 + j] = T.rat[k][j];
+  }
+  // rtrnmc's lookup tables, computed in double precision as rrtmg_lw_init.f90:120-142
+  // does (tfn = real(itr)/real(ntbl) is a default-real division there)
+  {
+    const int ntbl = 10000;
+    const double expeps = 1.e-20, bpade = 1.0 / 0.278;
+    while (blob.size() % 2) blob.push_back(0.0f);
+    T.tbl_tt = push(2 * (ntbl + 1));
+    T.tbl_tau = push(ntbl + 1);
+    for (int itr = 0; itr <= ntbl; ++itr) {
+      double tau, ex, tf;
+      if (itr == 0) {
+        tau = 0.0; ex = 1.0; tf = 0.0;
+      } else if (itr == ntbl) {
+        tau = 1.e10; ex = expeps; tf = 1.0;
+      } else {
+        const double t = (double)((float)itr / (float)ntbl);
+        tau = bpade * t / (1.0 - t);
+        ex = std::exp(-tau);
+        if (ex <= expeps) ex = expeps;
+        tf = tau < 0.06 ? tau / 6.0 : 1.0 - 2.0 * ((1.0 / tau) - (ex / (1. - ex)));
+      }
+      blob[T.tbl_tt + 2 * itr] = (float)ex;
+      blob[T.tbl_tt + 2 * itr + 1] = (float)tf;
+      blob[T.tbl_tau + itr] = (float)tau;
+    }
+  }
   for (int b = 0; b < 16; ++b) T.delwave[b] = (float)delw->d[b];
   T.grav = grav->d[0];
   T.avogad = avog->d[0];
