@@ -46,6 +46,9 @@ struct GbTables {
   // rtrnmc's lookup tables (rrtmg_lw_init.f90:120-142) in the float blob:
   // tbl_tt (exp_tbl, tfn_tbl) pairs [10001] (8-byte aligned), tbl_tau [10001]
   int tbl_tt, tbl_tau;
+  // per g-point in the float blob: the band (0-based, as int bits) and the
+  // flux weight 0.5 * delwave * fluxfac (rtrnmc.f90:538-583)
+  int gpt_band, gpt_wgt;
   int ngb[GB_NGPT];
   int nspa[GB_NBND], nspb[GB_NBND];
   double heatfac, fluxfac, grav, avogad;

@@ -557,11 +557,13 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
     if (__syncthreads_or(off)) return false;
   }
   if (tid < 4) S.h->iscal[tid] = 0;
-  // this thread's g-point
+  // this thread's g-point, its band and flux weight (read from the table blob:
+  // a constant-bank lookup indexed by the thread would be re-issued in the
+  // loops wherever the compiler does not keep the value in a register)
   const bool live = tid < GB_NGPT;
   const int g = live ? tid : GB_NGPT - 1;
-  const int band = c_T.ngb[g] - 1;
-  const float wgt = live ? (float)(0.5 * (double)c_T.delwave[band] * c_T.fluxfac) : 0.0f;
+  const int band = __float_as_int(__ldg(T + c_T.gpt_band + g));
+  const float wgt = live ? __ldg(T + c_T.gpt_wgt + g) : 0.0f;
   __syncthreads();
 
   // ---------------- per layer: inatm's column amounts (pwvcm), value checks, laytrop, Planck rows

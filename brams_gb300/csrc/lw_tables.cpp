@@ -287,6 +287,13 @@ bool gb_build_tables(const char* ref_path, const char* k_path, double cpdair, Gb
   T.avogad = avog->d[0];
   T.heatfac = grav->d[0] * secdy->d[0] / (cpdair * 1.e2);  // lwdatinit :298
   T.fluxfac = 2.0 * std::asin(1.0) * 2.e4;                   // rrtmg_lw_rad.f90:453
+  T.gpt_band = push(GB_NGPT);
+  T.gpt_wgt = push(GB_NGPT);
+  for (int g = 0; g < GB_NGPT; ++g) {
+    const int b = T.ngb[g] - 1;
+    std::memcpy(&blob[T.gpt_band + g], &b, 4);
+    blob[T.gpt_wgt + g] = (float)(0.5 * (double)T.delwave[b] * T.fluxfac);
+  }
   // pad to a multiple of 4 floats (16 bytes)
   while (blob.size() % 4) blob.push_back(0.0f);
   T.total_floats = (int)blob.size();
