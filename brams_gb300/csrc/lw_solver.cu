@@ -117,6 +117,32 @@ __device__ __forceinline__ float reduce4(float v0, float v1, float v2, float v3,
   return k;
 }
 
+// Warp sums of eight values per lane at once: lane i returns the sum over the
+// 32 lanes of v[i & 7] (three exchanges, then two xor steps: 9 shuffles).
+__device__ __forceinline__ float reduce8(float v0, float v1, float v2, float v3, float v4, float v5, float v6,
+                                         float v7, int lane) {
+  const unsigned F = 0xffffffffu;
+  const bool h4 = lane & 4;
+  float a0 = h4 ? v4 : v0, a1 = h4 ? v5 : v1, a2 = h4 ? v6 : v2, a3 = h4 ? v7 : v3;
+  const float b0 = h4 ? v0 : v4, b1 = h4 ? v1 : v5, b2 = h4 ? v2 : v6, b3 = h4 ? v3 : v7;
+  a0 += __shfl_xor_sync(F, b0, 4);
+  a1 += __shfl_xor_sync(F, b1, 4);
+  a2 += __shfl_xor_sync(F, b2, 4);
+  a3 += __shfl_xor_sync(F, b3, 4);
+  const bool h2 = lane & 2;
+  float c0 = h2 ? a2 : a0, c1 = h2 ? a3 : a1;
+  const float d0 = h2 ? a0 : a2, d1 = h2 ? a1 : a3;
+  c0 += __shfl_xor_sync(F, d0, 2);
+  c1 += __shfl_xor_sync(F, d1, 2);
+  const bool h1 = lane & 1;
+  float k = h1 ? c1 : c0;
+  const float e = h1 ? c0 : c1;
+  k += __shfl_xor_sync(F, e, 1);
+  k += __shfl_xor_sync(F, k, 8);
+  k += __shfl_xor_sync(F, k, 16);
+  return k;
+}
+
 // rtrnmc's table index of an optical depth (rrtmg_lw_rtrnmc.f90:385-388):
 // itr = int(tblint * od / (bpade + od) + 0.5), within 0 .. ntbl
 __device__ __forceinline__ int tbl_index(float od) {
@@ -442,35 +468,14 @@ struct Clr {
   int itr;
   bool thin;
 };
-__device__ __forceinline__ Clr clear_cell(float od, int itr, float2 e) {
+__device__ __forceinline__ Clr clear_cell(const float* __restrict__ T, float od) {
   Clr c;
   c.thin = od <= 0.06f;
-  c.itr = itr;
+  c.itr = tbl_index(od);
+  const float2 e = tbl_tt(T, c.itr);  // looked up for every cell (branch-free), used above 0.06
   c.atrans = c.thin ? fmaf(-0.5f * od, od, od) : 1.0f - e.x;
   c.x = c.thin ? REC_6 * od : e.y;
   return c;
-}
-
-// One layer of a g-point as the passes consume it: the Planck fraction, the
-// layer's Planck values and aerosol depth, the clear-sky optical depth along
-// the diffusivity angle, its table index and the table entry (looked up for
-// every cell, used above 0.06).  The passes set up the next layer's stage
-// while they finish the current one, so the table load is in flight meanwhile.
-struct Stage {
-  float pf, od;
-  float4 r;
-  int itr;
-  float2 tt;
-};
-__device__ __forceinline__ Stage stage_of(const RtSmem& S, const float* __restrict__ T, int lay, int band, float sd,
-                                          float tg, float pf) {
-  Stage st;
-  st.pf = pf;
-  st.r = S.L[lay].rec[band];
-  st.od = fmaxf(sd * (tg + st.r.w), 0.0f);
-  st.itr = tbl_index(st.od);
-  st.tt = tbl_tt(T, st.itr);
-  return st;
 }
 
 // Total (gas + cloud) absorptance and source factor of a cloudy cell
@@ -789,28 +794,17 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
   float* part = S.part + warp * (nl + 1) * 6;  // this warp's level sums
 
   // ---------------- downward pass (rtrnmc.f90:347-455): total and clear-sky streams
-  // Software pipeline: in the step for layer lay, the gas optics of lay-2 are
-  // loaded and the stage (table lookup) of lay-1 is set up.
-  float rd = 0.0f, rc = 0.0f, f1 = 0.0f, tga = 0.0f, pfa = 0.0f;
-  Stage cur;
-  {
-    float tg, pf;
-    gas_at<MODE>(src, layer_on_net<MODE>(src, nl - 1), nl - 1, g, tg, pf);
-    cur = stage_of(S, T, nl - 1, band, sd, tg, pf);
-    if (nl >= 2) gas_at<MODE>(src, layer_on_net<MODE>(src, nl - 2), nl - 2, g, tga, pfa);
-  }
+  // The next layer's gas optics are loaded while this one is done; the
+  // level sums of two layers share one transposed butterfly.
+  float rd = 0.0f, rc = 0.0f, f1 = 0.0f, tgn, pfn, p0 = 0.0f, p1 = 0.0f;
+  bool pend = false;  // a layer's weighted radiances wait in p0, p1 (the same in every lane)
+  gas_at<MODE>(src, layer_on_net<MODE>(src, nl - 1), nl - 1, g, tgn, pfn);
   for (int lay = nl - 1; lay >= 0; --lay) {
-    Stage nxt = cur;
-    if (lay >= 1) {
-      float tgb = 0.0f, pfb = 0.0f;
-      if (lay >= 2) gas_at<MODE>(src, layer_on_net<MODE>(src, lay - 2), lay - 2, g, tgb, pfb);
-      nxt = stage_of(S, T, lay - 1, band, sd, tga, pfa);
-      tga = tgb;
-      pfa = pfb;
-    }
-    const float pf = cur.pf, od = cur.od;
-    const float4 r = cur.r;
-    const Clr c = clear_cell(od, cur.itr, cur.tt);
+    const float tg = tgn, pf = pfn;
+    if (lay > 0) gas_at<MODE>(src, layer_on_net<MODE>(src, lay - 1), lay - 1, g, tgn, pfn);  // in flight meanwhile
+    const float4 r = S.L[lay].rec[band];
+    const float od = fmaxf(sd * (tg + r.w), 0.0f);
+    const Clr c = clear_cell(T, od);
     const float gsd = pf * fmaf(c.x, r.y, r.x) * c.atrans;
     const float tr = 1.0f - c.atrans;
     rc = fmaf(rc, tr, gsd);
@@ -827,9 +821,18 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
     }
     rd = fmaf(rd, A, B);
     if (lay == 0) f1 = pf;
-    const float s = reduce2(rd * wgt, rc * wgt, lane);
-    if (lane < 2) part[lay * 6 + lane] = s;
-    cur = nxt;
+    if (pend) {  // lanes 0, 1: layer lay+1; lanes 2, 3: layer lay
+      const float s = reduce4(p0, p1, rd * wgt, rc * wgt, lane);
+      if (lane < 4) part[(lay + 1 - (lane >> 1)) * 6 + (lane & 1)] = s;
+    } else {
+      p0 = rd * wgt;
+      p1 = rc * wgt;
+    }
+    pend = !pend;
+  }
+  if (pend) {  // layer 0 on its own
+    const float s = reduce2(p0, p1, lane);
+    if (lane < 2) part[lane] = s;
   }
 
   // ---------------- surface emission and reflection (rtrnmc.f90:465-485)
@@ -848,24 +851,15 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
     if (lane < 2) part[2 + lane] = s;
   }
   // ---------------- upward pass (rtrnmc.f90:486-529): level lay+1 above layer lay
-  {
-    float tg, pf;
-    gas_at<MODE>(src, layer_on_net<MODE>(src, 0), 0, g, tg, pf);
-    cur = stage_of(S, T, 0, band, sd, tg, pf);
-    if (nl >= 2) gas_at<MODE>(src, layer_on_net<MODE>(src, 1), 1, g, tga, pfa);
-  }
+  float q0 = 0.0f, q1 = 0.0f, q2 = 0.0f, q3 = 0.0f;
+  pend = false;  // a layer's weighted values wait in q0..q3
+  gas_at<MODE>(src, layer_on_net<MODE>(src, 0), 0, g, tgn, pfn);
   for (int lay = 0; lay < nl; ++lay) {
-    Stage nxt = cur;
-    if (lay + 1 < nl) {
-      float tgb = 0.0f, pfb = 0.0f;
-      if (lay + 2 < nl) gas_at<MODE>(src, layer_on_net<MODE>(src, lay + 2), lay + 2, g, tgb, pfb);
-      nxt = stage_of(S, T, lay + 1, band, sd, tga, pfa);
-      tga = tgb;
-      pfa = pfb;
-    }
-    const float pf = cur.pf, od = cur.od;
-    const float4 r = cur.r;
-    const Clr c = clear_cell(od, cur.itr, cur.tt);
+    const float tg = tgn, pf = pfn;
+    if (lay + 1 < nl) gas_at<MODE>(src, layer_on_net<MODE>(src, lay + 1), lay + 1, g, tgn, pfn);
+    const float4 r = S.L[lay].rec[band];
+    const float od = fmaxf(sd * (tg + r.w), 0.0f);
+    const Clr c = clear_cell(T, od);
     const float gsu = pf * fmaf(c.x, r.z, r.x) * c.atrans;
     const float tr = 1.0f - c.atrans;
     rcu = fmaf(rcu, tr, gsu);
@@ -884,15 +878,31 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
     }
     ru = fmaf(ru, A, B);
     du *= D;
-    float* p = part + (lay + 1) * 6 + 2;
+    if (pend) {  // levels lay (the layer below) and lay+1
+      if (idrv) {
+        const float s = reduce8(q0, q1, q2, q3, ru * wgt, rcu * wgt, du * wgt, dcu * wgt, lane);
+        if (lane < 8) part[(lay + (lane >> 2)) * 6 + 2 + (lane & 3)] = s;
+      } else {
+        const float s = reduce4(q0, q1, ru * wgt, rcu * wgt, lane);
+        if (lane < 4) part[(lay + (lane >> 1)) * 6 + 2 + (lane & 1)] = s;
+      }
+    } else {
+      q0 = ru * wgt;
+      q1 = rcu * wgt;
+      q2 = du * wgt;
+      q3 = dcu * wgt;
+    }
+    pend = !pend;
+  }
+  if (pend) {  // level nl on its own
+    float* p = part + nl * 6 + 2;
     if (idrv) {
-      const float s = reduce4(ru * wgt, rcu * wgt, du * wgt, dcu * wgt, lane);
+      const float s = reduce4(q0, q1, q2, q3, lane);
       if (lane < 4) p[lane] = s;
     } else {
-      const float s = reduce2(ru * wgt, rcu * wgt, lane);
+      const float s = reduce2(q0, q1, lane);
       if (lane < 2) p[lane] = s;
     }
-    cur = nxt;
   }
   __syncthreads();
 
