@@ -40,6 +40,9 @@ struct GbTables {
   // 0 h2o/co2, 1 h2o/o3, 2 h2o/n2o, 3 h2o/ch4, 4 n2o/co2, 5 o3/co2
   float rat[6][59];
   float delwave[GB_NBND];
+  // double-precision copies for the decisions near truncation and branch
+  // boundaries that are re-taken in fp64 (setcoef's jp/jt/jt1, taumol's specparm)
+  double preflog64[59], tref64[59], chi64[7][59];
   // the same reference-atmosphere values in the float blob, for lookups whose
   // index differs from thread to thread: preflog[59], tref[59], chi[7][59], rat[6][59]
   int ref_preflog, ref_tref, ref_chi, ref_rat;

@@ -55,13 +55,36 @@ __host__ __device__ constexpr int g0_const(int b) {
   return m[b];
 }
 
+// fp64 column amounts of the binary species kept per layer (for decisions
+// near a stencil switch or a truncation, re-taken in double precision)
+enum LayerDouble { D_H2O, D_CO2, D_O3, D_N2O, D_CH4, ND };
+
+// A binary-species amount: its fp32 value and the index of its fp64 copy.
+struct Amt {
+  float v;
+  int d;
+  __device__ __forceinline__ operator float() const { return v; }
+};
+// A chi_mls ratio chi(m1, jp) / chi(m2, jp): its fp32 value and how to form it in fp64.
+struct Rat {
+  float v;
+  int m1, m2, jp;
+};
+
 struct Cell {
   const float* f;  // [NF][nl] shared memory
   const int* iv;   // [NI][nl] shared memory
   int nl, lay;
   const float* T;  // device table blob
+  const double* d; // [ND][nl] shared memory: fp64 column amounts
   __device__ __forceinline__ float F(int k) const { return f[k * nl + lay]; }
   __device__ __forceinline__ int I(int k) const { return iv[k * nl + lay]; }
+  __device__ __forceinline__ double D(int k) const { return d[k * nl + lay]; }
+  __device__ __forceinline__ Amt A(int field) const {
+    const int k = field == F_COLH2O ? D_H2O : field == F_COLCO2 ? D_CO2 : field == F_COLO3 ? D_O3
+                : field == F_COLN2O ? D_N2O : D_CH4;
+    return Amt{F(field), k};
+  }
 };
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
@@ -95,23 +118,66 @@ struct Terms {
 // read from the table blob (global memory) rather than the constant bank,
 // which serialises loads whose address differs between threads
 __device__ __forceinline__ float chi(const Cell& c, int m, int jp) { return __ldg(c.T + c_T.ref_chi + (m - 1) * 59 + jp - 1); }
-__device__ __forceinline__ float rat(const Cell& c, int k, int jp) { return __ldg(c.T + c_T.ref_rat + k * 59 + jp - 1); }
+// setcoef's per-layer ratios (setcoef.f90:333-346, 387-394): 0 h2o/co2,
+// 1 h2o/o3, 2 h2o/n2o, 3 h2o/ch4, 4 n2o/co2, 5 o3/co2
+__device__ __forceinline__ Rat rat(const Cell& c, int k, int jp) {
+  constexpr int m1[6] = {1, 1, 1, 1, 4, 3}, m2[6] = {2, 3, 4, 6, 2, 2};
+  return Rat{__ldg(c.T + c_T.ref_rat + k * 59 + jp - 1), m1[k], m2[k], jp};
+}
+// a ratio of chi_mls entries at a fixed reference level (the refrat_* constants)
+__device__ __forceinline__ Rat ratio(const Cell& c, int m1, int m2, int jp) {
+  return Rat{chi(c, m1, jp) / chi(c, m2, jp), m1, m2, jp};
+}
 
 struct Spec {
   float comb, parm, f;
   int j;
+  int mode;  // 1: specparm < 0.125, 2: specparm > 0.875, 0: between (taumol.f90:582-611)
 };
-// speccomb/specparm/specmult/js/fs (e.g. taumol.f90:517-522); oneminus = 1 - 1e-6
-__device__ __forceinline__ Spec spec(float a, float rat, float b, float scale, int jmax) {
+// speccomb/specparm/specmult/js/fs (e.g. taumol.f90:517-522); oneminus = 1 - 1e-6.
+// Computed in fp32; where specparm lies within 1e-5 of 0.125 or 0.875, or
+// scale * specparm within 1e-4 of an integer, the decisions (stencil mode,
+// js, fs) are re-taken in fp64 from the fp64 column amounts and ratio, as the
+// reference computes them.
+// the fp64 decisions of spec() (rarely taken: kept out of line so that the
+// band prologues stay small)
+__device__ __noinline__ Spec spec_fp64(double a64, double b64, int m1, int m2, int jp, float scale, int jmax) {
   Spec s;
-  s.comb = a + rat * b;
-  s.parm = __fdividef(a, s.comb);
+  const double r64 = c_T.chi64[m1 - 1][jp - 1] / c_T.chi64[m2 - 1][jp - 1];
+  s.comb = (float)(a64 + r64 * b64);
+  double p64 = a64 / (a64 + r64 * b64);
+  if (p64 >= 1.0 - 1.e-6) p64 = 1.0 - 1.e-6;
+  if (!(p64 >= 0.0)) p64 = 0.0;
+  const double m64 = (double)scale * p64;
+  const int ji = (int)m64;
+  s.parm = (float)p64;
+  s.j = clampi(1 + ji, 1, jmax);
+  s.f = (float)(m64 - (double)ji);
+  s.mode = p64 < 0.125 ? 1 : (p64 > 0.875 ? 2 : 0);
+  return s;
+}
+
+__device__ __forceinline__ Spec spec(const Cell& c, Amt a, Rat rat, Amt b, float scale, int jmax) {
+  Spec s;
+  s.comb = a.v + rat.v * b.v;
+  s.parm = __fdividef(a.v, s.comb);
   if (!(s.parm < 0.999999f)) s.parm = 0.999999f;
   if (!(s.parm >= 0.0f)) s.parm = 0.0f;  // negative amounts: outside the tables' domain
   float mult = scale * s.parm;
+  const bool near = fabsf(s.parm - 0.125f) < 1.0e-5f || fabsf(s.parm - 0.875f) < 1.0e-5f ||
+                    fabsf(mult - rintf(mult)) < 1.0e-4f;
+  if (near) {
+    const Spec d = spec_fp64(c.D(a.d), c.D(b.d), rat.m1, rat.m2, rat.jp, scale, jmax);
+    s.parm = d.parm;
+    s.j = d.j;
+    s.f = d.f;
+    s.mode = d.mode;
+    return s;
+  }
   int ji = (int)mult;
   s.j = clampi(1 + ji, 1, jmax);
   s.f = mult - (float)ji;
+  s.mode = s.parm < 0.125f ? 1 : (s.parm > 0.875f ? 2 : 0);
   return s;
 }
 
@@ -171,12 +237,12 @@ __device__ __forceinline__ void single_upper_terms(Terms& t, const Cell& c, floa
 // six terms in every mode (the interior two-point mode pads with zeros)
 __device__ __forceinline__ void stencil9_terms(Terms& t, const Spec& s, int ind, float fa, float fb, int ka, int ng) {
   auto R = [&](int i) { return ka + (i - 1) * ng; };
-  if (s.parm < 0.125f) {
+  if (s.mode == 1) {
     float p = s.f - 1.0f, p4 = (p * p) * (p * p);
     float k0 = p4, k1 = 1.0f - p - 2.0f * p4, k2 = p + p4;
     t.add(s.comb * k0 * fa, R(ind)); t.add(s.comb * k1 * fa, R(ind + 1)); t.add(s.comb * k2 * fa, R(ind + 2));
     t.add(s.comb * k0 * fb, R(ind + 9)); t.add(s.comb * k1 * fb, R(ind + 10)); t.add(s.comb * k2 * fb, R(ind + 11));
-  } else if (s.parm > 0.875f) {
+  } else if (s.mode == 2) {
     float p = -s.f, p4 = (p * p) * (p * p);
     float k0 = p4, k1 = 1.0f - p - 2.0f * p4, k2 = p + p4;
     t.add(s.comb * k2 * fa, R(ind - 1)); t.add(s.comb * k1 * fa, R(ind)); t.add(s.comb * k0 * fa, R(ind + 1));
@@ -187,8 +253,8 @@ __device__ __forceinline__ void stencil9_terms(Terms& t, const Spec& s, int ind,
   }
 }
 __device__ __forceinline__ int js_lower(const Spec& s) {
-  if (s.parm < 0.125f) return clampi(s.j, 1, 7);
-  if (s.parm > 0.875f) return clampi(s.j, 2, 8);
+  if (s.mode == 1) return clampi(s.j, 1, 7);
+  if (s.mode == 2) return clampi(s.j, 2, 8);
   return clampi(s.j, 1, 8);
 }
 __device__ __forceinline__ void binary_lower_terms(Terms& t, const Cell& c, const Spec& s, const Spec& s1, int ka, int ng) {
@@ -278,20 +344,20 @@ template <>
 __device__ FracRec prologue<3>(const Cell& c, bool lower, Terms& t) {
   constexpr int b = 3;
   int jp = clampi(c.I(I_JP), 1, 58);
-  float h2o = c.F(F_COLH2O), co2 = c.F(F_COLCO2);
+  const Amt h2o = c.A(F_COLH2O), co2 = c.A(F_COLCO2);
   float adjcoln2o = adj_n2o(c);
   if (lower) {
-    Spec s = spec(h2o, rat(c, 0, jp), co2, 8.0f, 9), s1 = spec(h2o, rat(c, 0, jp + 1), co2, 8.0f, 9);
-    Spec sm = spec(h2o, chi(c, 1, 3) / chi(c, 2, 3), co2, 8.0f, 9);
-    Spec sp = spec(h2o, chi(c, 1, 9) / chi(c, 2, 9), co2, 8.0f, 9);
+    Spec s = spec(c, h2o, rat(c, 0, jp), co2, 8.0f, 9), s1 = spec(c, h2o, rat(c, 0, jp + 1), co2, 8.0f, 9);
+    Spec sm = spec(c, h2o, ratio(c, 1, 2, 3), co2, 8.0f, 9);
+    Spec sp = spec(c, h2o, ratio(c, 1, 2, 9), co2, 8.0f, 9);
     binary_lower_terms(t, c, s, s1, BT.ka, NGB);
     self_terms(t, c, BT.sr, NGB);
     for_terms(t, c, BT.fo, NGB);
     minor_et_terms(t, c, adjcoln2o, BT.ma0, 9, NGB, sm.j, sm.f);
     return {BT.fa + (sp.j - 1) * NGB, sp.f};
   }
-  Spec s = spec(h2o, rat(c, 0, jp), co2, 4.0f, 5), s1 = spec(h2o, rat(c, 0, jp + 1), co2, 4.0f, 5);
-  Spec sm = spec(h2o, chi(c, 1, 13) / chi(c, 2, 13), co2, 4.0f, 5);
+  Spec s = spec(c, h2o, rat(c, 0, jp), co2, 4.0f, 5), s1 = spec(c, h2o, rat(c, 0, jp + 1), co2, 4.0f, 5);
+  Spec sm = spec(c, h2o, ratio(c, 1, 2, 13), co2, 4.0f, 5);
   binary_upper_terms(t, c, s, s1, BT.kb, NGB);
   for_terms(t, c, BT.fo, NGB);
   minor_et_terms(t, c, adjcoln2o, BT.mb0, 5, NGB, sm.j, sm.f);
@@ -304,17 +370,17 @@ __device__ FracRec prologue<4>(const Cell& c, bool lower, Terms& t) {
   constexpr int b = 4;
   int jp = clampi(c.I(I_JP), 1, 58);
   if (lower) {
-    float h2o = c.F(F_COLH2O), co2 = c.F(F_COLCO2);
-    Spec s = spec(h2o, rat(c, 0, jp), co2, 8.0f, 9), s1 = spec(h2o, rat(c, 0, jp + 1), co2, 8.0f, 9);
-    Spec sp = spec(h2o, chi(c, 1, 11) / chi(c, 2, 11), co2, 8.0f, 9);
+    const Amt h2o = c.A(F_COLH2O), co2 = c.A(F_COLCO2);
+    Spec s = spec(c, h2o, rat(c, 0, jp), co2, 8.0f, 9), s1 = spec(c, h2o, rat(c, 0, jp + 1), co2, 8.0f, 9);
+    Spec sp = spec(c, h2o, ratio(c, 1, 2, 11), co2, 8.0f, 9);
     binary_lower_terms(t, c, s, s1, BT.ka, NGB);
     self_terms(t, c, BT.sr, NGB);
     for_terms(t, c, BT.fo, NGB);
     return {BT.fa + (sp.j - 1) * NGB, sp.f};
   }
-  float o3 = c.F(F_COLO3), co2 = c.F(F_COLCO2);
-  Spec s = spec(o3, rat(c, 5, jp), co2, 4.0f, 5), s1 = spec(o3, rat(c, 5, jp + 1), co2, 4.0f, 5);
-  Spec sp = spec(o3, chi(c, 3, 13) / chi(c, 2, 13), co2, 4.0f, 5);
+  const Amt o3 = c.A(F_COLO3), co2 = c.A(F_COLCO2);
+  Spec s = spec(c, o3, rat(c, 5, jp), co2, 4.0f, 5), s1 = spec(c, o3, rat(c, 5, jp + 1), co2, 4.0f, 5);
+  Spec sp = spec(c, o3, ratio(c, 3, 2, 13), co2, 4.0f, 5);
   binary_upper_terms(t, c, s, s1, BT.kb, NGB);
   return {BT.fb + (clampi(sp.j, 1, 4) - 1) * NGB, sp.f};
 }
@@ -325,10 +391,10 @@ __device__ FracRec prologue<5>(const Cell& c, bool lower, Terms& t) {
   constexpr int b = 5;
   int jp = clampi(c.I(I_JP), 1, 58);
   if (lower) {
-    float h2o = c.F(F_COLH2O), co2 = c.F(F_COLCO2);
-    Spec s = spec(h2o, rat(c, 0, jp), co2, 8.0f, 9), s1 = spec(h2o, rat(c, 0, jp + 1), co2, 8.0f, 9);
-    Spec sm = spec(h2o, chi(c, 1, 7) / chi(c, 2, 7), co2, 8.0f, 9);
-    Spec sp = spec(h2o, chi(c, 1, 5) / chi(c, 2, 5), co2, 8.0f, 9);
+    const Amt h2o = c.A(F_COLH2O), co2 = c.A(F_COLCO2);
+    Spec s = spec(c, h2o, rat(c, 0, jp), co2, 8.0f, 9), s1 = spec(c, h2o, rat(c, 0, jp + 1), co2, 8.0f, 9);
+    Spec sm = spec(c, h2o, ratio(c, 1, 2, 7), co2, 8.0f, 9);
+    Spec sp = spec(c, h2o, ratio(c, 1, 2, 5), co2, 8.0f, 9);
     binary_lower_terms(t, c, s, s1, BT.ka, NGB);
     self_terms(t, c, BT.sr, NGB);
     for_terms(t, c, BT.fo, NGB);
@@ -336,9 +402,9 @@ __device__ FracRec prologue<5>(const Cell& c, bool lower, Terms& t) {
     t.add(c.F(F_WX1), BT.x0);
     return {BT.fa + (sp.j - 1) * NGB, sp.f};
   }
-  float o3 = c.F(F_COLO3), co2 = c.F(F_COLCO2);
-  Spec s = spec(o3, rat(c, 5, jp), co2, 4.0f, 5), s1 = spec(o3, rat(c, 5, jp + 1), co2, 4.0f, 5);
-  Spec sp = spec(o3, chi(c, 3, 43) / chi(c, 2, 43), co2, 4.0f, 5);
+  const Amt o3 = c.A(F_COLO3), co2 = c.A(F_COLCO2);
+  Spec s = spec(c, o3, rat(c, 5, jp), co2, 4.0f, 5), s1 = spec(c, o3, rat(c, 5, jp + 1), co2, 4.0f, 5);
+  Spec sp = spec(c, o3, ratio(c, 3, 2, 43), co2, 4.0f, 5);
   binary_upper_terms(t, c, s, s1, BT.kb, NGB);
   t.add(c.F(F_WX1), BT.x0);
   return {BT.fb + (clampi(sp.j, 1, 4) - 1) * NGB, sp.f};
@@ -367,9 +433,9 @@ __device__ FracRec prologue<7>(const Cell& c, bool lower, Terms& t) {
   constexpr int b = 7;
   int jp = clampi(c.I(I_JP), 1, 58);
   if (lower) {
-    float h2o = c.F(F_COLH2O), o3 = c.F(F_COLO3);
-    Spec s = spec(h2o, rat(c, 1, jp), o3, 8.0f, 9), s1 = spec(h2o, rat(c, 1, jp + 1), o3, 8.0f, 9);
-    Spec sm = spec(h2o, chi(c, 1, 3) / chi(c, 3, 3), o3, 8.0f, 9);  // minor and planck use the same ratio
+    const Amt h2o = c.A(F_COLH2O), o3 = c.A(F_COLO3);
+    Spec s = spec(c, h2o, rat(c, 1, jp), o3, 8.0f, 9), s1 = spec(c, h2o, rat(c, 1, jp + 1), o3, 8.0f, 9);
+    Spec sm = spec(c, h2o, ratio(c, 1, 3, 3), o3, 8.0f, 9);  // minor and planck use the same ratio
     float adjcolco2 = adj_col(c.F(F_COLCO2), c.F(F_COLDRY), chi(c, 2, jp + 1), 3.0f, 3.0f, 0.79f);
     binary_lower_terms(t, c, s, s1, BT.ka, NGB);
     self_terms(t, c, BT.sr, NGB);
@@ -415,10 +481,10 @@ __device__ FracRec prologue<9>(const Cell& c, bool lower, Terms& t) {
   int jp = clampi(c.I(I_JP), 1, 58);
   float adjcoln2o = adj_n2o(c);
   if (lower) {
-    float h2o = c.F(F_COLH2O), ch4 = c.F(F_COLCH4);
-    Spec s = spec(h2o, rat(c, 3, jp), ch4, 8.0f, 9), s1 = spec(h2o, rat(c, 3, jp + 1), ch4, 8.0f, 9);
-    Spec sm = spec(h2o, chi(c, 1, 3) / chi(c, 6, 3), ch4, 8.0f, 9);
-    Spec sp = spec(h2o, chi(c, 1, 9) / chi(c, 6, 9), ch4, 8.0f, 9);
+    const Amt h2o = c.A(F_COLH2O), ch4 = c.A(F_COLCH4);
+    Spec s = spec(c, h2o, rat(c, 3, jp), ch4, 8.0f, 9), s1 = spec(c, h2o, rat(c, 3, jp + 1), ch4, 8.0f, 9);
+    Spec sm = spec(c, h2o, ratio(c, 1, 6, 3), ch4, 8.0f, 9);
+    Spec sp = spec(c, h2o, ratio(c, 1, 6, 9), ch4, 8.0f, 9);
     binary_lower_terms(t, c, s, s1, BT.ka, NGB);
     self_terms(t, c, BT.sr, NGB);
     for_terms(t, c, BT.fo, NGB);
@@ -469,9 +535,9 @@ __device__ FracRec prologue<12>(const Cell& c, bool lower, Terms& t) {
   constexpr int b = 12;
   if (!lower) return {c_T.zero_row, 0.0f};
   int jp = clampi(c.I(I_JP), 1, 58);
-  float h2o = c.F(F_COLH2O), co2 = c.F(F_COLCO2);
-  Spec s = spec(h2o, rat(c, 0, jp), co2, 8.0f, 9), s1 = spec(h2o, rat(c, 0, jp + 1), co2, 8.0f, 9);
-  Spec sp = spec(h2o, chi(c, 1, 10) / chi(c, 2, 10), co2, 8.0f, 9);
+  const Amt h2o = c.A(F_COLH2O), co2 = c.A(F_COLCO2);
+  Spec s = spec(c, h2o, rat(c, 0, jp), co2, 8.0f, 9), s1 = spec(c, h2o, rat(c, 0, jp + 1), co2, 8.0f, 9);
+  Spec sp = spec(c, h2o, ratio(c, 1, 2, 10), co2, 8.0f, 9);
   binary_lower_terms(t, c, s, s1, BT.ka, NGB);
   self_terms(t, c, BT.sr, NGB);
   for_terms(t, c, BT.fo, NGB);
@@ -487,11 +553,11 @@ __device__ FracRec prologue<13>(const Cell& c, bool lower, Terms& t) {
     return {BT.fb, 0.0f};
   }
   int jp = clampi(c.I(I_JP), 1, 58);
-  float h2o = c.F(F_COLH2O), n2o = c.F(F_COLN2O);
-  Spec s = spec(h2o, rat(c, 2, jp), n2o, 8.0f, 9), s1 = spec(h2o, rat(c, 2, jp + 1), n2o, 8.0f, 9);
-  Spec sm = spec(h2o, chi(c, 1, 1) / chi(c, 4, 1), n2o, 8.0f, 9);
-  Spec sm3 = spec(h2o, chi(c, 1, 3) / chi(c, 4, 3), n2o, 8.0f, 9);
-  Spec sp = spec(h2o, chi(c, 1, 5) / chi(c, 4, 5), n2o, 8.0f, 9);
+  const Amt h2o = c.A(F_COLH2O), n2o = c.A(F_COLN2O);
+  Spec s = spec(c, h2o, rat(c, 2, jp), n2o, 8.0f, 9), s1 = spec(c, h2o, rat(c, 2, jp + 1), n2o, 8.0f, 9);
+  Spec sm = spec(c, h2o, ratio(c, 1, 4, 1), n2o, 8.0f, 9);
+  Spec sm3 = spec(c, h2o, ratio(c, 1, 4, 3), n2o, 8.0f, 9);
+  Spec sp = spec(c, h2o, ratio(c, 1, 4, 5), n2o, 8.0f, 9);
   // CO2 adjustment against the fixed 3.55e-4 reference (taumol.f90:2532-2540)
   float co2 = c.F(F_COLCO2), coldry = c.F(F_COLDRY);
   float ratio = 1.e20f * __fdividef(__fdividef(co2, coldry), 3.55e-4f);
@@ -525,9 +591,9 @@ __device__ FracRec prologue<15>(const Cell& c, bool lower, Terms& t) {
   constexpr int b = 15;
   if (!lower) return {c_T.zero_row, 0.0f};
   int jp = clampi(c.I(I_JP), 1, 58);
-  float n2o = c.F(F_COLN2O), co2 = c.F(F_COLCO2);
-  Spec s = spec(n2o, rat(c, 4, jp), co2, 8.0f, 9), s1 = spec(n2o, rat(c, 4, jp + 1), co2, 8.0f, 9);
-  Spec sm = spec(n2o, chi(c, 4, 1) / chi(c, 2, 1), co2, 8.0f, 9);  // minor and planck share the ratio
+  const Amt n2o = c.A(F_COLN2O), co2 = c.A(F_COLCO2);
+  Spec s = spec(c, n2o, rat(c, 4, jp), co2, 8.0f, 9), s1 = spec(c, n2o, rat(c, 4, jp + 1), co2, 8.0f, 9);
+  Spec sm = spec(c, n2o, ratio(c, 4, 2, 1), co2, 8.0f, 9);  // minor and planck share the ratio
   binary_lower_terms(t, c, s, s1, BT.ka, NGB);
   self_terms(t, c, BT.sr, NGB);
   for_terms(t, c, BT.fo, NGB);
@@ -541,9 +607,9 @@ __device__ FracRec prologue<16>(const Cell& c, bool lower, Terms& t) {
   constexpr int b = 16;
   if (lower) {
     int jp = clampi(c.I(I_JP), 1, 58);
-    float h2o = c.F(F_COLH2O), ch4 = c.F(F_COLCH4);
-    Spec s = spec(h2o, rat(c, 3, jp), ch4, 8.0f, 9), s1 = spec(h2o, rat(c, 3, jp + 1), ch4, 8.0f, 9);
-    Spec sp = spec(h2o, chi(c, 1, 6) / chi(c, 6, 6), ch4, 8.0f, 9);
+    const Amt h2o = c.A(F_COLH2O), ch4 = c.A(F_COLCH4);
+    Spec s = spec(c, h2o, rat(c, 3, jp), ch4, 8.0f, 9), s1 = spec(c, h2o, rat(c, 3, jp + 1), ch4, 8.0f, 9);
+    Spec sp = spec(c, h2o, ratio(c, 1, 6, 6), ch4, 8.0f, 9);
     binary_lower_terms(t, c, s, s1, BT.ka, NGB);
     self_terms(t, c, BT.sr, NGB);
     for_terms(t, c, BT.fo, NGB);

@@ -200,11 +200,13 @@ struct GasSmem {
   int* iv;         // [NI][nl]
   float2* terms;   // [TGROUP][nl] gas-optics terms of the current band, term-major
   FracRec* frec;   // [nl] Planck-fraction records of the current band
+  double* d;       // [ND][nl] fp64 column amounts of the binary species
   int* iscal;      // [4]: laytrop
 };
 
 __host__ __device__ inline size_t gas_smem_bytes(int nl) {
-  return align16((size_t)(NF + NI) * nl * 4) + align16((size_t)nl * TGROUP * 8) + align16((size_t)nl * sizeof(FracRec)) + 16;
+  return align16((size_t)(NF + NI) * nl * 4) + align16((size_t)nl * TGROUP * 8) + align16((size_t)nl * sizeof(FracRec)) +
+         align16((size_t)ND * nl * 8) + 16;
 }
 
 __device__ inline GasSmem gas_carve(char* p, int nl) {
@@ -216,6 +218,8 @@ __device__ inline GasSmem gas_carve(char* p, int nl) {
   p += align16((size_t)nl * TGROUP * 8);
   s.frec = (FracRec*)p;
   p += align16((size_t)nl * sizeof(FracRec));
+  s.d = (double*)p;
+  p += align16((size_t)ND * nl * 8);
   s.iscal = (int*)p;
   return s;
 }
@@ -224,7 +228,7 @@ __device__ inline GasSmem gas_carve(char* p, int nl) {
 // (lw_gasoptics.cuh) writing the layer's terms and Planck-fraction record.
 template <int b>
 __device__ __forceinline__ void band_prologue(const GasSmem& s, int nl, int lay, bool lower, const float* T) {
-  Cell c{s.f, s.iv, nl, lay, T};
+  Cell c{s.f, s.iv, nl, lay, T, s.d};
   Terms t{s.terms + lay, nl, 0};
   FracRec r = prologue<b>(c, lower, t);
   t.pad(maxt(b), c_T.band[b - 1].sr);
@@ -301,26 +305,57 @@ __device__ void gas_column(const LwArgs& a, long long icol, const GasSmem& s, fl
     put(F_WX4, coldry * (float)in2(a.cfc22vmr, a.ld, icol, lay) * 1.e-20f);
     const float plog = __logf(pavel);
     const bool lower = lower_atmosphere(pd, plog);
-    int jp = clampi((int)(36.0f - 5.0f * (plog + 0.04f)), 1, 58);
+    // The truncations jp, jt, jt1 (setcoef.f90:276-306) are taken in fp32 and
+    // re-taken in fp64, as the reference computes them, where the fp32 value
+    // lies near an integer.
+    const double td = in2(a.tlay, a.ld, icol, lay);
+    const float xjp = 36.0f - 5.0f * (plog + 0.04f);
+    int jp = (int)xjp;
+    if (fabsf(xjp - rintf(xjp)) < 2.0e-3f) jp = (int)(36.0 - 5 * (log(pd) + 0.04));
+    jp = clampi(jp, 1, 58);
     jp = lower ? (jp > 12 ? 12 : jp) : (jp < 13 ? 13 : jp);
     const float fp = 5.0f * (__ldg(T + c_T.ref_preflog + jp - 1) - plog);
     const float dt0 = (tavel - __ldg(T + c_T.ref_tref + jp - 1)) / 15.0f;
-    const int jt = clampi((int)(3.0f + dt0), 1, 4);
+    int jt = (int)(3.0f + dt0);
+    if (fabsf(3.0f + dt0 - rintf(3.0f + dt0)) < 1.0e-4f) jt = (int)(3.0 + (td - c_T.tref64[jp - 1]) / 15.0);
+    jt = clampi(jt, 1, 4);
     const float ft = dt0 - (float)(jt - 3);
     const float dt1 = (tavel - __ldg(T + c_T.ref_tref + jp)) / 15.0f;
-    const int jt1 = clampi((int)(3.0f + dt1), 1, 4);
+    int jt1 = (int)(3.0f + dt1);
+    if (fabsf(3.0f + dt1 - rintf(3.0f + dt1)) < 1.0e-4f) jt1 = (int)(3.0 + (td - c_T.tref64[jp]) / 15.0);
+    jt1 = clampi(jt1, 1, 4);
     const float ft1 = dt1 - (float)(jt1 - 3);
+    // fp64 column amounts of the binary species (inatm :807-867, setcoef.f90:349-362)
+    {
+      const double amd64 = 28.9660, amw64 = 18.0160;
+      const double h = in2(a.h2ovmr, a.ld, icol, lay);
+      const double amm64 = (1.0 - h) * amd64 + h * amw64;
+      const double cd = dpz * 1.e3 * c_T.avogad / (1.e2 * c_T.grav * amm64 * (1.0 + h));
+      auto col = [&](const double* v) {
+        const double x = 1.e-20 * (cd * in2(v, a.ld, icol, lay));
+        return x == 0.0 ? 1.e-32 * cd : x;
+      };
+      s.d[D_H2O * nl + lay] = 1.e-20 * (cd * h);
+      s.d[D_CO2 * nl + lay] = col(a.co2vmr);
+      s.d[D_O3 * nl + lay] = col(a.o3vmr);
+      s.d[D_N2O * nl + lay] = col(a.n2ovmr);
+      s.d[D_CH4 * nl + lay] = col(a.ch4vmr);
+    }
     const float water = wk1 / coldry;
     const float scalefac = pavel * stpfac / tavel;
     const float forfac = scalefac / (1.0f + water);
     float forfrac, selffrac = 0.0f;
     int indfor, indself = 1;
+    // truncations of temperature factors, re-taken in fp64 near an integer
+    auto trunc_t = [&](float f32, double num64, double den) {
+      return fabsf(f32 - rintf(f32)) < 1.0e-4f ? (int)(num64 / den) : (int)f32;
+    };
     if (lower) {
       float factor = (332.0f - tavel) / 36.0f;
-      indfor = min(2, max(1, (int)factor));
+      indfor = min(2, max(1, trunc_t(factor, 332.0 - td, 36.0)));
       forfrac = factor - (float)indfor;
       factor = (tavel - 188.0f) / 7.2f;
-      indself = min(9, max(1, (int)factor - 7));
+      indself = min(9, max(1, trunc_t(factor, td - 188.0, 7.2) - 7));
       selffrac = factor - (float)(indself + 7);
     } else {
       const float factor = (tavel - 188.0f) / 36.0f;
@@ -331,7 +366,7 @@ __device__ void gas_column(const LwArgs& a, long long icol, const GasSmem& s, fl
     const float scaleminor = pavel / tavel;
     const float scaleminorn2 = scaleminor * (wbrodl / (coldry + wk1));
     const float factor = (tavel - 180.8f) / 7.2f;
-    const int indminor = min(18, max(1, (int)factor));
+    const int indminor = min(18, max(1, trunc_t(factor, td - 180.8, 7.2)));
     const float minorfrac = factor - (float)indminor;
     const float colh2o = 1.e-20f * wk1;
     float colco2 = 1.e-20f * wk2, colo3 = 1.e-20f * wk3, coln2o = 1.e-20f * wk4, colco = 0.0f;

@@ -237,6 +237,9 @@ bool gb_build_tables(const char* ref_path, const char* k_path, double cpdair, Gb
     T.preflog[j] = (float)preflog->d[j];
     T.tref[j] = (float)tref->d[j];
     for (int m = 0; m < 7; ++m) T.chi[m][j] = (float)chi->d[m + 7 * j];
+    T.preflog64[j] = preflog->d[j];
+    T.tref64[j] = tref->d[j];
+    for (int m = 0; m < 7; ++m) T.chi64[m][j] = chi->d[m + 7 * j];
     auto c = [&](int m) { return chi->d[(m - 1) + 7 * j]; };
     T.rat[0][j] = (float)(c(1) / c(2));
     T.rat[1][j] = (float)(c(1) / c(3));
