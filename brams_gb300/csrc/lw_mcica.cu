@@ -130,7 +130,11 @@ __global__ void kiss_percol_kernel(int ncol, long long ld, const double* __restr
   double p[4];
   for (int l = 0; l < 4; ++l) p[l] = play[c + ld * l] * 1.e2;
   if (p[0] < p[1]) {
+    // the reference stops here (status 8); the column's draws are set to 0 so
+    // that its sub-columns are the same on every call, not the previous
+    // contents of the draw buffer
     atomicMax(err, 8);
+    for (int d = 0; d < ndraw; ++d) draws[(long long)c * ndraw + d] = 0.0;
     return;
   }
   Kiss k;
@@ -283,7 +287,8 @@ size_t gb_mcica_draw_count(int ncol, int nlay, int icld) {
 // Layout: the first 256 bytes hold the status word, the rest holds draws.
 // All calls share the array and it keeps the previous call's contents: the
 // status word is cleared at the start of every call, and every draw slot a
-// call reads is written by that call first.  Calls whose kernels overlap on
+// call reads is written by that call first (a column whose KISS seeding
+// fails gets zero draws and status 8).  Calls whose kernels overlap on
 // the GPU (different streams without ordering, or several host threads)
 // race on the array and must be serialised by the caller.
 static __device__ __align__(256) double g_mcica_scratch[GB_MCICA_NOALLOC_STATUS_DOUBLES + GB_MCICA_NOALLOC_MAX_DRAWS];

@@ -186,8 +186,9 @@ def extract(ref_root: str) -> "OrderedDict[str, np.ndarray]":
 
 
 def main() -> None:
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    tabs = extract(ref)
+    if len(sys.argv) != 2:
+        sys.exit(f"usage: python -m brams_gb300.data.{os.path.basename(__file__)[:-3]} <luflarois/brams source tree>")
+    tabs = extract(sys.argv[1])
     dst = os.path.join(HERE, "lw_ref_tables.gblw")
     write_tables(dst, tabs)
     print(f"wrote {dst}: " + ", ".join(f"{k}{tuple(v.shape)}" for k, v in tabs.items()))

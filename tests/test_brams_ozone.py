@@ -55,3 +55,36 @@ def test_restatement_returns_the_table_on_its_nodes():
     o3l = BO.getoz(oz, sig, 18, sigmid, colrad, BO.RLAG, True)
     want = 1.0e-4 * oz[:, 10, 0]
     assert np.allclose(o3l, want, rtol=1e-9, atol=0.0)
+
+
+def test_restatement_against_hand_computed_values():
+    """getoz_rrtm (rtm_driver.f90:2638-2823) without interpolation at
+    latitudes between the table's 5-degree bands and at dates past one year
+    (doy > 365 wraps), against values computed once with the driver's
+    formulas written out by hand (seasonal harmonics of the four seasons at
+    the two bracketing latitude rows, blended by `rate`)."""
+    oz, sig = TAB["ozone"], TAB["ozsig"]
+    cases = {  # (glat, doy): {level k: 1e-4 * ozone at the column's latitude and date}
+        (37.3, 400): {1: 1.0190352056605059e-05, 9: 5.5347364120273215e-08, 18: 3.184062131023349e-08},
+        (-12.7, 59): {1: 1.0311197986310936e-05, 9: 4.600614880396558e-08, 18: 6.626378266628427e-09},
+        (81.1, 730): {1: 6.846653122921635e-06, 9: 9.63757620967659e-08, 18: 2.819129576826978e-08},
+    }
+    for (glat, doy), want in cases.items():
+        colrad = BO.PAI * (1.0 - (glat + 90.0) / 180.0)
+        o3l = BO.getoz(oz, sig, 18, [0.0] * 19, colrad, float(doy), False)
+        for k, v in want.items():
+            assert abs(o3l[k - 1] - v) <= 1e-12 * abs(v), (glat, doy, k)
+
+
+def test_eighteen_levels_still_interpolate():
+    """The driver skips the interpolation only when the column's sigma levels
+    equal the table's within 1e-4 (rtm_driver.f90:1130-1140); sig(1) is 1 by
+    construction and ozsig(18) = 0.995004, so a column of 18 levels is always
+    interpolated: its ozone equals the restatement's interpolated values."""
+    plev = _plev(5, 18, 11)
+    glat = np.array([37.3, -12.7, 81.1, 0.0, -60.0], dtype=np.float32)
+    oz = R.Ozone()
+    got = oz.o3vmr(plev, glat, 400)
+    oz.close()
+    want = np.array(BO.o3vmr_columns(TAB["ozone"], TAB["ozsig"], plev, glat, 400))
+    assert np.array_equal(got, want)

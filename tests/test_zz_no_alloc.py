@@ -23,9 +23,11 @@ INS = ("play", "cldfrac", "ciwp", "clwp", "rei", "rel", "tauc", "alpha")
 def _inputs(ncol, nlay, seed):
     import torch
 
-    import bench
+    import pyoracle
+    from brams_gb300.profiles import ProfileSpec, make_state
 
-    st, tauc = bench.make_inputs(ncol, nlay, seed)
+    st = make_state(ProfileSpec(ncol=ncol, nlay=nlay, seed=seed, t_noise=4.0, h2o_sigma=0.5))
+    tauc = pyoracle.cldprop_columns(st)
     dev = torch.device("cuda", 0)
 
     def dv(a):
@@ -59,15 +61,16 @@ def test_noalloc_matches_allocating_entry_point():
     ctx = Context()
     stream = torch.cuda.current_stream().cuda_stream
     ncol, nlay = 3000, 45
-    calls = [  # (icld, permuteseed, irng, seed_per_column): two calls in a row, then a third mode
+    calls = [  # (icld, permuteseed, irng, seed_per_column): two calls in a row, then other modes
         (3, 11, 1, 1),
         (3, 12345, 1, 0),
         (2, 7, 0, 1),
+        (4, 5, 1, 1),  # exponential overlap: two draws per cell and the overlap parameter
     ]
     d = _inputs(ncol, nlay, seed=5)
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
     for n, (icld, seed, irng, percol) in enumerate(calls):
-        ncall = ncol if icld == 3 else 400  # icld 2 needs 140*nlay draws per column
+        ncall = ncol if icld == 3 else (400 if icld == 2 else 200)  # icld 2/4 need 140*nlay (x2) draws per column
         got = _outputs(ncol, nlay)
         ref = _outputs(ncol, nlay)
         ir = C.c_int(irng)
@@ -106,3 +109,40 @@ def test_noalloc_rejects_calls_beyond_its_scratch():
     rc = L.gb_mcica_subcol_lw_noalloc(None, big, 10, 3, 1, C.byref(ir), *([p] * 8), *([p] * 6), big, 1, None)
     assert rc == -5
     assert b"scratch" in L.gb_rrtmg_lw_strerror(rc)
+
+
+def test_noalloc_reports_the_kiss_seeding_stop():
+    """KISS seeding needs the bottom layers' pressures in decreasing order
+    (the reference stops otherwise): the call reports status 8 and gives the
+    same sub-columns on a repeated call (zero draws, not stale ones)."""
+    import torch
+
+    from brams_gb300.rrtmg_lw import load_library
+
+    L = load_library()
+    stream = torch.cuda.current_stream().cuda_stream
+    ncol, nlay = 64, 20
+    good = _inputs(ncol, nlay, seed=9)
+    bad = _inputs(ncol, nlay, seed=9)
+    bad["play"][[0, 1], 3] = bad["play"][[1, 0], 3]  # column 3: pmid(1) < pmid(2)
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    OUT = ("cldfmcl", "ciwpmcl", "clwpmcl", "reicmcl", "relqmcl", "taucmcl")
+
+    def call(d, seed):
+        got = _outputs(ncol, nlay)
+        ir = C.c_int(0)
+        rc = L.gb_mcica_subcol_lw_noalloc(
+            C.c_void_p(stream), ncol, nlay, 2, seed, C.byref(ir), *[C.c_void_p(d[k].data_ptr()) for k in INS],
+            *[C.c_void_p(got[k].data_ptr()) for k in OUT], ncol, 1, C.c_void_p(status.data_ptr()))
+        assert rc == 0
+        torch.cuda.synchronize()
+        return got, int(status.item())
+
+    res = []
+    for seed in (100, 200):  # a clean call with other draws, then the failing one
+        _, st = call(good, seed)
+        assert st == 0
+        got, st = call(bad, 1)
+        assert st == 8  # GB_LW_E_KISS_PMID
+        res.append(got["cldfmcl"][:, 3].clone())
+    assert torch.equal(res[0], res[1])
