@@ -1420,20 +1420,32 @@ struct Args {
   const double *cldfmcl, *taucmcl, *ciwpmcl, *clwpmcl, *reicmcl, *relqmcl, *tauaer;
 };
 
+// The operation-counting build (flop_count.h) defines ORA_PHASE to attribute
+// the operations counted so far to a phase; in the oracle itself it is empty.
+#ifndef ORA_PHASE
+#define ORA_PHASE(k)
+#endif
+
 int run_column(const Args& a, int iplon, Col& c) {
   const int iaer = 10;
+  ORA_PHASE(-1);
   inatm(iplon, a.ncol, a.nlay, a.icld, iaer, a.play, a.plev, a.tlay, a.tlev, a.tsfc, a.h2ovmr,
         a.o3vmr, a.co2vmr, a.ch4vmr, a.n2ovmr, a.o2vmr, a.cfc11vmr, a.cfc12vmr, a.cfc22vmr,
         a.ccl4vmr, a.emis, a.inflglw, a.iceflglw, a.liqflglw, a.cldfmcl, a.taucmcl, a.ciwpmcl,
         a.clwpmcl, a.reicmcl, a.relqmcl, a.tauaer, c);
+  ORA_PHASE(0);
   int err = cldprmc(c);
   if (err) return err;
+  ORA_PHASE(1);
   err = setcoef(c, a.idrv);
   if (err) return err;
+  ORA_PHASE(2);
   taumol(c);
   for (int k = 1; k <= c.nlayers; ++k)
     for (int ig = 1; ig <= NGPT; ++ig) c.TAUT(k, ig) = c.TAUG(k, ig) + c.TAUA(k, ngb[ig - 1]);
+  ORA_PHASE(3);
   rtrnmc(c, a.idrv);
+  ORA_PHASE(4);
   return 0;
 }
 
@@ -1843,7 +1855,10 @@ int ora_mcica_subcol_lw(int ncol, int nlay, int icld, int permuteseed, int* irng
   if (*irng != 0) *irng = 1;
   const double cldmin = 1.0e-20;
   std::vector<double> cldf(nc);
-  for (size_t i = 0; i < nc; ++i) cldf[i] = cld[i] < cldmin ? 0.0 : cld[i];
+  for (size_t i = 0; i < nc; ++i) {
+    cldf[i] = cld[i];
+    if (cldf[i] < cldmin) cldf[i] = 0.0;
+  }
   auto IX = [&](int isub, int i, int ilev) {  // (nsub, ncol, nlay), 1-based
     return (size_t)(isub - 1) + (size_t)nsub * ((size_t)(i - 1) + (size_t)ncol * (ilev - 1));
   };

@@ -205,3 +205,42 @@ def lookup_tables():
     hf, ff = C.c_double(0), C.c_double(0)
     L.ora_get_tables(_p(tau), _p(ex), _p(tfn), C.byref(hf), C.byref(ff))
     return tau, ex, tfn, hf.value, ff.value
+
+
+def flops_per_column(state: dict, mc: dict, icld: int = 3, idrv: int = 1) -> dict:
+    """Floating-point operations (additions, subtractions, multiplications,
+    divisions) the restatement executes per column, by phase: a copy of the
+    oracle built with a counting number type (flop_count.h) runs rrtmg_lw
+    single-threaded on these columns."""
+    path = os.path.join(HERE, "_build", "liblworacle_count.so")
+    src = os.path.join(HERE, "lw_oracle.cpp")
+    if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    L = C.CDLL(path)
+    L.ora_init.restype = C.c_int
+    L.ora_init.argtypes = [C.c_double, C.c_char_p, C.c_char_p]
+    L.ora_flops.restype = C.c_uint64
+    L.ora_flops.argtypes = [C.c_int]
+    if L.ora_init(1004.0, os.path.join(DATA, "lw_ref_tables.gblw").encode(),
+                  os.path.join(DATA, "lw_ktables.gblw").encode()) != 0:
+        raise RuntimeError("oracle init failed")
+    ncol, nlay = state["play"].shape
+    st = [_f(state[k]) for k in STATE_ORDER]
+    cl = [_f(mc[k]) for k in CLOUD_ORDER]
+    out = {k: np.zeros((ncol, nlay + 1), order="F") for k in ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt")}
+    out["hr"] = np.zeros((ncol, nlay), order="F")
+    out["hrc"] = np.zeros((ncol, nlay), order="F")
+    ic = C.c_int(icld)
+    args = [C.c_int(ncol), C.c_int(nlay), C.byref(ic), C.c_int(idrv)] + [_p(a) for a in st]
+    args += [C.c_int(2), C.c_int(3), C.c_int(1)] + [_p(a) for a in cl] + [_p(_f(state["tauaer"]))]
+    args += [_p(out[k]) for k in ("uflx", "dflx", "hr", "uflxc", "dflxc", "hrc", "duflx_dt", "duflxc_dt")]
+    args += [C.c_int(1)]
+    L.ora_flops_reset()
+    rc = L.ora_rrtmg_lw(*args)
+    if rc != 0:
+        raise RuntimeError(f"counting oracle: status {rc}")
+    names = ("inatm", "cldprmc", "setcoef", "taumol", "rtrnmc")
+    res = {n: L.ora_flops(i) / ncol for i, n in enumerate(names)}
+    res["total"] = L.ora_flops(-1) / ncol
+    res["outputs"] = out
+    return res
