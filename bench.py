@@ -20,15 +20,26 @@ transfer with FP64 heating rates.  One step solves every column once by:
   e2e          -- the surrogate path with every step's inputs copied from
                   page-locked host memory chunk by chunk and every output read
                   back (host data: the generator tile, streamed for every chunk)
-  roofline     -- the column kernel (the dominant kernel) against the
-                  measured HBM copy bandwidth, with the algorithmic bytes of
-                  the fused-cloud, learned-gas-optics mode
+  roofline     -- the dominant kernel (the transfer kernel on the network's
+                  gas optics, fused clouds) against the measured HBM copy
+                  bandwidth with its algorithmic bytes, and against the
+                  nominal FP32 peak with the operations the oracle's counting
+                  copy counts for its phases (inatm, cldprmc, rtrnmc)
+  batched      -- three nested grids (200x180x45, 150x150x45, 97x97x38) x 8
+                  ensemble members with perturbed T and H2O, all in one
+                  persistent launch captured in a CUDA graph (taumol, fused
+                  clouds), with HBM and FP32 rooflines and an oracle check
+  eval         -- the learned gas optics on 512x512x45 columns: columns/s
+                  and heating-rate RMSE against the FP64 oracle, beside the
+                  plain path
   plain_abi    -- the drop-in path on the 360x300x45 BRAMS-scale workload:
                   gb_rrtmg_lw_device on the reference's (140, ncol, nlay)
                   McICA arrays, its roofline against 8*(600*nlay + 25) bytes
                   per column, and gb_rrtmg_lw with page-locked host buffers
   cpu_baseline -- the FP64 oracle (C++ restatement of the reference) on the
-                  host cores, on a bounded sample of the headline workload
+                  host cores, on a bounded sample of the headline workload;
+                  cpu_configs: the same on the 64x64x38 configuration in full
+                  and on a sample of the 360x300x45 one
 
 Inputs: a 131,072-column tile from the seeded generator (T noise N(0, 4 K),
 H2O x lognormal(0, 0.5)) is replicated to the 2048x1024 grid with a fresh
@@ -66,6 +77,22 @@ SAMPLE = 2048                                    # oracle columns for the accura
 
 def abi_bytes_per_column(nlay: int) -> int:
     return 8 * (600 * nlay + 25)
+
+
+# FP32 peak of a GB300 by its nominal figures (no measured FP32 peak is
+# available): 152 SMs x 128 FP32 lanes x 2 operations (FMA) x 2.07 GHz
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+
+
+def counted_flops(st: dict, mc: dict) -> dict:
+    """Floating-point operations per column by phase, counted by the
+    oracle's counting copy on these columns (single-threaded)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    r = pyoracle.flops_per_column(st, mc)
+    r.pop("outputs")
+    return r
 
 
 # --------------------------------------------------------------------------- inputs
@@ -382,7 +409,15 @@ def gpu_arm(args, rank, world):
     # ---------------- headline workload
     log("network ready; building the workload")
     nbase = args.nbase
-    seed = BASE_SEED + rank * 7919
+    # the job is world x NMEM members; the library's shard plan (balanced by
+    # layers, contiguous) gives this rank its members
+    from brams_gb300.shard import shard_plan
+
+    plan = shard_plan([(nbase, NLAY5)] * (NMEM * world), world, rank)
+    mine = [i for i, (a, b) in enumerate(plan) if b > a]
+    if len(mine) != NMEM or any(plan[i] != (0, nbase) for i in mine):
+        raise RuntimeError(f"shard plan does not give rank {rank} whole members: {plan}")
+    seed = BASE_SEED + 7919 * (mine[0] // NMEM)
     wl = Workload(dev, nbase, NLAY5, NMEM, seed)
     ncol = nbase * NMEM
     rows = CHUNK * NLAY5 * NMEM
@@ -479,6 +514,20 @@ def gpu_arm(args, rank, world):
     log("e2e")
     e2e = e2e_headline(ctx, mlp, wl, dev, stream, min(args.steps, 2), world, bufs)
 
+    # operations per column the oracle counts, on a few columns of member 0
+    c0 = nbase // 2
+    st_f = wl.host_columns(0, c0, 16)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    flops_sample = counted_flops(st_f, pyoracle.mcica_per_column(st_f, st_f["tauc"], icld=3, base_seed=wl.seed0(0) + c0))
+
+    # ---------------- batched nested grids (CUDA graph) and the network at 512x512x45
+    log("batched grids")
+    batched = None if args.no_batched else batched_block(ctx, dev, stream, args, hbm)
+    log("network evaluation at 512x512x45")
+    ev = None if args.no_batched else eval_block(ctx, mlp, dev, stream, args)
+
     # ---------------- drop-in block (ABI mode, 360x300x45)
     log("drop-in block")
     abi = None if args.no_abi else abi_block(ctx, dev, stream, args, rank, world, hbm)
@@ -491,7 +540,7 @@ def gpu_arm(args, rank, world):
         return
     alg = fused_bytes_per_column(NLAY5, True) * NMEM * min(CHUNK, nbase)
     achieved = alg / t_kernel / 1e9
-    traffic = traffic_from_profiles("lw_batch_kernel_learned_traffic.txt")
+    traffic = traffic_from_profiles("lw_rt_kernel_learned_traffic.txt")
     line = {
         "metric": METRIC, "value": world * ncol / t_sur, "unit": "columns/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_sur * 1e3, "higher_is_better": True,
@@ -500,6 +549,8 @@ def gpu_arm(args, rank, world):
                                f"x {NMEM} ensemble members" if nbase == NX * NY else
                                f"reduced: {nbase} columns x {NLAY5} layers x {NMEM} members",
                    "columns_per_gpu": ncol, "nlay": NLAY5, "members": NMEM, "icld": 3, "idrv": 1,
+                   "parallelism": f"{world} GPU(s), members of the {world * NMEM}-member job split by "
+                                  "gb_rrtmg_lw_shard_plan (no collective on the data path)",
                    "clouds": "McICA generated in the kernel, MT19937 seed = base + column",
                    "gas_optics": "learned (MLP, " + trained + "), taumol for layers outside the training range",
                    "chunk_columns_per_member": CHUNK,
@@ -513,14 +564,15 @@ def gpu_arm(args, rank, world):
         "accuracy": acc,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic,
-                     # what DRAM actually moved (ncu bytes per launch over this run's launch time): the
-                     # kernel is latency-bound, not bandwidth-bound, at either count
+                     # what DRAM actually moved (ncu bytes per launch over this run's launch time)
                      "dram_gbs": traffic / t_kernel / 1e9 if traffic else None,
                      "dram_frac": traffic / t_kernel / 1e9 / hbm if traffic else None,
-                     "kernel": "lw_batch_kernel (learned gas optics, fused clouds), one launch = 4 members x "
-                               f"{min(CHUNK, nbase)} columns; alg bytes/column {fused_bytes_per_column(NLAY5, True)}",
+                     "kernel": "lw_rt_kernel (transfer on the network's gas optics, fused clouds), one launch = 4 "
+                               f"members x {min(CHUNK, nbase)} columns; alg bytes/column {fused_bytes_per_column(NLAY5, True)}",
                      "alg_bytes_per_launch": alg, "launch_ms": t_kernel * 1e3,
-                     "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
+                     "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                     "fp32": fp32_roofline(flops_sample, ("inatm", "cldprmc", "rtrnmc"),
+                                           NMEM * min(CHUNK, nbase), t_kernel)},
         "e2e": {"value": world * ncol / t_e2e, "unit": "columns/s", "h2d_bytes_per_step": e2e["h2d"],
                 "d2h_bytes_per_step": e2e["d2h"], "host_data": e2e["note"],
                 "host_path_matches_device_path": e2e["matches"]},
@@ -528,8 +580,13 @@ def gpu_arm(args, rank, world):
     }
     if abi is not None:
         line["plain_abi"] = abi
+    if batched is not None:
+        line["batched"] = batched
+    if ev is not None:
+        line["eval"] = ev
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_headline(wl)
+        line["cpu_configs"] = cpu_configs()
     print(json.dumps(line), flush=True)
 
 
@@ -688,6 +745,205 @@ def cpu_baseline_headline(wl, seconds: float = 12.0, max_cols: int = 16384):
                       "beforehand, not timed"}
 
 
+def fp32_roofline(flops: dict, phases, columns: int, seconds: float) -> dict:
+    """Counted operations of `phases` per column times the columns of one
+    launch, over the launch time, against the nominal FP32 peak."""
+    per_col = sum(flops[p] for p in phases)
+    tf = per_col * columns / seconds / 1e12
+    return {"bound": "fp32", "achieved": tf, "peak": FP32_PEAK_TFLOPS, "unit": "TFLOP/s", "frac": tf / FP32_PEAK_TFLOPS,
+            "flops_per_column": per_col, "phases": list(phases),
+            "peak_source": "nominal: 152 SMs x 128 lanes x 2 (FMA) x 2.07 GHz",
+            "counted_by": "oracle/flop_count.h (additions, subtractions, multiplications, divisions of the FP64 restatement)"}
+
+
+def _perturbed_members(base, members, gen, dev):
+    """Ensemble members of a device grid: T + N(0, 1 K) and H2O x lognormal(0, 0.2) per (column, layer)."""
+    import torch
+
+    from brams_gb300 import surrogate as S
+
+    out = []
+    for _ in range(members):
+        m = S.DeviceGrid.__new__(S.DeviceGrid)
+        m.ncol, m.nlay = base.ncol, base.nlay
+        m.d = {k: v.clone() for k, v in base.d.items()}
+        m.d["tlay"] += torch.randn(m.d["tlay"].shape, generator=gen, device=dev, dtype=torch.float64)
+        m.d["h2ovmr"] = (m.d["h2ovmr"] * torch.exp(0.2 * torch.randn(m.d["h2ovmr"].shape, generator=gen, device=dev,
+                                                                     dtype=torch.float64))).clamp_(3.0e-6, 0.05)
+        out.append(m)
+    return out
+
+
+def _host_of(m, n):
+    """The first n columns of a device grid's inputs as Fortran numpy arrays (for the oracle)."""
+    st = {}
+    for k, t in m.d.items():
+        if k in ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt", "hr", "hrc"):
+            continue
+        a = t.cpu().numpy()
+        st[k] = np.asfortranarray(a[:, :n, :].T if k == "tauc" else a[..., :n].T)
+    return st
+
+
+def _errors(got, ref, n):
+    return {"hr_rmse_k_per_day": float(np.sqrt(np.mean((got["hr"][:n] - ref["hr"]) ** 2))),
+            "hr_max_k_per_day": float(np.abs(got["hr"][:n] - ref["hr"]).max()),
+            "flux_max_w_m2": float(max(np.abs(got[k][:n] - ref[k]).max() for k in ("uflx", "dflx")))}
+
+
+def batched_block(ctx, dev, stream, args, hbm):
+    """Three nested grids x 8 members in one persistent launch captured in a CUDA graph."""
+    import torch
+
+    from brams_gb300 import surrogate as S
+    from brams_gb300.profiles import ProfileSpec, make_state
+    from brams_gb300.tables_io import read_tables
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    tabs = read_tables(os.path.join(ROOT, "brams_gb300", "data", "lw_ref_tables.gblw"))
+    shapes = [(200, 180, 45), (150, 150, 45), (97, 97, 38)]
+    members = 8
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(BASE_SEED + 17)
+    grids, seeds = [], []
+    for gi, (nx, ny, nlay) in enumerate(shapes):
+        st = make_state(ProfileSpec(ncol=nx * ny, nlay=nlay, seed=BASE_SEED + 31 * gi, ptop=PTOP, t_noise=4.0,
+                                    h2o_sigma=0.5))
+        base = S.DeviceGrid(st, cldprop_numpy(st, tabs))
+        for m, mg in enumerate(_perturbed_members(base, members, gen, dev)):
+            grids.append(mg)
+            seeds.append((gi * members + m) * 100003 + BASE_SEED)
+        del base
+    descs = [g.desc(seed0=s) for g, s in zip(grids, seeds)]
+    ncols = sum(g.ncol for g in grids)
+    best = ctx.autotune(descs, sample_cols=65536, reps=2, stream=stream)
+    graph = ctx.batch_graph(descs)
+    try:
+        for _ in range(args.warmup):
+            graph.launch(stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            graph.launch(stream)
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3 / args.steps
+    finally:
+        graph.close()
+    status = ctx.sync_status(stream)
+    # oracle check: 512 columns of member 0 of the 45- and the 38-layer grid
+    acc = {}
+    for gi in (0, 2):
+        m = grids[gi * members]
+        st = _host_of(m, 512)
+        mc = pyoracle.mcica_per_column(st, st["tauc"], icld=3, base_seed=seeds[gi * members])
+        ref = pyoracle.rrtmg_lw(st, mc, nthreads=os.cpu_count() or 1, native=True)
+        acc[f"grid{gi}_member0"] = _errors(m.outputs(), ref, 512)
+    alg = sum(fused_bytes_per_column(g.nlay, False) * g.ncol for g in grids)
+    st45 = _host_of(grids[0], 16)
+    fl45 = counted_flops(st45, pyoracle.mcica_per_column(st45, st45["tauc"], icld=3, base_seed=seeds[0]))
+    st38 = _host_of(grids[2 * members], 16)
+    fl38 = counted_flops(st38, pyoracle.mcica_per_column(st38, st38["tauc"], icld=3, base_seed=seeds[2 * members]))
+    flops = sum((fl38 if g.nlay == 38 else fl45)["total"] * g.ncol for g in grids)
+    tf = flops / t / 1e12
+    return {"workload": "batched uneven grids 200x180x45 + 150x150x45 + 97x97x38, x 8 members (T + N(0,1 K), "
+                        "H2O x lognormal(0,0.2)), one persistent launch of taumol + transfer captured in a CUDA graph; "
+                        "McICA clouds in the kernel; autotuned launch shape",
+            "columns": ncols, "value": ncols / t, "unit": "columns/s", "ms_per_step": t * 1e3,
+            "launch_shape": {k: best[k] for k in ("threads", "min_blocks", "blocks_per_sm")},
+            "roofline": {"bound": "hbm", "achieved": alg / t / 1e9, "peak": hbm, "unit": "GB/s",
+                         "frac": alg / t / 1e9 / hbm, "alg_bytes_per_step": alg},
+            "fp32": {"bound": "fp32", "achieved": tf, "peak": FP32_PEAK_TFLOPS, "unit": "TFLOP/s",
+                     "frac": tf / FP32_PEAK_TFLOPS, "flops_per_column_45": fl45["total"], "flops_per_column_38": fl38["total"],
+                     "peak_source": "nominal", "counted_by": "oracle/flop_count.h"},
+            "accuracy": acc, "column_status": status}
+
+
+def eval_block(ctx, mlp, dev, stream, args):
+    """The learned gas optics on 512x512 columns x 45 layers against the plain path and the FP64 oracle."""
+    import torch
+
+    from brams_gb300 import surrogate as S
+    from brams_gb300.profiles import make_state, workload_spec
+    from brams_gb300.tables_io import read_tables
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    tabs = read_tables(os.path.join(ROOT, "brams_gb300", "data", "lw_ref_tables.gblw"))
+    st = make_state(workload_spec("eval_512x512x45"))
+    tauc = cldprop_numpy(st, tabs)
+    ncol, nlay = st["play"].shape
+    gl, gp = S.DeviceGrid(st, tauc), S.DeviceGrid(st, tauc)
+    rows = ncol * nlay
+    tau = torch.empty((rows, GB_NGPT), dtype=torch.float16, device=dev)
+    frac = torch.empty_like(tau)
+    flag = torch.empty(rows, dtype=torch.uint8, device=dev)
+    seed0 = 77
+
+    def learned():
+        mlp.infer(gl.desc(seed0=seed0), tau, frac, flag, stream=stream)
+        ctx.rrtmg_lw_batch_device([gl.desc(seed0=seed0, sur_tau=tau.data_ptr(), sur_frac=frac.data_ptr(),
+                                           sur_flag=flag.data_ptr())], stream=stream)
+
+    def plain():
+        ctx.rrtmg_lw_batch_device([gp.desc(seed0=seed0)], stream=stream)
+
+    res = {}
+    for name, fn in (("learned", learned), ("plain", plain)):
+        for _ in range(args.warmup):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        res[name] = {"value": ncol / (e0.elapsed_time(e1) / 1e3 / args.steps), "unit": "columns/s"}
+    n = 2048
+    sub = {k: np.asfortranarray(v[:n]) for k, v in st.items()}
+    mc = pyoracle.mcica_per_column(sub, np.asfortranarray(tauc[:, :n]), icld=3, base_seed=seed0)
+    ref = pyoracle.rrtmg_lw(sub, mc, nthreads=os.cpu_count() or 1, native=True)
+    res["learned"].update(_errors(gl.outputs(), ref, n))
+    res["plain"].update(_errors(gp.outputs(), ref, n))
+    res["layers_on_network"] = float(flag.float().mean().item())
+    res["speedup_of_learned"] = res["learned"]["value"] / res["plain"]["value"]
+    res["workload"] = ("512x512 columns x 45 layers (T noise N(0,4 K), H2O x lognormal(0,0.5)), McICA in the kernel; "
+                       f"errors against the FP64 oracle on the first {n} columns")
+    res["column_status"] = ctx.sync_status(stream)
+    return res
+
+
+def cpu_configs(seconds: float = 5.0) -> dict:
+    """The FP64 oracle on all host cores: the 64x64x38 configuration in full
+    and a sample of the 360x300x45 one (McICA sub-columns made beforehand)."""
+    from brams_gb300.profiles import make_state, workload_spec
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    pyoracle.build(native=True)
+    cores = os.cpu_count() or 1
+    out = {}
+    for name, ncol in (("oracle_64x64x38", None), ("drop_in_360x300x45", 8192)):
+        st = make_state(workload_spec(name, ncol=ncol))
+        mc = pyoracle.mcica_per_column(st, pyoracle.cldprop_columns(st), icld=3, base_seed=1)
+        n = st["play"].shape[0]
+        done, reps, t0 = 0, 0, time.perf_counter()
+        while reps < 3 or time.perf_counter() - t0 < seconds:
+            pyoracle.rrtmg_lw(st, mc, nthreads=cores, native=True)
+            done += n
+            reps += 1
+        dt = time.perf_counter() - t0
+        out[name] = {"value": done / dt, "unit": "columns/s", "cores": cores, "kind": "port",
+                     "sample": f"{n} columns x {st['play'].shape[1]} layers, {reps} passes ({dt:.1f} s)"}
+    return out
+
+
 def abi_block(ctx, dev, stream, args, rank, world, hbm):
     """Drop-in path: gb_rrtmg_lw_device on the reference's McICA arrays (360x300x45) and gb_rrtmg_lw on host buffers."""
     import torch
@@ -772,6 +1028,7 @@ def main():
     ap.add_argument("--no-abi", action="store_true", help="skip the 360x300x45 drop-in block")
     ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's")
     ap.add_argument("--abi-ncol", type=int, default=NCOL, help="columns of the drop-in block")
+    ap.add_argument("--no-batched", action="store_true", help="skip the nested-grid and 512x512x45 blocks")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -44,6 +44,7 @@ EXPORTS = [
     "gb_rrtmg_lw_batch_surrogate", "gb_lw_mlp_set_engine", "gb_rrtmg_lw_autotune_report",
     "gb_cldprop_lw_device", "gb_rtm_pack_lw_device", "gb_rtm_unpack_lw_device",
     "gb_rtm_ozone_load", "gb_rtm_ozone_free", "gb_rtm_ozone_lw",
+    "gb_rrtmg_lw_shard_plan", "gb_rrtmg_lw_grid_slice",
 ]
 MLP_MMA_SYNC, MLP_TCGEN05 = 0, 1
 MLP_NPARAM = 72352
@@ -143,6 +144,8 @@ def load_library(path: str = LIB_PATH):
         L.gb_rrtmg_lw_graph_destroy.argtypes = [P]
         L.gb_rrtmg_lw_tuning_set.argtypes = [P, I, I, C.POINTER(Tuning)]
         L.gb_rrtmg_lw_num_variants.argtypes = []
+        L.gb_rrtmg_lw_shard_plan.argtypes = [I, IP, IP, I, I, C.POINTER(LL), C.POINTER(LL)]
+        L.gb_rrtmg_lw_grid_slice.argtypes = [GP, LL, LL, GP]
         U64, F = C.c_uint64, C.c_float
         L.gb_lw_mlp_create.argtypes = [P, U64, C.POINTER(P)]
         L.gb_lw_mlp_destroy.argtypes = [P]

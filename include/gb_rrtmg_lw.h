@@ -253,6 +253,7 @@ int gb_mcica_subcol_lw_noalloc(void* stream, int ncol, int nlay, int icld, int p
 #define GB_LW_CLOUD_SUBCOL 0
 #define GB_LW_CLOUD_FUSED 1
 #define GB_LW_MAX_GRIDS 32
+#define GB_LW_NGPT 140 /* g-points (parrrtm.f90 ngptlw) */
 
 typedef struct gb_lw_grid {
   int ncol, nlay, icld, idrv, inflglw, iceflglw, liqflglw;
@@ -314,15 +315,33 @@ int gb_rrtmg_lw_tuning_set(gb_lw_context* ctx, int nlay, int kind, const gb_lw_t
 /* Number of compiled kernel variants (valid gb_lw_tuning.variant values). */
 int gb_rrtmg_lw_num_variants(void);
 
-/* CUDA graph of one batched launch: the descriptor and a scratch area owned
- * by the graph are fixed at creation, so the caller updates the input arrays
- * in place between replays (a time-stepping model's resident state).  The
- * graph holds the single persistent kernel. */
+/* CUDA graph of one batched launch: the descriptor and the gas-optics
+ * hand-over buffer owned by the graph are fixed at creation, so the caller
+ * updates the input arrays in place between replays (a time-stepping model's
+ * resident state).  The graph holds the batch's kernels (one persistent
+ * launch for taumol batches). */
 typedef struct gb_lw_graph gb_lw_graph;
 int gb_rrtmg_lw_batch_graph_create(gb_lw_context* ctx, int ngrid, const gb_lw_grid* grids,
                                    gb_lw_graph** graph);
 int gb_rrtmg_lw_graph_launch(gb_lw_graph* graph, void* stream);
 int gb_rrtmg_lw_graph_destroy(gb_lw_graph* graph);
+
+/* ---------------------------------------------------------------------------
+ * Multi-GPU column shards (host only; no device call).  BRAMS gives each MPI
+ * rank the columns of its own subdomain (rtm_driver.f90:830, nofcols) and
+ * each rank calls rrtmg_lw on those; the ranks exchange nothing.  A caller
+ * that drives several GPUs from one batch lays the batch's grids end to end
+ * and gives rank r the contiguous run of columns whose cumulative work
+ * (columns x layers) lies in [r/nranks, (r+1)/nranks) of the total:
+ * gb_rrtmg_lw_shard_plan returns that run as per-grid column ranges
+ * [c0[i], c1[i]) (empty where c0 == c1), and gb_rrtmg_lw_grid_slice cuts a
+ * grid descriptor to columns [c0, c1) by pointer offsets (leading dimensions
+ * kept, seed0 advanced by c0 so that McICA draws do not depend on the
+ * split).  Each rank passes its non-empty slices to gb_rrtmg_lw_batch_device
+ * on its own device; the outputs land in place. */
+int gb_rrtmg_lw_shard_plan(int ngrid, const int* ncol, const int* nlay, int nranks, int rank, int64_t* c0,
+                           int64_t* c1);
+int gb_rrtmg_lw_grid_slice(const gb_lw_grid* grid, int64_t c0, int64_t c1, gb_lw_grid* out);
 
 /* ---------------------------------------------------------------------------
  * Learned gas optics (no counterpart in the reference): a small MLP that maps
