@@ -1405,6 +1405,427 @@ void rtrnmc(Col& c, int idrv) {
   c.htrc[nlayers] = 0.0;
 }
 
+// ---------------------------------------------------------------- rtrnmr
+// rrtmg_lw_rtrnmr.f90:51-806: the non-McICA transfer with maximum/random
+// cloud overlap on layer cloud fractions and cldprop's band optical depths.
+// The overlap factors faccmb1/faccmb2 (and their downward copies) are read
+// at a cloudy layer whose neighbour is clear (istcld = 1) although the
+// reference writes them only where istcld /= 1 (:434-438, :507-512); its
+// automatic arrays leave those entries undefined.  They are taken as 0 here
+// (zeroed arrays), the value the rest of the algorithm expects at the first
+// cloudy layer of a block (rad is 0 there, so only faccmb enters radmod).
+void rtrnmr(Col& c, int idrv) {
+  const int nlayers = c.nlayers;
+  const double wtdiff = 0.5, rec_6 = 0.166667;
+  static const int ipat[3][16] = {{1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1, 1},
+                                  {1, 2, 3, 3, 3, 4, 4, 4, 5, 5, 5, 5, 5, 5, 5, 5},
+                                  {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16}};
+  static const double a0[16] = {1.66, 1.55, 1.58, 1.66, 1.54, 1.454, 1.89, 1.33,
+                                1.668, 1.66, 1.66, 1.66, 1.66, 1.66, 1.66, 1.66};
+  static const double a1[16] = {0.00, 0.25, 0.22, 0.00, 0.13, 0.446, -0.10, 0.40,
+                                -0.006, 0.00, 0.00, 0.00, 0.00, 0.00, 0.00, 0.00};
+  static const double a2[16] = {0.00, -12.0, -11.7, 0.00, -0.72, -0.243, 0.19, -0.062,
+                                0.414, 0.00, 0.00, 0.00, 0.00, 0.00, 0.00, 0.00};
+  double secdiff[16];
+  for (int ibnd = 1; ibnd <= 16; ++ibnd) {  // :287-295
+    if (ibnd == 1 || ibnd == 4 || ibnd >= 10) {
+      secdiff[ibnd - 1] = 1.66;
+    } else {
+      secdiff[ibnd - 1] = a0[ibnd - 1] + a1[ibnd - 1] * std::exp(a2[ibnd - 1] * c.pwvcm);
+      if (secdiff[ibnd - 1] > 1.80) secdiff[ibnd - 1] = 1.80;
+      if (secdiff[ibnd - 1] < 1.50) secdiff[ibnd - 1] = 1.50;
+    }
+  }
+  const int n = nlayers + 2;
+  std::vector<double> urad(n, 0), drad(n, 0), clrurad(n, 0), clrdrad(n, 0), d_urad_dt(n, 0),
+      d_clrurad_dt(n, 0), atrans(n, 0), atot(n, 0), bbugas(n, 0), bbutot(n, 0);
+  std::vector<double> odcld(n * 16, 0.0);
+  std::vector<int> icldlyr(n, 0), istcld(n, 0), istcldd(n, 0);
+  // faccld1..faccmb2 (1 .. nlayers+1) and faccld1d..faccmb2d (0 .. nlayers)
+  std::vector<double> faccld1(n, 0), faccld2(n, 0), facclr1(n, 0), facclr2(n, 0), faccmb1(n, 0), faccmb2(n, 0);
+  std::vector<double> faccld1d(n, 0), faccld2d(n, 0), facclr1d(n, 0), facclr2d(n, 0), faccmb1d(n, 0),
+      faccmb2d(n, 0);
+  auto OD = [&](int lay, int ib) -> double& { return odcld[lay + n * (ib - 1)]; };
+  const std::vector<double>& cf = c.cldfr_lay;  // cldfrac(1 .. nlayers)
+  auto CF = [&](int l) -> double {
+    if (l >= 1 && l <= nlayers) return cf[l];
+    return 0.0;
+  };
+  for (int lev = 0; lev <= nlayers; ++lev) {
+    c.totuflux[lev] = c.totdflux[lev] = c.totuclfl[lev] = c.totdclfl[lev] = 0.0;
+    if (idrv == 1) c.dtotuflux_dt[lev] = c.dtotuclfl_dt[lev] = 0.0;
+  }
+  for (int lay = 1; lay <= nlayers; ++lay) {  // :334-343
+    for (int ib = 1; ib <= c.ncbands; ++ib) {
+      if (cf[lay] >= 1.e-6) {
+        OD(lay, ib) = secdiff[ib - 1] * c.TAUCL(lay, ib);
+        icldlyr[lay] = 1;
+      } else {
+        OD(lay, ib) = 0.0;
+        icldlyr[lay] = 0;
+      }
+    }
+  }
+  // maximum/random overlap parameters, upward (:347-440)
+  double rat1 = 0.0, rat2 = 0.0, fmax, fmin;
+  istcld[1] = 1;
+  istcldd[nlayers] = 1;
+  for (int lev = 1; lev <= nlayers; ++lev) {
+    if (icldlyr[lev] == 1) {
+      istcld[lev + 1] = 0;
+      if (lev == nlayers) {
+        faccld1[lev + 1] = faccld2[lev + 1] = facclr1[lev + 1] = facclr2[lev + 1] = 0.0;
+        faccmb1[lev + 1] = faccmb2[lev + 1] = 0.0;
+      } else if (CF(lev + 1) >= CF(lev)) {
+        faccld1[lev + 1] = 0.0;
+        faccld2[lev + 1] = 0.0;
+        if (istcld[lev] == 1) {
+          facclr1[lev + 1] = 0.0;
+          facclr2[lev + 1] = 0.0;
+          if (CF(lev) < 1.0) facclr2[lev + 1] = (CF(lev + 1) - CF(lev)) / (1.0 - CF(lev));
+          facclr2[lev] = 0.0;
+          faccld2[lev] = 0.0;
+        } else {
+          fmax = std::max(CF(lev), CF(lev - 1));
+          if (CF(lev + 1) > fmax) {
+            facclr1[lev + 1] = rat2;
+            facclr2[lev + 1] = (CF(lev + 1) - fmax) / (1.0 - fmax);
+          } else if (CF(lev + 1) < fmax) {
+            facclr1[lev + 1] = (CF(lev + 1) - CF(lev)) / (CF(lev - 1) - CF(lev));
+            facclr2[lev + 1] = 0.0;
+          } else {
+            facclr1[lev + 1] = rat2;
+            facclr2[lev + 1] = 0.0;
+          }
+        }
+        if (facclr1[lev + 1] > 0.0 || facclr2[lev + 1] > 0.0) {
+          rat1 = 1.0;
+          rat2 = 0.0;
+        } else {
+          rat1 = 0.0;
+          rat2 = 0.0;
+        }
+      } else {
+        facclr1[lev + 1] = 0.0;
+        facclr2[lev + 1] = 0.0;
+        if (istcld[lev] == 1) {
+          faccld1[lev + 1] = 0.0;
+          faccld2[lev + 1] = (CF(lev) - CF(lev + 1)) / CF(lev);
+          facclr2[lev] = 0.0;
+          faccld2[lev] = 0.0;
+        } else {
+          fmin = std::min(CF(lev), CF(lev - 1));
+          if (CF(lev + 1) <= fmin) {
+            faccld1[lev + 1] = rat1;
+            faccld2[lev + 1] = (fmin - CF(lev + 1)) / fmin;
+          } else {
+            faccld1[lev + 1] = (CF(lev) - CF(lev + 1)) / (CF(lev) - fmin);
+            faccld2[lev + 1] = 0.0;
+          }
+        }
+        if (faccld1[lev + 1] > 0.0 || faccld2[lev + 1] > 0.0) {
+          rat1 = 0.0;
+          rat2 = 1.0;
+        } else {
+          rat1 = 0.0;
+          rat2 = 0.0;
+        }
+      }
+      if (istcld[lev] != 1) {  // max(0., ...): a default-real 0
+        faccmb1[lev + 1] = std::max<double>(0.0, std::min<double>(CF(lev + 1) - CF(lev), CF(lev - 1) - CF(lev)));
+        faccmb2[lev + 1] = std::max<double>(0.0, std::min<double>(CF(lev) - CF(lev + 1), CF(lev) - CF(lev - 1)));
+      }
+    } else {
+      istcld[lev + 1] = 1;
+    }
+  }
+  // downward (:442-514); rat1/rat2 carry over from the loop above
+  for (int lev = nlayers; lev >= 1; --lev) {
+    if (icldlyr[lev] == 1) {
+      istcldd[lev - 1] = 0;
+      if (lev == 1) {
+        faccld1d[lev - 1] = faccld2d[lev - 1] = facclr1d[lev - 1] = facclr2d[lev - 1] = 0.0;
+        faccmb1d[lev - 1] = faccmb2d[lev - 1] = 0.0;
+      } else if (CF(lev - 1) >= CF(lev)) {
+        faccld1d[lev - 1] = 0.0;
+        faccld2d[lev - 1] = 0.0;
+        if (istcldd[lev] == 1) {
+          facclr1d[lev - 1] = 0.0;
+          facclr2d[lev - 1] = 0.0;
+          if (CF(lev) < 1.0) facclr2d[lev - 1] = (CF(lev - 1) - CF(lev)) / (1.0 - CF(lev));
+          facclr2d[lev] = 0.0;
+          faccld2d[lev] = 0.0;
+        } else {
+          fmax = std::max(CF(lev), CF(lev + 1));
+          if (CF(lev - 1) > fmax) {
+            facclr1d[lev - 1] = rat2;
+            facclr2d[lev - 1] = (CF(lev - 1) - fmax) / (1.0 - fmax);
+          } else if (CF(lev - 1) < fmax) {
+            facclr1d[lev - 1] = (CF(lev - 1) - CF(lev)) / (CF(lev + 1) - CF(lev));
+            facclr2d[lev - 1] = 0.0;
+          } else {
+            facclr1d[lev - 1] = rat2;
+            facclr2d[lev - 1] = 0.0;
+          }
+        }
+        if (facclr1d[lev - 1] > 0.0 || facclr2d[lev - 1] > 0.0) {
+          rat1 = 1.0;
+          rat2 = 0.0;
+        } else {
+          rat1 = 0.0;
+          rat2 = 0.0;
+        }
+      } else {
+        facclr1d[lev - 1] = 0.0;
+        facclr2d[lev - 1] = 0.0;
+        if (istcldd[lev] == 1) {
+          faccld1d[lev - 1] = 0.0;
+          faccld2d[lev - 1] = (CF(lev) - CF(lev - 1)) / CF(lev);
+          facclr2d[lev] = 0.0;
+          faccld2d[lev] = 0.0;
+        } else {
+          fmin = std::min(CF(lev), CF(lev + 1));
+          if (CF(lev - 1) <= fmin) {
+            faccld1d[lev - 1] = rat1;
+            faccld2d[lev - 1] = (fmin - CF(lev - 1)) / fmin;
+          } else {
+            faccld1d[lev - 1] = (CF(lev) - CF(lev - 1)) / (CF(lev) - fmin);
+            faccld2d[lev - 1] = 0.0;
+          }
+        }
+        if (faccld1d[lev - 1] > 0.0 || faccld2d[lev - 1] > 0.0) {
+          rat1 = 0.0;
+          rat2 = 1.0;
+        } else {
+          rat1 = 0.0;
+          rat2 = 0.0;
+        }
+      }
+      if (istcldd[lev] != 1) {
+        faccmb1d[lev - 1] = std::max<double>(0.0, std::min<double>(CF(lev + 1) - CF(lev), CF(lev - 1) - CF(lev)));
+        faccmb2d[lev - 1] = std::max<double>(0.0, std::min<double>(CF(lev) - CF(lev + 1), CF(lev) - CF(lev - 1)));
+      }
+    } else {
+      istcldd[lev - 1] = 1;
+    }
+  }
+  const int row = c.ncbands == 1 ? 0 : (c.ncbands == 5 ? 1 : 2);
+  int igc = 1;
+  for (int iband = 1; iband <= 16; ++iband) {  // :516-806
+    const int ib = ipat[row][iband - 1];
+    for (; igc <= ngs[iband - 1]; ++igc) {
+      double radld = 0.0, radclrd = 0.0, bbd = 0.0;
+      double cldradd = 0.0, clrradd = 0.0, rad = 0.0, oldcld, oldclr, radmod;
+      int iclddn = 0;
+      for (int lev = nlayers; lev >= 1; --lev) {
+        const double plfrac = c.FRACS(lev, igc);
+        const double blay = c.PLAY(lev, iband);
+        const double dplankup = c.PLEV(lev, iband) - blay;
+        const double dplankdn = c.PLEV(lev - 1, iband) - blay;
+        double odepth = secdiff[iband - 1] * c.TAUT(lev, igc);
+        if (odepth < 0.0) odepth = 0.0;
+        if (icldlyr[lev] == 1) {
+          iclddn = 1;
+          double odtot = odepth + OD(lev, ib), gassrc, bbdtot;
+          if (odtot < 0.06) {
+            atrans[lev] = odepth - 0.5 * odepth * odepth;
+            const double odepth_rec = rec_6 * odepth;
+            gassrc = plfrac * (blay + dplankdn * odepth_rec) * atrans[lev];
+            atot[lev] = odtot - 0.5 * odtot * odtot;
+            const double odtot_rec = rec_6 * odtot;
+            bbdtot = plfrac * (blay + dplankdn * odtot_rec);
+            bbd = plfrac * (blay + dplankdn * odepth_rec);
+            bbugas[lev] = plfrac * (blay + dplankup * odepth_rec);
+            bbutot[lev] = plfrac * (blay + dplankup * odtot_rec);
+          } else if (odepth <= 0.06) {
+            atrans[lev] = odepth - 0.5 * odepth * odepth;
+            const double odepth_rec = rec_6 * odepth;
+            gassrc = plfrac * (blay + dplankdn * odepth_rec) * atrans[lev];
+            odtot = odepth + OD(lev, ib);
+            const double tblind = odtot / (bpade + odtot);
+            const int ittot = (int)(TBLINT * tblind + 0.5);
+            const double tfactot = tfn_tbl[ittot];
+            bbdtot = plfrac * (blay + tfactot * dplankdn);
+            bbd = plfrac * (blay + dplankdn * odepth_rec);
+            atot[lev] = 1.0 - exp_tbl[ittot];
+            bbugas[lev] = plfrac * (blay + dplankup * odepth_rec);
+            bbutot[lev] = plfrac * (blay + tfactot * dplankup);
+          } else {
+            double tblind = odepth / (bpade + odepth);
+            const int itgas = (int)(TBLINT * tblind + 0.5);
+            odepth = tau_tbl[itgas];
+            atrans[lev] = 1.0 - exp_tbl[itgas];
+            const double tfacgas = tfn_tbl[itgas];
+            gassrc = atrans[lev] * plfrac * (blay + tfacgas * dplankdn);
+            odtot = odepth + OD(lev, ib);
+            tblind = odtot / (bpade + odtot);
+            const int ittot = (int)(TBLINT * tblind + 0.5);
+            const double tfactot = tfn_tbl[ittot];
+            bbdtot = plfrac * (blay + tfactot * dplankdn);
+            bbd = plfrac * (blay + tfacgas * dplankdn);
+            atot[lev] = 1.0 - exp_tbl[ittot];
+            bbugas[lev] = plfrac * (blay + tfacgas * dplankup);
+            bbutot[lev] = plfrac * (blay + tfactot * dplankup);
+          }
+          if (istcldd[lev] == 1) {
+            cldradd = cf[lev] * radld;
+            clrradd = radld - cldradd;
+            oldcld = cldradd;
+            oldclr = clrradd;
+            rad = 0.0;
+          }
+          const double ttot = 1.0 - atot[lev];
+          const double cldsrc = bbdtot * atot[lev];
+          cldradd = cldradd * ttot + cf[lev] * cldsrc;
+          clrradd = clrradd * (1.0 - atrans[lev]) + (1.0 - cf[lev]) * gassrc;
+          radld = cldradd + clrradd;
+          drad[lev - 1] = drad[lev - 1] + radld;
+          radmod = rad * (facclr1d[lev - 1] * (1. - atrans[lev]) + faccld1d[lev - 1] * ttot) -
+                   faccmb1d[lev - 1] * gassrc + faccmb2d[lev - 1] * cldsrc;
+          oldcld = cldradd - radmod;
+          oldclr = clrradd + radmod;
+          rad = -radmod + facclr2d[lev - 1] * oldclr - faccld2d[lev - 1] * oldcld;
+          cldradd = cldradd + rad;
+          clrradd = clrradd - rad;
+        } else {
+          if (odepth <= 0.06) {
+            atrans[lev] = odepth - 0.5 * odepth * odepth;
+            odepth = rec_6 * odepth;
+            bbd = plfrac * (blay + dplankdn * odepth);
+            bbugas[lev] = plfrac * (blay + dplankup * odepth);
+          } else {
+            const double tblind = odepth / (bpade + odepth);
+            const int itr = (int)(TBLINT * tblind + 0.5);
+            const double transc = exp_tbl[itr];
+            atrans[lev] = 1.0 - transc;
+            const double tausfac = tfn_tbl[itr];
+            bbd = plfrac * (blay + tausfac * dplankdn);
+            bbugas[lev] = plfrac * (blay + tausfac * dplankup);
+          }
+          radld = radld + (bbd - radld) * atrans[lev];
+          drad[lev - 1] = drad[lev - 1] + radld;
+        }
+        if (iclddn == 1) {
+          radclrd = radclrd + (bbd - radclrd) * atrans[lev];
+          clrdrad[lev - 1] = clrdrad[lev - 1] + radclrd;
+        } else {
+          radclrd = radld;
+          clrdrad[lev - 1] = drad[lev - 1];
+        }
+      }
+      const double rad0 = c.FRACS(1, igc) * c.plankbnd[iband - 1];
+      double d_rad0_dt = 0.0;
+      if (idrv == 1) d_rad0_dt = c.FRACS(1, igc) * c.dplankbnd_dt[iband - 1];
+      const double reflect = 1.0 - c.semiss[iband - 1];
+      double radlu = rad0 + reflect * radld;
+      double radclru = rad0 + reflect * radclrd;
+      urad[0] = urad[0] + radlu;
+      clrurad[0] = clrurad[0] + radclru;
+      double d_radlu_dt = 0.0, d_radclru_dt = 0.0;
+      if (idrv == 1) {
+        d_radlu_dt = d_rad0_dt;
+        d_urad_dt[0] = d_urad_dt[0] + d_radlu_dt;
+        d_radclru_dt = d_rad0_dt;
+        d_clrurad_dt[0] = d_clrurad_dt[0] + d_radclru_dt;
+      }
+      double cldradu = 0.0, clrradu = 0.0;
+      for (int lev = 1; lev <= nlayers; ++lev) {
+        if (icldlyr[lev] == 1) {
+          const double gassrc = bbugas[lev] * atrans[lev];
+          if (istcld[lev] == 1) {
+            cldradu = cf[lev] * radlu;
+            clrradu = radlu - cldradu;
+            oldcld = cldradu;
+            oldclr = clrradu;
+            rad = 0.0;
+          }
+          const double ttot = 1.0 - atot[lev];
+          const double cldsrc = bbutot[lev] * atot[lev];
+          cldradu = cldradu * ttot + cf[lev] * cldsrc;
+          clrradu = clrradu * (1.0 - atrans[lev]) + (1.0 - cf[lev]) * gassrc;
+          radlu = cldradu + clrradu;
+          urad[lev] = urad[lev] + radlu;
+          radmod = rad * (facclr1[lev + 1] * (1.0 - atrans[lev]) + faccld1[lev + 1] * ttot) -
+                   faccmb1[lev + 1] * gassrc + faccmb2[lev + 1] * cldsrc;
+          oldcld = cldradu - radmod;
+          oldclr = clrradu + radmod;
+          rad = -radmod + facclr2[lev + 1] * oldclr - faccld2[lev + 1] * oldcld;
+          cldradu = cldradu + rad;
+          clrradu = clrradu - rad;
+          if (idrv == 1) {
+            d_radlu_dt = d_radlu_dt * cf[lev] * (1.0 - atot[lev]) + d_radlu_dt * (1.0 - cf[lev]) * (1.0 - atrans[lev]);
+            d_urad_dt[lev] = d_urad_dt[lev] + d_radlu_dt;
+          }
+        } else {
+          radlu = radlu + (bbugas[lev] - radlu) * atrans[lev];
+          urad[lev] = urad[lev] + radlu;
+          if (idrv == 1) {
+            d_radlu_dt = d_radlu_dt * (1.0 - atrans[lev]);
+            d_urad_dt[lev] = d_urad_dt[lev] + d_radlu_dt;
+          }
+        }
+        if (iclddn == 1) {
+          radclru = radclru + (bbugas[lev] - radclru) * atrans[lev];
+          clrurad[lev] = clrurad[lev] + radclru;
+        } else {
+          radclru = radlu;
+          clrurad[lev] = urad[lev];
+        }
+        if (idrv == 1) {
+          if (iclddn == 1) {
+            d_radclru_dt = d_radclru_dt * (1.0 - atrans[lev]);
+            d_clrurad_dt[lev] = d_clrurad_dt[lev] + d_radclru_dt;
+          } else {
+            d_radclru_dt = d_radlu_dt;
+            d_clrurad_dt[lev] = d_urad_dt[lev];
+          }
+        }
+      }
+    }
+    for (int lev = nlayers; lev >= 0; --lev) {  // band output (:762-775)
+      const double uflux = urad[lev] * wtdiff, dflux = drad[lev] * wtdiff;
+      urad[lev] = 0.0;
+      drad[lev] = 0.0;
+      c.totuflux[lev] = c.totuflux[lev] + uflux * delwave[iband - 1];
+      c.totdflux[lev] = c.totdflux[lev] + dflux * delwave[iband - 1];
+      const double uclfl = clrurad[lev] * wtdiff, dclfl = clrdrad[lev] * wtdiff;
+      clrurad[lev] = 0.0;
+      clrdrad[lev] = 0.0;
+      c.totuclfl[lev] = c.totuclfl[lev] + uclfl * delwave[iband - 1];
+      c.totdclfl[lev] = c.totdclfl[lev] + dclfl * delwave[iband - 1];
+    }
+    if (idrv == 1) {
+      for (int lev = nlayers; lev >= 0; --lev) {
+        const double duflux_dt = d_urad_dt[lev] * wtdiff;
+        d_urad_dt[lev] = 0.0;
+        c.dtotuflux_dt[lev] = c.dtotuflux_dt[lev] + duflux_dt * delwave[iband - 1] * fluxfac;
+        const double duclfl_dt = d_clrurad_dt[lev] * wtdiff;
+        d_clrurad_dt[lev] = 0.0;
+        c.dtotuclfl_dt[lev] = c.dtotuclfl_dt[lev] + duclfl_dt * delwave[iband - 1] * fluxfac;
+      }
+    }
+  }
+  c.totuflux[0] = c.totuflux[0] * fluxfac;  // :779-806
+  c.totdflux[0] = c.totdflux[0] * fluxfac;
+  c.fnet[0] = c.totuflux[0] - c.totdflux[0];
+  c.totuclfl[0] = c.totuclfl[0] * fluxfac;
+  c.totdclfl[0] = c.totdclfl[0] * fluxfac;
+  c.fnetc[0] = c.totuclfl[0] - c.totdclfl[0];
+  for (int lev = 1; lev <= nlayers; ++lev) {
+    c.totuflux[lev] = c.totuflux[lev] * fluxfac;
+    c.totdflux[lev] = c.totdflux[lev] * fluxfac;
+    c.fnet[lev] = c.totuflux[lev] - c.totdflux[lev];
+    c.totuclfl[lev] = c.totuclfl[lev] * fluxfac;
+    c.totdclfl[lev] = c.totdclfl[lev] * fluxfac;
+    c.fnetc[lev] = c.totuclfl[lev] - c.totdclfl[lev];
+    const int l = lev - 1;
+    c.htr[l] = heatfac * (c.fnet[l] - c.fnet[lev]) / (c.pz[l] - c.pz[lev]);
+    c.htrc[l] = heatfac * (c.fnetc[l] - c.fnetc[lev]) / (c.pz[l] - c.pz[lev]);
+  }
+  c.htr[nlayers] = 0.0;
+  c.htrc[nlayers] = 0.0;
+}
+
 }  // namespace
 extern "C" int ora_cldprop(int nlayers, int inflag, int iceflag, int liqflag, const double* cldfrac,
                            const double* tauc, const double* ciwp, const double* clwp, const double* rei,
@@ -1456,10 +1877,11 @@ struct CloudsR {
   const double *cldfr, *taucld, *cicewp, *cliqwp, *reice, *reliq;
 };
 
-// one column of the non-McICA driver with random overlap, icld = 1
-// (rrtmg_lw_rad.nomcica.f90:470-553: inatm, cldprop, setcoef, taumol, rtrn;
-// the state part of inatm is the McICA driver's, its cloud part :886-920
-// copies the band-level clouds below)
+// one column of the non-McICA driver (rrtmg_lw_rad.nomcica.f90:470-553:
+// inatm, cldprop, setcoef, taumol, then rtrn for icld = 1 and rtrnmr
+// otherwise; the state part of inatm is the McICA driver's, its cloud part
+// :886-920 copies the band-level clouds below for icld >= 1 and leaves them
+// zero for icld = 0)
 int run_column_rtrn(const Args& a, const CloudsR& cl, int iplon, Col& c) {
   const int iaer = 10;
   inatm(iplon, a.ncol, a.nlay, 0, iaer, a.play, a.plev, a.tlay, a.tlev, a.tsfc, a.h2ovmr, a.o3vmr,
@@ -1468,7 +1890,7 @@ int run_column_rtrn(const Args& a, const CloudsR& cl, int iplon, Col& c) {
         a.tauaer, c);
   const int nl = c.nlayers;
   std::vector<double> cf(nl), ci(nl), cw(nl), ri(nl), rl(nl), tc(16 * nl);
-  for (int l = 1; l <= nl; ++l) {
+  for (int l = 1; l <= nl && a.icld >= 1; ++l) {
     const size_t o = (iplon - 1) + (size_t)a.ncol * (l - 1);
     cf[l - 1] = cl.cldfr[o];
     ci[l - 1] = cl.cicewp[o];
@@ -1489,7 +1911,10 @@ int run_column_rtrn(const Args& a, const CloudsR& cl, int iplon, Col& c) {
   taumol(c);
   for (int k = 1; k <= c.nlayers; ++k)
     for (int ig = 1; ig <= NGPT; ++ig) c.TAUT(k, ig) = c.TAUG(k, ig) + c.TAUA(k, ngb[ig - 1]);
-  rtrnmc(c, a.idrv);
+  if (a.icld == 1)
+    rtrnmc(c, a.idrv);
+  else
+    rtrnmr(c, a.idrv);
   c.rtrn = 0;
   return 0;
 }
@@ -1596,10 +2021,10 @@ int ora_rrtmg_lw(int ncol, int nlay, int* icld, int idrv, const double* play, co
   return 0;
 }
 
-// rrtmg_lw of the non-McICA driver (rrtmg_lw_rad.nomcica.f90:99-560) for
-// icld = 1, random cloud overlap through rtrn; other icld values (rtrnmr)
-// are not restated here and return ERR_ICLD.
-int ora_rrtmg_lw_rtrn(int ncol, int nlay, int icld, int idrv, const double* play, const double* plev,
+// rrtmg_lw of the non-McICA driver (rrtmg_lw_rad.nomcica.f90:99-560): icld
+// outside 0..3 becomes 2 (:456); icld 1 takes random cloud overlap (rtrn),
+// the others maximum/random overlap (rtrnmr; icld 0 with no clouds).
+int ora_rrtmg_lw_nomcica(int ncol, int nlay, int* icld_io, int idrv, const double* play, const double* plev,
                       const double* tlay, const double* tlev, const double* tsfc, const double* h2ovmr,
                       const double* o3vmr, const double* co2vmr, const double* ch4vmr, const double* n2ovmr,
                       const double* o2vmr, const double* cfc11vmr, const double* cfc12vmr,
@@ -1609,8 +2034,9 @@ int ora_rrtmg_lw_rtrn(int ncol, int nlay, int icld, int idrv, const double* play
                       const double* tauaer, double* uflx, double* dflx, double* hr, double* uflxc,
                       double* dflxc, double* hrc, double* duflx_dt, double* duflxc_dt) {
   if (!g_ready) return ERR_NOT_INIT;
-  if (ncol < 0 || nlay < 1) return ERR_ARGS;
-  if (icld != 1) return ERR_ICLD;
+  if (ncol < 0 || nlay < 1 || !icld_io) return ERR_ARGS;
+  if (*icld_io < 0 || *icld_io > 3) *icld_io = 2;
+  const int icld = *icld_io;
   Args a{ncol, nlay, icld, idrv, play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr,
          n2ovmr, o2vmr, cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis, inflglw, iceflglw,
          liqflglw, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, tauaer};

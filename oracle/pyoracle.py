@@ -83,10 +83,18 @@ def rrtmg_lw(state: dict, mc: dict, icld: int = 3, idrv: int = 1, inflglw: int =
 
 def rrtmg_lw_rtrn(state: dict, idrv: int = 1, inflglw: int = 2, iceflglw: int = 3,
                   liqflglw: int = 1) -> dict:
-    """rrtmg_lw of the non-McICA driver with random cloud overlap (icld 1,
-    rtrn) on band-level clouds: state['cldfrac'], 'ciwp', 'clwp', 'rei', 'rel'
-    (ncol, nlay) and optional 'tauc_band' (16, ncol, nlay, read for inflag 0)."""
-    L = lib()
+    """The non-McICA driver with random cloud overlap (icld 1, rtrn)."""
+    return rrtmg_lw_nomcica(state, 1, idrv, inflglw, iceflglw, liqflglw)
+
+
+def rrtmg_lw_nomcica(state: dict, icld: int = 2, idrv: int = 1, inflglw: int = 2, iceflglw: int = 3,
+                     liqflglw: int = 1, native: bool = False) -> dict:
+    """rrtmg_lw of the non-McICA driver (rrtmg_lw_rad.nomcica.f90) on
+    band-level clouds: state['cldfrac'], 'ciwp', 'clwp', 'rei', 'rel' (ncol,
+    nlay) and optional 'tauc_band' (16, ncol, nlay, read for inflag 0).
+    icld 1: random overlap (rtrn); 0, 2, 3: maximum/random overlap (rtrnmr);
+    other values become 2 (returned in out['icld'])."""
+    L = lib(native)
     ncol, nlay = state["play"].shape
     st = [_f(state[k]) for k in STATE_ORDER]
     tb = state.get("tauc_band")
@@ -95,12 +103,14 @@ def rrtmg_lw_rtrn(state: dict, idrv: int = 1, inflglw: int = 2, iceflglw: int = 
     out = {k: np.zeros((ncol, nlay + 1), order="F") for k in ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt")}
     out["hr"] = np.zeros((ncol, nlay), order="F")
     out["hrc"] = np.zeros((ncol, nlay), order="F")
-    args = [C.c_int(ncol), C.c_int(nlay), C.c_int(1), C.c_int(idrv)] + [_p(a) for a in st]
+    ic = C.c_int(icld)
+    args = [C.c_int(ncol), C.c_int(nlay), C.byref(ic), C.c_int(idrv)] + [_p(a) for a in st]
     args += [C.c_int(inflglw), C.c_int(iceflglw), C.c_int(liqflglw)] + [_p(a) for a in cl] + [_p(_f(state["tauaer"]))]
     args += [_p(out[k]) for k in ("uflx", "dflx", "hr", "uflxc", "dflxc", "hrc", "duflx_dt", "duflxc_dt")]
-    rc = L.ora_rrtmg_lw_rtrn(*args)
+    rc = L.ora_rrtmg_lw_nomcica(*args)
     if rc != 0:
-        raise RuntimeError(f"oracle rrtmg_lw (rtrn): {L.ora_error_string(rc).decode()}")
+        raise RuntimeError(f"oracle rrtmg_lw (non-McICA): {L.ora_error_string(rc).decode()}")
+    out["icld"] = ic.value
     return out
 
 
