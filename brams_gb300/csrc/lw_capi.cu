@@ -450,6 +450,8 @@ int gb_rrtmg_lw_free(gb_lw_context* ctx) {
   cudaFree(ctx->d_fall);
   cudaFree(ctx->d_nfall);
   cudaFree(ctx->d_cloud64);
+  cudaFree(ctx->d_band);
+  cudaFree(ctx->d_ncb);
   delete ctx;
   return GB_LW_OK;
 }
@@ -594,6 +596,215 @@ int gb_rrtmg_lw(gb_lw_context* ctx, int ncol, int nlay, int* icld, int idrv, con
     a.col_err = nullptr;
     a.err_flag = ctx->d_err_host;
     rc = launch_one(ctx, a, k & 1, s);
+    if (rc) return rc;
+    auto D2H = [&](double* dst, size_t soff, size_t rows) {
+      return copy2d(dst + c0, (size_t)ld_out, O + soff, P, nc, rows, cudaMemcpyDeviceToHost, s);
+    };
+    CK(D2H(uflx, lo.uflx, nlay + 1));
+    CK(D2H(dflx, lo.dflx, nlay + 1));
+    CK(D2H(uflxc, lo.uflxc, nlay + 1));
+    CK(D2H(dflxc, lo.dflxc, nlay + 1));
+    CK(D2H(hr, lo.hr, nlay));
+    CK(D2H(hrc, lo.hrc, nlay));
+    if (idrv == 1) {
+      CK(D2H(duflx_dt, lo.duflx, nlay + 1));
+      CK(D2H(duflxc_dt, lo.duflxc, nlay + 1));
+    }
+  }
+  CK(cudaStreamSynchronize(ctx->streams[0]));
+  CK(cudaStreamSynchronize(ctx->streams[1]));
+  int h = 0;
+  CK(cudaMemcpy(&h, ctx->d_err_host, 4, cudaMemcpyDeviceToHost));
+  return h;
+}
+
+namespace {
+
+// grows a device array of the context to at least `n` elements of `size` bytes
+int ensure_elems(gb_lw_context* ctx, void** p, size_t* have, size_t n, size_t size, const char* what) {
+  if (*p && *have >= n) return 0;
+  cudaFree(*p);
+  *p = nullptr;
+  *have = 0;
+  if (cudaMalloc(p, n * size) != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    ctx->last_error = std::string("device allocation failed: ") + what;
+    return GB_LW_E_NOMEM;
+  }
+  *have = n;
+  return 0;
+}
+
+// argument checks shared by the non-McICA entry points
+int nomcica_check(gb_lw_context* ctx, int ncol, int nlay, int* icld, int idrv, int inflglw, int iceflglw,
+                  int liqflglw, int64_t ld_in, int64_t ld_out) {
+  if (!ctx || !icld) return GB_LW_E_ARGS;
+  if (*icld < 0 || *icld > 3) *icld = 2;  // rrtmg_lw_rad.nomcica.f90:456
+  if (ncol < 0 || nlay < 1 || nlay > GB_MAXLAY || ld_in < ncol || ld_out < ncol) return GB_LW_E_ARGS;
+  if (!flags_ok(idrv, inflglw, iceflglw, liqflglw)) return GB_LW_E_ARGS;
+  if (gb_lw_smem_bytes(nlay) > ctx->max_smem) {
+    ctx->last_error = "nlay too large for one thread block's shared memory";
+    return GB_LW_E_ARGS;
+  }
+  return 0;
+}
+
+// one grid of band clouds: cldprop into the context's band buffers, then the
+// band-cloud kernel (status into `err`, per-column codes into col_err)
+int nomcica_launch(gb_lw_context* ctx, LwArgs a, const double* cldfr, const double* taucld, const double* cicewp,
+                   const double* cliqwp, const double* reice, const double* reliq, int k, cudaStream_t stream) {
+  a.cloud_mode = LW_CLOUD_BAND;
+  if (a.icld >= 1) {
+    int rc = ensure_elems(ctx, reinterpret_cast<void**>(&ctx->d_band), &ctx->band_elems, (size_t)16 * a.ld * a.nlay,
+                          sizeof(double), "band cloud depths");
+    if (!rc)
+      rc = ensure_elems(ctx, reinterpret_cast<void**>(&ctx->d_ncb), &ctx->ncb_elems, (size_t)a.ld, sizeof(int),
+                        "cloud-band counts");
+    if (!rc)
+      rc = gb_ctx_cldprop(ctx, stream, a.ncol, a.nlay, a.inflag, a.iceflag, a.liqflag, cldfr, taucld, cicewp, cliqwp,
+                          reice, reliq, ctx->d_band, a.ld, a.col_err, ctx->d_ncb, a.err_flag);
+    if (rc) return rc;
+    a.cldfrac = cldfr;
+    a.tauc = ctx->d_band;
+    a.ncbands = ctx->d_ncb;
+  } else if (a.col_err) {
+    CK(cudaMemsetAsync(a.col_err, 0, sizeof(int) * (size_t)a.ncol, stream));
+  }
+  return launch_one(ctx, a, k, stream);
+}
+
+}  // namespace
+
+int gb_rrtmg_lw_nomcica_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int* icld, int idrv,
+                               const double* play, const double* plev, const double* tlay, const double* tlev,
+                               const double* tsfc, const double* h2ovmr, const double* o3vmr, const double* co2vmr,
+                               const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+                               const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr,
+                               const double* ccl4vmr, const double* emis, int inflglw, int iceflglw, int liqflglw,
+                               const double* cldfr, const double* taucld, const double* cicewp, const double* cliqwp,
+                               const double* reice, const double* reliq, const double* tauaer, double* uflx,
+                               double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc, double* duflx_dt,
+                               double* duflxc_dt, int64_t ld_in, int64_t ld_out, int* d_col_status) {
+  int rc = nomcica_check(ctx, ncol, nlay, icld, idrv, inflglw, iceflglw, liqflglw, ld_in, ld_out);
+  if (rc || ncol == 0) return rc;
+  const double* req[] = {play, plev, tlay, tlev, tsfc, h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr,
+                         cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr, emis, tauaer, uflx, dflx, hr, uflxc, dflxc, hrc};
+  for (const double* p : req)
+    if (!p) return GB_LW_E_ARGS;
+  if (*icld >= 1 && (!cldfr || !taucld || !cicewp || !cliqwp || !reice || !reliq)) return GB_LW_E_ARGS;
+  if (idrv == 1 && (!duflx_dt || !duflxc_dt)) return GB_LW_E_ARGS;
+  LwArgs a{};
+  a.ncol = ncol;
+  a.nlay = nlay;
+  a.ld = ld_in;
+  a.ldo = ld_out;
+  a.icld = *icld;
+  a.idrv = idrv;
+  a.inflag = inflglw;
+  a.iceflag = iceflglw;
+  a.liqflag = liqflglw;
+  a.play = play; a.plev = plev; a.tlay = tlay; a.tlev = tlev; a.tsfc = tsfc;
+  a.h2ovmr = h2ovmr; a.o3vmr = o3vmr; a.co2vmr = co2vmr; a.ch4vmr = ch4vmr; a.n2ovmr = n2ovmr; a.o2vmr = o2vmr;
+  a.cfc11vmr = cfc11vmr; a.cfc12vmr = cfc12vmr; a.cfc22vmr = cfc22vmr; a.ccl4vmr = ccl4vmr; a.emis = emis;
+  a.tauaer = tauaer;
+  a.uflx = uflx; a.dflx = dflx; a.hr = hr; a.uflxc = uflxc; a.dflxc = dflxc; a.hrc = hrc;
+  a.duflx_dt = duflx_dt; a.duflxc_dt = duflxc_dt;
+  a.col_err = d_col_status;
+  a.err_flag = ctx->d_err;
+  cudaSetDevice(ctx->device);
+  return nomcica_launch(ctx, a, cldfr, taucld, cicewp, cliqwp, reice, reliq, 0, (cudaStream_t)stream);
+}
+
+int gb_rrtmg_lw_nomcica(gb_lw_context* ctx, int ncol, int nlay, int* icld, int idrv, const double* play,
+                        const double* plev, const double* tlay, const double* tlev, const double* tsfc,
+                        const double* h2ovmr, const double* o3vmr, const double* co2vmr, const double* ch4vmr,
+                        const double* n2ovmr, const double* o2vmr, const double* cfc11vmr, const double* cfc12vmr,
+                        const double* cfc22vmr, const double* ccl4vmr, const double* emis, int inflglw,
+                        int iceflglw, int liqflglw, const double* cldfr, const double* taucld,
+                        const double* cicewp, const double* cliqwp, const double* reice, const double* reliq,
+                        const double* tauaer, double* uflx, double* dflx, double* hr, double* uflxc, double* dflxc,
+                        double* hrc, double* duflx_dt, double* duflxc_dt, int64_t ld_in, int64_t ld_out) {
+  int rc = nomcica_check(ctx, ncol, nlay, icld, idrv, inflglw, iceflglw, liqflglw, ld_in, ld_out);
+  if (rc || ncol == 0) return rc;
+  const bool clouds = *icld >= 1;
+  if (clouds && (!cldfr || !taucld || !cicewp || !cliqwp || !reice || !reliq)) return GB_LW_E_ARGS;
+  if (idrv == 1 && (!duflx_dt || !duflxc_dt)) return GB_LW_E_ARGS;
+  cudaSetDevice(ctx->device);
+  // chunks of the same buffers as gb_rrtmg_lw; the band clouds take the
+  // space of the McICA arrays: cldfr, cicewp, cliqwp and taucld in the
+  // cldfmcl area, cldprop's depths in the taucmcl area
+  const size_t per_col = (size_t)(600 * nlay + 64) * 8;
+  int C = (int)std::max<size_t>(1, std::min<size_t>((size_t)ncol, (size_t)(2ull << 30) / per_col));
+  rc = ensure_chunks(ctx, C, nlay);
+  if (rc) return rc;
+  const InLayout li = in_layout(C, nlay);
+  const OutLayout lo = out_layout(C, nlay);
+  CK(cudaMemsetAsync(ctx->d_err_host, 0, 4, ctx->streams[0]));
+  CK(cudaStreamSynchronize(ctx->streams[0]));
+  const double* gas_src[10] = {h2ovmr, o3vmr, co2vmr, ch4vmr, n2ovmr, o2vmr, cfc11vmr, cfc12vmr, cfc22vmr, ccl4vmr};
+  const size_t lay = (size_t)C * nlay;
+  const int nchunks = (ncol + C - 1) / C;
+  for (int k = 0; k < nchunks; ++k) {
+    const int c0 = k * C, nc = std::min(C, ncol - c0);
+    cudaStream_t s = ctx->streams[k & 1];
+    double* I = ctx->bufs[k & 1].in;
+    double* O = ctx->bufs[k & 1].out;
+    const size_t P = C;
+    auto H2D = [&](size_t doff, const double* src, size_t rows) {
+      return copy2d(I + doff, P, src + c0, (size_t)ld_in, nc, rows, cudaMemcpyHostToDevice, s);
+    };
+    CK(H2D(li.play, play, nlay));
+    CK(H2D(li.plev, plev, nlay + 1));
+    CK(H2D(li.tlay, tlay, nlay));
+    CK(H2D(li.tlev, tlev, nlay + 1));
+    CK(H2D(li.tsfc, tsfc, 1));
+    for (int g = 0; g < 10; ++g) CK(H2D(li.gas[g], gas_src[g], nlay));
+    CK(H2D(li.emis, emis, 16));
+    CK(H2D(li.tauaer, tauaer, (size_t)nlay * 16));
+    const size_t cf_o = li.cldf, ci_o = li.cldf + lay, cw_o = li.cldf + 2 * lay, tc_o = li.cldf + 3 * lay;
+    if (clouds) {
+      CK(H2D(cf_o, cldfr, nlay));
+      CK(H2D(ci_o, cicewp, nlay));
+      CK(H2D(cw_o, cliqwp, nlay));
+      CK(H2D(li.reic, reice, nlay));
+      CK(H2D(li.relq, reliq, nlay));
+      CK(copy2d(I + tc_o, 16 * P, taucld + (size_t)16 * c0, (size_t)16 * ld_in, (size_t)16 * nc, nlay,
+                cudaMemcpyHostToDevice, s));
+    }
+    LwArgs a{};
+    a.ncol = nc;
+    a.nlay = nlay;
+    a.ld = P;
+    a.ldo = P;
+    a.icld = *icld;
+    a.idrv = idrv;
+    a.inflag = inflglw;
+    a.iceflag = iceflglw;
+    a.liqflag = liqflglw;
+    a.play = I + li.play; a.plev = I + li.plev; a.tlay = I + li.tlay; a.tlev = I + li.tlev; a.tsfc = I + li.tsfc;
+    a.h2ovmr = I + li.gas[0]; a.o3vmr = I + li.gas[1]; a.co2vmr = I + li.gas[2]; a.ch4vmr = I + li.gas[3];
+    a.n2ovmr = I + li.gas[4]; a.o2vmr = I + li.gas[5]; a.cfc11vmr = I + li.gas[6]; a.cfc12vmr = I + li.gas[7];
+    a.cfc22vmr = I + li.gas[8]; a.ccl4vmr = I + li.gas[9]; a.emis = I + li.emis; a.tauaer = I + li.tauaer;
+    a.uflx = O + lo.uflx; a.dflx = O + lo.dflx; a.uflxc = O + lo.uflxc; a.dflxc = O + lo.dflxc;
+    a.duflx_dt = O + lo.duflx; a.duflxc_dt = O + lo.duflxc; a.hr = O + lo.hr; a.hrc = O + lo.hrc;
+    a.col_err = nullptr;
+    a.err_flag = ctx->d_err_host;
+    if (clouds) {
+      // cldprop's outputs in the chunk's own buffers (the chunks of the two streams overlap)
+      a.cloud_mode = LW_CLOUD_BAND;
+      double* band = I + li.tauc;
+      int* ncb = reinterpret_cast<int*>(I + li.ciwp);
+      rc = gb_ctx_cldprop(ctx, s, nc, nlay, inflglw, iceflglw, liqflglw, I + cf_o, I + tc_o, I + ci_o, I + cw_o,
+                          I + li.reic, I + li.relq, band, (int64_t)P, nullptr, ncb, ctx->d_err_host);
+      if (rc) return rc;
+      a.cldfrac = I + cf_o;
+      a.tauc = band;
+      a.ncbands = ncb;
+      rc = launch_one(ctx, a, k & 1, s);
+    } else {
+      rc = nomcica_launch(ctx, a, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, k & 1, s);
+    }
     if (rc) return rc;
     auto D2H = [&](double* dst, size_t soff, size_t rows) {
       return copy2d(dst + c0, (size_t)ld_out, O + soff, P, nc, rows, cudaMemcpyDeviceToHost, s);

@@ -73,13 +73,25 @@ __global__ void __launch_bounds__(64) cldprop_kernel(int ncol, int nlay, long lo
                                                      const double* __restrict__ ciwp, const double* __restrict__ clwp,
                                                      const double* __restrict__ rei, const double* __restrict__ rel,
                                                      double* __restrict__ taucloud, int pairs,
-                                                     int* __restrict__ col_err, int* __restrict__ err_flag, Cloud64 c) {
+                                                     int* __restrict__ col_err, int* __restrict__ err_flag, Cloud64 c,
+                                                     int* __restrict__ ncb_col) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)ncol * nlay) return;
   const int lay = (int)(idx / ncol);
   const long long icol = idx - (long long)lay * ncol;
   const double cldmin = 1.e-20;
   const long long o = icol + ld * lay;
+  if (ncb_col && lay == nlay - 1) {
+    // the column's ncbands after the whole layer loop (what the non-McICA
+    // driver hands to rtrn/rtrnmr): the setting of the highest layer that
+    // makes one, else the initial 1 (rrtmg_lw_cldprop.f90:173)
+    int nb = -1;
+    for (int l = nlay - 1; nb < 0 && l >= 0; --l) {
+      const long long ol = icol + ld * l;
+      nb = layer_sets_ncbands(inflag, iceflag, liqflag, cldfrac[ol], ciwp[ol], clwp[ol], tau_total(tauc_in, ol));
+    }
+    ncb_col[icol] = nb < 0 ? 1 : nb;
+  }
   double* out = taucloud + 16 * o;
   const double tauctot = tau_total(tauc_in, o);
   const double ci = ciwp[o], cl = clwp[o], cf = cldfrac[o];
@@ -199,6 +211,14 @@ __global__ void __launch_bounds__(64) cldprop_kernel(int ncol, int nlay, long lo
 int gb_cldprop_lw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int inflag, int iceflag, int liqflag,
                          const double* cldfrac, const double* tauc, const double* ciwp, const double* clwp,
                          const double* rei, const double* rel, double* taucloud, int64_t ld, int* d_col_status) {
+  return gb_ctx_cldprop(ctx, stream, ncol, nlay, inflag, iceflag, liqflag, cldfrac, tauc, ciwp, clwp, rei, rel,
+                        taucloud, ld, d_col_status, nullptr, nullptr);
+}
+
+int gb_ctx_cldprop(gb_lw_context* ctx, void* stream, int ncol, int nlay, int inflag, int iceflag, int liqflag,
+                   const double* cldfrac, const double* tauc, const double* ciwp, const double* clwp, const double* rei,
+                   const double* rel, double* taucloud, int64_t ld, int* d_col_status, int* d_ncbands,
+                   int* d_err_flag) {
   if (!ctx || ncol < 0 || nlay < 1 || nlay > GB_MAXLAY || ld < ncol || inflag < 0 || inflag > 2 || iceflag < 0 ||
       iceflag > 3 || liqflag < 0 || liqflag > 1 || !cldfrac || !ciwp || !clwp || !rei || !rel || !taucloud ||
       (inflag == 0 && !tauc))
@@ -223,7 +243,8 @@ int gb_cldprop_lw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, i
   const int blocks = (int)((n + threads - 1) / threads);
   gbcp::cldprop_kernel<<<blocks, threads, 0, (cudaStream_t)stream>>>(ncol, nlay, ld, inflag, iceflag, liqflag, cldfrac,
                                                                       tauc, ciwp, clwp, rei, rel, taucloud, pairs,
-                                                                      d_col_status, ctx->d_err, c);
+                                                                      d_col_status, d_err_flag ? d_err_flag : ctx->d_err, c,
+                                                                      d_ncbands);
   e = cudaGetLastError();
   if (e != cudaSuccess) return gb_ctx_fail(ctx, e, "cldprop launch");
   return GB_LW_OK;

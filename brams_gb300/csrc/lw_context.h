@@ -51,6 +51,12 @@ struct gb_lw_context {
   uint16_t* d_sur = nullptr;  // fp16 taug and Planck fractions
   unsigned char* d_sur_flag = nullptr;
   size_t sur_rows = 0;
+  // band clouds of the non-McICA calls: cldprop's optical depths (16, ncol,
+  // nlay) and cloud-band counts (ncol) (grown on demand)
+  double* d_band = nullptr;
+  size_t band_elems = 0;
+  int* d_ncb = nullptr;
+  size_t ncb_elems = 0;
 };
 
 // records a CUDA error on the context; returns GB_LW_E_CUDA
@@ -61,6 +67,13 @@ int gb_ctx_make_batch(gb_lw_context* ctx, int ngrid, const gb_lw_grid* grids, do
 // (first the McICA draws of its fused-cloud grids, into `draws` when given,
 // else into a context buffer)
 int gb_ctx_launch_batch(gb_lw_context* ctx, LwBatch& b, cudaStream_t stream);
+// cldprop on device arrays (gb_cldprop_lw_device), with each column's final
+// cloud-band count into d_ncbands when that is not NULL, and the status into
+// d_err_flag (NULL: the context's device-call status)
+int gb_ctx_cldprop(gb_lw_context* ctx, void* stream, int ncol, int nlay, int inflag, int iceflag, int liqflag,
+                   const double* cldfrac, const double* tauc, const double* ciwp, const double* clwp, const double* rei,
+                   const double* rel, double* taucloud, int64_t ld, int* d_col_status, int* d_ncbands,
+                   int* d_err_flag);
 // doubles of McICA draws a descriptor's fused-cloud grids need
 size_t gb_ctx_fused_draws(const LwBatch& b);
 // launches the draw kernels of a descriptor's fused-cloud grids into buf and sets their draws pointers

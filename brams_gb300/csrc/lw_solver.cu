@@ -49,6 +49,7 @@
 #include <cmath>
 #include <stdint.h>
 #include <climits>
+#include <cstddef>
 
 #include "lw_common.h"
 #include "lw_solver.h"
@@ -426,17 +427,26 @@ struct RtLayer {
   float4 rec[16];     // per band: Planck value of the layer, level-minus-layer Planck below and
                       // above (dplankdn, dplankup), aerosol optical depth
   float tcl[16];      // fused clouds: cloud optical depth per band; caller sub-columns: the
-                      // first five words are fbits (bit g: cldfmcl neither 0 nor 1)
+                      // first five words are fbits (bit g: cldfmcl neither 0 nor 1); band
+                      // clouds: secdiff(ib) * taucloud per cloud band ib (rtrn's odcld)
+  int cldlay;         // 1: a cell of the layer has cldfmc == 1 (rtrnmc's icldlyr), or band
+                      // clouds: cldfrac >= 1e-6; in the first phase: 1 where the layer is in
+                      // the lower atmosphere
+  int lfl;            // cloud flags of the layer (bits 0-2) and cldprmc's stop code (bits
+                      // 8..); band clouds: istcld (bit 0) and istcldd (bit 1) of rtrnmr
+  // McICA clouds use the words below as named; band clouds overlay them with
+  // 14 floats (RtSmem::ovl): cldfrac, rtrnmr's upward overlap factors at lev+1
+  // (facclr1, facclr2, faccld1, faccld2, faccmb1, faccmb2) and the downward
+  // ones at lev-1, in that order
   unsigned cbits[5];  // bit g set where the cell is cloudy (cldfmc == 1)
-  int cldlay;         // 1: a cell of the layer has cldfmc == 1 (rtrnmc's icldlyr); in the first
-                      // phase: 1 where the layer is in the lower atmosphere
-  int lfl;            // cloud flags of the layer (bits 0-2) and cldprmc's stop code (bits 8..)
   int pad0;
   long long cthr;     // fused clouds: McICA threshold 1 - cldf as double bits
   long long pad1;
   float4 lcw;         // (ciwp, clwp, radice, radliq) as floats
 };
 static_assert(sizeof(RtHead) == 320 && sizeof(RtLayer) == 384, "transfer shared-memory records");
+static_assert(offsetof(RtLayer, lcw) + sizeof(float4) - offsetof(RtLayer, cbits) == 14 * sizeof(float),
+              "band-cloud overlay of the McICA words");
 
 struct RtSmem {
   RtHead* h;
@@ -445,6 +455,7 @@ struct RtSmem {
                 // dup clear/dT; in the first phase: float4 per level, the Planck-table row and
                 // fraction of tlev and tlay
   __device__ __forceinline__ unsigned* fbits(int lay) const { return reinterpret_cast<unsigned*>(L[lay].tcl); }
+  __device__ __forceinline__ float* ovl(int lay) const { return reinterpret_cast<float*>(L[lay].cbits); }
 };
 
 __host__ __device__ inline size_t rt_layers_bytes(int nl) {
@@ -580,10 +591,189 @@ __device__ __forceinline__ int liq_code(int liqflag, double rliq) {
   return liqflag == 1 && (rliq < 2.5 || rliq > 60.0) ? GB_COL_LIQ_BOUNDS : 0;
 }
 
+// rtrnmr's maximum/random overlap factors (rrtmg_lw_rtrnmr.f90:345-514), by
+// one thread in fp64 from the layer fractions cf[0 .. nl-1]; lev is the
+// reference's 1-based layer.  The fractions beyond the column (lev 0 and
+// nl+1) are 0: the driver's cloud array is zeroed above the column
+// (nomcica.f90 inatm), and below it the reference reads outside its array,
+// where the surface (no cloud) is taken.  faccmb, which the reference leaves
+// undefined where istcld = 1, is 0 there.  Layer lev keeps its istcld
+// (istcldd) in bit 0 (1) of lfl, the upward factors at lev+1 in ovl[1..6]
+// and the downward ones at lev-1 in ovl[7..12].
+__device__ __noinline__ void band_overlap(const RtSmem& S, const double* __restrict__ cf, int nl) {
+  auto CF = [&](int lev) -> double { return lev >= 1 && lev <= nl ? cf[lev - 1] : 0.0; };
+  auto cloudy = [&](int lev) { return S.L[lev - 1].cldlay != 0; };
+  enum { CLR1 = 0, CLR2, CLD1, CLD2, CMB1, CMB2 };
+  double rat1 = 0.0, rat2 = 0.0;
+  int st = 1;  // istcld(lev)
+  for (int lev = 1; lev <= nl; ++lev) {
+    if (st) S.L[lev - 1].lfl |= 1;
+    float* u = S.ovl(lev - 1) + 1;  // factors at lev+1
+    if (!cloudy(lev)) {
+      st = 1;
+      continue;
+    }
+    double f[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    const double c0 = CF(lev), cp = CF(lev + 1), cm = CF(lev - 1);
+    if (lev == nl) {
+      // all six 0
+    } else if (cp >= c0) {
+      if (st) {
+        if (c0 < 1.0) f[CLR2] = (cp - c0) / (1.0 - c0);
+        if (lev >= 2) S.ovl(lev - 2)[1 + CLR2] = S.ovl(lev - 2)[1 + CLD2] = 0.0f;  // facclr2(lev), faccld2(lev)
+      } else {
+        const double fmax = c0 > cm ? c0 : cm;
+        if (cp > fmax) {
+          f[CLR1] = rat2;
+          f[CLR2] = (cp - fmax) / (1.0 - fmax);
+        } else if (cp < fmax) {
+          f[CLR1] = (cp - c0) / (cm - c0);
+        } else {
+          f[CLR1] = rat2;
+        }
+      }
+      if (f[CLR1] > 0.0 || f[CLR2] > 0.0) {
+        rat1 = 1.0;
+        rat2 = 0.0;
+      } else {
+        rat1 = rat2 = 0.0;
+      }
+    } else {
+      if (st) {
+        f[CLD2] = (c0 - cp) / c0;
+        if (lev >= 2) S.ovl(lev - 2)[1 + CLR2] = S.ovl(lev - 2)[1 + CLD2] = 0.0f;
+      } else {
+        const double fmin = c0 < cm ? c0 : cm;
+        if (cp <= fmin) {
+          f[CLD1] = rat1;
+          f[CLD2] = (fmin - cp) / fmin;
+        } else {
+          f[CLD1] = (c0 - cp) / (c0 - fmin);
+        }
+      }
+      if (f[CLD1] > 0.0 || f[CLD2] > 0.0) {
+        rat1 = 0.0;
+        rat2 = 1.0;
+      } else {
+        rat1 = rat2 = 0.0;
+      }
+    }
+    if (!st) {
+      f[CMB1] = fmax(0.0, fmin(cp - c0, cm - c0));
+      f[CMB2] = fmax(0.0, fmin(c0 - cp, c0 - cm));
+    }
+    for (int k = 0; k < 6; ++k) u[k] = (float)f[k];
+    st = 0;
+  }
+  int sd = 1;  // istcldd(lev); rat1 and rat2 carry over from the loop above
+  for (int lev = nl; lev >= 1; --lev) {
+    if (sd) S.L[lev - 1].lfl |= 2;
+    float* d = S.ovl(lev - 1) + 7;  // factors at lev-1
+    if (!cloudy(lev)) {
+      sd = 1;
+      continue;
+    }
+    double f[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    const double c0 = CF(lev), cp = CF(lev + 1), cm = CF(lev - 1);
+    if (lev == 1) {
+      // all six 0
+    } else if (cm >= c0) {
+      if (sd) {
+        if (c0 < 1.0) f[CLR2] = (cm - c0) / (1.0 - c0);
+        if (lev < nl) S.ovl(lev)[7 + CLR2] = S.ovl(lev)[7 + CLD2] = 0.0f;  // facclr2d(lev), faccld2d(lev)
+      } else {
+        const double fmax = c0 > cp ? c0 : cp;
+        if (cm > fmax) {
+          f[CLR1] = rat2;
+          f[CLR2] = (cm - fmax) / (1.0 - fmax);
+        } else if (cm < fmax) {
+          f[CLR1] = (cm - c0) / (cp - c0);
+        } else {
+          f[CLR1] = rat2;
+        }
+      }
+      if (f[CLR1] > 0.0 || f[CLR2] > 0.0) {
+        rat1 = 1.0;
+        rat2 = 0.0;
+      } else {
+        rat1 = rat2 = 0.0;
+      }
+    } else {
+      if (sd) {
+        f[CLD2] = (c0 - cm) / c0;
+        if (lev < nl) S.ovl(lev)[7 + CLR2] = S.ovl(lev)[7 + CLD2] = 0.0f;
+      } else {
+        const double fmin = c0 < cp ? c0 : cp;
+        if (cm <= fmin) {
+          f[CLD1] = rat1;
+          f[CLD2] = (fmin - cm) / fmin;
+        } else {
+          f[CLD1] = (c0 - cm) / (c0 - fmin);
+        }
+      }
+      if (f[CLD1] > 0.0 || f[CLD2] > 0.0) {
+        rat1 = 0.0;
+        rat2 = 1.0;
+      } else {
+        rat1 = rat2 = 0.0;
+      }
+    }
+    if (!sd) {
+      f[CMB1] = fmax(0.0, fmin(cp - c0, cm - c0));
+      f[CMB2] = fmax(0.0, fmin(c0 - cp, c0 - cm));
+    }
+    for (int k = 0; k < 6; ++k) d[k] = (float)f[k];
+    sd = 0;
+  }
+}
+
+// The band clouds of the non-McICA driver (nomcica.f90:886-920, rtrn.f90:319-336,
+// rtrnmr.f90:334-343): per layer the fraction, icldlyr (cldfrac >= 1e-6) and
+// odcld = secdiff(ib) * taucloud(ib) for the cloud bands ib < ncbands, then
+// for maximum/random overlap the overlap factors.  Ends with a barrier when
+// it computes them.
+__device__ __forceinline__ void band_clouds(const LwArgs& a, long long icol, const RtSmem& S, int nl, bool clouds) {
+  const int tid = threadIdx.x;
+  if (!clouds) {
+    for (int lay = tid; lay < nl; lay += RT_NT) S.L[lay].cldlay = 0;
+    return;
+  }
+  // fp64 fractions for the overlap factors, after the Planck-table rows of the first phase
+  double* cf64 = reinterpret_cast<double*>(S.part + 4 * (nl + 1));
+  const int ncb = __ldg(a.ncbands + icol);
+  if (tid == 0) S.h->iscal[2] = ncb;
+  for (int lay = tid; lay < nl; lay += RT_NT) {
+    const double cf = in2(a.cldfrac, a.ld, icol, lay);
+    S.L[lay].cldlay = cf >= 1.e-6;
+    S.L[lay].lfl = 0;
+    float* ov = S.ovl(lay);
+    ov[0] = (float)cf;
+#pragma unroll
+    for (int k = 1; k < 14; ++k) ov[k] = 0.0f;
+    cf64[lay] = cf;
+  }
+  for (int it = tid; it < nl * 16; it += RT_NT) {
+    const int lay = it >> 4, ib = it & 15;
+    S.L[lay].tcl[ib] = ib < ncb ? S.h->misc[ib] * (float)__ldg(a.tauc + ib + 16 * (icol + a.ld * lay)) : 0.0f;
+  }
+  if (a.icld >= 2) {
+    __syncthreads();
+    if (tid == 0) band_overlap(S, cf64, nl);
+  }
+}
+
+// cloud band of spectral band `band` for cldprop's band count (rtrn.f90:253-255, 345-351)
+__device__ __forceinline__ int cloud_band(int ncb, int band) {
+  if (ncb == 1) return 0;
+  if (ncb == 5) return band < 1 ? 0 : band < 2 ? 1 : band < 5 ? 2 : band < 8 ? 3 : 4;
+  return band;
+}
+
 // The transfer of one column by the block (see the file header).  RT_NET: a
 // column with any layer off the network is not solved (returns false in
-// every thread).  Ends with a barrier.
-template <int MODE>
+// every thread).  BAND: the non-McICA driver's band clouds (random overlap
+// for icld 1, maximum/random otherwise).  Ends with a barrier.
+template <int MODE, bool BAND = false>
 __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, const GasSrc& src,
                           const float* __restrict__ T) {
   const unsigned FULL = 0xffffffffu;
@@ -695,6 +885,9 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
   }
   // ---------------- clouds: the cells' McICA bits, cldprmc's optical depths and stop conditions
   int err = 0;
+  if constexpr (BAND) {
+    band_clouds(a, icol, S, nl, clouds);
+  } else {
   for (int i = tid; i < nl * 5; i += RT_NT) {
     const int l = i / 5, w = i - 5 * l;
     S.L[l].cbits[w] = 0u;
@@ -810,13 +1003,19 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
   } else {
     for (int lay = tid; lay < nl; lay += RT_NT) S.L[lay].cldlay = 0;
   }
+  }
   if (err) atomicMax(&S.h->iscal[0], err);
   __syncthreads();
   if (tid == 0) {
     err = S.h->iscal[0];
     if (notpre) err = GB_COL_LAYTROP;
     if (bad) err = GB_COL_BADVAL;
-    if (err) {
+    if (BAND) {  // the column status already holds cldprop's code
+      if (err) {
+        if (a.col_err) atomicMax(a.col_err + icol, err);
+        atomicMax(a.err_flag, err);
+      }
+    } else if (err) {
       if (a.col_err) a.col_err[icol] = err;
       atomicMax(a.err_flag, err);
     } else if (a.col_err) {
@@ -826,6 +1025,9 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
 
   const float sd = S.h->misc[band];
   const unsigned bit = 1u << lane;
+  const int cband = BAND ? cloud_band(S.h->iscal[2], band) : 0;
+  const bool maxrand = BAND && a.icld >= 2;
+  float cr = 0.0f, kr = 0.0f, radm = 0.0f;  // rtrnmr's cloudy and clear radiances and overlap term
   float* part = S.part + warp * (nl + 1) * 6;  // this warp's level sums
 
   // ---------------- downward pass (rtrnmc.f90:347-455): total and clear-sky streams
@@ -845,13 +1047,42 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
     rc = fmaf(rc, tr, gsd);
     float A = tr, B = gsd;
     if (clouds && S.L[lay].cldlay) {
-      const bool one = S.L[lay].cbits[warp] & bit;
-      if (one || (!fused && (S.fbits(lay)[warp] & bit))) {
-        float odcld, efcl, atot, x;
-        const float cldf = cell_cloud(a, S, icol, g, lay, band, sd, one, T, odcld, efcl);
+      if constexpr (BAND) {
+        const float* ov = S.ovl(lay);
+        const float cf = ov[0], odcld = S.L[lay].tcl[cband];
+        float atot, x;
         cloud_total(T, c, od, odcld, atot, x);
-        A = 1.0f - fmaf(efcl, 1.0f - c.atrans, c.atrans);
-        B = fmaf(cldf, fmaf(pf * fmaf(x, r.y, r.x), atot, -gsd), gsd);
+        const float bbdtot = pf * fmaf(x, r.y, r.x);
+        if (!maxrand) {  // rtrn.f90:370-432
+          const float efcl = (1.0f - __expf(-odcld)) * cf;
+          A = 1.0f - fmaf(efcl, 1.0f - c.atrans, c.atrans);
+          B = fmaf(cf, fmaf(bbdtot, atot, -gsd), gsd);
+        } else {  // rtrnmr.f90:590-609
+          if (S.L[lay].lfl & 2) {
+            cr = cf * rd;
+            kr = rd - cr;
+            radm = 0.0f;
+          }
+          const float ttot = 1.0f - atot, cldsrc = bbdtot * atot;
+          cr = fmaf(cr, ttot, cf * cldsrc);
+          kr = fmaf(kr, tr, (1.0f - cf) * gsd);
+          A = 0.0f;
+          B = cr + kr;
+          const float radmod = fmaf(radm, fmaf(ov[7], tr, ov[9] * ttot), fmaf(ov[12], cldsrc, -ov[11] * gsd));
+          const float oc = cr - radmod, ok = kr + radmod;
+          radm = fmaf(ov[8], ok, fmaf(-ov[10], oc, -radmod));
+          cr += radm;
+          kr -= radm;
+        }
+      } else {
+        const bool one = S.L[lay].cbits[warp] & bit;
+        if (one || (!fused && (S.fbits(lay)[warp] & bit))) {
+          float odcld, efcl, atot, x;
+          const float cldf = cell_cloud(a, S, icol, g, lay, band, sd, one, T, odcld, efcl);
+          cloud_total(T, c, od, odcld, atot, x);
+          A = 1.0f - fmaf(efcl, 1.0f - c.atrans, c.atrans);
+          B = fmaf(cldf, fmaf(pf * fmaf(x, r.y, r.x), atot, -gsd), gsd);
+        }
       }
     }
     rd = fmaf(rd, A, B);
@@ -901,14 +1132,44 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
     dcu *= tr;
     float A = tr, B = gsu, D = tr;
     if (clouds && S.L[lay].cldlay) {
-      const bool one = S.L[lay].cbits[warp] & bit;
-      if (one || (!fused && (S.fbits(lay)[warp] & bit))) {
-        float odcld, efcl, atot, x;
-        const float cldf = cell_cloud(a, S, icol, g, lay, band, sd, one, T, odcld, efcl);
+      if constexpr (BAND) {
+        const float* ov = S.ovl(lay);
+        const float cf = ov[0], odcld = S.L[lay].tcl[cband];
+        float atot, x;
         cloud_total(T, c, od, odcld, atot, x);
-        A = 1.0f - fmaf(efcl, 1.0f - c.atrans, c.atrans);
-        B = fmaf(cldf, fmaf(pf * fmaf(x, r.z, r.x), atot, -gsu), gsu);
-        D = fmaf(cldf, 1.0f - atot, (1.0f - cldf) * (1.0f - c.atrans));
+        const float bbutot = pf * fmaf(x, r.z, r.x);
+        D = fmaf(cf, 1.0f - atot, (1.0f - cf) * (1.0f - c.atrans));
+        if (!maxrand) {  // rtrn.f90:495-507
+          const float efcl = (1.0f - __expf(-odcld)) * cf;
+          A = 1.0f - fmaf(efcl, 1.0f - c.atrans, c.atrans);
+          B = fmaf(cf, fmaf(bbutot, atot, -gsu), gsu);
+        } else {  // rtrnmr.f90:688-713
+          if (S.L[lay].lfl & 1) {
+            cr = cf * ru;
+            kr = ru - cr;
+            radm = 0.0f;
+          }
+          const float ttot = 1.0f - atot, cldsrc = bbutot * atot;
+          cr = fmaf(cr, ttot, cf * cldsrc);
+          kr = fmaf(kr, tr, (1.0f - cf) * gsu);
+          A = 0.0f;
+          B = cr + kr;
+          const float radmod = fmaf(radm, fmaf(ov[1], tr, ov[3] * ttot), fmaf(ov[6], cldsrc, -ov[5] * gsu));
+          const float oc = cr - radmod, ok = kr + radmod;
+          radm = fmaf(ov[2], ok, fmaf(-ov[4], oc, -radmod));
+          cr += radm;
+          kr -= radm;
+        }
+      } else {
+        const bool one = S.L[lay].cbits[warp] & bit;
+        if (one || (!fused && (S.fbits(lay)[warp] & bit))) {
+          float odcld, efcl, atot, x;
+          const float cldf = cell_cloud(a, S, icol, g, lay, band, sd, one, T, odcld, efcl);
+          cloud_total(T, c, od, odcld, atot, x);
+          A = 1.0f - fmaf(efcl, 1.0f - c.atrans, c.atrans);
+          B = fmaf(cldf, fmaf(pf * fmaf(x, r.z, r.x), atot, -gsu), gsu);
+          D = fmaf(cldf, 1.0f - atot, (1.0f - cldf) * (1.0f - c.atrans));
+        }
       }
     }
     ru = fmaf(ru, A, B);
@@ -1081,7 +1342,31 @@ __global__ void __launch_bounds__(RT_NT, MINB) lw_full_kernel(const __grid_const
   }
 }
 
+// The fused taumol and transfer kernel for the non-McICA driver's band
+// clouds (batch columns [c0, c1), block k in slot k).
+template <int MINB>
+__global__ void __launch_bounds__(RT_NT, MINB) lw_band_kernel(const __grid_constant__ LwBatch B,
+                                                               const float* __restrict__ T, long long c0, long long c1) {
+  extern __shared__ __align__(16) char smem_raw[];
+  const GasSmem gs = gas_carve(smem_raw + ARGS_BYTES, B.nsmax);
+  const RtSmem S = rt_carve(smem_raw + ARGS_BYTES, B.nsmax);
+  float* gt = B.gtau + (long long)blockIdx.x * B.gstride;
+  float* gf = B.gfrac + (long long)blockIdx.x * B.gstride;
+  int gi = 0;
+  for (long long i = c0 + blockIdx.x; i < c1; i += gridDim.x) {
+    gi = grid_of(B, i, gi);
+    const LwArgs& a = stage_args(B.g[gi], smem_raw);
+    const long long icol = i - B.col0[gi];
+    gas_column<RT_NT>(a, icol, gs, gt, gf, T);
+    GasSrc src{};
+    src.gt = gt;
+    src.gf = gf;
+    rt_column<RT_GAS, true>(a, icol, S, src, T);
+  }
+}
+
 constexpr int GAS_NT = 128;      // threads of the taumol kernel
+constexpr int BAND_MINB = 6;
 constexpr int LIST_PER_SM = 2;   // hand-over kernel blocks per SM
 constexpr int LIST_MINB = 6;
 
@@ -1235,7 +1520,25 @@ cudaError_t gb_lw_launch_batch(const LwBatch& b, const float* d_tables, int vari
   for (int i = 0; i < b.ngrid; ++i)  // fused-cloud grids come with their McICA draws
     if (b.g[i].cloud_mode == LW_CLOUD_FUSED && b.g[i].icld >= 1 && b.g[i].ncol > 0 && !b.g[i].draws)
       return cudaErrorInvalidValue;
+  int nband = 0;
+  for (int i = 0; i < b.ngrid; ++i) {
+    const LwArgs& g = b.g[i];
+    if (g.cloud_mode != LW_CLOUD_BAND) continue;
+    ++nband;
+    if (g.icld >= 1 && g.ncol > 0 && (!g.ncbands || !g.cldfrac || !g.tauc)) return cudaErrorInvalidValue;
+  }
   if ((long long)nblocks > n) nblocks = (int)n;
+  if (nband) {
+    // band clouds: every grid in that mode, taumol gas optics
+    if (nband != b.ngrid || b.fall) return cudaErrorInvalidValue;
+    if ((long long)nblocks > b.gslots) nblocks = (int)b.gslots;
+    const void* fn = (const void*)gb::lw_band_kernel<gb::BAND_MINB>;
+    const size_t smem = block_smem(b.nsmax, false);
+    return launch_resident(fn, gb::RT_NT, smem, nblocks, [&](int nb) {
+      gb::lw_band_kernel<gb::BAND_MINB><<<nb, gb::RT_NT, smem, stream>>>(b, d_tables, 0, n);
+      return cudaGetLastError();
+    });
+  }
   if (!b.fall || !b.nfall) {
     // taumol and the transfer, one block per column, taumol's planes in the block's slot
     if ((long long)nblocks > b.gslots) nblocks = (int)b.gslots;

@@ -11,6 +11,10 @@ enum LwCloudMode {
   LW_CLOUD_SUBCOL = 0,  // caller-supplied (140, ld, nlay) arrays cldfmcl/ciwpmcl/clwpmcl/taucmcl
   LW_CLOUD_FUSED = 1,   // generated from layer clouds (icld 3, Mersenne twister,
                         // column c seeded with seed0 + c), as mcica_subcol_lw would for one column
+  LW_CLOUD_BAND = 2,    // the non-McICA driver's band-level clouds (rrtmg_lw_rad.nomcica.f90):
+                        // layer fractions cldfrac (ld, nlay), cldprop's optical depths tauc
+                        // (16, ld, nlay) and its cloud-band count ncbands (ld); icld 1 random
+                        // overlap (rtrn), 2 and 3 maximum/random overlap (rtrnmr)
 };
 
 // Device pointers in the reference's Fortran layout.  (ncol, .) arrays have
@@ -39,6 +43,8 @@ struct LwArgs {
   // fused cloud mode: the columns' 140 McICA draws [ncol][140] (gb_mcica_percol_mt);
   // required when cloud_mode is LW_CLOUD_FUSED and icld >= 1
   const double* draws;
+  // band cloud mode: cldprop's cloud-band count per column (1, 5 or 16)
+  const int* ncbands;
 };
 
 // Grids of one launch: grid i owns batch columns col0[i] .. col0[i+1]-1.  The
@@ -94,7 +100,8 @@ cudaError_t gb_lw_set_tables(const GbTables& T);
 // All grids of `b` with `variant` at `nblocks` persistent blocks: taumol
 // batches through the fused taumol + transfer kernel (block k in slot k);
 // with b.fall set the learned-gas-optics transfer kernel, then the hand-over
-// kernel.
+// kernel.  Batches of LW_CLOUD_BAND grids (all grids in that mode, taumol
+// only) run the band-cloud flavour of the fused kernel.
 cudaError_t gb_lw_launch_batch(const LwBatch& b, const float* d_tables, int variant, int nblocks,
                                cudaStream_t stream);
 // The taumol kernel alone over batch columns [c0, c1) into slots 0 .. c1-c0-1.

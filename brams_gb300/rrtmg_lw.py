@@ -28,6 +28,7 @@ DATA_DIR = os.path.join(HERE, "data")
 STATE_ORDER = ["play", "plev", "tlay", "tlev", "tsfc", "h2ovmr", "o3vmr", "co2vmr", "ch4vmr",
                "n2ovmr", "o2vmr", "cfc11vmr", "cfc12vmr", "cfc22vmr", "ccl4vmr", "emis"]
 CLOUD_ORDER = ["cldfmcl", "taucmcl", "ciwpmcl", "clwpmcl", "reicmcl", "relqmcl"]
+BAND_ORDER = ["cldfrac", "tauc_band", "ciwp", "clwp", "rei", "rel"]  # non-McICA clouds (device keys)
 OUT_ORDER = ["uflx", "dflx", "hr", "uflxc", "dflxc", "hrc", "duflx_dt", "duflxc_dt"]
 
 # C prototypes (see include/gb_rrtmg_lw.h)
@@ -44,7 +45,7 @@ EXPORTS = [
     "gb_rrtmg_lw_batch_surrogate", "gb_lw_mlp_set_engine", "gb_rrtmg_lw_autotune_report",
     "gb_cldprop_lw_device", "gb_rtm_pack_lw_device", "gb_rtm_unpack_lw_device",
     "gb_rtm_ozone_load", "gb_rtm_ozone_free", "gb_rtm_ozone_lw",
-    "gb_rrtmg_lw_shard_plan", "gb_rrtmg_lw_grid_slice",
+    "gb_rrtmg_lw_shard_plan", "gb_rrtmg_lw_grid_slice", "gb_rrtmg_lw_nomcica", "gb_rrtmg_lw_nomcica_device",
 ]
 MLP_MMA_SYNC, MLP_TCGEN05 = 0, 1
 MLP_NPARAM = 72352
@@ -125,6 +126,9 @@ def load_library(path: str = LIB_PATH):
         L.gb_rrtmg_lw.argtypes = [P, I, I, IP, I] + [P] * 16 + [I, I, I] + [P] * 7 + [P] * 8 + [LL, LL]
         L.gb_rrtmg_lw_device.argtypes = [P, P, I, I, IP, I] + [P] * 16 + [I, I, I] + [P] * 7 + [P] * 8 + [LL, LL, P]
         L.gb_rrtmg_lw_sync_status.argtypes = [P, P]
+        L.gb_rrtmg_lw_nomcica.argtypes = [P, I, I, IP, I] + [P] * 16 + [I, I, I] + [P] * 7 + [P] * 8 + [LL, LL]
+        L.gb_rrtmg_lw_nomcica_device.argtypes = [P, P, I, I, IP, I] + [P] * 16 + [I, I, I] + [P] * 7 + [P] * 8 + \
+            [LL, LL, P]
         L.gb_mcica_subcol_lw.argtypes = [P, I, I, I, I, IP] + [P] * 8 + [P] * 6 + [LL, I]
         L.gb_mcica_subcol_lw_device.argtypes = [P, P, I, I, I, I, IP] + [P] * 8 + [P] * 6 + [LL, I]
         L.gb_rrtmg_lw_gas_optics_diag.argtypes = [P, I, I] + [P] * 17 + [P, P]
@@ -251,6 +255,42 @@ class Context:
         args += [inflglw, iceflglw, liqflglw] + [_ptr(ptrs.get(k)) for k in CLOUD_ORDER] + [_ptr(ptrs["tauaer"])]
         args += [_ptr(ptrs.get(k)) for k in OUT_ORDER] + [ld_in or ncol, ld_out or ncol, _ptr(col_status)]
         _check(self.L, self.h, self.L.gb_rrtmg_lw_device(*args))
+
+    # ------------------------------------------------------------ non-McICA rrtmg_lw
+    def rrtmg_lw_nomcica(self, state: dict, icld: int = 2, idrv: int = 1, inflglw: int = 2, iceflglw: int = 3,
+                         liqflglw: int = 1, out: dict | None = None) -> dict:
+        """rrtmg_lw of the non-McICA driver on host arrays: band-level clouds
+        state['cldfrac'], 'ciwp', 'clwp', 'rei', 'rel' (ncol, nlay) and
+        optional 'tauc_band' (16, ncol, nlay).  icld 1: random overlap;
+        0, 2, 3: maximum/random (0 without clouds)."""
+        ncol, nlay = state["play"].shape
+        st = [_f64(state[k]) for k in STATE_ORDER]
+        tauaer = _f64(state.get("tauaer", np.zeros((ncol, nlay, 16))))
+        tb = state.get("tauc_band")
+        cl = [_f64(state["cldfrac"]), _f64(np.zeros((16, ncol, nlay)) if tb is None else tb)]
+        cl += [_f64(state[k]) for k in ("ciwp", "clwp", "rei", "rel")]
+        if out is None:
+            out = {k: np.zeros((ncol, nlay + 1), order="F") for k in ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt")}
+            out["hr"] = np.zeros((ncol, nlay), order="F")
+            out["hrc"] = np.zeros((ncol, nlay), order="F")
+        ic = C.c_int(icld)
+        args = [self.h, ncol, nlay, C.byref(ic), idrv] + [_ptr(a) for a in st] + [inflglw, iceflglw, liqflglw]
+        args += [_ptr(a) for a in cl] + [_ptr(tauaer)] + [_ptr(out[k]) for k in OUT_ORDER] + [ncol, ncol]
+        _check(self.L, self.h, self.L.gb_rrtmg_lw_nomcica(*args))
+        out["icld"] = ic.value
+        return out
+
+    def rrtmg_lw_nomcica_device(self, ncol: int, nlay: int, ptrs: dict, stream=None, icld: int = 2, idrv: int = 1,
+                                inflglw: int = 2, iceflglw: int = 3, liqflglw: int = 1,
+                                ld_in: int | None = None, ld_out: int | None = None, col_status=None) -> int:
+        """The non-McICA driver on device pointers/tensors (Fortran layout)
+        keyed as rrtmg_lw_nomcica's state; returns icld after the clamp."""
+        ic = C.c_int(icld)
+        args = [self.h, _ptr(stream or 0), ncol, nlay, C.byref(ic), idrv] + [_ptr(ptrs[k]) for k in STATE_ORDER]
+        args += [inflglw, iceflglw, liqflglw] + [_ptr(ptrs.get(k)) for k in BAND_ORDER] + [_ptr(ptrs["tauaer"])]
+        args += [_ptr(ptrs.get(k)) for k in OUT_ORDER] + [ld_in or ncol, ld_out or ncol, _ptr(col_status)]
+        _check(self.L, self.h, self.L.gb_rrtmg_lw_nomcica_device(*args))
+        return ic.value
 
     def sync_status(self, stream=None) -> int:
         return self.L.gb_rrtmg_lw_sync_status(self.h, _ptr(stream or 0))

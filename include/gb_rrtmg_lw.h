@@ -100,6 +100,42 @@ int gb_rrtmg_lw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int
                        double* uflxc, double* dflxc, double* hrc, double* duflx_dt,
                        double* duflxc_dt, int64_t ld_in, int64_t ld_out, int* d_col_status);
 
+/* Replaces rrtmg_lw of the non-McICA build (rrtmg_lw_rad.nomcica.f90:99-108)
+ * for HOST arrays: the state arguments of gb_rrtmg_lw, then band-level
+ * clouds as that driver takes them: cldfr cicewp cliqwp reice reliq (ld,
+ * nlay) and taucld (16, ld, nlay; read for inflglw 0, summed by cldprop's
+ * cloud test otherwise).  Per column it runs cldprop
+ * (rrtmg_lw_cldprop.f90:50-295), setcoef, taumol and the transfer with the
+ * driver's overlap choice (:546-560): icld 1 random overlap (rtrn,
+ * rrtmg_lw_rtrn.f90), 2 and 3 maximum/random overlap (rtrnmr,
+ * rrtmg_lw_rtrnmr.f90), 0 clear sky; values outside 0..3 become 2 (:456).
+ * The cloud arrays may be NULL when icld == 0. */
+int gb_rrtmg_lw_nomcica(gb_lw_context* ctx, int ncol, int nlay, int* icld, int idrv,
+                        const double* play, const double* plev, const double* tlay, const double* tlev,
+                        const double* tsfc, const double* h2ovmr, const double* o3vmr, const double* co2vmr,
+                        const double* ch4vmr, const double* n2ovmr, const double* o2vmr,
+                        const double* cfc11vmr, const double* cfc12vmr, const double* cfc22vmr,
+                        const double* ccl4vmr, const double* emis, int inflglw, int iceflglw, int liqflglw,
+                        const double* cldfr, const double* taucld, const double* cicewp, const double* cliqwp,
+                        const double* reice, const double* reliq, const double* tauaer, double* uflx,
+                        double* dflx, double* hr, double* uflxc, double* dflxc, double* hrc,
+                        double* duflx_dt, double* duflxc_dt, int64_t ld_in, int64_t ld_out);
+
+/* Same on DEVICE arrays on `stream`, with the status handling of
+ * gb_rrtmg_lw_device (cldprop's radius stops included in d_col_status). */
+int gb_rrtmg_lw_nomcica_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int* icld, int idrv,
+                               const double* play, const double* plev, const double* tlay,
+                               const double* tlev, const double* tsfc, const double* h2ovmr,
+                               const double* o3vmr, const double* co2vmr, const double* ch4vmr,
+                               const double* n2ovmr, const double* o2vmr, const double* cfc11vmr,
+                               const double* cfc12vmr, const double* cfc22vmr, const double* ccl4vmr,
+                               const double* emis, int inflglw, int iceflglw, int liqflglw,
+                               const double* cldfr, const double* taucld, const double* cicewp,
+                               const double* cliqwp, const double* reice, const double* reliq,
+                               const double* tauaer, double* uflx, double* dflx, double* hr,
+                               double* uflxc, double* dflxc, double* hrc, double* duflx_dt,
+                               double* duflxc_dt, int64_t ld_in, int64_t ld_out, int* d_col_status);
+
 /* Waits for `stream` and returns (then clears) the maximum column status of
  * the device calls made since the previous call. */
 int gb_rrtmg_lw_sync_status(gb_lw_context* ctx, void* stream);

@@ -1414,6 +1414,10 @@ void rtrnmc(Col& c, int idrv) {
 // automatic arrays leave those entries undefined.  They are taken as 0 here
 // (zeroed arrays), the value the rest of the algorithm expects at the first
 // cloudy layer of a block (rad is 0 there, so only faccmb enters radmod).
+// faccmb1/2 at the top (:434-438 with lev = nlayers) read cldfrac(nlayers+1),
+// which the driver zeroes (nomcica.f90 inatm); faccmb1d/2d at the bottom
+// (:507-512 with lev = 1) read cldfrac(0), outside the array: 0 is taken
+// there too (no cloud below the surface).
 void rtrnmr(Col& c, int idrv) {
   const int nlayers = c.nlayers;
   const double wtdiff = 0.5, rec_6 = 0.166667;
