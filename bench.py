@@ -32,6 +32,8 @@ transfer with FP64 heating rates.  One step solves every column once by:
   eval         -- the learned gas optics on 512x512x45 columns: columns/s
                   and heating-rate RMSE against the FP64 oracle, beside the
                   plain path
+  nomcica      -- the non-McICA driver (cldprop, taumol, random or
+                  maximum/random overlap) on 360x300x45 device arrays
   plain_abi    -- the drop-in path on the 360x300x45 BRAMS-scale workload:
                   gb_rrtmg_lw_device on the reference's (140, ncol, nlay)
                   McICA arrays, its roofline against 8*(600*nlay + 25) bytes
@@ -527,6 +529,8 @@ def gpu_arm(args, rank, world):
     batched = None if args.no_batched else batched_block(ctx, dev, stream, args, hbm)
     log("network evaluation at 512x512x45")
     ev = None if args.no_batched else eval_block(ctx, mlp, dev, stream, args)
+    log("non-McICA driver at 360x300x45")
+    nomc = None if args.no_batched else nomcica_block(ctx, dev, stream, args)
 
     # ---------------- drop-in block (ABI mode, 360x300x45)
     log("drop-in block")
@@ -584,6 +588,8 @@ def gpu_arm(args, rank, world):
         line["batched"] = batched
     if ev is not None:
         line["eval"] = ev
+    if nomc is not None:
+        line["nomcica"] = nomc
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_headline(wl)
         line["cpu_configs"] = cpu_configs()
@@ -918,6 +924,53 @@ def eval_block(ctx, mlp, dev, stream, args):
     return res
 
 
+def nomcica_block(ctx, dev, stream, args):
+    """The non-McICA driver (gb_rrtmg_lw_nomcica_device: cldprop, taumol and
+    the transfer with random or maximum/random overlap) on 360x300x45
+    device arrays, and its error against the FP64 oracle on 512 columns."""
+    import torch
+
+    from brams_gb300 import rrtmg_lw as R
+    from brams_gb300.profiles import make_state, workload_spec
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    st = make_state(workload_spec("drop_in_360x300x45"))
+    ncol, nlay = st["play"].shape
+
+    def dv(a):
+        return torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=np.float64).T)).to(dev)
+
+    d = {k: dv(st[k]) for k in R.STATE_ORDER + ["tauaer", "cldfrac", "ciwp", "clwp", "rei", "rel"]}
+    d["tauc_band"] = torch.zeros((nlay, ncol, 16), dtype=torch.float64, device=dev)
+    for k in ("uflx", "dflx", "uflxc", "dflxc", "duflx_dt", "duflxc_dt"):
+        d[k] = torch.zeros((nlay + 1, ncol), dtype=torch.float64, device=dev)
+    d["hr"] = torch.zeros((nlay, ncol), dtype=torch.float64, device=dev)
+    d["hrc"] = torch.zeros((nlay, ncol), dtype=torch.float64, device=dev)
+    res = {"workload": "rrtmg_lw of the non-McICA driver, 360x300 columns x 45 layers on device arrays "
+                       "(cldprop + taumol + transfer per call); errors against the FP64 oracle on 512 columns"}
+    n = 512
+    sub = {k: np.asfortranarray(v[:n]) for k, v in st.items()}
+    for icld, name in ((1, "random_overlap"), (2, "max_random_overlap")):
+        call = lambda: ctx.rrtmg_lw_nomcica_device(ncol, nlay, d, stream=stream, icld=icld)  # noqa: E731
+        for _ in range(args.warmup):
+            call()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            call()
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3 / args.steps
+        got = {k: d[k].cpu().numpy().T for k in ("uflx", "dflx", "hr")}
+        ref = pyoracle.rrtmg_lw_nomcica(sub, icld, native=True)
+        res[name] = {"value": ncol / t, "unit": "columns/s", "ms_per_step": t * 1e3, **_errors(got, ref, n)}
+    res["column_status"] = ctx.sync_status(stream)
+    return res
+
+
 def cpu_configs(seconds: float = 5.0) -> dict:
     """The FP64 oracle on all host cores: the 64x64x38 configuration in full
     and a sample of the 360x300x45 one (McICA sub-columns made beforehand)."""
@@ -1028,7 +1081,8 @@ def main():
     ap.add_argument("--no-abi", action="store_true", help="skip the 360x300x45 drop-in block")
     ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's")
     ap.add_argument("--abi-ncol", type=int, default=NCOL, help="columns of the drop-in block")
-    ap.add_argument("--no-batched", action="store_true", help="skip the nested-grid and 512x512x45 blocks")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the nested-grid, 512x512x45 and non-McICA blocks")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
