@@ -1064,7 +1064,7 @@ def abi_block(ctx, dev, stream, args, rank, world, hbm):
                         + ("360x300 columns x 45 layers" if ncol == NCOL else f"{ncol} columns x 45 layers"),
             "value": world * ncol / t_dev, "unit": "columns/s", "ms_per_step": t_dev * 1e3,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": traffic_from_profiles("lw_batch_kernel_drop_in_traffic.txt"), "alg_bytes_per_launch": alg},
+                         "traffic": traffic_from_profiles("lw_full_kernel_drop_in_traffic.txt"), "alg_bytes_per_launch": alg},
             "e2e": {"value": world * ncol / t_e2e, "unit": "columns/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "host_path_matches_device_path": same},
             "column_status": status}
