@@ -16,14 +16,15 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libgb_rrtmg_lw.so")
 UNITS = ["lw_solver.cu", "lw_mcica.cu", "lw_capi.cu", "lw_tables.cpp", "lw_mlp.cu", "lw_mlp_capi.cu", "lw_mlp_tc.cu",
-         "lw_cldprop.cu", "lw_pack.cu", "lw_ozone.cpp", "lw_shard.cpp"]
+         "lw_cldprop.cu", "lw_pack.cu", "lw_ozone.cpp", "lw_shard.cpp",
+         "sw_solver.cu", "sw_capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # The column kernel is compiled without multiply-add contraction: every fused
 # multiply-add in it is an explicit fmaf, so that its results are fixed by the
 # source and every launch shape and kernel flavour (full, learned-only,
 # hand-over list) gives the same bits for a column.  cldprop likewise, so
 # that its fp64 results follow the reference's operations one by one.
-UNIT_FLAGS = {"lw_solver.cu": ["-fmad=false"], "lw_cldprop.cu": ["-fmad=false"], "lw_pack.cu": ["-fmad=false"],
+UNIT_FLAGS = {"lw_solver.cu": ["-fmad=false"], "sw_solver.cu": ["-fmad=false"], "lw_cldprop.cu": ["-fmad=false"], "lw_pack.cu": ["-fmad=false"],
               "lw_ozone.cpp": ["-Xcompiler", "-ffp-contract=off"]}
 
 

@@ -395,6 +395,7 @@ int gb_rrtmg_lw_ini(double cpdair, const char* table_dir, int device, gb_lw_cont
     return r;
   }
   std::string dir = table_dir ? table_dir : default_table_dir();
+  ctx->table_dir = dir;
   std::string ref = dir + "/lw_ref_tables.gblw", kt = dir + "/lw_ktables.gblw";
   std::vector<float> blob;
   std::vector<double> cloud64;
@@ -452,6 +453,8 @@ int gb_rrtmg_lw_free(gb_lw_context* ctx) {
   cudaFree(ctx->d_cloud64);
   cudaFree(ctx->d_band);
   cudaFree(ctx->d_ncb);
+  cudaFree(ctx->d_sw_tables);
+  cudaFree(ctx->d_sw_scratch);
   delete ctx;
   return GB_LW_OK;
 }

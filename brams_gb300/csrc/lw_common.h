@@ -73,4 +73,6 @@ enum GbColError {
   GB_COL_LAYTROP = 9,     // lower-atmosphere layers not a prefix of the column
   GB_COL_BADVAL = 11,     // non-finite or non-positive pressure / temperature
   GB_COL_TCWAIT = 12,     // learned gas optics: a tensor-core wait ran out (kernel stopped early)
+  GB_COL_SW_OPTICS = 13,  // cldprmc_sw: cloud extinction, albedo, asymmetry or fdelta out of range
+  GB_COL_SW_UNSUPPORTED = 14,  // cldprmc_sw: ice option 0 or liquid option 0 with a nonzero path
 };

@@ -57,6 +57,14 @@ struct gb_lw_context {
   size_t band_elems = 0;
   int* d_ncb = nullptr;
   size_t ncb_elems = 0;
+  // RRTMG_SW: tables (fp64 blob, loaded by gb_rrtmg_sw_ini) and the column
+  // kernel's scratch slots (grown on demand)
+  std::string table_dir;
+  double* d_sw_tables = nullptr;
+  bool sw_ready = false;
+  double sw_scon = 0.0;  // rrsw_scon of the tables (parrrsw.f90)
+  double* d_sw_scratch = nullptr;
+  size_t sw_scratch_doubles = 0;
 };
 
 // records a CUDA error on the context; returns GB_LW_E_CUDA

@@ -15,17 +15,10 @@
 #include <vector>
 
 namespace {
+using Entry = GbTableEntry;
+}  // namespace
 
-struct Entry {
-  std::vector<double> d;
-  std::vector<int> i;
-  int dims[4] = {1, 1, 1, 1};
-  int ndim = 0;
-  bool is_int = false;
-  size_t size() const { return is_int ? i.size() : d.size(); }
-};
-
-bool read_container(const char* path, std::map<std::string, Entry>& out, std::string& err) {
+bool gb_read_container(const char* path, std::map<std::string, Entry>& out, std::string& err) {
   FILE* f = std::fopen(path, "rb");
   if (!f) {
     err = std::string("cannot open table file ") + path;
@@ -60,11 +53,9 @@ bool read_container(const char* path, std::map<std::string, Entry>& out, std::st
   return ok;
 }
 
-}  // namespace
-
 bool gb_read_table_f64(const char* path, const char* name, std::vector<double>& out, std::string& err) {
   std::map<std::string, Entry> tab;
-  if (!read_container(path, tab, err)) return false;
+  if (!gb_read_container(path, tab, err)) return false;
   auto it = tab.find(name);
   if (it == tab.end() || it->second.is_int) {
     err = std::string("table file ") + path + " has no float64 array " + name;
@@ -77,7 +68,7 @@ bool gb_read_table_f64(const char* path, const char* name, std::vector<double>& 
 bool gb_build_tables(const char* ref_path, const char* k_path, double cpdair, GbTables& T,
                      std::vector<float>& blob, std::string& err, std::vector<double>* cloud64) {
   std::map<std::string, Entry> tab;
-  if (!read_container(ref_path, tab, err) || !read_container(k_path, tab, err)) return false;
+  if (!gb_read_container(ref_path, tab, err) || !gb_read_container(k_path, tab, err)) return false;
   auto need = [&](const std::string& n) -> const Entry* {
     auto it = tab.find(n);
     if (it == tab.end()) {

@@ -29,6 +29,10 @@ STATE_ORDER = ["play", "plev", "tlay", "tlev", "tsfc", "h2ovmr", "o3vmr", "co2vm
                "n2ovmr", "o2vmr", "cfc11vmr", "cfc12vmr", "cfc22vmr", "ccl4vmr", "emis"]
 CLOUD_ORDER = ["cldfmcl", "taucmcl", "ciwpmcl", "clwpmcl", "reicmcl", "relqmcl"]
 BAND_ORDER = ["cldfrac", "tauc_band", "ciwp", "clwp", "rei", "rel"]  # non-McICA clouds (device keys)
+SW_STATE = ["play", "plev", "tlay", "tlev", "tsfc", "h2ovmr", "o3vmr", "co2vmr", "ch4vmr", "n2ovmr", "o2vmr",
+            "asdir", "asdif", "aldir", "aldif", "coszen"]
+SW_CLOUD = ["cldfmcl", "taucmcl", "ssacmcl", "asmcmcl", "fsfcmcl", "ciwpmcl", "clwpmcl", "reicmcl", "relqmcl"]
+SW_OUT = ["swuflx", "swdflx", "swhr", "swuflxc", "swdflxc", "swhrc"]
 OUT_ORDER = ["uflx", "dflx", "hr", "uflxc", "dflxc", "hrc", "duflx_dt", "duflxc_dt"]
 
 # C prototypes (see include/gb_rrtmg_lw.h)
@@ -46,6 +50,7 @@ EXPORTS = [
     "gb_cldprop_lw_device", "gb_rtm_pack_lw_device", "gb_rtm_unpack_lw_device",
     "gb_rtm_ozone_load", "gb_rtm_ozone_free", "gb_rtm_ozone_lw",
     "gb_rrtmg_lw_shard_plan", "gb_rrtmg_lw_grid_slice", "gb_rrtmg_lw_nomcica", "gb_rrtmg_lw_nomcica_device",
+    "gb_rrtmg_sw_ini", "gb_rrtmg_sw", "gb_rrtmg_sw_device",
 ]
 MLP_MMA_SYNC, MLP_TCGEN05 = 0, 1
 MLP_NPARAM = 72352
@@ -148,6 +153,10 @@ def load_library(path: str = LIB_PATH):
         L.gb_rrtmg_lw_graph_destroy.argtypes = [P]
         L.gb_rrtmg_lw_tuning_set.argtypes = [P, I, I, C.POINTER(Tuning)]
         L.gb_rrtmg_lw_num_variants.argtypes = []
+        SWA = [P] * 16 + [D, I, D, I, I, I, I] + [P] * 9 + [P] * 4 + [P] * 6
+        L.gb_rrtmg_sw_ini.argtypes = [P, D, C.c_char_p]
+        L.gb_rrtmg_sw.argtypes = [P, I, I, IP, IP] + SWA + [LL, LL]
+        L.gb_rrtmg_sw_device.argtypes = [P, P, I, I, IP, IP] + SWA + [LL, LL, P]
         L.gb_rrtmg_lw_shard_plan.argtypes = [I, IP, IP, I, I, C.POINTER(LL), C.POINTER(LL)]
         L.gb_rrtmg_lw_grid_slice.argtypes = [GP, LL, LL, GP]
         U64, F = C.c_uint64, C.c_float
@@ -291,6 +300,31 @@ class Context:
         args += [_ptr(ptrs.get(k)) for k in OUT_ORDER] + [ld_in or ncol, ld_out or ncol, _ptr(col_status)]
         _check(self.L, self.h, self.L.gb_rrtmg_lw_nomcica_device(*args))
         return ic.value
+
+    # ------------------------------------------------------------ RRTMG_SW
+    def sw_ini(self, cpdair: float = 1004.0, table_dir: str | None = None) -> None:
+        """gb_rrtmg_sw_ini: the shortwave tables into this context."""
+        _check(self.L, self.h, self.L.gb_rrtmg_sw_ini(self.h, cpdair, table_dir.encode() if table_dir else None))
+
+    def rrtmg_sw(self, state: dict, mc: dict | None, icld: int = 3, iaer: int = 10, adjes: float = 1.0,
+                 dyofyr: int = 0, scon: float = 1368.22, isolvar: int = -1, inflgsw: int = 2, iceflgsw: int = 3,
+                 liqflgsw: int = 1) -> dict:
+        """rrtmg_sw on host arrays (keys as oracle/pyoracle.py rrtmg_sw);
+        returns swuflx, swdflx, swhr, swuflxc, swdflxc, swhrc, icld, iaer."""
+        ncol, nlay = state["play"].shape
+        st = [_f64(state[k]) for k in SW_STATE]
+        cl = [_f64(mc[k]) if mc is not None else None for k in SW_CLOUD]
+        aer = [_f64(state[k]) if k in state else None for k in ("tauaer_sw", "ssaaer_sw", "asmaer_sw")]
+        out = {k: np.zeros((ncol, nlay + 1), order="F") for k in ("swuflx", "swdflx", "swuflxc", "swdflxc")}
+        out["swhr"] = np.zeros((ncol, nlay), order="F")
+        out["swhrc"] = np.zeros((ncol, nlay), order="F")
+        ic, ia = C.c_int(icld), C.c_int(iaer)
+        args = [self.h, ncol, nlay, C.byref(ic), C.byref(ia)] + [_ptr(a) for a in st]
+        args += [adjes, dyofyr, scon, isolvar, inflgsw, iceflgsw, liqflgsw] + [_ptr(a) for a in cl]
+        args += [_ptr(a) for a in aer] + [None] + [_ptr(out[k]) for k in SW_OUT] + [ncol, ncol]
+        _check(self.L, self.h, self.L.gb_rrtmg_sw(*args))
+        out["icld"], out["iaer"] = ic.value, ia.value
+        return out
 
     def sync_status(self, stream=None) -> int:
         return self.L.gb_rrtmg_lw_sync_status(self.h, _ptr(stream or 0))

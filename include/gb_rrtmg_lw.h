@@ -40,6 +40,8 @@ typedef struct gb_lw_context gb_lw_context;
 #define GB_LW_E_LAYTROP 9      /* pressure does not decrease with layer index            */
 #define GB_LW_E_BADVAL 11      /* non-positive or non-finite layer pressure/temperature  */
 #define GB_LW_E_TCWAIT 12      /* learned gas optics: a tensor-core wait ran out          */
+#define GB_LW_E_SW_OPTICS 13   /* cldprmc_sw: cloud optics out of range (the reference's other STOPs) */
+#define GB_LW_E_SW_UNSUPPORTED 14 /* option the SW path does not implement (see gb_rrtmg_sw)  */
 #define GB_LW_E_ARGS (-1)      /* invalid sizes, flags or null pointers                  */
 #define GB_LW_E_CUDA (-2)      /* CUDA runtime error (see gb_rrtmg_lw_last_error)        */
 #define GB_LW_E_TABLES (-3)    /* table files missing or malformed                       */
@@ -361,6 +363,50 @@ int gb_rrtmg_lw_batch_graph_create(gb_lw_context* ctx, int ngrid, const gb_lw_gr
                                    gb_lw_graph** graph);
 int gb_rrtmg_lw_graph_launch(gb_lw_graph* graph, void* stream);
 int gb_rrtmg_lw_graph_destroy(gb_lw_graph* graph);
+
+/* ---------------------------------------------------------------------------
+ * RRTMG_SW, the shortwave scheme BRAMS calls right after the longwave one
+ * (rtm_driver.f90:1386).  gb_rrtmg_sw_ini replaces rrtmg_sw_ini
+ * (rrtmg_sw_init.f90:47): it loads sw_tables.gbsw (the reference's
+ * k-distribution data reduced to 112 g-points) of table_dir (NULL: the
+ * context's table directory) into the context.  gb_rrtmg_sw replaces
+ * rrtmg_sw (rrtmg_sw_rad.f90:243-255) with its argument order: layer arrays
+ * (ld, nlay), plev/tlev (ld, nlay+1), tsfc and the albedos and coszen (ncol),
+ * McICA arrays cldfmcl taucmcl ssacmcl asmcmcl fsfcmcl ciwpmcl clwpmcl
+ * (112, ld, nlay) and reicmcl relqmcl (ld, nlay), aerosols tauaer ssaaer
+ * asmaer (ld, nlay, 14); outputs swuflx swdflx swuflxc swdflxc (ld_out,
+ * nlay+1), swhr swhrc (ld_out, nlay).  icld and iaer are in/out as in the
+ * reference.  The solar-variability option isolvar must be negative (BRAMS
+ * passes -1) and iaer 0 or 10 (ecaer, for iaer 6, is not read); cloud
+ * options inflag 0 or 2 with iceflag 1-3 and liqflag 1 (the reference
+ * leaves the coefficients of ice option 0 and liquid option 0 unset).  The
+ * whole path is fp64.  tlev, tsfc and n2ovmr are not used by the reference's
+ * shortwave computation and may be NULL. */
+int gb_rrtmg_sw_ini(gb_lw_context* ctx, double cpdair, const char* table_dir);
+int gb_rrtmg_sw(gb_lw_context* ctx, int ncol, int nlay, int* icld, int* iaer, const double* play,
+                const double* plev, const double* tlay, const double* tlev, const double* tsfc,
+                const double* h2ovmr, const double* o3vmr, const double* co2vmr, const double* ch4vmr,
+                const double* n2ovmr, const double* o2vmr, const double* asdir, const double* asdif,
+                const double* aldir, const double* aldif, const double* coszen, double adjes, int dyofyr,
+                double scon, int isolvar, int inflgsw, int iceflgsw, int liqflgsw, const double* cldfmcl,
+                const double* taucmcl, const double* ssacmcl, const double* asmcmcl, const double* fsfcmcl,
+                const double* ciwpmcl, const double* clwpmcl, const double* reicmcl, const double* relqmcl,
+                const double* tauaer, const double* ssaaer, const double* asmaer, const double* ecaer,
+                double* swuflx, double* swdflx, double* swhr, double* swuflxc, double* swdflxc, double* swhrc,
+                int64_t ld_in, int64_t ld_out);
+/* Same on DEVICE arrays on `stream`, with the status handling of
+ * gb_rrtmg_lw_device. */
+int gb_rrtmg_sw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int* icld, int* iaer,
+                       const double* play, const double* plev, const double* tlay, const double* tlev,
+                       const double* tsfc, const double* h2ovmr, const double* o3vmr, const double* co2vmr,
+                       const double* ch4vmr, const double* n2ovmr, const double* o2vmr, const double* asdir,
+                       const double* asdif, const double* aldir, const double* aldif, const double* coszen,
+                       double adjes, int dyofyr, double scon, int isolvar, int inflgsw, int iceflgsw, int liqflgsw,
+                       const double* cldfmcl, const double* taucmcl, const double* ssacmcl, const double* asmcmcl,
+                       const double* fsfcmcl, const double* ciwpmcl, const double* clwpmcl, const double* reicmcl,
+                       const double* relqmcl, const double* tauaer, const double* ssaaer, const double* asmaer,
+                       const double* ecaer, double* swuflx, double* swdflx, double* swhr, double* swuflxc,
+                       double* swdflxc, double* swhrc, int64_t ld_in, int64_t ld_out, int* d_col_status);
 
 /* ---------------------------------------------------------------------------
  * Multi-GPU column shards (host only; no device call).  BRAMS gives each MPI

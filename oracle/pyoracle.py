@@ -254,3 +254,59 @@ def flops_per_column(state: dict, mc: dict, icld: int = 3, idrv: int = 1) -> dic
     res["total"] = L.ora_flops(-1) / ncol
     res["outputs"] = out
     return res
+
+
+# ---------------------------------------------------------------- RRTMG_SW
+SW_STATE = ["play", "plev", "tlay", "tlev", "tsfc", "h2ovmr", "o3vmr", "co2vmr", "ch4vmr", "n2ovmr", "o2vmr",
+            "asdir", "asdif", "aldir", "aldif", "coszen"]
+SW_CLOUD = ["cldfmcl", "taucmcl", "ssacmcl", "asmcmcl", "fsfcmcl", "ciwpmcl", "clwpmcl", "reicmcl", "relqmcl"]
+SW_OUT = ["swuflx", "swdflx", "swhr", "swuflxc", "swdflxc", "swhrc"]
+
+
+def sw_lib(native: bool = False):
+    """The SW oracle (sw_oracle.cpp), built on first use and initialised with cpdair 1004."""
+    key = "sw_native" if native else "sw"
+    if key in _lib:
+        return _lib[key]
+    path = os.path.join(HERE, "_build", "libsworacle_native.so" if native else "libsworacle.so")
+    src = os.path.join(HERE, "sw_oracle.cpp")
+    if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", HERE, os.path.join("_build", os.path.basename(path))], check=True)
+    L = C.CDLL(path)
+    L.ora_sw_init.restype = C.c_int
+    L.ora_sw_init.argtypes = [C.c_double, C.c_char_p]
+    if L.ora_sw_init(1004.0, os.path.join(DATA, "sw_tables.gbsw").encode()) != 0:
+        raise RuntimeError("SW oracle init failed")
+    _lib[key] = L
+    return L
+
+
+def rrtmg_sw(state: dict, mc: dict | None, icld: int = 3, iaer: int = 10, adjes: float = 1.0, dyofyr: int = 0,
+             scon: float = 1368.22, isolvar: int = -1, inflgsw: int = 2, iceflgsw: int = 3, liqflgsw: int = 1,
+             nthreads: int = 1, native: bool = False) -> dict:
+    """rrtmg_sw (rrtmg_sw_rad.f90:243) on Fortran-ordered arrays: state keys
+    SW_STATE ((ncol, nlay), (ncol, nlay+1), (ncol,)), aerosols 'tauaer_sw',
+    'ssaaer_sw', 'asmaer_sw' (ncol, nlay, 14), McICA arrays SW_CLOUD ((112,
+    ncol, nlay); reicmcl/relqmcl (ncol, nlay)).  Returns the outputs, icld,
+    iaer."""
+    L = sw_lib(native)
+    ncol, nlay = state["play"].shape
+    st = [_f(state[k]) for k in SW_STATE]
+    z3 = np.zeros((112, ncol, nlay), order="F")
+    z2 = np.zeros((ncol, nlay), order="F")
+    cl = [_f(mc[k]) if mc is not None else (z2 if k in ("reicmcl", "relqmcl") else z3) for k in SW_CLOUD]
+    aer = [_f(state.get(k, np.zeros((ncol, nlay, 14)) if k != "ssaaer_sw" else np.ones((ncol, nlay, 14))))
+           for k in ("tauaer_sw", "ssaaer_sw", "asmaer_sw")]
+    out = {k: np.zeros((ncol, nlay + 1), order="F") for k in ("swuflx", "swdflx", "swuflxc", "swdflxc")}
+    out["swhr"] = np.zeros((ncol, nlay), order="F")
+    out["swhrc"] = np.zeros((ncol, nlay), order="F")
+    ic, ia = C.c_int(icld), C.c_int(iaer)
+    args = [C.c_int(ncol), C.c_int(nlay), C.byref(ic), C.byref(ia)] + [_p(a) for a in st]
+    args += [C.c_double(adjes), C.c_int(dyofyr), C.c_double(scon), C.c_int(isolvar), C.c_int(inflgsw),
+             C.c_int(iceflgsw), C.c_int(liqflgsw)] + [_p(a) for a in cl] + [_p(a) for a in aer]
+    args += [_p(out[k]) for k in SW_OUT] + [C.c_int(nthreads)]
+    rc = L.ora_rrtmg_sw(*args)
+    if rc != 0:
+        raise RuntimeError(f"SW oracle status {rc}")
+    out["icld"], out["iaer"] = ic.value, ia.value
+    return out

@@ -1,0 +1,241 @@
+"""RRTMG_SW: the tables, the FP64 oracle and the GPU path.
+
+Tables: ``brams_gb300/data/sw_tables.gbsw`` holds the reference's own
+k-distribution data (rrtmg_sw_k_g.f90) reduced to 112 g-points with the
+reference's reduction (rrtmg_sw_init.f90:492-1689); the reduction keeps the
+solar source of every band (plain sums) and every weighted table is a convex
+combination of the original g-points (the weights of each reduced g-point
+sum to 1).
+
+Oracle pins (project-made; the reference has no tests or fixtures):
+* the incoming flux at the top is coszen x the Kurucz source (1368.22 W m-2)
+  x the Earth-Sun factor, for every column;
+* over a grey surface the clear-sky up/down flux ratio at the surface is the
+  albedo;
+* a purely scattering atmosphere (no absorbers, Rayleigh only) conserves
+  energy: the net flux is the same at every level and the heating rates
+  vanish;
+* clouds only add reflection: total-sky TOA upward flux >= clear-sky.
+
+GPU: the whole path is FP64, so the library matches the oracle at rounding
+level (fluxes within 1e-6 W m-2, heating rates within 1e-8 K/day) for
+clear and McICA-cloudy columns, every ice option, the direct cloud-optics
+input (inflag 0), aerosols, day-of-year and solar-constant scaling, low sun
+and night columns, and wide leading dimensions.
+"""
+import numpy as np
+import pytest
+
+import pyoracle
+from brams_gb300.profiles import ProfileSpec, make_state
+from brams_gb300.tables_io import read_tables
+
+NGS = [6, 12, 8, 8, 10, 10, 2, 10, 8, 6, 6, 8, 6, 12]
+
+
+def _tables():
+    import os
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    return read_tables(os.path.join(root, "brams_gb300", "data", "sw_tables.gbsw"))
+
+
+def sw_state(ncol=8, nlay=45, seed=5, cloud_prob=0.5):
+    """A generator profile with the SW inputs: albedos, solar zenith, aerosols."""
+    st = make_state(ProfileSpec(ncol=ncol, nlay=nlay, seed=seed, t_noise=3.0, h2o_sigma=0.4, cloud_prob=cloud_prob))
+    rng = np.random.default_rng(seed)
+    for k in ("asdir", "asdif", "aldir", "aldif"):
+        st[k] = rng.uniform(0.05, 0.6, ncol)
+    st["coszen"] = rng.uniform(0.05, 1.0, ncol)
+    st["tauaer_sw"] = np.asfortranarray(rng.uniform(0.0, 0.05, (ncol, nlay, 14)))
+    st["ssaaer_sw"] = np.asfortranarray(rng.uniform(0.8, 0.99, (ncol, nlay, 14)))
+    st["asmaer_sw"] = np.asfortranarray(rng.uniform(0.5, 0.8, (ncol, nlay, 14)))
+    return st
+
+
+def sw_mcica(st, seed=1, iceflag=3, inflag=2):
+    """McICA arrays (112, ncol, nlay): each g-point's cell cloudy with the
+    layer's fraction; water paths and radii of the layer; for inflag 0, cloud
+    optical depth, single-scattering albedo, asymmetry and forward fraction."""
+    ncol, nlay = st["play"].shape
+    rng = np.random.default_rng(seed)
+    cf = (rng.uniform(size=(112, ncol, nlay)) < st["cldfrac"][None]).astype(np.float64)
+    mc = {"cldfmcl": np.asfortranarray(cf),
+          "ciwpmcl": np.asfortranarray(cf * st["ciwp"][None]),
+          "clwpmcl": np.asfortranarray(cf * st["clwp"][None]),
+          "taucmcl": np.asfortranarray(cf * rng.uniform(0.5, 20.0, cf.shape)),
+          "ssacmcl": np.asfortranarray(rng.uniform(0.9, 0.9999, cf.shape)),
+          "asmcmcl": np.asfortranarray(rng.uniform(0.7, 0.9, cf.shape)),
+          "fsfcmcl": np.asfortranarray(rng.uniform(0.0, 0.5, cf.shape)),
+          "relqmcl": np.asfortranarray(rng.uniform(4.0, 20.0, (ncol, nlay)))}
+    lo, hi = {1: (14.0, 125.0), 2: (6.0, 128.0), 3: (6.0, 135.0)}[iceflag]
+    mc["reicmcl"] = np.asfortranarray(rng.uniform(lo, hi, (ncol, nlay)))
+    return mc
+
+
+# ---------------------------------------------------------------- tables
+def test_reduced_tables_shapes_and_solar_source():
+    t = _tables()
+    assert list(t["ngc"]) == NGS and int(t["ngs"][-1]) == 112
+    assert list(np.bincount(t["ngb"] - 16, minlength=14)) == NGS
+    total = 0.0
+    for k, b in enumerate(range(16, 30)):
+        sf = np.asarray(t[f"b{b}.sfluxref"])
+        assert sf.shape[0] == NGS[k]
+        col = sf if sf.ndim == 1 else sf[:, 0]
+        total += col.sum()
+    # the Kurucz source of the reference (the bands with a binary-species
+    # source hold one column per species ratio; the first column's totals)
+    assert 1360.0 < total < 1375.0
+
+
+def test_reduction_weights_are_convex():
+    import os
+
+    from brams_gb300.data.extract_sw_tables import reduction_weights
+
+    t = _tables()
+    rw = reduction_weights(t).reshape(14, 16)
+    gs = 0
+    for k in range(14):
+        counts = t["ngn"][gs:gs + NGS[k]]
+        gs += NGS[k]
+        ipr = 0
+        for n in counts:
+            assert abs(rw[k, ipr:ipr + n].sum() - 1.0) < 1e-12
+            ipr += n
+        assert ipr == 16
+
+
+# ---------------------------------------------------------------- oracle pins
+def test_incoming_flux_is_the_solar_source():
+    st = sw_state()
+    o = pyoracle.rrtmg_sw(st, None, icld=0, iaer=0, scon=0.0, adjes=1.0)
+    assert np.allclose(o["swdflx"][:, -1] / st["coszen"], 1368.22, atol=0.01)
+    o2 = pyoracle.rrtmg_sw(st, None, icld=0, iaer=0, scon=0.0, dyofyr=3)  # near perihelion
+    assert (o2["swdflx"][:, -1] > o["swdflx"][:, -1] * 1.03).all()
+    o3 = pyoracle.rrtmg_sw(st, None, icld=0, iaer=0, scon=1361.0)
+    assert np.allclose(o3["swdflx"][:, -1] / st["coszen"], 1361.0, atol=0.02)
+
+
+def test_surface_reflects_its_albedo():
+    st = sw_state()
+    for k in ("asdir", "asdif", "aldir", "aldif"):
+        st[k] = np.full_like(st[k], 0.3)
+    o = pyoracle.rrtmg_sw(st, None, icld=0, iaer=0)
+    assert np.allclose(o["swuflxc"][:, 0] / o["swdflxc"][:, 0], 0.3, rtol=1e-12)
+
+
+def test_scattering_atmosphere_conserves_energy():
+    st = sw_state(ncol=4)
+    for k in ("h2ovmr", "o3vmr", "co2vmr", "ch4vmr", "n2ovmr", "o2vmr"):
+        st[k] = np.zeros_like(st[k], order="F")
+    o = pyoracle.rrtmg_sw(st, None, icld=0, iaer=0)
+    net = o["swdflx"] - o["swuflx"]
+    assert np.abs(net - net[:, -1:]).max() < 1e-6 * net.max()
+    assert np.abs(o["swhr"]).max() < 1e-6
+
+
+def test_clouds_add_reflection():
+    st = sw_state(cloud_prob=0.8)
+    mc = sw_mcica(st)
+    o = pyoracle.rrtmg_sw(st, mc, icld=3, iaer=10)
+    assert (o["swuflx"][:, -1] >= o["swuflxc"][:, -1] - 1e-9).all()
+    assert (o["swuflx"][:, -1] - o["swuflxc"][:, -1]).max() > 10.0
+
+
+# ---------------------------------------------------------------- GPU parity
+FLUX_TOL, HR_TOL = 1e-6, 1e-8
+
+
+def _parity(out, ref):
+    for k in ("swuflx", "swdflx", "swuflxc", "swdflxc"):
+        assert np.abs(out[k] - ref[k]).max() <= FLUX_TOL, (k, float(np.abs(out[k] - ref[k]).max()))
+    for k in ("swhr", "swhrc"):
+        assert np.abs(out[k] - ref[k]).max() <= HR_TOL, (k, float(np.abs(out[k] - ref[k]).max()))
+
+
+@pytest.fixture(scope="module")
+def swctx(ctx):
+    ctx.sw_ini(1004.0)
+    return ctx
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nlay", [38, 45, 60])
+def test_clear_sky_matches_oracle(swctx, nlay):
+    st = sw_state(ncol=96, nlay=nlay, seed=nlay)
+    st["coszen"][:3] = [1.0, 1e-3, -0.2]  # overhead, grazing and night
+    for iaer in (0, 10):
+        ref = pyoracle.rrtmg_sw(st, None, icld=0, iaer=iaer)
+        out = swctx.rrtmg_sw(st, None, icld=0, iaer=iaer)
+        _parity(out, ref)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("iceflag", [1, 2, 3])
+def test_mcica_clouds_match_oracle(swctx, iceflag):
+    st = sw_state(ncol=128, nlay=45, seed=10 + iceflag, cloud_prob=0.7)
+    mc = sw_mcica(st, seed=iceflag, iceflag=iceflag)
+    ref = pyoracle.rrtmg_sw(st, mc, icld=3, iaer=10, iceflgsw=iceflag, dyofyr=172, scon=1361.0)
+    out = swctx.rrtmg_sw(st, mc, icld=3, iaer=10, iceflgsw=iceflag, dyofyr=172, scon=1361.0)
+    _parity(out, ref)
+    assert np.abs(out["swdflx"] - out["swdflxc"]).max() > 10.0
+
+
+@pytest.mark.gpu
+def test_direct_cloud_optics_match_oracle(swctx):
+    """inflag 0: the caller's cloud optical depth, albedo, asymmetry and
+    forward-scattering fraction, delta-scaled by cldprmc_sw."""
+    st = sw_state(ncol=64, nlay=38, seed=77, cloud_prob=0.6)
+    mc = sw_mcica(st, seed=5)
+    ref = pyoracle.rrtmg_sw(st, mc, icld=2, iaer=0, inflgsw=0)
+    out = swctx.rrtmg_sw(st, mc, icld=2, iaer=0, inflgsw=0)
+    _parity(out, ref)
+
+
+@pytest.mark.gpu
+def test_device_entry_with_wide_leading_dimension(swctx):
+    import torch
+
+    from brams_gb300 import rrtmg_lw as R
+
+    st = sw_state(ncol=40, nlay=45, seed=91, cloud_prob=0.6)
+    mc = sw_mcica(st, seed=9)
+    ref = pyoracle.rrtmg_sw(st, mc, icld=3, iaer=10)
+    ncol, nlay = st["play"].shape
+    ld = 53
+    dev = torch.device("cuda", 0)
+
+    def dv(a, axis):  # Fortran array padded to leading dimension ld on `axis`, on the device
+        a = np.asarray(a, dtype=np.float64)
+        shape = list(a.shape)
+        shape[axis] = ld
+        w = np.zeros(shape, order="F")
+        idx = [slice(None)] * a.ndim
+        idx[axis] = slice(0, a.shape[axis])
+        w[tuple(idx)] = a
+        return torch.from_numpy(np.ascontiguousarray(w.T)).to(dev)
+
+    d = {k: dv(st[k], 0) for k in R.SW_STATE}
+    for k in ("tauaer_sw", "ssaaer_sw", "asmaer_sw"):
+        d[k] = dv(st[k], 0)
+    for k in R.SW_CLOUD:
+        d[k] = dv(mc[k], 1 if mc[k].ndim == 3 else 0)
+    outs = {k: torch.zeros((nlay + 1, ld), dtype=torch.float64, device=dev) for k in ("swuflx", "swdflx", "swuflxc", "swdflxc")}
+    outs["swhr"] = torch.zeros((nlay, ld), dtype=torch.float64, device=dev)
+    outs["swhrc"] = torch.zeros((nlay, ld), dtype=torch.float64, device=dev)
+    status = torch.full((ncol,), -1, dtype=torch.int32, device=dev)
+    import ctypes as C
+
+    ic, ia = C.c_int(3), C.c_int(10)
+    args = [swctx.h, None, ncol, nlay, C.byref(ic), C.byref(ia)] + [d[k].data_ptr() for k in R.SW_STATE]
+    args += [1.0, 0, 1368.22, -1, 2, 3, 1] + [d[k].data_ptr() for k in R.SW_CLOUD]
+    args += [d["tauaer_sw"].data_ptr(), d["ssaaer_sw"].data_ptr(), d["asmaer_sw"].data_ptr(), None]
+    args += [outs[k].data_ptr() for k in R.SW_OUT] + [ld, ld, status.data_ptr()]
+    rc = swctx.L.gb_rrtmg_sw_device(*args)
+    assert rc == 0
+    torch.cuda.synchronize()
+    assert (status.cpu().numpy() == 0).all()
+    got = {k: v.cpu().numpy().T[:ncol] for k, v in outs.items()}
+    _parity(got, ref)
