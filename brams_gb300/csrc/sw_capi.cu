@@ -146,8 +146,10 @@ int gb_rrtmg_sw(gb_lw_context* ctx, int ncol, int nlay, int* icld, int* iaer, co
   const size_t C = (size_t)ncol, L = (size_t)nlay, G = 112;
   const bool clouds = *icld >= 1, aer = *iaer == 10;
   // one device buffer for the call: inputs at leading dimension ncol, then outputs
-  size_t n = C * L * 6 + C * (L + 1) + C * 5 + (clouds ? G * C * L * 7 + 2 * C * L : 0) + (aer ? 3 * C * L * 14 : 0) +
-             4 * C * (L + 1) + 2 * C * L;
+  // (play, tlay and five gases by layer, plev by level, five surface arrays,
+  // the clouds and aerosols when read, four level and two layer outputs)
+  const size_t n = C * L * 7 + C * (L + 1) + C * 5 + (clouds ? G * C * L * 7 + 2 * C * L : 0) +
+                   (aer ? 3 * C * L * 14 : 0) + 4 * C * (L + 1) + 2 * C * L;
   double* d = nullptr;
   if (cudaMalloc(&d, n * sizeof(double)) != cudaSuccess) {
     cudaGetLastError();
@@ -155,11 +157,16 @@ int gb_rrtmg_sw(gb_lw_context* ctx, int ncol, int nlay, int* icld, int* iaer, co
     return GB_LW_E_NOMEM;
   }
   double* p = d;
-  auto take = [&](size_t k) { double* r = p; p += k; return r; };
+  auto take = [&](size_t k) {
+    double* r = p;
+    p += k;
+    if ((size_t)(p - d) > n) rc = GB_LW_E_ARGS;  // never copied to or launched on: checked before each use
+    return r;
+  };
   auto up = [&](const double* src, size_t width, size_t rows, size_t spitch) -> const double* {
     double* dst = take(width * rows);
-    if (cudaMemcpy2DAsync(dst, width * 8, src, spitch * 8, width * 8, rows, cudaMemcpyHostToDevice, s) !=
-        cudaSuccess)
+    if (!rc && cudaMemcpy2DAsync(dst, width * 8, src, spitch * 8, width * 8, rows, cudaMemcpyHostToDevice, s) !=
+                   cudaSuccess)
       rc = GB_LW_E_CUDA;
     return dst;
   };
