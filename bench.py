@@ -34,6 +34,9 @@ transfer with FP64 heating rates.  One step solves every column once by:
                   plain path
   nomcica      -- the non-McICA driver (cldprop, taumol, random or
                   maximum/random overlap) on 360x300x45 device arrays
+  shortwave    -- RRTMG_SW (McICA generator and solver) on 360x300x45 device
+                  arrays, its error against the FP64 oracle and the oracle's
+                  throughput on the host cores
   plain_abi    -- the drop-in path on the 360x300x45 BRAMS-scale workload:
                   gb_rrtmg_lw_device on the reference's (140, ncol, nlay)
                   McICA arrays, its roofline against 8*(600*nlay + 25) bytes
@@ -531,6 +534,8 @@ def gpu_arm(args, rank, world):
     ev = None if args.no_batched else eval_block(ctx, mlp, dev, stream, args)
     log("non-McICA driver at 360x300x45")
     nomc = None if args.no_batched else nomcica_block(ctx, dev, stream, args)
+    log("shortwave at 360x300x45")
+    sw = None if args.no_batched else sw_block(ctx, dev, stream, args)
 
     # ---------------- drop-in block (ABI mode, 360x300x45)
     log("drop-in block")
@@ -590,6 +595,8 @@ def gpu_arm(args, rank, world):
         line["eval"] = ev
     if nomc is not None:
         line["nomcica"] = nomc
+    if sw is not None:
+        line["shortwave"] = sw
     if not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_headline(wl)
         line["cpu_configs"] = cpu_configs()
@@ -968,6 +975,110 @@ def nomcica_block(ctx, dev, stream, args):
         ref = pyoracle.rrtmg_lw_nomcica(sub, icld, native=True)
         res[name] = {"value": ncol / t, "unit": "columns/s", "ms_per_step": t * 1e3, **_errors(got, ref, n)}
     res["column_status"] = ctx.sync_status(stream)
+    return res
+
+
+def sw_block(ctx, dev, stream, args):
+    """RRTMG_SW on 360x300 columns x 45 layers of device arrays: McICA
+    sub-columns (gb_mcica_subcol_sw_device, per-column seeds) and the
+    solver (gb_rrtmg_sw_device) timed per step, its error against the FP64
+    oracle on 256 columns, and the oracle's throughput on the host cores."""
+    import ctypes as C
+
+    import torch
+
+    from brams_gb300 import rrtmg_lw as R
+    from brams_gb300.profiles import make_state, workload_spec
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+
+    ctx.sw_ini(1004.0)
+    st = make_state(workload_spec("drop_in_360x300x45"))
+    ncol, nlay = st["play"].shape
+    rng = np.random.default_rng(2024)
+    for k in ("asdir", "asdif", "aldir", "aldif"):
+        st[k] = rng.uniform(0.05, 0.4, ncol)
+    st["coszen"] = rng.uniform(0.05, 1.0, ncol)
+    st["tauaer_sw"] = np.asfortranarray(rng.uniform(0.0, 0.05, (ncol, nlay, 14)))
+    st["ssaaer_sw"] = np.asfortranarray(rng.uniform(0.8, 0.99, (ncol, nlay, 14)))
+    st["asmaer_sw"] = np.asfortranarray(rng.uniform(0.5, 0.8, (ncol, nlay, 14)))
+    band = {k: np.asfortranarray(rng.uniform(lo, hi, (14, ncol, nlay)))
+            for k, lo, hi in (("tauc", 0.5, 10.0), ("ssac", 0.9, 1.0), ("asmc", 0.7, 0.9), ("fsfc", 0.0, 0.5))}
+
+    def dv(a):
+        return torch.from_numpy(np.ascontiguousarray(np.asarray(a, dtype=np.float64).T)).to(dev)
+
+    d = {k: dv(st[k]) for k in R.SW_STATE + ["tauaer_sw", "ssaaer_sw", "asmaer_sw", "cldfrac", "ciwp", "clwp",
+                                             "rei", "rel"]}
+    b = {k: dv(v) for k, v in band.items()}
+    m = {k: torch.zeros((nlay, ncol, 112), dtype=torch.float64, device=dev)
+         for k in ("cldfmcl", "ciwpmcl", "clwpmcl", "taucmcl", "ssacmcl", "asmcmcl", "fsfcmcl")}
+    m["reicmcl"] = torch.zeros((nlay, ncol), dtype=torch.float64, device=dev)
+    m["relqmcl"] = torch.zeros((nlay, ncol), dtype=torch.float64, device=dev)
+    o = {k: torch.zeros((nlay + 1, ncol), dtype=torch.float64, device=dev) for k in ("swuflx", "swdflx", "swuflxc", "swdflxc")}
+    o["swhr"] = torch.zeros((nlay, ncol), dtype=torch.float64, device=dev)
+    o["swhrc"] = torch.zeros((nlay, ncol), dtype=torch.float64, device=dev)
+    L = ctx.L
+    seed0 = 5
+
+    def mcica():
+        ir = C.c_int(1)
+        rc = L.gb_mcica_subcol_sw_device(ctx.h, stream, ncol, nlay, 3, seed0, C.byref(ir),
+                                         *[d[k].data_ptr() for k in ("play", "cldfrac", "ciwp", "clwp", "rei", "rel")],
+                                         *[b[k].data_ptr() for k in ("tauc", "ssac", "asmc", "fsfc")], None,
+                                         *[m[k].data_ptr() for k in ("cldfmcl", "ciwpmcl", "clwpmcl", "reicmcl",
+                                                                     "relqmcl", "taucmcl", "ssacmcl", "asmcmcl",
+                                                                     "fsfcmcl")], ncol, 1)
+        assert rc == 0
+
+    def solve():
+        ic, ia = C.c_int(3), C.c_int(10)
+        rc = L.gb_rrtmg_sw_device(ctx.h, stream, ncol, nlay, C.byref(ic), C.byref(ia),
+                                  *[d[k].data_ptr() for k in R.SW_STATE], 1.0, 0, 1368.22, -1, 2, 3, 1,
+                                  *[m[k].data_ptr() for k in R.SW_CLOUD],
+                                  *[d[k].data_ptr() for k in ("tauaer_sw", "ssaaer_sw", "asmaer_sw")], None,
+                                  *[o[k].data_ptr() for k in R.SW_OUT], ncol, ncol, None)
+        assert rc == 0
+
+    res = {"workload": "rrtmg_sw (McICA, icld 3, iaer 10, iceflag 3, liqflag 1), 360x300 columns x 45 layers of "
+                       "device arrays; mcica_subcol_sw on the device with per-column seeds; FP64 throughout"}
+    for name, fn in (("mcica_subcol_sw", mcica), ("rrtmg_sw", solve)):
+        for _ in range(args.warmup):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3 / args.steps
+        res[name] = {"value": ncol / t, "unit": "columns/s", "ms_per_step": t * 1e3}
+    res["column_status"] = ctx.sync_status(stream)
+    n = 256
+    sub = {k: (np.asfortranarray(v[:n]) if v.ndim < 3 or k.endswith("_sw") else np.asfortranarray(v[:n]))
+           for k, v in st.items()}
+    mc = {k: np.asfortranarray(v.cpu().numpy().T[:, :n] if v.dim() == 3 else v.cpu().numpy().T[:n])
+          for k, v in m.items()}
+    ref = pyoracle.rrtmg_sw(sub, mc, icld=3, iaer=10, native=True, nthreads=os.cpu_count() or 1)
+    got = {k: v.cpu().numpy().T[:n] for k, v in o.items()}
+    res["accuracy"] = {"flux_max_w_m2": float(max(np.abs(got[k] - ref[k]).max() for k in ("swuflx", "swdflx"))),
+                       "hr_max_k_per_day": float(np.abs(got["swhr"] - ref["swhr"]).max()), "columns": n}
+    # the FP64 oracle on the host cores, 4,096 columns of the same inputs
+    nc = 4096
+    sub = {k: np.asfortranarray(v[:nc]) for k, v in st.items()}
+    mcs = {k: np.asfortranarray(v.cpu().numpy().T[:, :nc] if v.dim() == 3 else v.cpu().numpy().T[:nc])
+           for k, v in m.items()}
+    cores = os.cpu_count() or 1
+    pyoracle.rrtmg_sw(sub, mcs, icld=3, iaer=10, native=True, nthreads=cores)
+    t0, reps = time.perf_counter(), 0
+    while reps < 3 or time.perf_counter() - t0 < 5.0:
+        pyoracle.rrtmg_sw(sub, mcs, icld=3, iaer=10, native=True, nthreads=cores)
+        reps += 1
+    dt = time.perf_counter() - t0
+    res["cpu_oracle"] = {"value": nc * reps / dt, "unit": "columns/s", "cores": cores, "kind": "port",
+                         "sample": f"{nc} columns x {nlay} layers, {reps} passes ({dt:.1f} s)"}
     return res
 
 

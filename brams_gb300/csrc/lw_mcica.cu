@@ -123,7 +123,7 @@ struct Kiss {
 // skip_per_draw > 0 reproduces icld 4/5, where every kissvec call of the
 // reference advances all columns although only column c's value is kept.
 __global__ void kiss_percol_kernel(int ncol, long long ld, const double* __restrict__ play, int change_seed,
-                                   int seed_step, int ndraw, int ncol_call, int* __restrict__ err,
+                                   int seed_step, int ndraw, int ncol_call, int nsub, int* __restrict__ err,
                                    double* __restrict__ draws) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncol) return;
@@ -148,10 +148,10 @@ __global__ void kiss_percol_kernel(int ncol, long long ld, const double* __restr
   } else {
     // icld 4/5 in one call over ncol_call columns: pairs of draws per
     // (isub, column, layer), each advancing every column; keep column c's
-    int nlay_pairs = ndraw / 2 / GB_NGPT;  // = nlay
+    int nlay_pairs = ndraw / 2 / nsub;  // = nlay
     int col_in_call = c % ncol_call;
     int d = 0;
-    for (int isub = 0; isub < GB_NGPT; ++isub)
+    for (int isub = 0; isub < nsub; ++isub)
       for (int i = 0; i < ncol_call; ++i)
         for (int l = 0; l < nlay_pairs; ++l) {
           double a = k.next(), b = k.next();
@@ -169,7 +169,7 @@ __global__ void kiss_percol_kernel(int ncol, long long ld, const double* __restr
 __global__ void mcica_fill_kernel(McicaArgs a, const double* __restrict__ draws) {
   const int c = blockIdx.x;
   const int isub = threadIdx.x;
-  if (c >= a.ncol || isub >= GB_NGPT) return;
+  if (c >= a.ncol || isub >= a.nsub) return;
   const int nlay = a.nlay;
   const long long ld = a.ld;
   auto D = [&](int ilev, int which) -> double {
@@ -212,19 +212,31 @@ __global__ void mcica_fill_kernel(McicaArgs a, const double* __restrict__ draws)
     }
     cdf_prev = cdf;
     bool cloudy = cdf >= 1.0 - cldf_at(ilev);
-    long long o = (long long)isub + GB_NGPT * ((long long)c + ld * ilev);
+    long long o = (long long)isub + a.nsub * ((long long)c + ld * ilev);
     long long oc = c + ld * ilev;
+    // the band of the sub-column's optical properties (mcica_subcol_gen_sw.f90:
+    // n = ngb(isubcol) - ngbm; the longwave one uses ngb itself)
+    const long long ob = (a.ngb[isub] - a.band0 - 1) + (long long)a.nbnd * (c + ld * (long long)ilev);
     if (cloudy) {
       a.cldfmcl[o] = 1.0;
       a.clwpmcl[o] = a.clwp[oc];
       a.ciwpmcl[o] = a.ciwp[oc];
-      int nb = a.ngb[isub];
-      a.taucmcl[o] = a.tauc[(nb - 1) + 16 * (c + ld * (long long)ilev)];
+      a.taucmcl[o] = a.tauc[ob];
+      if (a.ssacmcl) {
+        a.ssacmcl[o] = a.ssac[ob];
+        a.asmcmcl[o] = a.asmc[ob];
+        a.fsfcmcl[o] = a.fsfc[ob];
+      }
     } else {
       a.cldfmcl[o] = 0.0;
       a.clwpmcl[o] = 0.0;
       a.ciwpmcl[o] = 0.0;
       a.taucmcl[o] = 0.0;
+      if (a.ssacmcl) {
+        a.ssacmcl[o] = 1.0;
+        a.asmcmcl[o] = 0.0;
+        a.fsfcmcl[o] = 0.0;
+      }
     }
   }
   // reicmcl / relqmcl copies (:264-265)
@@ -243,14 +255,14 @@ cudaError_t gb_mcica_launch(const McicaArgs& a, double* d_draws, int* d_err, cud
                             bool seed_per_column) {
   if (a.ncol <= 0) return cudaSuccess;
   const int per = a.icld == 3 ? 1 : (a.icld <= 2 ? a.nlay : 2 * a.nlay);
-  const int ndraw = GB_NGPT * per;
+  const int ndraw = a.nsub * per;
   if (a.mode == MCICA_PERCOL_MT) {
     gbm::mt_percol_kernel<<<(a.ncol + 127) / 128, 128, 0, stream>>>(a.ncol, a.seed, ndraw, d_draws);
   } else if (a.mode == MCICA_STREAM_MT) {
     gbm::mt_stream_kernel<<<1, 256, 0, stream>>>((uint32_t)a.seed, (long long)ndraw * a.ncol, d_draws);
   } else {
     gbm::kiss_percol_kernel<<<(a.ncol + 127) / 128, 128, 0, stream>>>(
-        a.ncol, a.ld, a.play, a.seed, seed_per_column ? 1 : 0, ndraw, a.icld >= 4 ? a.ncol_call : 1, d_err,
+        a.ncol, a.ld, a.play, a.seed, seed_per_column ? 1 : 0, ndraw, a.icld >= 4 ? a.ncol_call : 1, a.nsub, d_err,
         d_draws);
   }
   cudaError_t e = cudaGetLastError();
@@ -267,9 +279,9 @@ cudaError_t gb_mcica_percol_mt(int ncol, unsigned seed0, int ndraw, double* d_dr
   return cudaGetLastError();
 }
 
-size_t gb_mcica_draw_count(int ncol, int nlay, int icld) {
+size_t gb_mcica_draw_count(int ncol, int nlay, int icld, int nsub) {
   const int per = icld == 3 ? 1 : (icld <= 2 ? nlay : 2 * nlay);
-  return (size_t)GB_NGPT * per * (size_t)ncol;
+  return (size_t)nsub * per * (size_t)ncol;
 }
 
 // ----------------------------------------------------------------------------

@@ -8,6 +8,7 @@
 
 #include "../../include/gb_rrtmg_lw.h"
 #include "lw_context.h"
+#include "lw_mcica.h"
 #include "sw_solver.h"
 
 namespace {
@@ -232,4 +233,137 @@ int gb_rrtmg_sw(gb_lw_context* ctx, int ncol, int nlay, int* icld, int* iaer, co
     return rc;
   }
   return h;
+}
+
+// ---------------------------------------------------------------- mcica_subcol_sw
+namespace {
+
+// the shortwave g-point bands (rrtmg_sw_init.f90 swcmbdat ngb: 6, 12, 8, 8, 10,
+// 10, 2, 10, 8, 6, 6, 8, 6, 12 g-points in bands 16..29)
+void sw_ngb(int* ngb) {
+  static const int ng[14] = {6, 12, 8, 8, 10, 10, 2, 10, 8, 6, 6, 8, 6, 12};
+  int k = 0;
+  for (int b = 0; b < 14; ++b)
+    for (int g = 0; g < ng[b]; ++g) ngb[k++] = 16 + b;
+}
+
+}  // namespace
+
+int gb_mcica_subcol_sw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int icld, int permuteseed,
+                              int* irng, const double* play, const double* cldfrac, const double* ciwp,
+                              const double* clwp, const double* rei, const double* rel, const double* tauc,
+                              const double* ssac, const double* asmc, const double* fsfc, const double* alpha,
+                              double* cldfmcl, double* ciwpmcl, double* clwpmcl, double* reicmcl, double* relqmcl,
+                              double* taucmcl, double* ssacmcl, double* asmcmcl, double* fsfcmcl, int64_t ld,
+                              int seed_per_column) {
+  if (!ctx || !irng) return GB_LW_E_ARGS;
+  if (icld == 0) return GB_LW_OK;  // mcica_subcol_gen_sw.f90:264
+  if (icld < 0 || icld > 5) return GB_LW_E_ICLD;
+  if (ncol < 0 || nlay < 1 || ld < ncol) return GB_LW_E_ARGS;
+  if (*irng != 0) *irng = 1;
+  if (icld >= 4 && !alpha) return GB_LW_E_ARGS;
+  if (*irng == 0 && nlay < 4) return GB_LW_E_ARGS;
+  const double* req[] = {play, cldfrac, ciwp, clwp, rei, rel, tauc, ssac, asmc, fsfc};
+  for (const double* p : req)
+    if (!p) return GB_LW_E_ARGS;
+  double* outs[] = {cldfmcl, ciwpmcl, clwpmcl, reicmcl, relqmcl, taucmcl, ssacmcl, asmcmcl, fsfcmcl};
+  for (double* p : outs)
+    if (!p) return GB_LW_E_ARGS;
+  if (ncol == 0) return GB_LW_OK;
+  cudaSetDevice(ctx->device);
+  const size_t need = gb_mcica_draw_count(ncol, nlay, icld, SW_NGPT);
+  if (need > ctx->draws_elems) {
+    cudaFree(ctx->d_draws);
+    ctx->d_draws = nullptr;
+    ctx->draws_elems = 0;
+    if (cudaMalloc(&ctx->d_draws, need * 8) != cudaSuccess) {
+      cudaGetLastError();
+      return GB_LW_E_NOMEM;
+    }
+    ctx->draws_elems = need;
+  }
+  McicaArgs a{};
+  a.mode = *irng == 0 ? MCICA_PERCOL_KISS : (seed_per_column ? MCICA_PERCOL_MT : MCICA_STREAM_MT);
+  a.ncol = ncol;
+  a.nlay = nlay;
+  a.icld = icld;
+  a.seed = permuteseed;
+  a.ncol_call = seed_per_column ? 1 : ncol;
+  a.ld = ld;
+  a.play = play; a.cldfrac = cldfrac; a.ciwp = ciwp; a.clwp = clwp; a.rei = rei; a.rel = rel;
+  a.tauc = tauc; a.alpha = alpha;
+  a.cldfmcl = cldfmcl; a.ciwpmcl = ciwpmcl; a.clwpmcl = clwpmcl; a.taucmcl = taucmcl;
+  a.reicmcl = reicmcl; a.relqmcl = relqmcl;
+  a.nsub = SW_NGPT;
+  a.nbnd = 14;
+  a.band0 = 15;
+  a.ssac = ssac; a.asmc = asmc; a.fsfc = fsfc;
+  a.ssacmcl = ssacmcl; a.asmcmcl = asmcmcl; a.fsfcmcl = fsfcmcl;
+  sw_ngb(a.ngb);
+  CKS(gb_mcica_launch(a, ctx->d_draws, ctx->d_err, (cudaStream_t)stream, seed_per_column != 0));
+  return GB_LW_OK;
+}
+
+int gb_mcica_subcol_sw(gb_lw_context* ctx, int ncol, int nlay, int icld, int permuteseed, int* irng,
+                       const double* play, const double* cldfrac, const double* ciwp, const double* clwp,
+                       const double* rei, const double* rel, const double* tauc, const double* ssac,
+                       const double* asmc, const double* fsfc, const double* alpha, double* cldfmcl,
+                       double* ciwpmcl, double* clwpmcl, double* reicmcl, double* relqmcl, double* taucmcl,
+                       double* ssacmcl, double* asmcmcl, double* fsfcmcl, int64_t ld, int seed_per_column) {
+  if (!ctx || !irng) return GB_LW_E_ARGS;
+  if (icld == 0) return GB_LW_OK;
+  if (icld < 0 || icld > 5) return GB_LW_E_ICLD;
+  if (ncol < 0 || nlay < 1 || ld < ncol) return GB_LW_E_ARGS;
+  if (ncol == 0) return GB_LW_OK;
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->streams[0];
+  const size_t C = (size_t)ncol, L = (size_t)nlay, n2 = C * L, nm = (size_t)SW_NGPT * n2, nb = 14 * n2;
+  // inputs: 7 layer arrays (play, cldfrac, ciwp, clwp, rei, rel, alpha), 4 band
+  // arrays (tauc, ssac, asmc, fsfc); outputs: 7 sub-column arrays and 2 radii
+  const size_t total = 7 * n2 + 4 * nb + 7 * nm + 2 * n2;
+  double* d = nullptr;
+  if (cudaMalloc(&d, total * 8) != cudaSuccess) {
+    cudaGetLastError();
+    return GB_LW_E_NOMEM;
+  }
+  double* lay[7];
+  for (int k = 0; k < 7; ++k) lay[k] = d + k * n2;
+  double* band[4];
+  for (int k = 0; k < 4; ++k) band[k] = d + 7 * n2 + k * nb;
+  double* sub[7];
+  for (int k = 0; k < 7; ++k) sub[k] = d + 7 * n2 + 4 * nb + k * nm;
+  double* rad[2] = {d + 7 * n2 + 4 * nb + 7 * nm, d + 7 * n2 + 4 * nb + 7 * nm + n2};
+  int rc = GB_LW_OK;
+  auto h2d = [&](double* dst, const double* src, size_t w, size_t spitch) {
+    if (!rc && cudaMemcpy2DAsync(dst, w * 8, src, spitch * 8, w * 8, L, cudaMemcpyHostToDevice, s) != cudaSuccess)
+      rc = gb_ctx_fail(ctx, cudaGetLastError(), "mcica_sw H2D");
+  };
+  const double* lin[6] = {play, cldfrac, ciwp, clwp, rei, rel};
+  for (int k = 0; k < 6; ++k) h2d(lay[k], lin[k], C, (size_t)ld);
+  if (alpha) h2d(lay[6], alpha, C, (size_t)ld);
+  const double* bin[4] = {tauc, ssac, asmc, fsfc};
+  for (int k = 0; k < 4; ++k) h2d(band[k], bin[k], 14 * C, 14 * (size_t)ld);
+  if (!rc)
+    rc = gb_mcica_subcol_sw_device(ctx, s, ncol, nlay, icld, permuteseed, irng, lay[0], lay[1], lay[2], lay[3],
+                                   lay[4], lay[5], band[0], band[1], band[2], band[3], alpha ? lay[6] : nullptr,
+                                   sub[0], sub[1], sub[2], rad[0], rad[1], sub[3], sub[4], sub[5], sub[6], ncol,
+                                   seed_per_column);
+  auto d2h = [&](double* dst, const double* src, size_t w, size_t dpitch) {
+    if (!rc && cudaMemcpy2DAsync(dst, dpitch * 8, src, w * 8, w * 8, L, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+      rc = gb_ctx_fail(ctx, cudaGetLastError(), "mcica_sw D2H");
+  };
+  double* hout[7] = {cldfmcl, ciwpmcl, clwpmcl, taucmcl, ssacmcl, asmcmcl, fsfcmcl};
+  for (int k = 0; k < 7; ++k) d2h(hout[k], sub[k], (size_t)SW_NGPT * C, (size_t)SW_NGPT * ld);
+  d2h(reicmcl, rad[0], C, (size_t)ld);
+  d2h(relqmcl, rad[1], C, (size_t)ld);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (!rc && e != cudaSuccess) rc = gb_ctx_fail(ctx, e, "mcica_sw sync");
+  if (!rc) {
+    int h = 0;
+    cudaMemcpy(&h, ctx->d_err, 4, cudaMemcpyDeviceToHost);
+    cudaMemset(ctx->d_err, 0, 4);
+    rc = h;
+  }
+  cudaFree(d);
+  return rc;
 }

@@ -50,7 +50,7 @@ EXPORTS = [
     "gb_cldprop_lw_device", "gb_rtm_pack_lw_device", "gb_rtm_unpack_lw_device",
     "gb_rtm_ozone_load", "gb_rtm_ozone_free", "gb_rtm_ozone_lw",
     "gb_rrtmg_lw_shard_plan", "gb_rrtmg_lw_grid_slice", "gb_rrtmg_lw_nomcica", "gb_rrtmg_lw_nomcica_device",
-    "gb_rrtmg_sw_ini", "gb_rrtmg_sw", "gb_rrtmg_sw_device",
+    "gb_rrtmg_sw_ini", "gb_rrtmg_sw", "gb_rrtmg_sw_device", "gb_mcica_subcol_sw", "gb_mcica_subcol_sw_device",
 ]
 MLP_MMA_SYNC, MLP_TCGEN05 = 0, 1
 MLP_NPARAM = 72352
@@ -157,6 +157,8 @@ def load_library(path: str = LIB_PATH):
         L.gb_rrtmg_sw_ini.argtypes = [P, D, C.c_char_p]
         L.gb_rrtmg_sw.argtypes = [P, I, I, IP, IP] + SWA + [LL, LL]
         L.gb_rrtmg_sw_device.argtypes = [P, P, I, I, IP, IP] + SWA + [LL, LL, P]
+        L.gb_mcica_subcol_sw.argtypes = [P, I, I, I, I, IP] + [P] * 11 + [P] * 9 + [LL, I]
+        L.gb_mcica_subcol_sw_device.argtypes = [P, P, I, I, I, I, IP] + [P] * 11 + [P] * 9 + [LL, I]
         L.gb_rrtmg_lw_shard_plan.argtypes = [I, IP, IP, I, I, C.POINTER(LL), C.POINTER(LL)]
         L.gb_rrtmg_lw_grid_slice.argtypes = [GP, LL, LL, GP]
         U64, F = C.c_uint64, C.c_float
@@ -325,6 +327,27 @@ class Context:
         _check(self.L, self.h, self.L.gb_rrtmg_sw(*args))
         out["icld"], out["iaer"] = ic.value, ia.value
         return out
+
+    def mcica_subcol_sw(self, state: dict, band: dict, icld: int, permuteseed: int, irng: int = 1,
+                        seed_per_column: bool = False) -> dict:
+        """mcica_subcol_sw on host arrays: state['play', 'cldfrac', 'ciwp',
+        'clwp', 'rei', 'rel'] (ncol, nlay), band['tauc', 'ssac', 'asmc',
+        'fsfc'] (14, ncol, nlay), optional state['alpha']."""
+        ncol, nlay = state["play"].shape
+        ins = [_f64(state[k]) for k in ("play", "cldfrac", "ciwp", "clwp", "rei", "rel")]
+        ins += [_f64(band[k]) for k in ("tauc", "ssac", "asmc", "fsfc")]
+        alpha = _f64(state["alpha"]) if "alpha" in state else None
+        o = {k: np.zeros((112, ncol, nlay), order="F") for k in ("cldfmcl", "ciwpmcl", "clwpmcl", "taucmcl",
+                                                                 "ssacmcl", "asmcmcl", "fsfcmcl")}
+        o["reicmcl"] = np.zeros((ncol, nlay), order="F")
+        o["relqmcl"] = np.zeros((ncol, nlay), order="F")
+        ir = C.c_int(irng)
+        outs = [o[k] for k in ("cldfmcl", "ciwpmcl", "clwpmcl", "reicmcl", "relqmcl", "taucmcl", "ssacmcl",
+                               "asmcmcl", "fsfcmcl")]
+        rc = self.L.gb_mcica_subcol_sw(self.h, ncol, nlay, icld, permuteseed, C.byref(ir), *[_ptr(a) for a in ins],
+                                       _ptr(alpha), *[_ptr(a) for a in outs], ncol, int(seed_per_column))
+        _check(self.L, self.h, rc)
+        return o
 
     def sync_status(self, stream=None) -> int:
         return self.L.gb_rrtmg_lw_sync_status(self.h, _ptr(stream or 0))

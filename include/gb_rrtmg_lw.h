@@ -408,6 +408,27 @@ int gb_rrtmg_sw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int
                        const double* ecaer, double* swuflx, double* swdflx, double* swhr, double* swuflxc,
                        double* swdflxc, double* swhrc, int64_t ld_in, int64_t ld_out, int* d_col_status);
 
+/* Replaces mcica_subcol_sw (mcica_subcol_gen_sw.f90:181-296, called at
+ * rtm_driver.f90:1373) for HOST arrays: as gb_mcica_subcol_lw with 112
+ * sub-columns, band optical properties tauc ssac asmc fsfc (14, ld, nlay)
+ * and the McICA outputs cldfmcl ciwpmcl clwpmcl taucmcl ssacmcl asmcmcl
+ * fsfcmcl (112, ld, nlay), reicmcl relqmcl (ld, nlay).  Draws are bit-equal
+ * to the reference's for icld 1-5, both generators and both seeding modes. */
+int gb_mcica_subcol_sw(gb_lw_context* ctx, int ncol, int nlay, int icld, int permuteseed, int* irng,
+                       const double* play, const double* cldfrac, const double* ciwp, const double* clwp,
+                       const double* rei, const double* rel, const double* tauc, const double* ssac,
+                       const double* asmc, const double* fsfc, const double* alpha, double* cldfmcl,
+                       double* ciwpmcl, double* clwpmcl, double* reicmcl, double* relqmcl, double* taucmcl,
+                       double* ssacmcl, double* asmcmcl, double* fsfcmcl, int64_t ld, int seed_per_column);
+/* Same on DEVICE arrays on `stream`. */
+int gb_mcica_subcol_sw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int icld, int permuteseed,
+                              int* irng, const double* play, const double* cldfrac, const double* ciwp,
+                              const double* clwp, const double* rei, const double* rel, const double* tauc,
+                              const double* ssac, const double* asmc, const double* fsfc, const double* alpha,
+                              double* cldfmcl, double* ciwpmcl, double* clwpmcl, double* reicmcl, double* relqmcl,
+                              double* taucmcl, double* ssacmcl, double* asmcmcl, double* fsfcmcl, int64_t ld,
+                              int seed_per_column);
+
 /* ---------------------------------------------------------------------------
  * Multi-GPU column shards (host only; no device call).  BRAMS gives each MPI
  * rank the columns of its own subdomain (rtm_driver.f90:830, nofcols) and

@@ -2267,15 +2267,21 @@ void ora_kiss_draws(int32_t s1, int32_t s2, int32_t s3, int32_t s4, int n, doubl
   for (int i = 0; i < n; ++i) reals[i] = k.next();
 }
 
-// mcica_subcol_lw + generate_stochastic_clouds (mcica_subcol_gen_lw.f90:183-703)
-int ora_mcica_subcol_lw(int ncol, int nlay, int icld, int permuteseed, int* irng,
-                        const double* play, const double* cld, const double* ciwp,
-                        const double* clwp, const double* rei, const double* rel,
-                        const double* tauc, const double* alpha, double* cld_stoch,
-                        double* ciwp_stoch, double* clwp_stoch, double* reicmcl, double* relqmcl,
-                        double* tauc_stoch) {
-  if (!g_ready) return ERR_NOT_INIT;
-  const int nsub = NGPT;
+}  // extern "C"
+
+namespace {
+
+// generate_stochastic_clouds (mcica_subcol_gen_lw.f90:403-703) and its
+// shortwave twin generate_stochastic_clouds_sw (mcica_subcol_gen_sw.f90:
+// 298-757): nsub sub-columns, sub-column isub takes the band optical
+// properties of band ngb_of[isub] - band0 (tauc is (nbnd, ncol, nlay)); the
+// shortwave one also copies ssac, asmc, fsfc (1, 0, 0 in clear cells).
+int mcica_generate(int nsub, const int* ngb_of, int band0, int nbnd, int ncol, int nlay, int icld, int permuteseed,
+                   int* irng, const double* play, const double* cld, const double* ciwp, const double* clwp,
+                   const double* rei, const double* rel, const double* tauc, const double* ssac, const double* asmc,
+                   const double* fsfc, const double* alpha, double* cld_stoch, double* ciwp_stoch,
+                   double* clwp_stoch, double* reicmcl, double* relqmcl, double* tauc_stoch, double* ssac_stoch,
+                   double* asmc_stoch, double* fsfc_stoch) {
   if (icld == 0) return 0;
   if (icld < 0 || icld > 5) return ERR_ICLD;
   size_t nc = (size_t)ncol * nlay;
@@ -2374,20 +2380,67 @@ int ora_mcica_subcol_lw(int ncol, int nlay, int icld, int permuteseed, int* irng
       for (int isub = 1; isub <= nsub; ++isub) {
         size_t o = IX(isub, i, ilev);
         bool cloudy = CDF[o] >= 1.0 - cldf[CI(i, ilev)];
+        const int n = ngb_of[isub - 1] - band0;  // 1-based band of the optical properties
+        const size_t ob = (size_t)(n - 1) + (size_t)nbnd * CI(i, ilev);
         if (cloudy) {
           cld_stoch[o] = 1.0;
           clwp_stoch[o] = clwp[CI(i, ilev)];
           ciwp_stoch[o] = ciwp[CI(i, ilev)];
-          int nb = ngb[isub - 1];
-          tauc_stoch[o] = tauc[(nb - 1) + 16 * CI(i, ilev)];
+          tauc_stoch[o] = tauc[ob];
+          if (ssac_stoch) {
+            ssac_stoch[o] = ssac[ob];
+            asmc_stoch[o] = asmc[ob];
+            fsfc_stoch[o] = fsfc[ob];
+          }
         } else {
           cld_stoch[o] = 0.0;
           clwp_stoch[o] = 0.0;
           ciwp_stoch[o] = 0.0;
           tauc_stoch[o] = 0.0;
+          if (ssac_stoch) {
+            ssac_stoch[o] = 1.0;
+            asmc_stoch[o] = 0.0;
+            fsfc_stoch[o] = 0.0;
+          }
         }
       }
   return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// mcica_subcol_lw (mcica_subcol_gen_lw.f90:183-265)
+int ora_mcica_subcol_lw(int ncol, int nlay, int icld, int permuteseed, int* irng,
+                        const double* play, const double* cld, const double* ciwp,
+                        const double* clwp, const double* rei, const double* rel,
+                        const double* tauc, const double* alpha, double* cld_stoch,
+                        double* ciwp_stoch, double* clwp_stoch, double* reicmcl, double* relqmcl,
+                        double* tauc_stoch) {
+  if (!g_ready) return ERR_NOT_INIT;
+  return mcica_generate(NGPT, ngb, 0, 16, ncol, nlay, icld, permuteseed, irng, play, cld, ciwp, clwp, rei, rel, tauc,
+                        nullptr, nullptr, nullptr, alpha, cld_stoch, ciwp_stoch, clwp_stoch, reicmcl, relqmcl,
+                        tauc_stoch, nullptr, nullptr, nullptr);
+}
+
+// mcica_subcol_sw (mcica_subcol_gen_sw.f90:181-296): 112 sub-columns; the
+// g-point bands are the shortwave ones (rrtmg_sw_init.f90 swcmbdat ngb:
+// 6, 12, 8, 8, 10, 10, 2, 10, 8, 6, 6, 8, 6, 12 g-points in bands 16..29);
+// tauc, ssac, asmc, fsfc are (14, ncol, nlay).  Needs no oracle tables.
+int ora_mcica_subcol_sw(int ncol, int nlay, int icld, int permuteseed, int* irng, const double* play,
+                        const double* cld, const double* ciwp, const double* clwp, const double* rei,
+                        const double* rel, const double* tauc, const double* ssac, const double* asmc,
+                        const double* fsfc, const double* alpha, double* cld_stoch, double* ciwp_stoch,
+                        double* clwp_stoch, double* reicmcl, double* relqmcl, double* tauc_stoch,
+                        double* ssac_stoch, double* asmc_stoch, double* fsfc_stoch) {
+  static const int ng[14] = {6, 12, 8, 8, 10, 10, 2, 10, 8, 6, 6, 8, 6, 12};
+  int ngb_sw[112], k = 0;
+  for (int b = 0; b < 14; ++b)
+    for (int g = 0; g < ng[b]; ++g) ngb_sw[k++] = 16 + b;
+  return mcica_generate(112, ngb_sw, 15, 14, ncol, nlay, icld, permuteseed, irng, play, cld, ciwp, clwp, rei, rel,
+                        tauc, ssac, asmc, fsfc, alpha, cld_stoch, ciwp_stoch, clwp_stoch, reicmcl, relqmcl,
+                        tauc_stoch, ssac_stoch, asmc_stoch, fsfc_stoch);
 }
 
 void ora_get_tables(double* tau, double* ex, double* tfn, double* hf, double* ff) {

@@ -310,3 +310,24 @@ def rrtmg_sw(state: dict, mc: dict | None, icld: int = 3, iaer: int = 10, adjes:
         raise RuntimeError(f"SW oracle status {rc}")
     out["icld"], out["iaer"] = ic.value, ia.value
     return out
+
+
+def mcica_subcol_sw(state: dict, band: dict, icld: int, permuteseed: int, irng: int = 1) -> dict:
+    """mcica_subcol_sw (mcica_subcol_gen_sw.f90:181): one call over all columns."""
+    L = lib()
+    ncol, nlay = state["play"].shape
+    ins = [_f(state[k]) for k in ("play", "cldfrac", "ciwp", "clwp", "rei", "rel")]
+    ins += [_f(band[k]) for k in ("tauc", "ssac", "asmc", "fsfc")]
+    alpha = _f(state["alpha"]) if "alpha" in state else None
+    o = {k: np.zeros((112, ncol, nlay), order="F") for k in ("cldfmcl", "ciwpmcl", "clwpmcl", "taucmcl", "ssacmcl",
+                                                             "asmcmcl", "fsfcmcl")}
+    o["reicmcl"] = np.zeros((ncol, nlay), order="F")
+    o["relqmcl"] = np.zeros((ncol, nlay), order="F")
+    ir = C.c_int(irng)
+    outs = [o[k] for k in ("cldfmcl", "ciwpmcl", "clwpmcl", "reicmcl", "relqmcl", "taucmcl", "ssacmcl", "asmcmcl",
+                           "fsfcmcl")]
+    rc = L.ora_mcica_subcol_sw(C.c_int(ncol), C.c_int(nlay), C.c_int(icld), C.c_int(permuteseed), C.byref(ir),
+                               *[_p(a) for a in ins], _p(alpha), *[_p(a) for a in outs])
+    if rc != 0:
+        raise RuntimeError(f"oracle mcica_subcol_sw: {L.ora_error_string(rc).decode()}")
+    return o

@@ -239,3 +239,69 @@ def test_device_entry_with_wide_leading_dimension(swctx):
     assert (status.cpu().numpy() == 0).all()
     got = {k: v.cpu().numpy().T[:ncol] for k, v in outs.items()}
     _parity(got, ref)
+
+
+# ---------------------------------------------------------------- McICA for the shortwave
+def _sw_band(st, seed=3):
+    ncol, nlay = st["play"].shape
+    rng = np.random.default_rng(seed)
+    return {"tauc": np.asfortranarray(rng.uniform(0.1, 10.0, (14, ncol, nlay))),
+            "ssac": np.asfortranarray(rng.uniform(0.8, 1.0, (14, ncol, nlay))),
+            "asmc": np.asfortranarray(rng.uniform(0.6, 0.9, (14, ncol, nlay))),
+            "fsfc": np.asfortranarray(rng.uniform(0.0, 0.5, (14, ncol, nlay)))}
+
+
+def test_oracle_sw_mcica_maps_bands_and_clear_cells():
+    st = make_state(ProfileSpec(ncol=6, nlay=20, seed=4, cloud_prob=0.7))
+    band = _sw_band(st)
+    o = pyoracle.mcica_subcol_sw(st, band, 3, 11)
+    cloudy = o["cldfmcl"] == 1.0
+    assert cloudy.any() and (~cloudy).any()
+    assert (o["ssacmcl"][~cloudy] == 1.0).all() and (o["asmcmcl"][~cloudy] == 0.0).all()
+    ngb = np.repeat(np.arange(14), NGS)  # sub-column -> band (0-based)
+    for k, src in (("taucmcl", "tauc"), ("ssacmcl", "ssac"), ("fsfcmcl", "fsfc")):
+        want = np.where(cloudy, band[src][ngb], o[k])
+        assert np.array_equal(o[k], want), k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("icld", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("irng", [0, 1])
+def test_sw_mcica_is_bit_exact(swctx, icld, irng):
+    st = make_state(ProfileSpec(ncol=24, nlay=30, seed=40 + icld, cloud_prob=0.6))
+    st["alpha"] = np.asfortranarray(np.exp(-np.linspace(0.1, 2.0, 30))[None, :] * np.ones((24, 1)))
+    band = _sw_band(st, seed=icld)
+    ref = pyoracle.mcica_subcol_sw(st, band, icld, 17, irng)
+    got = swctx.mcica_subcol_sw(st, band, icld, 17, irng)
+    for k in ref:
+        assert np.array_equal(got[k], ref[k]), k
+
+
+@pytest.mark.gpu
+def test_sw_mcica_seed_per_column(swctx):
+    """Per-column seeding: column c is the reference called alone with seed base + c."""
+    st = make_state(ProfileSpec(ncol=12, nlay=25, seed=9, cloud_prob=0.6))
+    band = _sw_band(st)
+    got = swctx.mcica_subcol_sw(st, band, 3, 100, 1, seed_per_column=True)
+    for c in range(12):
+        sub = {k: np.asfortranarray(st[k][c:c + 1]) for k in ("play", "cldfrac", "ciwp", "clwp", "rei", "rel")}
+        sb = {k: np.asfortranarray(v[:, c:c + 1]) for k, v in band.items()}
+        ref = pyoracle.mcica_subcol_sw(sub, sb, 3, 100 + c, 1)
+        for k in ("cldfmcl", "taucmcl", "ssacmcl", "asmcmcl", "fsfcmcl"):
+            assert np.array_equal(got[k][:, c], ref[k][:, 0]), (c, k)
+
+
+@pytest.mark.gpu
+def test_sw_chain_mcica_then_solver_matches_oracle(swctx):
+    """BRAMS's order: mcica_subcol_sw, then rrtmg_sw, both on the GPU."""
+    st = sw_state(ncol=64, nlay=45, seed=31, cloud_prob=0.7)
+    for k in ("rei", "rel"):
+        st[k] = np.asfortranarray(np.clip(st[k], 6.0, 50.0))
+    band = _sw_band(st, seed=8)
+    mc_ref = pyoracle.mcica_subcol_sw(st, band, 3, 5)
+    mc = swctx.mcica_subcol_sw(st, band, 3, 5)
+    for k in mc_ref:
+        assert np.array_equal(mc[k], mc_ref[k]), k
+    ref = pyoracle.rrtmg_sw(st, mc_ref, icld=3, iaer=10)
+    out = swctx.rrtmg_sw(st, mc, icld=3, iaer=10)
+    _parity(out, ref)
