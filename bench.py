@@ -1042,8 +1042,12 @@ def sw_block(ctx, dev, stream, args):
         assert rc == 0
 
     res = {"workload": "rrtmg_sw (McICA, icld 3, iaer 10, iceflag 3, liqflag 1), 360x300 columns x 45 layers of "
-                       "device arrays; mcica_subcol_sw on the device with per-column seeds; FP64 throughout"}
-    for name, fn in (("mcica_subcol_sw", mcica), ("rrtmg_sw", solve)):
+                       "device arrays; mcica_subcol_sw on the device with per-column seeds; the solver in both "
+                       "precisions of its column kernel: rrtmg_sw = fp32 gas optics, cloud optics and two-stream "
+                       "solution with fp64 flux sums and heating rates (the default), rrtmg_sw_fp64 = fp64 "
+                       "throughout"}
+
+    def timed(fn):
         for _ in range(args.warmup):
             fn()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -1054,17 +1058,25 @@ def sw_block(ctx, dev, stream, args):
         e1.record()
         torch.cuda.synchronize()
         t = e0.elapsed_time(e1) / 1e3 / args.steps
-        res[name] = {"value": ncol / t, "unit": "columns/s", "ms_per_step": t * 1e3}
-    res["column_status"] = ctx.sync_status(stream)
+        return {"value": ncol / t, "unit": "columns/s", "ms_per_step": t * 1e3}
+
+    res["mcica_subcol_sw"] = timed(mcica)
     n = 256
-    sub = {k: (np.asfortranarray(v[:n]) if v.ndim < 3 or k.endswith("_sw") else np.asfortranarray(v[:n]))
-           for k, v in st.items()}
+    sub = {k: np.asfortranarray(v[:n]) for k, v in st.items()}
     mc = {k: np.asfortranarray(v.cpu().numpy().T[:, :n] if v.dim() == 3 else v.cpu().numpy().T[:n])
           for k, v in m.items()}
     ref = pyoracle.rrtmg_sw(sub, mc, icld=3, iaer=10, native=True, nthreads=os.cpu_count() or 1)
-    got = {k: v.cpu().numpy().T[:n] for k, v in o.items()}
-    res["accuracy"] = {"flux_max_w_m2": float(max(np.abs(got[k] - ref[k]).max() for k in ("swuflx", "swdflx"))),
-                       "hr_max_k_per_day": float(np.abs(got["swhr"] - ref["swhr"]).max()), "columns": n}
+    for name, bits in (("rrtmg_sw", 32), ("rrtmg_sw_fp64", 64)):
+        ctx.sw_set_precision(bits)
+        res[name] = timed(solve)
+        res[name]["column_status"] = ctx.sync_status(stream)
+        got = {k: v.cpu().numpy().T[:n] for k, v in o.items()}
+        res[name]["accuracy"] = {
+            "flux_max_w_m2": float(max(np.abs(got[k] - ref[k]).max() for k in ("swuflx", "swdflx", "swuflxc",
+                                                                               "swdflxc"))),
+            "hr_max_k_per_day": float(max(np.abs(got[k] - ref[k]).max() for k in ("swhr", "swhrc"))),
+            "hr_rmse_k_per_day": float(np.sqrt(np.mean((got["swhr"] - ref["swhr"]) ** 2))), "columns": n}
+    ctx.sw_set_precision(32)
     # the FP64 oracle on the host cores, 4,096 columns of the same inputs
     nc = 4096
     sub = {k: np.asfortranarray(v[:nc]) for k, v in st.items()}

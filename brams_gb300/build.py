@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libgb_rrtmg_lw.so")
 UNITS = ["lw_solver.cu", "lw_mcica.cu", "lw_capi.cu", "lw_tables.cpp", "lw_mlp.cu", "lw_mlp_capi.cu", "lw_mlp_tc.cu",
          "lw_cldprop.cu", "lw_pack.cu", "lw_ozone.cpp", "lw_shard.cpp",
-         "sw_solver.cu", "sw_capi.cu"]
+         "sw_solver.cu", "sw_solver_f32.cu", "sw_capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # The column kernel is compiled without multiply-add contraction: every fused
 # multiply-add in it is an explicit fmaf, so that its results are fixed by the

@@ -454,6 +454,7 @@ int gb_rrtmg_lw_free(gb_lw_context* ctx) {
   cudaFree(ctx->d_band);
   cudaFree(ctx->d_ncb);
   cudaFree(ctx->d_sw_tables);
+  cudaFree(ctx->d_sw_tables_f);
   cudaFree(ctx->d_sw_scratch);
   delete ctx;
   return GB_LW_OK;

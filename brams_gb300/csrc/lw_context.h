@@ -57,14 +57,17 @@ struct gb_lw_context {
   size_t band_elems = 0;
   int* d_ncb = nullptr;
   size_t ncb_elems = 0;
-  // RRTMG_SW: tables (fp64 blob, loaded by gb_rrtmg_sw_ini) and the column
-  // kernel's scratch slots (grown on demand)
+  // RRTMG_SW: tables (fp64 and fp32 blobs, loaded by gb_rrtmg_sw_ini), the
+  // precision of the column kernel (gb_rrtmg_sw_set_precision) and the
+  // column blocks' scratch slots
   std::string table_dir;
   double* d_sw_tables = nullptr;
+  float* d_sw_tables_f = nullptr;
   bool sw_ready = false;
+  int sw_bits = 32;
   double sw_scon = 0.0;  // rrsw_scon of the tables (parrrsw.f90)
-  double* d_sw_scratch = nullptr;
-  size_t sw_scratch_doubles = 0;
+  void* d_sw_scratch = nullptr;
+  size_t sw_scratch_bytes = 0;
 };
 
 // records a CUDA error on the context; returns GB_LW_E_CUDA

@@ -62,20 +62,22 @@ int prepare(gb_lw_context* ctx, int ncol, int nlay, int* icld, int* iaer, double
 }
 
 int launch(gb_lw_context* ctx, const SwArgs& a, cudaStream_t stream) {
-  const long long slots = (long long)ctx->num_sms * 4;
-  const size_t need = (size_t)slots * gb_sw_slot_doubles(a.nlay);
-  if (need > ctx->sw_scratch_doubles) {
+  const int bits = ctx->sw_bits;
+  const long long slots = gb_sw_slots(ctx->num_sms, bits);
+  const size_t need = gb_sw_scratch_bytes(a.nlay, bits, slots);
+  if (need > ctx->sw_scratch_bytes) {
     cudaFree(ctx->d_sw_scratch);
     ctx->d_sw_scratch = nullptr;
-    ctx->sw_scratch_doubles = 0;
-    if (cudaMalloc(&ctx->d_sw_scratch, need * sizeof(double)) != cudaSuccess) {
+    ctx->sw_scratch_bytes = 0;
+    if (cudaMalloc(&ctx->d_sw_scratch, need) != cudaSuccess) {
       cudaGetLastError();
       ctx->last_error = "device allocation of the SW scratch slots failed";
       return GB_LW_E_NOMEM;
     }
-    ctx->sw_scratch_doubles = need;
+    ctx->sw_scratch_bytes = need;
   }
-  cudaError_t e = gb_sw_launch(a, ctx->d_sw_tables, ctx->d_sw_scratch, slots, stream);
+  const void* tables = bits == 32 ? (const void*)ctx->d_sw_tables_f : (const void*)ctx->d_sw_tables;
+  cudaError_t e = gb_sw_launch(a, bits, tables, ctx->d_sw_scratch, slots, stream);
   return e == cudaSuccess ? GB_LW_OK : gb_ctx_fail(ctx, e, "SW column kernel");
 }
 
@@ -84,6 +86,12 @@ int launch(gb_lw_context* ctx, const SwArgs& a, cudaStream_t stream) {
 int gb_rrtmg_sw_ini(gb_lw_context* ctx, double cpdair, const char* table_dir) {
   if (!ctx) return GB_LW_E_ARGS;
   return gb_sw_load(ctx, cpdair, table_dir);
+}
+
+int gb_rrtmg_sw_set_precision(gb_lw_context* ctx, int bits) {
+  if (!ctx || (bits != 32 && bits != 64)) return GB_LW_E_ARGS;
+  ctx->sw_bits = bits;
+  return GB_LW_OK;
 }
 
 int gb_rrtmg_sw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int* icld, int* iaer,

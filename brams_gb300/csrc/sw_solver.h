@@ -26,9 +26,19 @@ struct SwArgs {
 struct gb_lw_context;
 // loads sw_tables.gbsw of table_dir (NULL: the context's table directory) into the context
 int gb_sw_load(gb_lw_context* ctx, double cpdair, const char* table_dir);
-// shared memory of a column block, and doubles of one block's scratch slot
-size_t gb_sw_smem_bytes(int nlay);
-size_t gb_sw_slot_doubles(int nlay);
-// all columns of `a` with at most `slots` persistent blocks (block k uses slot k of scratch)
-cudaError_t gb_sw_launch(const SwArgs& a, const double* d_tables, double* scratch, long long slots,
+
+// blocks per SM of the column kernel in each precision (its launch bounds)
+#define SW_MINB_F64 4
+#define SW_MINB_F32 5
+// persistent blocks (= scratch slots) for a device of num_sms SMs, and the
+// scratch bytes of `slots` slots, for a precision of 32 or 64 bits
+long long gb_sw_slots(int num_sms, int bits);
+size_t gb_sw_scratch_bytes(int nlay, int bits, long long slots);
+// all columns of `a` with at most `slots` persistent blocks (block k uses slot
+// k of scratch); d_tables is the table blob of the precision (fp32 or fp64)
+cudaError_t gb_sw_launch(const SwArgs& a, int bits, const void* d_tables, void* scratch, long long slots,
                          cudaStream_t stream);
+// the fp32 kernels' unit (sw_solver_f32.cu): its table directory (a gbsw::SwTab) and its launch
+cudaError_t gb_sw_set_tab_f32(const void* tab);
+cudaError_t gb_sw_launch_f32(const SwArgs& a, const float* d_tables, float* scratch, long long slots,
+                             cudaStream_t stream);

@@ -50,7 +50,7 @@ EXPORTS = [
     "gb_cldprop_lw_device", "gb_rtm_pack_lw_device", "gb_rtm_unpack_lw_device",
     "gb_rtm_ozone_load", "gb_rtm_ozone_free", "gb_rtm_ozone_lw",
     "gb_rrtmg_lw_shard_plan", "gb_rrtmg_lw_grid_slice", "gb_rrtmg_lw_nomcica", "gb_rrtmg_lw_nomcica_device",
-    "gb_rrtmg_sw_ini", "gb_rrtmg_sw", "gb_rrtmg_sw_device", "gb_mcica_subcol_sw", "gb_mcica_subcol_sw_device",
+    "gb_rrtmg_sw_ini", "gb_rrtmg_sw_set_precision", "gb_rrtmg_sw", "gb_rrtmg_sw_device", "gb_mcica_subcol_sw", "gb_mcica_subcol_sw_device",
 ]
 MLP_MMA_SYNC, MLP_TCGEN05 = 0, 1
 MLP_NPARAM = 72352
@@ -155,6 +155,7 @@ def load_library(path: str = LIB_PATH):
         L.gb_rrtmg_lw_num_variants.argtypes = []
         SWA = [P] * 16 + [D, I, D, I, I, I, I] + [P] * 9 + [P] * 4 + [P] * 6
         L.gb_rrtmg_sw_ini.argtypes = [P, D, C.c_char_p]
+        L.gb_rrtmg_sw_set_precision.argtypes = [P, I]
         L.gb_rrtmg_sw.argtypes = [P, I, I, IP, IP] + SWA + [LL, LL]
         L.gb_rrtmg_sw_device.argtypes = [P, P, I, I, IP, IP] + SWA + [LL, LL, P]
         L.gb_mcica_subcol_sw.argtypes = [P, I, I, I, I, IP] + [P] * 11 + [P] * 9 + [LL, I]
@@ -307,6 +308,10 @@ class Context:
     def sw_ini(self, cpdair: float = 1004.0, table_dir: str | None = None) -> None:
         """gb_rrtmg_sw_ini: the shortwave tables into this context."""
         _check(self.L, self.h, self.L.gb_rrtmg_sw_ini(self.h, cpdair, table_dir.encode() if table_dir else None))
+
+    def sw_set_precision(self, bits: int) -> None:
+        """gb_rrtmg_sw_set_precision: 32 (fp32 solution, fp64 sums) or 64."""
+        _check(self.L, self.h, self.L.gb_rrtmg_sw_set_precision(self.h, bits))
 
     def rrtmg_sw(self, state: dict, mc: dict | None, icld: int = 3, iaer: int = 10, adjes: float = 1.0,
                  dyofyr: int = 0, scon: float = 1368.22, isolvar: int = -1, inflgsw: int = 2, iceflgsw: int = 3,

@@ -383,6 +383,14 @@ int gb_rrtmg_lw_graph_destroy(gb_lw_graph* graph);
  * whole path is fp64.  tlev, tsfc and n2ovmr are not used by the reference's
  * shortwave computation and may be NULL. */
 int gb_rrtmg_sw_ini(gb_lw_context* ctx, double cpdair, const char* table_dir);
+/* Precision of the shortwave column kernel of this context: 32 (the
+ * default) runs the gas optics, cloud optics and two-stream solution in fp32
+ * and keeps fp64 for the layer coefficients, the flux accumulation over
+ * g-points and the heating rates (fluxes within 0.05 W m-2 and heating rates
+ * within 0.01 K/day of the fp64 reference); 64 runs everything in fp64, as
+ * the reference does.  Returns GB_LW_E_ARGS for any other value.  No
+ * reference counterpart: the reference's precision is fixed at build time. */
+int gb_rrtmg_sw_set_precision(gb_lw_context* ctx, int bits);
 int gb_rrtmg_sw(gb_lw_context* ctx, int ncol, int nlay, int* icld, int* iaer, const double* play,
                 const double* plev, const double* tlay, const double* tlev, const double* tsfc,
                 const double* h2ovmr, const double* o3vmr, const double* co2vmr, const double* ch4vmr,

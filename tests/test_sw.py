@@ -17,11 +17,15 @@ Oracle pins (project-made; the reference has no tests or fixtures):
   vanish;
 * clouds only add reflection: total-sky TOA upward flux >= clear-sky.
 
-GPU: the whole path is FP64, so the library matches the oracle at rounding
-level (fluxes within 1e-6 W m-2, heating rates within 1e-8 K/day) for
-clear and McICA-cloudy columns, every ice option, the direct cloud-optics
-input (inflag 0), aerosols, day-of-year and solar-constant scaling, low sun
-and night columns, and wide leading dimensions.
+GPU, both precisions of the column kernel: with everything in FP64 the
+library matches the oracle at rounding level (fluxes within 1e-6 W m-2,
+heating rates within 1e-8 K/day); with the gas optics, cloud optics and
+two-stream solution in FP32 (FP64 flux sums and heating rates) within
+0.05 W m-2 and 0.01 K/day.  Cases: clear and McICA-cloudy columns, every ice
+option, the direct cloud-optics input (inflag 0), aerosols, day-of-year and
+solar-constant scaling, low sun and night columns, wide leading dimensions,
+and the radius bounds the reference stops on, decided on the double inputs
+in both precisions.
 """
 import numpy as np
 import pytest
@@ -145,57 +149,69 @@ def test_clouds_add_reflection():
 
 
 # ---------------------------------------------------------------- GPU parity
-FLUX_TOL, HR_TOL = 1e-6, 1e-8
+TOL = {64: (1e-6, 1e-8), 32: (0.05, 0.01)}  # bits -> (W m-2, K/day)
+BITS = [64, 32]
 
 
-def _parity(out, ref):
+def _parity(out, ref, bits=64):
+    flux_tol, hr_tol = TOL[bits]
     for k in ("swuflx", "swdflx", "swuflxc", "swdflxc"):
-        assert np.abs(out[k] - ref[k]).max() <= FLUX_TOL, (k, float(np.abs(out[k] - ref[k]).max()))
+        assert np.abs(out[k] - ref[k]).max() <= flux_tol, (k, float(np.abs(out[k] - ref[k]).max()))
     for k in ("swhr", "swhrc"):
-        assert np.abs(out[k] - ref[k]).max() <= HR_TOL, (k, float(np.abs(out[k] - ref[k]).max()))
+        assert np.abs(out[k] - ref[k]).max() <= hr_tol, (k, float(np.abs(out[k] - ref[k]).max()))
 
 
 @pytest.fixture(scope="module")
 def swctx(ctx):
     ctx.sw_ini(1004.0)
-    return ctx
+    yield ctx
+    ctx.sw_set_precision(32)
+
+
+def _solve(swctx, bits, *args, **kw):
+    swctx.sw_set_precision(bits)
+    return swctx.rrtmg_sw(*args, **kw)
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("bits", BITS)
 @pytest.mark.parametrize("nlay", [38, 45, 60])
-def test_clear_sky_matches_oracle(swctx, nlay):
+def test_clear_sky_matches_oracle(swctx, nlay, bits):
     st = sw_state(ncol=96, nlay=nlay, seed=nlay)
     st["coszen"][:3] = [1.0, 1e-3, -0.2]  # overhead, grazing and night
     for iaer in (0, 10):
         ref = pyoracle.rrtmg_sw(st, None, icld=0, iaer=iaer)
-        out = swctx.rrtmg_sw(st, None, icld=0, iaer=iaer)
-        _parity(out, ref)
+        out = _solve(swctx, bits, st, None, icld=0, iaer=iaer)
+        _parity(out, ref, bits)
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("bits", BITS)
 @pytest.mark.parametrize("iceflag", [1, 2, 3])
-def test_mcica_clouds_match_oracle(swctx, iceflag):
+def test_mcica_clouds_match_oracle(swctx, iceflag, bits):
     st = sw_state(ncol=128, nlay=45, seed=10 + iceflag, cloud_prob=0.7)
     mc = sw_mcica(st, seed=iceflag, iceflag=iceflag)
     ref = pyoracle.rrtmg_sw(st, mc, icld=3, iaer=10, iceflgsw=iceflag, dyofyr=172, scon=1361.0)
-    out = swctx.rrtmg_sw(st, mc, icld=3, iaer=10, iceflgsw=iceflag, dyofyr=172, scon=1361.0)
-    _parity(out, ref)
+    out = _solve(swctx, bits, st, mc, icld=3, iaer=10, iceflgsw=iceflag, dyofyr=172, scon=1361.0)
+    _parity(out, ref, bits)
     assert np.abs(out["swdflx"] - out["swdflxc"]).max() > 10.0
 
 
 @pytest.mark.gpu
-def test_direct_cloud_optics_match_oracle(swctx):
+@pytest.mark.parametrize("bits", BITS)
+def test_direct_cloud_optics_match_oracle(swctx, bits):
     """inflag 0: the caller's cloud optical depth, albedo, asymmetry and
     forward-scattering fraction, delta-scaled by cldprmc_sw."""
     st = sw_state(ncol=64, nlay=38, seed=77, cloud_prob=0.6)
     mc = sw_mcica(st, seed=5)
     ref = pyoracle.rrtmg_sw(st, mc, icld=2, iaer=0, inflgsw=0)
-    out = swctx.rrtmg_sw(st, mc, icld=2, iaer=0, inflgsw=0)
-    _parity(out, ref)
+    out = _solve(swctx, bits, st, mc, icld=2, iaer=0, inflgsw=0)
+    _parity(out, ref, bits)
 
 
 @pytest.mark.gpu
-def test_device_entry_with_wide_leading_dimension(swctx):
+@pytest.mark.parametrize("bits", BITS)
+def test_device_entry_with_wide_leading_dimension(swctx, bits):
     import torch
 
     from brams_gb300 import rrtmg_lw as R
@@ -228,6 +244,7 @@ def test_device_entry_with_wide_leading_dimension(swctx):
     status = torch.full((ncol,), -1, dtype=torch.int32, device=dev)
     import ctypes as C
 
+    swctx.sw_set_precision(bits)
     ic, ia = C.c_int(3), C.c_int(10)
     args = [swctx.h, None, ncol, nlay, C.byref(ic), C.byref(ia)] + [d[k].data_ptr() for k in R.SW_STATE]
     args += [1.0, 0, 1368.22, -1, 2, 3, 1] + [d[k].data_ptr() for k in R.SW_CLOUD]
@@ -238,7 +255,36 @@ def test_device_entry_with_wide_leading_dimension(swctx):
     torch.cuda.synchronize()
     assert (status.cpu().numpy() == 0).all()
     got = {k: v.cpu().numpy().T[:ncol] for k, v in outs.items()}
-    _parity(got, ref)
+    _parity(got, ref, bits)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bits", BITS)
+def test_radius_bounds_are_decided_on_the_double_inputs(swctx, bits):
+    """cldprmc_sw's stops (ice option 3: generalized effective size 5-140 um;
+    liquid option 1: radius 2.5-60 um) on the double radii: a radius on a
+    bound passes, one a rounding step beyond it stops the call, in both
+    precisions (the fp32 kernel rounds both to the same float)."""
+    from brams_gb300.rrtmg_lw import RrtmgLwError
+
+    st = sw_state(ncol=8, nlay=20, seed=3, cloud_prob=1.0)
+    mc = sw_mcica(st, seed=2)
+    shape = mc["cldfmcl"].shape
+    mc["cldfmcl"] = np.asfortranarray(np.ones(shape))
+    mc["ciwpmcl"] = np.asfortranarray(np.full(shape, 5.0))
+    mc["clwpmcl"] = np.asfortranarray(np.full(shape, 8.0))
+    for key, edge, code in (("reicmcl", 140.0, 5), ("reicmcl", 5.0, 5), ("relqmcl", 60.0, 6), ("relqmcl", 2.5, 6)):
+        ok = {k: np.array(v, order="F") for k, v in mc.items()}
+        ok[key][3, 7] = edge
+        ref = pyoracle.rrtmg_sw(st, ok, icld=3, iaer=10)
+        _parity(_solve(swctx, bits, st, ok, icld=3, iaer=10), ref, bits)
+        beyond = np.nextafter(edge, np.inf if edge > 10.0 else -np.inf)
+        assert np.float32(beyond) == np.float32(edge)
+        bad = {k: np.array(v, order="F") for k, v in ok.items()}
+        bad[key][3, 7] = beyond
+        with pytest.raises(RrtmgLwError) as e:
+            _solve(swctx, bits, st, bad, icld=3, iaer=10)
+        assert e.value.code == code, (key, edge)
 
 
 # ---------------------------------------------------------------- McICA for the shortwave
@@ -292,7 +338,8 @@ def test_sw_mcica_seed_per_column(swctx):
 
 
 @pytest.mark.gpu
-def test_sw_chain_mcica_then_solver_matches_oracle(swctx):
+@pytest.mark.parametrize("bits", BITS)
+def test_sw_chain_mcica_then_solver_matches_oracle(swctx, bits):
     """BRAMS's order: mcica_subcol_sw, then rrtmg_sw, both on the GPU."""
     st = sw_state(ncol=64, nlay=45, seed=31, cloud_prob=0.7)
     for k in ("rei", "rel"):
@@ -303,5 +350,5 @@ def test_sw_chain_mcica_then_solver_matches_oracle(swctx):
     for k in mc_ref:
         assert np.array_equal(mc[k], mc_ref[k]), k
     ref = pyoracle.rrtmg_sw(st, mc_ref, icld=3, iaer=10)
-    out = swctx.rrtmg_sw(st, mc, icld=3, iaer=10)
-    _parity(out, ref)
+    out = _solve(swctx, bits, st, mc, icld=3, iaer=10)
+    _parity(out, ref, bits)
