@@ -112,6 +112,67 @@ __device__ __forceinline__ bool nonzero_in(double x) {
   return (__double_as_longlong(x) << 1) != 0;
 }
 
+// Ampere-style asynchronous global -> shared copies (cp.async): each thread
+// stages the next layer's (or level's) values while it computes this one;
+// a thread only reads back what it copied itself, so waiting on its own
+// copy groups is enough
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+template <typename R>
+__device__ __forceinline__ void cp_async_r(void* smem, const R* gmem) {
+  if constexpr (sizeof(R) == 4)
+    cp_async4(smem, gmem);
+  else
+    cp_async8(smem, gmem);
+}
+
+// double -> float on the integer pipes (the fp64 pipe is GB300's narrowest):
+// round to nearest (ties away from zero) for results in the normal float
+// range, +-0 for double zeros and subnormals, the hardware conversion for the
+// rest (float subnormals, overflow, inf, NaN)
+__device__ __forceinline__ float d2f_fast(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  if (e - 897u < 254u) {
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    return __uint_as_float(((hi & 0x80000000u) | ((e - 896u) << 23)) + m + ((lo >> 28) & 1u));
+  }
+  if (e == 0u) return __uint_as_float(hi & 0x80000000u);
+  return (float)x;
+}
+// float -> double (exact) on the integer pipes: normal floats and zeros by
+// rebiasing the exponent, subnormals, inf and NaN by the hardware conversion
+__device__ __forceinline__ double f2d_fast(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e - 1u < 254u) {
+    const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0xfffffu);
+    return __hiloint2double((int)hi, (int)(u << 29));
+  }
+  if ((u << 1) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+  return (double)x;
+}
+template <typename R>
+__device__ __forceinline__ R to_r(double x) {
+  if constexpr (sizeof(R) == 4)
+    return d2f_fast(x);
+  else
+    return x;
+}
+
 // exp(-ze) as the reference forms it: Taylor below od_lo, else exp_tbl at
 // the quantised index (reftra.f90:150-159, spcvmc.f90:445-456)
 template <typename R>
@@ -313,11 +374,25 @@ struct Smem {
   Lay<R>* L;       // [nl]
   double* sfz;     // [NG] sfluxzen, then the incoming flux of each g-point
   double* flx;     // [4 * (nl + 1)] level sums: up, down, clear up, clear down
+  float* aer;      // fp32 kernels: [nl][NB][3] aerosol tau, ssa, asymmetry of the column
+  char* stage;     // [2][NT][sw_stage_bytes] per-thread copy stages of the two passes
   int* iscal;      // [0] laytrop, [1] status, [4 + k] solar-source layer of band k
 };
+// bytes a thread stages per layer (down pass: six McICA doubles, taug, taur)
+// or per level (up pass: the NVL values of its g-point), padded to 16
+template <typename R>
+__host__ __device__ constexpr int sw_stage_bytes() {
+  return (6 * 8 + 2 * (int)sizeof(R)) > NVL * (int)sizeof(R) ? ((6 * 8 + 2 * (int)sizeof(R)) + 15) / 16 * 16
+                                                               : NVL * (int)sizeof(R);
+}
+template <typename R>
+__host__ __device__ inline size_t sw_aer_floats(int nl) {
+  return sizeof(R) == 4 ? (size_t)nl * NB * 3 : 0;
+}
 template <typename R>
 __host__ __device__ inline size_t sw_smem_bytes(int nl) {
-  return (size_t)nl * sizeof(Lay<R>) + NG * 8 + (size_t)4 * (nl + 1) * 8 + 32 * 4;
+  return (size_t)nl * sizeof(Lay<R>) + NG * 8 + (size_t)4 * (nl + 1) * 8 + sw_aer_floats<R>(nl) * 4 + 15 +
+         (size_t)2 * NT * sw_stage_bytes<R>() + 32 * 4;
 }
 template <typename R>
 __device__ inline Smem<R> carve(char* p, int nl) {
@@ -328,6 +403,11 @@ __device__ inline Smem<R> carve(char* p, int nl) {
   p += NG * 8;
   s.flx = reinterpret_cast<double*>(p);
   p += (size_t)4 * (nl + 1) * 8;
+  s.aer = reinterpret_cast<float*>(p);
+  p += sw_aer_floats<R>(nl) * 4;
+  p = reinterpret_cast<char*>((reinterpret_cast<uintptr_t>(p) + 15) & ~(uintptr_t)15);
+  s.stage = p;
+  p += (size_t)2 * NT * sw_stage_bytes<R>();
   s.iscal = reinterpret_cast<int*>(p);
   return s;
 }
@@ -568,17 +648,20 @@ __device__ double solar_source(const R* __restrict__ T, const Smem<R>& S, int k,
 // co-albedo tables; returns a stop code
 template <typename R>
 __device__ int cloud_cell(const R* __restrict__ T, const SwArgs& a, int band, double cfd, R cf, double ciwpd,
-                          double clwpd, double radiced, double radliqd, R fsfc, double ssacd, R& tauc, R& ssac,
-                          R& asmc, R& coc) {
+                          double clwpd, const double* prei, const double* prel, const double* pfsfc, double ssacd,
+                          R& tauc, R& ssac, R& asmc, R& coc) {
   const double cldmin = 1.e-20;
   const R eps = R(1.e-06);
-  const R ciwp = (R)ciwpd, clwp = (R)clwpd;
-  const double cwpd = ciwpd + clwpd;
-  bool cloudy = ge_in(cfd, cf, cldmin);
-  if (cloudy) cloudy = ge_in(cwpd, (R)cwpd, cldmin) || tauc >= R(cldmin);
-  if (!cloudy) return 0;
+  if (!ge_in(cfd, cf, cldmin)) return 0;
+  const R ciwp = to_r<R>(ciwpd), clwp = to_r<R>(clwpd);
+  bool wp;  // cwp >= cldmin (in fp32 a tie with the threshold is not resolved)
+  if constexpr (sizeof(R) == 8)
+    wp = ciwpd + clwpd >= cldmin;
+  else
+    wp = ciwp + clwp >= (float)cldmin;
+  if (!(wp || tauc >= R(cldmin))) return 0;
   if (a.inflag == 0) {
-    const R ffp = fsfc, ffp1 = R(1.0) - ffp, ffpssa = R(1.0) - ffp * ssac;
+    const R ffp = to_r<R>(__ldg(pfsfc)), ffp1 = R(1.0) - ffp, ffpssa = R(1.0) - ffp * ssac;
     const R ssacloud_a = ffp1 * ssac / ffpssa;
     const R taucloud_a = ffpssa * tauc;
     if (sizeof(R) == 4) coc = (R)(1.0 - ssacd) / ffpssa;  // 1 - ssacloud_a
@@ -594,7 +677,8 @@ __device__ int cloud_cell(const R* __restrict__ T, const SwArgs& a, int band, do
   R extcoliq = R(0), ssacoliq = R(0), gliq = R(0), forwliq = R(0);
   R coice = R(0), coliq = R(0);  // co-albedos of the ice and liquid optics (fp32 kernels)
   if (nonzero_in(ciwpd)) {
-    const R radice = (R)radiced;
+    const double radiced = __ldg(prei);
+    const R radice = to_r<R>(radiced);
     if (a.iceflag == 1) {
       if (outside_in(radiced, radice, 13.0, 130.0)) return GB_COL_ICE_BOUNDS;
       const double w2 = c_S.wavenum2[ib - 16];
@@ -640,7 +724,8 @@ __device__ int cloud_cell(const R* __restrict__ T, const SwArgs& a, int band, do
   }
   if (nonzero_in(clwpd)) {
     if (a.liqflag != 1) return GB_COL_SW_UNSUPPORTED;
-    const R radliq = (R)radliqd;
+    const double radliqd = __ldg(prel);
+    const R radliq = to_r<R>(radliqd);
     if (outside_in(radliqd, radliq, 2.5, 60.0)) return GB_COL_LIQ_BOUNDS;
     int index = (int)(radliq - R(1.5));
     if (index == 0) index = 1;
@@ -680,6 +765,20 @@ __device__ int cloud_cell(const R* __restrict__ T, const SwArgs& a, int band, do
     asmc = (scatliq * (gliq - forwliq) / (R(1.0) - forwliq) + scatice * (gice - forwice) / (R(1.0) - forwice)) /
            (scatliq + scatice);
   return 0;
+}
+
+// one (level, g-point) record of the slot, written with 16-byte stores
+template <typename R>
+__device__ __forceinline__ void store_rec(R* dst, const R (&v)[NVL]) {
+  if constexpr (sizeof(R) == 4) {
+    float4* p = reinterpret_cast<float4*>(dst);
+#pragma unroll
+    for (int i = 0; i < NVL / 4; ++i) p[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+  } else {
+    double2* p = reinterpret_cast<double2*>(dst);
+#pragma unroll
+    for (int i = 0; i < NVL / 2; ++i) p[i] = make_double2(v[2 * i], v[2 * i + 1]);
+  }
 }
 
 // one column by the block
@@ -783,6 +882,17 @@ __device__ void sw_column(const SwArgs& a, long long icol, const Smem<R>& S, R* 
     const int k = c_S.ngb[tid] - 16;
     S.sfz[tid] = solar_source(T, S, k, tid - c_S.b[k].g0 + 1, S.iscal[4 + k], lt, nl);
   }
+  if constexpr (sizeof(R) == 4) {
+    // the column's aerosol optics once per (layer, band) instead of per g-point
+    if (a.iaer == 10)
+      for (int i = tid; i < nl * NB; i += NT) {
+        const int lay = i / NB, b = i - lay * NB;
+        const long long o = icol + ld * (lay + (long long)nl * b);
+        S.aer[3 * i] = d2f_fast(__ldg(a.tauaer + o));
+        S.aer[3 * i + 1] = d2f_fast(__ldg(a.ssaaer + o));
+        S.aer[3 * i + 2] = d2f_fast(__ldg(a.asmaer + o));
+      }
+  }
   __syncthreads();
   // ---- 3. per g-point: optics, reftra, adding (spcvmc_sw :150-440, vrtqdr_sw)
   const bool live = tid < NG;
@@ -796,37 +906,71 @@ __device__ void sw_column(const SwArgs& a, long long icol, const Smem<R>& S, R* 
   const R albd = (R)(ibm >= 10 && ibm <= 13 ? __ldg(a.asdif + icol) : __ldg(a.aldif + icol));
   // the incoming flux of the g-point (fp64) replaces its source in shared memory
   if (live) S.sfz[g] = a.adjflux[band - 16] * S.sfz[g] * prmu0d;
-  // slot layout after taug/taur: per (level k = 1..nl+1, value v) at ((2*nl) + (k-1)*NVL + v) * NG + g
+  // slot layout after taug/taur: one record of NVL values per (level k = 1..nl+1, g-point),
+  // record (k, g) at ((k - 1) * NG + g) * NVL
   R* V = scr + (size_t)2 * nl * NG;
-  auto at = [&](int k, int v) -> R& { return V[((size_t)(k - 1) * NVL + v) * NG + g]; };
+  auto rec_of = [&](int k) { return V + ((size_t)(k - 1) * NG + g) * NVL; };
   enum { RC, RDC, TC, TDC, DBC, RT, RDT, TT, TDT, DBT, ZTDC, RDNDC, TDBC, ZTDT, RDNDT, TDBT };
+  constexpr int SB = sw_stage_bytes<R>();
+  auto stage = [&](int i) { return S.stage + ((size_t)(i & 1) * NT + tid) * SB; };
+  // down pass: layer jk's McICA cell (six doubles) and gas optical depths, staged one layer ahead
+  auto issue_down = [&](int jk) {
+    char* d = stage(jk);
+    const int lay = nl - jk;
+    if (a.icld >= 1) {
+      const long long o = g + (long long)NG * (icol + ld * lay);
+      cp_async8(d, a.cldfmcl + o);
+      cp_async8(d + 8, a.taucmcl + o);
+      cp_async8(d + 16, a.ssacmcl + o);
+      cp_async8(d + 24, a.asmcmcl + o);
+      cp_async8(d + 32, a.ciwpmcl + o);
+      cp_async8(d + 40, a.clwpmcl + o);
+    }
+    cp_async_r(d + 48, sg + (size_t)lay * NG + g);
+    cp_async_r(d + 48 + sizeof(R), sr + (size_t)lay * NG + g);
+    cp_commit();
+  };
   int err = 0;
   // top-down: layer jk (1 = top) is model layer ikl = nl + 1 - jk
   R tdbc = R(1.0), tdbt = R(1.0), ztdc = R(1.0), ztdt = R(1.0), rdndc = R(0.0), rdndt = R(0.0);
+  issue_down(1);
   for (int jk = 1; jk <= nl; ++jk) {
     const int lay = nl - jk;  // 0-based model layer
-    const R taug = sg[(size_t)lay * NG + g], taur = sr[(size_t)lay * NG + g];
+    if (jk < nl)
+      issue_down(jk + 1);
+    else
+      cp_commit();  // an empty group keeps one group in flight
+    cp_wait1();
+    const char* d = stage(jk);
+    const double* m = reinterpret_cast<const double*>(d);
+    const R taug = *reinterpret_cast<const R*>(d + 48), taur = *reinterpret_cast<const R*>(d + 48 + sizeof(R));
     R taua = R(0.0), ssaa = R(1.0), asma = R(0.0);
     if (a.iaer == 10) {
-      const long long o = icol + ld * (lay + (long long)nl * (ibm - 1));
-      taua = (R)__ldg(a.tauaer + o);
-      ssaa = (R)__ldg(a.ssaaer + o);
-      asma = (R)__ldg(a.asmaer + o);
+      if constexpr (sizeof(R) == 4) {
+        const float* pa = S.aer + 3 * (lay * NB + ibm - 1);
+        taua = pa[0];
+        ssaa = pa[1];
+        asma = pa[2];
+      } else {
+        const long long o = icol + ld * (lay + (long long)nl * (ibm - 1));
+        taua = __ldg(a.tauaer + o);
+        ssaa = __ldg(a.ssaaer + o);
+        asma = __ldg(a.asmaer + o);
+      }
     }
     double cfd = 0.0;
     R cf = R(0.0), tcm = R(0.0), wcm = R(1.0), gcm = R(0.0), coc = R(0.0);
     if (a.icld >= 1) {
-      const long long o = g + (long long)NG * (icol + ld * lay);
-      cfd = __ldg(a.cldfmcl + o);
-      cf = (R)cfd;
-      tcm = (R)__ldg(a.taucmcl + o);
-      const double wcmd = __ldg(a.ssacmcl + o);
-      wcm = (R)wcmd;
+      cfd = m[0];
+      cf = to_r<R>(cfd);
+      tcm = to_r<R>(m[1]);
+      const double wcmd = m[2];
+      wcm = to_r<R>(wcmd);
       coc = R(1.0) - wcm;  // cells cldprmc_sw leaves alone keep the caller's optics
-      gcm = (R)__ldg(a.asmcmcl + o);
-      const int e = cloud_cell(T, a, band, cfd, cf, __ldg(a.ciwpmcl + o), __ldg(a.clwpmcl + o),
-                               in2(a.reicmcl, ld, icol, lay), in2(a.relqmcl, ld, icol, lay),
-                               (R)__ldg(a.fsfcmcl + o), wcmd, tcm, wcm, gcm, coc);
+      gcm = to_r<R>(m[3]);
+      const long long o = g + (long long)NG * (icol + ld * lay);
+      const int e = cloud_cell(T, a, band, cfd, cf, m[4], m[5], a.reicmcl + icol + ld * lay,
+                               a.relqmcl + icol + ld * lay, a.fsfcmcl + o, wcmd, tcm, wcm, gcm, coc);
       if (e && live) err = e;
     }
     // clear-sky optics with delta scaling, then the cloud's added (spcvmc.f90:180-227)
@@ -875,24 +1019,10 @@ __device__ void sw_column(const SwArgs& a, long long icol, const Smem<R>& S, R* 
     const R tt = zclear * trc + zcloud * tro, tdt = zclear * tdc + zcloud * tdo;
     const R dbc = expo(T, ztauc / prmu0);
     const R dbt = zclear * dbc + zcloud * expo(T, ztauo / prmu0);
-    // level jk values, then the downward recurrence to level jk+1 (vrtqdr.f90:63-80)
+    // level jk's record, then the downward recurrence to level jk+1 (vrtqdr.f90:63-80)
     if (live) {
-      at(jk, ZTDC) = ztdc;
-      at(jk, RDNDC) = rdndc;
-      at(jk, TDBC) = tdbc;
-      at(jk, ZTDT) = ztdt;
-      at(jk, RDNDT) = rdndt;
-      at(jk, TDBT) = tdbt;
-      at(jk, RC) = rc;
-      at(jk, RDC) = rdc;
-      at(jk, TC) = trc;
-      at(jk, TDC) = tdc;
-      at(jk, DBC) = dbc;
-      at(jk, RT) = rt;
-      at(jk, RDT) = rdt;
-      at(jk, TT) = tt;
-      at(jk, TDT) = tdt;
-      at(jk, DBT) = dbt;
+      const R rec[NVL] = {rc, rdc, trc, tdc, dbc, rt, rdt, tt, tdt, dbt, ztdc, rdndc, tdbc, ztdt, rdndt, tdbt};
+      store_rec(rec_of(jk), rec);
     }
     if (jk == 1) {
       ztdc = trc;
@@ -913,40 +1043,54 @@ __device__ void sw_column(const SwArgs& a, long long icol, const Smem<R>& S, R* 
     tdbt = dbt * tdbt;
   }
   if (live) {
-    at(nl + 1, ZTDC) = ztdc;
-    at(nl + 1, RDNDC) = rdndc;
-    at(nl + 1, TDBC) = tdbc;
-    at(nl + 1, ZTDT) = ztdt;
-    at(nl + 1, RDNDT) = rdndt;
-    at(nl + 1, TDBT) = tdbt;
+    const R rec[NVL] = {R(0), R(0), R(0), R(0), R(0), R(0), R(0), R(0), R(0), R(0), ztdc, rdndc, tdbc, ztdt, rdndt, tdbt};
+    store_rec(rec_of(nl + 1), rec);
   }
-  // bottom-up (vrtqdr.f90:44-60) and the level flux fractions (:82-88); the
-  // four fractions of level jk replace its (consumed) values RC..TDC
+  // bottom-up (vrtqdr.f90:44-60) and the level flux fractions (:82-88); level
+  // jk's record is staged one level ahead, and its first four values are
+  // replaced by the level's fractions fu, fd, cu, cd
+  auto issue_up = [&](int jk) {
+    char* d = stage(jk);
+    const char* src = reinterpret_cast<const char*>(rec_of(jk));
+#pragma unroll
+    for (int i = 0; i < NVL * (int)sizeof(R) / 16; ++i) cp_async16(d + 16 * i, src + 16 * i);
+    cp_commit();
+  };
   R rupc = albp, rupdc = albd, rupt = albp, rupdt = albd;
+  issue_up(nl + 1);
   for (int jk = nl + 1; jk >= 1; --jk) {
+    if (jk > 1)
+      issue_up(jk - 1);
+    else
+      cp_commit();
+    cp_wait1();
+    const R* v = reinterpret_cast<const R*>(stage(jk));
     if (jk <= nl) {
-      R zr = R(1.0) / (R(1.0) - rupdc * at(jk, RDC));
-      const R nrupc = at(jk, RC) + (at(jk, TDC) * ((at(jk, TC) - at(jk, DBC)) * rupdc + at(jk, DBC) * rupc)) * zr;
-      rupdc = at(jk, RDC) + at(jk, TDC) * at(jk, TDC) * rupdc * zr;
+      R zr = R(1.0) / (R(1.0) - rupdc * v[RDC]);
+      const R nrupc = v[RC] + (v[TDC] * ((v[TC] - v[DBC]) * rupdc + v[DBC] * rupc)) * zr;
+      rupdc = v[RDC] + v[TDC] * v[TDC] * rupdc * zr;
       rupc = nrupc;
-      zr = R(1.0) / (R(1.0) - rupdt * at(jk, RDT));
-      const R nrupt = at(jk, RT) + (at(jk, TDT) * ((at(jk, TT) - at(jk, DBT)) * rupdt + at(jk, DBT) * rupt)) * zr;
-      rupdt = at(jk, RDT) + at(jk, TDT) * at(jk, TDT) * rupdt * zr;
+      zr = R(1.0) / (R(1.0) - rupdt * v[RDT]);
+      const R nrupt = v[RT] + (v[TDT] * ((v[TT] - v[DBT]) * rupdt + v[DBT] * rupt)) * zr;
+      rupdt = v[RDT] + v[TDT] * v[TDT] * rupdt * zr;
       rupt = nrupt;
     }
-    R zr = R(1.0) / (R(1.0) - at(jk, RDNDC) * rupdc);
-    const R tdcl = at(jk, TDBC), ztc = at(jk, ZTDC);
+    R zr = R(1.0) / (R(1.0) - v[RDNDC] * rupdc);
+    const R tdcl = v[TDBC], ztc = v[ZTDC];
     const R cu = (tdcl * rupc + (ztc - tdcl) * rupdc) * zr;
-    const R cd = tdcl + (ztc - tdcl + tdcl * rupc * at(jk, RDNDC)) * zr;
-    zr = R(1.0) / (R(1.0) - at(jk, RDNDT) * rupdt);
-    const R tdtl = at(jk, TDBT), ztt = at(jk, ZTDT);
+    const R cd = tdcl + (ztc - tdcl + tdcl * rupc * v[RDNDC]) * zr;
+    zr = R(1.0) / (R(1.0) - v[RDNDT] * rupdt);
+    const R tdtl = v[TDBT], ztt = v[ZTDT];
     const R fu = (tdtl * rupt + (ztt - tdtl) * rupdt) * zr;
-    const R fd = tdtl + (ztt - tdtl + tdtl * rupt * at(jk, RDNDT)) * zr;
+    const R fd = tdtl + (ztt - tdtl + tdtl * rupt * v[RDNDT]) * zr;
     if (live) {
-      at(jk, 0) = fu;
-      at(jk, 1) = fd;
-      at(jk, 2) = cu;
-      at(jk, 3) = cd;
+      R* r = rec_of(jk);
+      if constexpr (sizeof(R) == 4) {
+        *reinterpret_cast<float4*>(r) = make_float4(fu, fd, cu, cd);
+      } else {
+        reinterpret_cast<double2*>(r)[0] = make_double2(fu, fd);
+        reinterpret_cast<double2*>(r)[1] = make_double2(cu, cd);
+      }
     }
   }
   if (err) atomicMax(&S.iscal[1], err);
@@ -954,10 +1098,15 @@ __device__ void sw_column(const SwArgs& a, long long icol, const Smem<R>& S, R* 
   // ---- 4. fp64 sums over the g-points in order: level jk, flux q
   for (int t = tid; t < 4 * (nl + 1); t += NT) {
     const int jk = t >> 2, q = t & 3;
-    const R* f = V + ((size_t)jk * NVL + q) * NG;
+    const R* f = V + (size_t)jk * NG * NVL + q;  // record (jk + 1, g) value q at f[g * NVL]
     double s = 0.0;
 #pragma unroll 4
-    for (int gg = 0; gg < NG; ++gg) s = s + S.sfz[gg] * (double)f[gg];
+    for (int gg = 0; gg < NG; ++gg) {
+      if constexpr (sizeof(R) == 4)
+        s = fma(S.sfz[gg], f2d_fast(f[gg * NVL]), s);
+      else
+        s = s + S.sfz[gg] * f[gg * NVL];
+    }
     S.flx[t] = s;
   }
   __syncthreads();
