@@ -156,9 +156,10 @@ int ensure_buffer(gb_lw_context* ctx, float** buf, size_t* have, size_t bytes) {
 // points a descriptor at a hand-over buffer of `bytes` (slots of nsmax layers)
 void attach_gas(LwBatch& b, float* buf, size_t bytes) {
   b.gstride = (long long)b.nsmax * GB_NGPT;
-  b.gslots = (long long)(bytes / (2 * sizeof(float) * (size_t)b.gstride));
+  b.gslots = (long long)(bytes / (3 * sizeof(float) * (size_t)b.gstride));
   b.gtau = buf;
   b.gfrac = buf + (size_t)b.gslots * b.gstride;
+  b.gcld = buf + (size_t)2 * b.gslots * b.gstride;
 }
 
 // hand-over bytes a batch of `ncols` columns at `nlay` layers is solved with

@@ -480,6 +480,7 @@ __device__ inline RtSmem rt_carve(char* p, int nl) {
 struct GasSrc {
   const float* gt;            // fp32 planes [nl][140] (taumol), or NULL
   const float* gf;
+  float* gc;                  // caller sub-columns: the cells' cloud plane [nl][140], or NULL
   const __half* nt;           // fp16 rows [nl][140] (network), or NULL
   const __half* nf;
   const unsigned char* flag;  // per layer: 1 -> network, 0 -> fp32 planes
@@ -574,6 +575,40 @@ __device__ __forceinline__ float cell_cloud(const LwArgs& a, const RtSmem& S, lo
     tauc = cloud_tau_layer(a, band, T, make_float4((float)ciwp, (float)clwp, r.z, r.w), fl);
   }
   odcld = secdiff * tauc;
+  efcl = 1.0f - __expf(-odcld);
+  return 1.0f;
+}
+
+// a caller sub-column cell's cloud value for the transfer: its cloud optical
+// depth (cldprmc.f90:178-266, formed as cell_cloud does) where cldfmcl = 1,
+// the fraction itself where it is neither 0 nor 1
+__device__ __forceinline__ float cell_value(const LwArgs& a, const RtSmem& S, int lay, int band, bool one,
+                                            double cf, double ciwp, double clwp, double tin,
+                                            const float* __restrict__ T) {
+  if (!one) return (float)cf;
+  float tauc = 0.0f;
+  bool from_paths = a.inflag == 2 && ciwp + clwp >= 1.e-20;
+  if (!from_paths) {
+    const long long tb = __double_as_longlong(tin);
+    from_paths = a.inflag == 2 && tb >= __double_as_longlong(1.0e-20) && tb <= 0x7FF0000000000000LL;
+    tauc = (float)tin;
+  }
+  if (from_paths) {
+    const int fl = ((__double_as_longlong(ciwp) << 1) != 0LL ? 1 : 0) | ((__double_as_longlong(clwp) << 1) != 0LL ? 2 : 0);
+    const float4 r = S.L[lay].lcw;
+    tauc = cloud_tau_layer(a, band, T, make_float4((float)ciwp, (float)clwp, r.z, r.w), fl);
+  }
+  return tauc;
+}
+
+// the transfer's cloud of a caller sub-column cell from its hand-over value
+__device__ __forceinline__ float cell_from_value(bool one, float v, float secdiff, float& odcld, float& efcl) {
+  if (!one) {
+    odcld = 0.0f;
+    efcl = 0.0f;
+    return v;
+  }
+  odcld = secdiff * v;
   efcl = 1.0f - __expf(-odcld);
   return 1.0f;
 }
@@ -971,10 +1006,16 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
     // patterns: == 1, /= 0, >= 1e-20
     const long long kOne = 0x3FF0000000000000LL, kInf = 0x7FF0000000000000LL;
     const long long kMin = __double_as_longlong(1.0e-20);
-#pragma unroll 4
+    // the four McICA arrays of a layer are read together (several layers in
+    // flight); where the transfer has a cloud plane, each cloudy cell's
+    // optical depth is formed here once instead of in both passes
+#pragma unroll 2
     for (int lay = 0; lay < nl; ++lay) {
       const long long o = g + GB_NGPT * (icol + a.ld * lay);
-      const long long cb = live ? __double_as_longlong(__ldg(a.cldfmcl + o)) : 0LL;
+      const double cfv = live ? __ldg(a.cldfmcl + o) : 0.0;
+      const double ciwp = live ? __ldg(a.ciwpmcl + o) : 0.0, clwp = live ? __ldg(a.clwpmcl + o) : 0.0;
+      const double tin = live ? __ldg(a.taucmcl + o) : 0.0;
+      const long long cb = __double_as_longlong(cfv);
       const bool one = cb == kOne;
       const bool frac = !one && (cb << 1) != 0LL;  // neither +-0 nor 1 (NaN included, as /= 0 is)
       const unsigned m1 = __ballot_sync(FULL, one), mf = __ballot_sync(FULL, frac);
@@ -982,9 +1023,9 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
         S.L[lay].cbits[warp] = m1;
         S.fbits(lay)[warp] = mf;
       }
+      if (src.gc && (one || frac)) src.gc[lay * GB_NGPT + g] = cell_value(a, S, lay, band, one, cfv, ciwp, clwp, tin, T);
       if (cb >= kMin && cb <= kInf) {  // cldfmc >= cldmin (cldprmc.f90:178)
-        const double ciwp = __ldg(a.ciwpmcl + o), clwp = __ldg(a.clwpmcl + o);
-        const long long tb = __double_as_longlong(__ldg(a.taucmcl + o));
+        const long long tb = __double_as_longlong(tin);
         if (ciwp + clwp >= 1.e-20 || (tb >= kMin && tb <= kInf)) {
           const int e = S.L[lay].lfl;
           if (a.inflag == 1) err = GB_COL_INFLAG1;
@@ -1034,11 +1075,17 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
   // The next layer's gas optics are loaded while this one is done; the
   // level sums of two layers share one transposed butterfly.
   float rd = 0.0f, rc = 0.0f, f1 = 0.0f, tgn, pfn, p0 = 0.0f, p1 = 0.0f;
+  const float* gcp = !BAND && clouds && !fused ? src.gc : nullptr;  // the cells' cloud values, if handed over
+  float cvn = 0.0f;
   bool pend = false;  // a layer's weighted radiances wait in p0, p1 (the same in every lane)
   gas_at<MODE>(src, layer_on_net<MODE>(src, nl - 1), nl - 1, g, tgn, pfn);
+  if (gcp) cvn = gcp[(nl - 1) * GB_NGPT + g];
   for (int lay = nl - 1; lay >= 0; --lay) {
-    const float tg = tgn, pf = pfn;
-    if (lay > 0) gas_at<MODE>(src, layer_on_net<MODE>(src, lay - 1), lay - 1, g, tgn, pfn);  // in flight meanwhile
+    const float tg = tgn, pf = pfn, cv = cvn;
+    if (lay > 0) {  // in flight meanwhile
+      gas_at<MODE>(src, layer_on_net<MODE>(src, lay - 1), lay - 1, g, tgn, pfn);
+      if (gcp) cvn = gcp[(lay - 1) * GB_NGPT + g];
+    }
     const float4 r = S.L[lay].rec[band];
     const float od = fmaxf(sd * (tg + r.w), 0.0f);
     const Clr c = clear_cell(T, od);
@@ -1078,7 +1125,8 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
         const bool one = S.L[lay].cbits[warp] & bit;
         if (one || (!fused && (S.fbits(lay)[warp] & bit))) {
           float odcld, efcl, atot, x;
-          const float cldf = cell_cloud(a, S, icol, g, lay, band, sd, one, T, odcld, efcl);
+          const float cldf = gcp ? cell_from_value(one, cv, sd, odcld, efcl)
+                                 : cell_cloud(a, S, icol, g, lay, band, sd, one, T, odcld, efcl);
           cloud_total(T, c, od, odcld, atot, x);
           A = 1.0f - fmaf(efcl, 1.0f - c.atrans, c.atrans);
           B = fmaf(cldf, fmaf(pf * fmaf(x, r.y, r.x), atot, -gsd), gsd);
@@ -1120,9 +1168,13 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
   float q0 = 0.0f, q1 = 0.0f, q2 = 0.0f, q3 = 0.0f;
   pend = false;  // a layer's weighted values wait in q0..q3
   gas_at<MODE>(src, layer_on_net<MODE>(src, 0), 0, g, tgn, pfn);
+  if (gcp) cvn = gcp[g];
   for (int lay = 0; lay < nl; ++lay) {
-    const float tg = tgn, pf = pfn;
-    if (lay + 1 < nl) gas_at<MODE>(src, layer_on_net<MODE>(src, lay + 1), lay + 1, g, tgn, pfn);
+    const float tg = tgn, pf = pfn, cv = cvn;
+    if (lay + 1 < nl) {
+      gas_at<MODE>(src, layer_on_net<MODE>(src, lay + 1), lay + 1, g, tgn, pfn);
+      if (gcp) cvn = gcp[(lay + 1) * GB_NGPT + g];
+    }
     const float4 r = S.L[lay].rec[band];
     const float od = fmaxf(sd * (tg + r.w), 0.0f);
     const Clr c = clear_cell(T, od);
@@ -1164,7 +1216,8 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
         const bool one = S.L[lay].cbits[warp] & bit;
         if (one || (!fused && (S.fbits(lay)[warp] & bit))) {
           float odcld, efcl, atot, x;
-          const float cldf = cell_cloud(a, S, icol, g, lay, band, sd, one, T, odcld, efcl);
+          const float cldf = gcp ? cell_from_value(one, cv, sd, odcld, efcl)
+                                 : cell_cloud(a, S, icol, g, lay, band, sd, one, T, odcld, efcl);
           cloud_total(T, c, od, odcld, atot, x);
           A = 1.0f - fmaf(efcl, 1.0f - c.atrans, c.atrans);
           B = fmaf(cldf, fmaf(pf * fmaf(x, r.z, r.x), atot, -gsu), gsu);
@@ -1330,6 +1383,7 @@ __global__ void __launch_bounds__(RT_NT, MINB) lw_full_kernel(const __grid_const
     GasSrc src{};
     src.gt = gt;
     src.gf = gf;
+    src.gc = B.gcld ? B.gcld + (long long)blockIdx.x * B.gstride : nullptr;
     if (LIST && a.sur_flag) {
       const long long row = icol * a.nlay * GB_NGPT;
       src.nt = a.sur_tau + row;
@@ -1500,7 +1554,7 @@ long long gb_lw_gas_slots(int nlay, long long ncols) {
   return (long long)device_sms() * kMaxPerSm;  // one per resident block of the fused or hand-over kernel
 }
 
-size_t gb_lw_gas_bytes(int nlay, long long slots) { return (size_t)slots * 2 * nlay * GB_NGPT * sizeof(float); }
+size_t gb_lw_gas_bytes(int nlay, long long slots) { return (size_t)slots * 3 * nlay * GB_NGPT * sizeof(float); }
 
 long long gb_lw_list_slots() { return (long long)device_sms() * gb::LIST_PER_SM; }
 

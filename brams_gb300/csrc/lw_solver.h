@@ -68,6 +68,8 @@ struct LwBatch {
   long long col0[GB_LW_MAX_GRIDS + 1];
   float* gtau = nullptr;                  // gas-optics hand-over (see above)
   float* gfrac = nullptr;
+  float* gcld = nullptr;                  // caller sub-columns: each cloudy cell's optical depth
+                                          // (or fractional cldfmcl), same slots; may be NULL
   long long gstride = 0;                  // floats per slot (>= nsmax * 140)
   long long gslots = 0;                   // slots available
   long long* fall = nullptr;              // columns handed over off the network
@@ -92,7 +94,7 @@ size_t gb_lw_smem_bytes(int nlay);
 int gb_lw_slots(int nlay, int variant = 0, bool lean = false);
 // hand-over slots a batch is solved with (one per resident block)
 long long gb_lw_gas_slots(int nlay, long long ncols);
-// bytes of a hand-over buffer of `slots` slots (taug and fractions, fp32)
+// bytes of a hand-over buffer of `slots` slots (taug, fractions and cell clouds, fp32)
 size_t gb_lw_gas_bytes(int nlay, long long slots);
 // hand-over slots the hand-over kernel of a learned batch uses (one per block)
 long long gb_lw_list_slots();
