@@ -1006,15 +1006,13 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
     // patterns: == 1, /= 0, >= 1e-20
     const long long kOne = 0x3FF0000000000000LL, kInf = 0x7FF0000000000000LL;
     const long long kMin = __double_as_longlong(1.0e-20);
-    // the four McICA arrays of a layer are read together (several layers in
-    // flight); where the transfer has a cloud plane, each cloudy cell's
-    // optical depth is formed here once instead of in both passes
-#pragma unroll 2
+    // where the transfer has a cloud plane, each cloudy cell's optical depth
+    // is formed here once (from the water paths read for the checks anyway)
+    // instead of in both passes
+#pragma unroll 4
     for (int lay = 0; lay < nl; ++lay) {
       const long long o = g + GB_NGPT * (icol + a.ld * lay);
       const double cfv = live ? __ldg(a.cldfmcl + o) : 0.0;
-      const double ciwp = live ? __ldg(a.ciwpmcl + o) : 0.0, clwp = live ? __ldg(a.clwpmcl + o) : 0.0;
-      const double tin = live ? __ldg(a.taucmcl + o) : 0.0;
       const long long cb = __double_as_longlong(cfv);
       const bool one = cb == kOne;
       const bool frac = !one && (cb << 1) != 0LL;  // neither +-0 nor 1 (NaN included, as /= 0 is)
@@ -1023,8 +1021,10 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
         S.L[lay].cbits[warp] = m1;
         S.fbits(lay)[warp] = mf;
       }
-      if (src.gc && (one || frac)) src.gc[lay * GB_NGPT + g] = cell_value(a, S, lay, band, one, cfv, ciwp, clwp, tin, T);
       if (cb >= kMin && cb <= kInf) {  // cldfmc >= cldmin (cldprmc.f90:178)
+        const double ciwp = __ldg(a.ciwpmcl + o), clwp = __ldg(a.clwpmcl + o);
+        const double tin = __ldg(a.taucmcl + o);
+        if (src.gc) src.gc[lay * GB_NGPT + g] = cell_value(a, S, lay, band, one, cfv, ciwp, clwp, tin, T);
         const long long tb = __double_as_longlong(tin);
         if (ciwp + clwp >= 1.e-20 || (tb >= kMin && tb <= kInf)) {
           const int e = S.L[lay].lfl;
@@ -1034,6 +1034,8 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
             if ((__double_as_longlong(clwp) << 1) != 0LL && (e >> 8)) err = e >> 8;      // clwp /= 0
           }
         }
+      } else if (src.gc && frac) {
+        src.gc[lay * GB_NGPT + g] = (float)cfv;  // a fraction below cldmin: cldfmcl itself, no cloud optics
       }
     }
     __syncthreads();
