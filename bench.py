@@ -1151,6 +1151,12 @@ def abi_block(ctx, dev, stream, args, rank, world, hbm):
     def step():
         ctx.rrtmg_lw_device(ncol, nlay, d, stream=stream)
 
+    # the autotuner picks the launch shape for this layer count and kind (caller sub-columns)
+    shape = None
+    if not args.no_tune:
+        from brams_gb300 import rrtmg_lw as R
+        shape = ctx.autotune([R.grid_desc(ncol, nlay, d, cloud_mode=R.CLOUD_SUBCOL)],
+                             sample_cols=min(ncol, 16384), reps=2, stream=stream)
     for _ in range(args.warmup):
         step()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -1190,6 +1196,8 @@ def abi_block(ctx, dev, stream, args, rank, world, hbm):
                          "traffic": traffic_from_profiles("lw_full_kernel_drop_in_traffic.txt"), "alg_bytes_per_launch": alg},
             "e2e": {"value": world * ncol / t_e2e, "unit": "columns/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "host_path_matches_device_path": same},
+            "launch_shape": ({k: shape[k] for k in ("threads", "min_blocks", "blocks_per_sm")} if shape
+                             else "default"),
             "column_status": status}
 
 

@@ -1006,14 +1006,10 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
     // patterns: == 1, /= 0, >= 1e-20
     const long long kOne = 0x3FF0000000000000LL, kInf = 0x7FF0000000000000LL;
     const long long kMin = __double_as_longlong(1.0e-20);
-    // where the transfer has a cloud plane, each cloudy cell's optical depth
-    // is formed here once (from the water paths read for the checks anyway)
-    // instead of in both passes
-#pragma unroll 4
+#pragma unroll 8
     for (int lay = 0; lay < nl; ++lay) {
       const long long o = g + GB_NGPT * (icol + a.ld * lay);
-      const double cfv = live ? __ldg(a.cldfmcl + o) : 0.0;
-      const long long cb = __double_as_longlong(cfv);
+      const long long cb = live ? __double_as_longlong(__ldg(a.cldfmcl + o)) : 0LL;
       const bool one = cb == kOne;
       const bool frac = !one && (cb << 1) != 0LL;  // neither +-0 nor 1 (NaN included, as /= 0 is)
       const unsigned m1 = __ballot_sync(FULL, one), mf = __ballot_sync(FULL, frac);
@@ -1021,6 +1017,20 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
         S.L[lay].cbits[warp] = m1;
         S.fbits(lay)[warp] = mf;
       }
+    }
+    __syncwarp();
+    // then, per cell with a cloud (independent iterations, so that several
+    // cells' loads are in flight): the water paths for cldprmc's checks and,
+    // where the transfer has a cloud plane, the cell's optical depth formed
+    // once instead of in both passes
+    const unsigned mybit = 1u << lane;
+#pragma unroll 4
+    for (int lay = 0; lay < nl; ++lay) {
+      const bool one = S.L[lay].cbits[warp] & mybit, frac = S.fbits(lay)[warp] & mybit;
+      if (!(one || frac)) continue;
+      const long long o = g + GB_NGPT * (icol + a.ld * lay);
+      const double cfv = one ? 1.0 : __ldg(a.cldfmcl + o);
+      const long long cb = __double_as_longlong(cfv);
       if (cb >= kMin && cb <= kInf) {  // cldfmc >= cldmin (cldprmc.f90:178)
         const double ciwp = __ldg(a.ciwpmcl + o), clwp = __ldg(a.clwpmcl + o);
         const double tin = __ldg(a.taucmcl + o);
@@ -1034,7 +1044,7 @@ __device__ bool rt_column(const LwArgs& a, long long icol, const RtSmem& S, cons
             if ((__double_as_longlong(clwp) << 1) != 0LL && (e >> 8)) err = e >> 8;      // clwp /= 0
           }
         }
-      } else if (src.gc && frac) {
+      } else if (src.gc) {
         src.gc[lay * GB_NGPT + g] = (float)cfv;  // a fraction below cldmin: cldfmcl itself, no cloud optics
       }
     }
