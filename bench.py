@@ -535,7 +535,7 @@ def gpu_arm(args, rank, world):
     log("non-McICA driver at 360x300x45")
     nomc = None if args.no_batched else nomcica_block(ctx, dev, stream, args)
     log("shortwave at 360x300x45")
-    sw = None if args.no_batched else sw_block(ctx, dev, stream, args)
+    sw = None if args.no_sw else sw_block(ctx, dev, stream, args)
 
     # ---------------- drop-in block (ABI mode, 360x300x45)
     log("drop-in block")
@@ -994,7 +994,7 @@ def sw_block(ctx, dev, stream, args):
     import pyoracle
 
     ctx.sw_ini(1004.0)
-    st = make_state(workload_spec("drop_in_360x300x45"))
+    st = make_state(workload_spec("drop_in_360x300x45", ncol=args.sw_ncol))
     ncol, nlay = st["play"].shape
     rng = np.random.default_rng(2024)
     for k in ("asdir", "asdif", "aldir", "aldif"):
@@ -1041,7 +1041,8 @@ def sw_block(ctx, dev, stream, args):
                                   *[o[k].data_ptr() for k in R.SW_OUT], ncol, ncol, None)
         assert rc == 0
 
-    res = {"workload": "rrtmg_sw (McICA, icld 3, iaer 10, iceflag 3, liqflag 1), 360x300 columns x 45 layers of "
+    res = {"workload": "rrtmg_sw (McICA, icld 3, iaer 10, iceflag 3, liqflag 1), "
+                       + ("360x300 columns" if ncol == NCOL else f"{ncol} columns") + " x 45 layers of "
                        "device arrays; mcica_subcol_sw on the device with per-column seeds; the solver in both "
                        "precisions of its column kernel: rrtmg_sw = fp32 gas optics, cloud optics and two-stream "
                        "solution with fp64 flux sums and heating rates (the default), rrtmg_sw_fp64 = fp64 "
@@ -1061,6 +1062,13 @@ def sw_block(ctx, dev, stream, args):
         return {"value": ncol / t, "unit": "columns/s", "ms_per_step": t * 1e3}
 
     res["mcica_subcol_sw"] = timed(mcica)
+    if args.no_cpu:  # both precisions timed, no oracle
+        for name, bits in (("rrtmg_sw", 32), ("rrtmg_sw_fp64", 64)):
+            ctx.sw_set_precision(bits)
+            res[name] = timed(solve)
+            res[name]["column_status"] = ctx.sync_status(stream)
+        ctx.sw_set_precision(32)
+        return res
     n = 256
     sub = {k: np.asfortranarray(v[:n]) for k, v in st.items()}
     mc = {k: np.asfortranarray(v.cpu().numpy().T[:, :n] if v.dim() == 3 else v.cpu().numpy().T[:n])
@@ -1212,6 +1220,8 @@ def main():
     ap.add_argument("--no-abi", action="store_true", help="skip the 360x300x45 drop-in block")
     ap.add_argument("--no-tune", action="store_true", help="default launch shapes instead of the autotuner's")
     ap.add_argument("--abi-ncol", type=int, default=NCOL, help="columns of the drop-in block")
+    ap.add_argument("--sw-ncol", type=int, default=NCOL, help="columns of the shortwave block")
+    ap.add_argument("--no-sw", action="store_true", help="skip the shortwave block")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the nested-grid, 512x512x45 and non-McICA blocks")
     args = ap.parse_args()
