@@ -89,6 +89,27 @@ def test_rrtmg_lw_parity(ctx, nlay, ptop):
     _assert_tol(_compare(out, ref))
 
 
+def test_fractional_subcolumn_cells(ctx):
+    """Caller sub-columns are not only 0 or 1: rtrnmc gives a cell whose
+    cldfmcl is a fraction no cloud optical depth but weights its cloudy
+    source by the fraction (rrtmg_lw_rtrnmc.f90:300-312, 380-455); cells at
+    and below cldmin and fractions next to cloudy cells of the same layer go
+    through the transfer's cloud hand-over as the fraction itself."""
+    st, tauc = _case(48, 45, seed=321, t_noise=3.0, h2o_sigma=0.4, cloud_prob=0.8)
+    mc = pyoracle.mcica_per_column(st, tauc, icld=3, base_seed=3)
+    rng = np.random.default_rng(9)
+    cf = np.array(mc["cldfmcl"], order="F")
+    pick = rng.uniform(size=cf.shape) < 0.15
+    vals = rng.choice(np.array([0.3, 0.75, 1e-20, 1e-25, 0.999]), size=cf.shape)
+    cf[pick] = vals[pick]
+    mc = dict(mc)
+    mc["cldfmcl"] = np.asfortranarray(cf)
+    assert ((cf > 0) & (cf < 1)).sum() > 1000 and (cf == 1.0).sum() > 1000
+    ref = pyoracle.rrtmg_lw(st, mc, nthreads=4)
+    out = ctx.rrtmg_lw(st, mc)
+    _assert_tol(_compare(out, ref))
+
+
 def test_clear_sky_equals_total_without_clouds(ctx):
     st, tauc = _case(32, 45, seed=5)
     st["cldfrac"][:] = 0.0
