@@ -87,6 +87,7 @@ def abi_bytes_per_column(nlay: int) -> int:
 # FP32 peak of a GB300 by its nominal figures (no measured FP32 peak is
 # available): 152 SMs x 128 FP32 lanes x 2 operations (FMA) x 2.07 GHz
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+FP64_PEAK_TFLOPS = 1.25  # GB300 dense FP64, nominal
 
 
 def counted_flops(st: dict, mc: dict) -> dict:
@@ -1074,9 +1075,19 @@ def sw_block(ctx, dev, stream, args):
     mc = {k: np.asfortranarray(v.cpu().numpy().T[:, :n] if v.dim() == 3 else v.cpu().numpy().T[:n])
           for k, v in m.items()}
     ref = pyoracle.rrtmg_sw(sub, mc, icld=3, iaer=10, native=True, nthreads=os.cpu_count() or 1)
+    # operations per column counted on the oracle's code path (64 of the sampled columns)
+    cs = {k: np.asfortranarray(v[:64]) for k, v in sub.items()}
+    cm = {k: np.asfortranarray(v[:, :64] if v.ndim == 3 else v[:64]) for k, v in mc.items()}
+    flops = pyoracle.sw_flops_per_column(cs, cm, icld=3, iaer=10)
     for name, bits in (("rrtmg_sw", 32), ("rrtmg_sw_fp64", 64)):
         ctx.sw_set_precision(bits)
         res[name] = timed(solve)
+        peak = FP32_PEAK_TFLOPS if bits == 32 else FP64_PEAK_TFLOPS
+        ach = flops * res[name]["value"] / 1e12
+        res[name]["roofline"] = {"bound": f"fp{bits}", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                                 "frac": ach / peak, "flops_per_column": flops, "peak_source": "nominal",
+                                 "counted_by": "oracle/flop_count.h on the shortwave restatement (a division "
+                                               "or square root counts as one operation)"}
         res[name]["column_status"] = ctx.sync_status(stream)
         got = {k: v.cpu().numpy().T[:n] for k, v in o.items()}
         res[name]["accuracy"] = {

@@ -263,16 +263,22 @@ SW_CLOUD = ["cldfmcl", "taucmcl", "ssacmcl", "asmcmcl", "fsfcmcl", "ciwpmcl", "c
 SW_OUT = ["swuflx", "swdflx", "swhr", "swuflxc", "swdflxc", "swhrc"]
 
 
-def sw_lib(native: bool = False):
-    """The SW oracle (sw_oracle.cpp), built on first use and initialised with cpdair 1004."""
-    key = "sw_native" if native else "sw"
+def sw_lib(native: bool = False, count: bool = False):
+    """The SW oracle (sw_oracle.cpp), built on first use and initialised with
+    cpdair 1004; count=True: the copy whose arithmetic counts its operations
+    (flop_count.h, single-threaded use)."""
+    key = "sw_count" if count else ("sw_native" if native else "sw")
     if key in _lib:
         return _lib[key]
-    path = os.path.join(HERE, "_build", "libsworacle_native.so" if native else "libsworacle.so")
+    name = "libsworacle_count.so" if count else ("libsworacle_native.so" if native else "libsworacle.so")
+    path = os.path.join(HERE, "_build", name)
     src = os.path.join(HERE, "sw_oracle.cpp")
     if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
         subprocess.run(["make", "-s", "-C", HERE, os.path.join("_build", os.path.basename(path))], check=True)
     L = C.CDLL(path)
+    if count:
+        L.ora_flops.restype = C.c_uint64
+        L.ora_flops.argtypes = [C.c_int]
     L.ora_sw_init.restype = C.c_int
     L.ora_sw_init.argtypes = [C.c_double, C.c_char_p]
     if L.ora_sw_init(1004.0, os.path.join(DATA, "sw_tables.gbsw").encode()) != 0:
@@ -283,13 +289,13 @@ def sw_lib(native: bool = False):
 
 def rrtmg_sw(state: dict, mc: dict | None, icld: int = 3, iaer: int = 10, adjes: float = 1.0, dyofyr: int = 0,
              scon: float = 1368.22, isolvar: int = -1, inflgsw: int = 2, iceflgsw: int = 3, liqflgsw: int = 1,
-             nthreads: int = 1, native: bool = False) -> dict:
+             nthreads: int = 1, native: bool = False, _count: bool = False) -> dict:
     """rrtmg_sw (rrtmg_sw_rad.f90:243) on Fortran-ordered arrays: state keys
     SW_STATE ((ncol, nlay), (ncol, nlay+1), (ncol,)), aerosols 'tauaer_sw',
     'ssaaer_sw', 'asmaer_sw' (ncol, nlay, 14), McICA arrays SW_CLOUD ((112,
     ncol, nlay); reicmcl/relqmcl (ncol, nlay)).  Returns the outputs, icld,
     iaer."""
-    L = sw_lib(native)
+    L = sw_lib(native, count=_count)
     ncol, nlay = state["play"].shape
     st = [_f(state[k]) for k in SW_STATE]
     z3 = np.zeros((112, ncol, nlay), order="F")
@@ -310,6 +316,16 @@ def rrtmg_sw(state: dict, mc: dict | None, icld: int = 3, iaer: int = 10, adjes:
         raise RuntimeError(f"SW oracle status {rc}")
     out["icld"], out["iaer"] = ic.value, ia.value
     return out
+
+
+def sw_flops_per_column(state: dict, mc: dict | None, **kw) -> float:
+    """Floating-point operations (additions, subtractions, multiplications,
+    divisions) the SW restatement executes per column: the counting copy of
+    the oracle (flop_count.h) runs rrtmg_sw single-threaded on these columns."""
+    L = sw_lib(count=True)
+    L.ora_flops_reset()
+    rrtmg_sw(state, mc, nthreads=1, _count=True, **kw)
+    return L.ora_flops(-1) / state["play"].shape[0]
 
 
 def mcica_subcol_sw(state: dict, band: dict, icld: int, permuteseed: int, irng: int = 1) -> dict:

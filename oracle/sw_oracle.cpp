@@ -201,7 +201,7 @@ void inatm_sw(const Args& a, int iplon, Col& c) {
   // solar variability option -1 (BRAMS): solvar = scon / rrsw_scon if scon > 0 else 1 (:905-939)
   double adjflx = a.adjes;
   if (a.dyofyr > 0) adjflx = earth_sun(a.dyofyr);
-  const double solvar = a.scon > 0.0 ? a.scon / rrsw_scon : 1.0;
+  const double solvar = a.scon > 0.0 ? a.scon / rrsw_scon : double(1.0);
   for (int ib = 16; ib <= 29; ++ib) c.adjflux[ib] = adjflx * solvar;
   c.tbound = a.tsfc[iplon - 1];
   c.pz[0] = a.plev[(iplon - 1)];
@@ -812,7 +812,7 @@ void reftra_sw(int nlayers, const std::vector<char>& lrtchk, const double* pgg, 
       const double za = zgamma1 * prmuz;
       const double za1 = za - zgamma3;
       const double zgt = zgamma1 * zto1;
-      const double ze1 = std::min(zto1 / prmuz, 500.0);
+      const double ze1 = std::min<double>(zto1 / prmuz, 500.0);
       const double ze2 = expo(ze1);
       pref[jk] = (zgt - za1 * (1.0 - ze2)) / (1.0 + zgt);
       ptra[jk] = 1.0 - pref[jk];
@@ -846,8 +846,8 @@ void reftra_sw(int nlayers, const std::vector<char>& lrtchk, const double* pgg, 
       const double zt4 = zr4;
       const double zt5 = zr5;
       const double zbeta = (zgamma1 - zrk) / zrkg;
-      const double ze1 = std::min(zrk * zto1, 500.0);
-      const double ze2 = std::min(zto1 / prmuz, 500.0);
+      const double ze1 = std::min<double>(zrk * zto1, 500.0);
+      const double ze2 = std::min<double>(zto1 / prmuz, 500.0);
       const double zem1 = expo(ze1);
       const double zep1 = 1.0 / zem1;
       const double zem2 = expo(ze2);

@@ -34,3 +34,20 @@ def test_phase_counts():
     st2, mc2 = _case(8, 90, 4)
     r2 = pyoracle.flops_per_column(st2, mc2)
     assert 1.6 < r2["rtrnmc"] / r["rtrnmc"] < 2.4
+
+
+def test_sw_counting_copy():
+    """The shortwave restatement's counting copy: the oracle's outputs, and a
+    count per column that grows with the layers (cells of 112 g-points)."""
+    from test_sw import sw_mcica, sw_state
+
+    st, st2 = sw_state(ncol=6, nlay=30, seed=3, cloud_prob=0.6), sw_state(ncol=6, nlay=60, seed=3, cloud_prob=0.6)
+    mc, mc2 = sw_mcica(st, seed=2), sw_mcica(st2, seed=2)
+    ref = pyoracle.rrtmg_sw(st, mc, icld=3, iaer=10)
+    got = pyoracle.rrtmg_sw(st, mc, icld=3, iaer=10, _count=True)
+    for k in ("swuflx", "swdflx", "swhr", "swuflxc", "swdflxc", "swhrc"):
+        assert np.array_equal(got[k], ref[k]), k
+    f1 = pyoracle.sw_flops_per_column(st, mc, icld=3, iaer=10)
+    f2 = pyoracle.sw_flops_per_column(st2, mc2, icld=3, iaer=10)
+    assert 100 < f1 / (30 * 112) < 1000
+    assert 1.6 < f2 / f1 < 2.4
