@@ -156,7 +156,15 @@ __device__ __forceinline__ int tbl_index(float od) {
 __device__ __forceinline__ float2 tbl_tt(const float* __restrict__ T, int itr) {
   return __ldg(reinterpret_cast<const float2*>(T + c_T.tbl_tt) + itr);
 }
-__device__ __forceinline__ float tbl_tau(const float* __restrict__ T, int itr) { return __ldg(T + c_T.tbl_tau + itr); }
+// tau_tbl at an index formed in registers, bpade * t / (1 - t) at t = itr /
+// 10000 (1e10 at the last entry; rrtmg_lw_init.f90:120-142), instead of a
+// table load that depends on the clear cell's lookup (fp32 arithmetic: within
+// a few units in the last place of the fp64-built table's float)
+__device__ __forceinline__ float tbl_tau(const float* __restrict__ T, int itr) {
+  (void)T;
+  const float t = (float)itr * 1.0e-4f;
+  return itr >= 10000 ? 1.0e10f : BPADE * t / (1.0f - t);
+}
 
 // cldprmc's optical depth ciwp*abscoice + clwp*abscoliq of one cell
 // (cldprmc.f90:194-266; the radius bounds are checked beforehand), from
