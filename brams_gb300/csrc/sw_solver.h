@@ -29,7 +29,7 @@ int gb_sw_load(gb_lw_context* ctx, double cpdair, const char* table_dir);
 
 // blocks per SM of the column kernel in each precision (its launch bounds)
 #define SW_MINB_F64 4
-#define SW_MINB_F32 5
+#define SW_MINB_F32 6
 // persistent blocks (= scratch slots) for a device of num_sms SMs, and the
 // scratch bytes of `slots` slots, for a precision of 32 or 64 bits
 long long gb_sw_slots(int num_sms, int bits);
