@@ -380,7 +380,9 @@ int gb_rrtmg_lw_graph_destroy(gb_lw_graph* graph);
  * passes -1) and iaer 0 or 10 (ecaer, for iaer 6, is not read); cloud
  * options inflag 0 or 2 with iceflag 1-3 and liqflag 1 (the reference
  * leaves the coefficients of ice option 0 and liquid option 0 unset).  The
- * whole path is fp64.  tlev, tsfc and n2ovmr are not used by the reference's
+ * arithmetic is the context's shortwave precision (gb_rrtmg_sw_set_precision:
+ * fp32 solution with fp64 sums by default, or fp64 throughout).  tlev, tsfc
+ * and n2ovmr are not used by the reference's
  * shortwave computation and may be NULL. */
 int gb_rrtmg_sw_ini(gb_lw_context* ctx, double cpdair, const char* table_dir);
 /* Precision of the shortwave column kernel of this context: 32 (the
