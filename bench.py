@@ -34,9 +34,11 @@ transfer with FP64 heating rates.  One step solves every column once by:
                   plain path
   nomcica      -- the non-McICA driver (cldprop, taumol, random or
                   maximum/random overlap) on 360x300x45 device arrays
-  shortwave    -- RRTMG_SW (McICA generator and solver) on 360x300x45 device
-                  arrays, its error against the FP64 oracle and the oracle's
-                  throughput on the host cores
+  shortwave    -- RRTMG_SW (McICA generator and solver in both precisions)
+                  on 360x300x45 device arrays (--sw-ncol), their error
+                  against the FP64 oracle, FP32/FP64 rooflines from counted
+                  operations and the oracle's throughput on the host cores
+                  (--no-sw skips it, --no-cpu its oracle parts)
   plain_abi    -- the drop-in path on the 360x300x45 BRAMS-scale workload:
                   gb_rrtmg_lw_device on the reference's (140, ncol, nlay)
                   McICA arrays, its roofline against 8*(600*nlay + 25) bytes
