@@ -10,7 +10,9 @@
 // tcgen05.ld (warp w: TMEM lanes 32*(w%4).., column quarter w/4), apply bias and
 // SiLU, and write the next layer's operand tile.  The output layer
 // (N = 288 = 2 x 144) is un-standardised and written as binary16 per
-// (column, layer) in the layout the column kernel reads.
+// (column, layer) in the layout the column kernel reads.  The next tile's
+// features are formed while the output layer's MMAs run, and its raw inputs
+// loaded (into registers) a tile ahead.
 //
 // Every wait on the mbarrier is bounded; a wait that runs out records an
 // error flag, and the kernel frees its tensor memory and returns.
@@ -104,16 +106,41 @@ __device__ __forceinline__ bool wait_parity(uint32_t bar, uint32_t parity) {
   return false;
 }
 
-__device__ __forceinline__ void ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
+// 16 accumulator columns of the warp's 32 lanes, without waiting: the values
+// are defined only after wait_ld16 / wait_ld32 on the same registers
+__device__ __forceinline__ void ld16_async(uint32_t taddr, uint32_t* r) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
         "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// wait for the thread's tensor-memory loads; the registers they fill are
+// read-write operands, so no use of them moves above the wait
+__device__ __forceinline__ void wait_ld16(uint32_t* r) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
+               :
+               : "memory");
+}
+__device__ __forceinline__ void wait_ld32(uint32_t* a, uint32_t* b) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n"
+               : "+r"(a[0]), "+r"(a[1]), "+r"(a[2]), "+r"(a[3]), "+r"(a[4]), "+r"(a[5]), "+r"(a[6]), "+r"(a[7]),
+                 "+r"(a[8]), "+r"(a[9]), "+r"(a[10]), "+r"(a[11]), "+r"(a[12]), "+r"(a[13]), "+r"(a[14]), "+r"(a[15]),
+                 "+r"(b[0]), "+r"(b[1]), "+r"(b[2]), "+r"(b[3]), "+r"(b[4]), "+r"(b[5]), "+r"(b[6]), "+r"(b[7]),
+                 "+r"(b[8]), "+r"(b[9]), "+r"(b[10]), "+r"(b[11]), "+r"(b[12]), "+r"(b[13]), "+r"(b[14]), "+r"(b[15])
+               :
+               : "memory");
+}
+
+// layer and column of row r of the layer-major row space (32-bit division
+// where the row index fits, the 64-bit one otherwise; both exact)
+__device__ __forceinline__ int row_layer(long long r, int ncol, long long& icol) {
+  const int lay = r <= 0x7fffffffLL ? (int)((uint32_t)r / (uint32_t)ncol) : (int)(r / ncol);
+  icol = r - (long long)lay * ncol;
+  return lay;
 }
 
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
@@ -130,10 +157,15 @@ __device__ __forceinline__ float ex2(float x) {
 // silu(acc + bias) of 32 consecutive hidden units (from n0) of this thread's
 // row, into the next layer's operand tile
 __device__ __forceinline__ void hidden_epilogue(uint32_t tcol, int row, int n0, const float* bias, char* hbase) {
+  uint32_t r[32];  // both 16-column loads in flight before the one wait
+  ld16_async(tcol, r);
+  ld16_async(tcol + 16, r + 16);
+  wait_ld32(r, r + 16);
 #pragma unroll
   for (int c16 = 0; c16 < 2; ++c16) {
     float v[16];
-    ld16(tcol + c16 * 16, v);
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[c16 * 16 + i]);
     float b[16];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {  // n0 is a multiple of 32 and bias 16-byte aligned
@@ -203,56 +235,75 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
   const uint32_t tlane = tmem + ((uint32_t)(q * 32) << 16);     // TMEM address of the warp's lane quarter
   const long long rows = (long long)g.ncol * g.nlay;
   const long long ntile = (rows + M - 1) / M;
+  constexpr int NCH = 2 * (NOH / 16);  // output chunks of 16 columns
   uint32_t phase = 0;
-  // inputs of this thread's row of the next tile, loaded one tile ahead
+  // inputs of this thread's row of tile t (rows are layer-major: coalesced loads)
   auto fetch = [&](long long t) {
     gbmlp::RawLayer rw{};
     const long long r = t * M + tid;
     if (tid < M && t < ntile && r < rows) {
-      const int lay = (int)(r / g.ncol);
-      const long long icol = r - (long long)lay * g.ncol;
+      long long icol;
+      const int lay = row_layer(r, g.ncol, icol);
       rw = gbmlp::load_raw(g.play, g.plev, g.tlay, g.tlev, g.h2ovmr, g.o3vmr, g.co2vmr, g.ch4vmr, g.n2ovmr, g.ld,
                            icol, lay);
     }
     return rw;
   };
-  gbmlp::RawLayer raw = fetch(blockIdx.x);
-  for (long long tile = blockIdx.x; tile < ntile && ok; tile += gridDim.x) {
+  // features of this thread's row of tile t from `raw`, standardised and
+  // packed as bf16 pairs into xp (rows past the end get the means); the row's
+  // flag (on the network or not) is stored here
+  gbmlp::RawLayer raw;
+  uint32_t xp[8];
+  auto features = [&](long long t) {
+    if (tid >= M) return;
+    const long long r = t * M + tid;
+    float f[GB_MLP_NF];
+    if (r < rows) {
+      long long icol;
+      const int lay = row_layer(r, g.ncol, icol);
+      gbmlp::raw_features(raw, grav, avogad, f);
+      flag[icol * g.nlay + lay] = gbmlp::in_range(f, nm) ? 1 : 0;
+    } else {
+#pragma unroll
+      for (int i = 0; i < GB_MLP_NF; ++i) f[i] = nm.in_mu[i];
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int j0 = 2 * i, j1 = 2 * i + 1;
+      const float x0 = j0 < GB_MLP_NF ? (f[j0] - nm.in_mu[j0]) / nm.in_sd[j0] : 0.0f;
+      const float x1 = j1 < GB_MLP_NF ? (f[j1] - nm.in_mu[j1]) / nm.in_sd[j1] : 0.0f;
+      xp[i] = gbmlp::pack_bf16(x0, x1);
+    }
+  };
+  // The first tile's features before the loop; every later tile's are formed
+  // (and its inputs for the tile after it loaded) while the output layer's
+  // MMAs of the tile before it run.
+  raw = fetch(blockIdx.x);
+  features(blockIdx.x);
+  raw = fetch(blockIdx.x + gridDim.x);
+  // A wait that runs out leaves `ok` false in its warp; every block-wide
+  // barrier below is also the vote that ends the kernel in all threads.
+  for (long long tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
     const long long r0 = tile * M;
-    __syncthreads();  // the previous tile's output staging (input and hidden tiles) is done
-    // ---- features of the tile's rows (rows are layer-major: coalesced loads)
+    if (__syncthreads_or(!ok)) {  // and the previous tile's output staging (input tile) is done
+      ok = false;
+      break;
+    }
     if (tid < M) {
-      const long long r = r0 + tid;
-      float f[GB_MLP_NF];
-      if (r < rows) {
-        const int lay = (int)(r / g.ncol);
-        const long long icol = r - (long long)lay * g.ncol;
-        gbmlp::raw_features(raw, grav, avogad, f);
-        flag[icol * g.nlay + lay] = gbmlp::in_range(f, nm) ? 1 : 0;
-      } else {
-#pragma unroll
-        for (int i = 0; i < GB_MLP_NF; ++i) f[i] = nm.in_mu[i];
-      }
-      uint32_t p[8];
-#pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const int j0 = 2 * i, j1 = 2 * i + 1;
-        const float x0 = j0 < GB_MLP_NF ? (f[j0] - nm.in_mu[j0]) / nm.in_sd[j0] : 0.0f;
-        const float x1 = j1 < GB_MLP_NF ? (f[j1] - nm.in_mu[j1]) / nm.in_sd[j1] : 0.0f;
-        p[i] = gbmlp::pack_bf16(x0, x1);
-      }
       char* xb = sm + OFF_X;
-      *reinterpret_cast<uint4*>(xb + sw128(M, tid, 0)) = make_uint4(p[0], p[1], p[2], p[3]);
-      *reinterpret_cast<uint4*>(xb + sw128(M, tid, 8)) = make_uint4(p[4], p[5], p[6], p[7]);
+      *reinterpret_cast<uint4*>(xb + sw128(M, tid, 0)) = make_uint4(xp[0], xp[1], xp[2], xp[3]);
+      *reinterpret_cast<uint4*>(xb + sw128(M, tid, 8)) = make_uint4(xp[4], xp[5], xp[6], xp[7]);
 #pragma unroll
       for (int c = 2; c < 8; ++c) *reinterpret_cast<uint4*>(xb + sw128(M, tid, 8 * c)) = make_uint4(0, 0, 0, 0);
     }
-    raw = fetch(tile + gridDim.x);  // consumed by the next tile; in flight during this one's layers
     // ---- four layers
     for (int l = 0; l < 4; ++l) {
       fence_async_smem();
       fence_before();
-      __syncthreads();
+      if (__syncthreads_or(!ok)) {
+        ok = false;
+        break;
+      }
       fence_after();
       if (tid == 0) {
         if (l == 0) {
@@ -274,13 +325,17 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
         }
         commit(bar_a);
       }
+      if (l == 3) {
+        features(tile + gridDim.x);
+        raw = fetch(tile + 2 * (long long)gridDim.x);
+      }
       ok = wait_parity(bar_a, phase);
       phase ^= 1u;
       fence_after();
-      if (__syncthreads_or(!ok)) {
-        ok = false;
-        break;
-      }
+      // warp-uniform, since the tensor-memory loads below are .sync.aligned;
+      // a warp whose wait ran out skips the epilogue and the next vote ends the kernel
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok) continue;
       if (l < 3) {
         hidden_epilogue(tlane + part * 32, row, part * 32, l == 0 ? b1 : (l == 1 ? b2 : b3), sm + OFF_H);
       } else {
@@ -288,13 +343,14 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
         const bool live = r < rows;
         long long o = 0;
         if (live) {
-          const int lay = (int)(r / g.ncol);
-          const long long icol = r - (long long)lay * g.ncol;
+          long long icol;
+          const int lay = row_layer(r, g.ncol, icol);
           o = (icol * g.nlay + lay) * GB_NGPT_MLP;
         }
-        // 18 chunks of 16 outputs (two halves of 144); warp quarter `part` takes chunks part, part+4, ...
-        // A chunk goes through shared memory (the free input and hidden tiles)
-        // as binary16: each lane puts its row's 16 values there (four 8-byte
+        // 18 chunks of 16 outputs (two halves of 144); warp quarter `part` takes chunks part, part+4, ...,
+        // two per wait for the tensor-memory loads.
+        // A chunk goes through shared memory (the free input tile) as
+        // binary16: each lane puts its row's 16 values there (four 8-byte
         // groups, group m of row r at slot m ^ ((r >> 2) & 3), so that neither
         // the puts nor the gets conflict on banks), then every store writes 32
         // contiguous bytes (16 outputs) of eight rows instead of 8 bytes of 32.
@@ -307,19 +363,17 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
           orow[k] = __shfl_sync(0xffffffffu, o, src);
           lrow[k] = __shfl_sync(0xffffffffu, live ? 1 : 0, src) != 0;
         }
-#pragma unroll 1
-        for (int c = part; c < 2 * (NOH / 16); c += 4) {
+        auto chunk_col = [](int c) { return (uint32_t)((c / (NOH / 16)) * 256 + (c % (NOH / 16)) * 16); };
+        auto out_chunk = [&](int c, const uint32_t* rv) {
           const int hh = c / (NOH / 16), c16 = c % (NOH / 16);
-          const int j0 = hh * NOH + c16 * 16;  // output index of v[0]
-          float v[16];
-          ld16(tlane + hh * 256 + c16 * 16, v);
+          const int j0 = hh * NOH + c16 * 16;  // output index of rv[0]
           const float4* sc = reinterpret_cast<const float4*>(oscale + j0);
           const float4* sh = reinterpret_cast<const float4*>(oshift + j0);
 #pragma unroll
           for (int m = 0; m < 4; ++m) {
             const float4 a = sc[m], b = sh[m];
-            float y0 = fmaf(v[4 * m], a.x, b.x), y1 = fmaf(v[4 * m + 1], a.y, b.y);
-            float y2 = fmaf(v[4 * m + 2], a.z, b.z), y3 = fmaf(v[4 * m + 3], a.w, b.w);
+            float y0 = fmaf(__uint_as_float(rv[4 * m]), a.x, b.x), y1 = fmaf(__uint_as_float(rv[4 * m + 1]), a.y, b.y);
+            float y2 = fmaf(__uint_as_float(rv[4 * m + 2]), a.z, b.z), y3 = fmaf(__uint_as_float(rv[4 * m + 3]), a.w, b.w);
             if (j0 + 4 * m < GB_NGPT_MLP) {  // groups of four never straddle 140
               y0 = fminf(ex2(y0), GB_MLP_HALF_MAX), y1 = fminf(ex2(y1), GB_MLP_HALF_MAX);
               y2 = fminf(ex2(y2), GB_MLP_HALF_MAX), y3 = fminf(ex2(y3), GB_MLP_HALF_MAX);
@@ -343,14 +397,28 @@ __global__ void __launch_bounds__(NT, 1) infer_tc_kernel(GbMlpGridIn g, GbMlpNor
             }  // four-output groups never straddle 140 or 280 (both multiples of 4)
           }
           __syncwarp();
+        };
+#pragma unroll 1
+        for (int c = part; c < NCH; c += 8) {
+          uint32_t ra[16], rb[16];
+          ld16_async(tlane + chunk_col(c), ra);
+          if (c + 4 < NCH) {  // warp-uniform
+            ld16_async(tlane + chunk_col(c + 4), rb);
+            wait_ld32(ra, rb);
+            out_chunk(c, ra);
+            out_chunk(c + 4, rb);
+          } else {
+            wait_ld16(ra);
+            out_chunk(c, ra);
+          }
         }
       }
     }
   }
-  if (!ok && tid == 0) atomicMax(err, GB_COL_TCWAIT);
   fence_before();
-  __syncthreads();
+  const bool failed = __syncthreads_or(!ok);  // a warp's wait in the last layer can have run out
   fence_after();
+  if (failed && tid == 0) atomicMax(err, GB_COL_TCWAIT);
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
 }
