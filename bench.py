@@ -189,10 +189,10 @@ def cpu_baseline(st, mc, max_seconds: float = 12.0):
     import pyoracle
 
     try:
-        pyoracle.build(native=True)
-        native = True
+        pyoracle.build(tuned=True)
+        tuned = True
     except Exception:
-        native = False
+        tuned = False
     cores = os.cpu_count() or 1
     ncol = st["play"].shape[0]
 
@@ -204,16 +204,16 @@ def cpu_baseline(st, mc, max_seconds: float = 12.0):
     probe = min(ncol, 64 * cores)
     s, m = sub(probe)
     t0 = time.perf_counter()
-    pyoracle.rrtmg_lw(s, m, nthreads=cores, native=native)
+    pyoracle.rrtmg_lw(s, m, nthreads=cores, tuned=tuned)
     dt = time.perf_counter() - t0
     n = int(min(ncol, max(probe, probe * max_seconds / max(dt, 1e-6))))
     s, m = sub(n)
     t0 = time.perf_counter()
-    pyoracle.rrtmg_lw(s, m, nthreads=cores, native=native)
+    pyoracle.rrtmg_lw(s, m, nthreads=cores, tuned=tuned)
     dt = time.perf_counter() - t0
     return {"value": n / dt, "unit": "columns/s", "cores": cores, "kind": "port",
             "sample": f"first {n} of {ncol} columns of the 360x300x45 workload, one pass, "
-                      f"{cores} threads, FP64 C++ restatement ({'-O3 native' if native else '-O2'})"}
+                      f"{cores} threads, FP64 C++ restatement ({'-O3, Neoverse V2 tuning on aarch64' if tuned else '-O2'})"}
 
 
 def reference_arm(args, rank, world):
@@ -227,7 +227,7 @@ def reference_arm(args, rank, world):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
-    pyoracle.build(native=True)
+    pyoracle.build(tuned=True)
     cores = os.cpu_count() or 1
     n = max(256, 256 * cores)
     st = make_state(ProfileSpec(ncol=n, nlay=NLAY5, seed=BASE_SEED, ptop=PTOP5, t_noise=4.0, h2o_sigma=0.5))
@@ -235,10 +235,10 @@ def reference_arm(args, rank, world):
     tauc = cldprop_numpy(st, tabs)
     mc = pyoracle.mcica_per_column(st, tauc, icld=3, base_seed=BASE_SEED)
     for _ in range(args.warmup):
-        pyoracle.rrtmg_lw(st, mc, nthreads=cores, native=True)
+        pyoracle.rrtmg_lw(st, mc, nthreads=cores, tuned=True)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        pyoracle.rrtmg_lw(st, mc, nthreads=cores, native=True)
+        pyoracle.rrtmg_lw(st, mc, nthreads=cores, tuned=True)
     dt = (time.perf_counter() - t0) / args.steps
     v = n / dt
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "columns/s", "n_gpus": world,
@@ -505,11 +505,11 @@ def gpu_arm(args, rank, world):
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import pyoracle
 
-        pyoracle.build(native=True)
+        pyoracle.build(tuned=True)
         c0 = nbase // 2
         st = wl.host_columns(0, c0, SAMPLE)
         mc = pyoracle.mcica_per_column(st, st["tauc"], icld=3, base_seed=wl.seed0(0) + c0)
-        ref = pyoracle.rrtmg_lw(st, mc, nthreads=os.cpu_count() or 1, native=True)
+        ref = pyoracle.rrtmg_lw(st, mc, nthreads=os.cpu_count() or 1, tuned=True)
         for name, o in (("surrogate", sur_out), ("plain", plain_out)):
             acc[name] = {"hr_rmse_k_per_day": float(np.sqrt(np.mean((o["hr"] - ref["hr"]) ** 2))),
                          "hr_max_k_per_day": float(np.abs(o["hr"] - ref["hr"]).max()),
@@ -743,21 +743,21 @@ def cpu_baseline_headline(wl, seconds: float = 12.0, max_cols: int = 16384):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
-    pyoracle.build(native=True)
+    pyoracle.build(tuned=True)
     cores = os.cpu_count() or 1
     n = min(wl.nbase, max_cols)
     st = wl.host_columns(0, 0, n)
     mc = pyoracle.mcica_per_column(st, st["tauc"], icld=3, base_seed=wl.seed0(0))
     done, t0 = 0, time.perf_counter()
     while True:
-        pyoracle.rrtmg_lw(st, mc, nthreads=cores, native=True)
+        pyoracle.rrtmg_lw(st, mc, nthreads=cores, tuned=True)
         done += n
         dt = time.perf_counter() - t0
         if dt >= seconds:
             break
     return {"value": done / dt, "unit": "columns/s", "cores": cores, "kind": "port",
             "sample": f"the first {n} columns of member 0 of the {NX}x{NY}x{NLAY5} workload, {done // n} passes "
-                      f"({dt:.1f} s), {cores} threads, FP64 C++ restatement (-O3 native); McICA sub-columns made "
+                      f"({dt:.1f} s), {cores} threads, FP64 C++ restatement (-O3, Neoverse V2 tuning on aarch64); McICA sub-columns made "
                       "beforehand, not timed"}
 
 
@@ -857,7 +857,7 @@ def batched_block(ctx, dev, stream, args, hbm):
         m = grids[gi * members]
         st = _host_of(m, 512)
         mc = pyoracle.mcica_per_column(st, st["tauc"], icld=3, base_seed=seeds[gi * members])
-        ref = pyoracle.rrtmg_lw(st, mc, nthreads=os.cpu_count() or 1, native=True)
+        ref = pyoracle.rrtmg_lw(st, mc, nthreads=os.cpu_count() or 1, tuned=True)
         acc[f"grid{gi}_member0"] = _errors(m.outputs(), ref, 512)
     alg = sum(fused_bytes_per_column(g.nlay, False) * g.ncol for g in grids)
     st45 = _host_of(grids[0], 16)
@@ -924,7 +924,7 @@ def eval_block(ctx, mlp, dev, stream, args):
     n = 2048
     sub = {k: np.asfortranarray(v[:n]) for k, v in st.items()}
     mc = pyoracle.mcica_per_column(sub, np.asfortranarray(tauc[:, :n]), icld=3, base_seed=seed0)
-    ref = pyoracle.rrtmg_lw(sub, mc, nthreads=os.cpu_count() or 1, native=True)
+    ref = pyoracle.rrtmg_lw(sub, mc, nthreads=os.cpu_count() or 1, tuned=True)
     res["learned"].update(_errors(gl.outputs(), ref, n))
     res["plain"].update(_errors(gp.outputs(), ref, n))
     res["layers_on_network"] = float(flag.float().mean().item())
@@ -976,7 +976,7 @@ def nomcica_block(ctx, dev, stream, args):
         torch.cuda.synchronize()
         t = e0.elapsed_time(e1) / 1e3 / args.steps
         got = {k: d[k].cpu().numpy().T for k in ("uflx", "dflx", "hr")}
-        ref = pyoracle.rrtmg_lw_nomcica(sub, icld, native=True)
+        ref = pyoracle.rrtmg_lw_nomcica(sub, icld, tuned=True)
         res[name] = {"value": ncol / t, "unit": "columns/s", "ms_per_step": t * 1e3, **_errors(got, ref, n)}
     res["column_status"] = ctx.sync_status(stream)
     return res
@@ -1077,7 +1077,7 @@ def sw_block(ctx, dev, stream, args):
     sub = {k: np.asfortranarray(v[:n]) for k, v in st.items()}
     mc = {k: np.asfortranarray(v.cpu().numpy().T[:, :n] if v.dim() == 3 else v.cpu().numpy().T[:n])
           for k, v in m.items()}
-    ref = pyoracle.rrtmg_sw(sub, mc, icld=3, iaer=10, native=True, nthreads=os.cpu_count() or 1)
+    ref = pyoracle.rrtmg_sw(sub, mc, icld=3, iaer=10, tuned=True, nthreads=os.cpu_count() or 1)
     # operations per column counted on the oracle's code path (64 of the sampled columns)
     cs = {k: np.asfortranarray(v[:64]) for k, v in sub.items()}
     cm = {k: np.asfortranarray(v[:, :64] if v.ndim == 3 else v[:64]) for k, v in mc.items()}
@@ -1105,10 +1105,10 @@ def sw_block(ctx, dev, stream, args):
     mcs = {k: np.asfortranarray(v.cpu().numpy().T[:, :nc] if v.dim() == 3 else v.cpu().numpy().T[:nc])
            for k, v in m.items()}
     cores = os.cpu_count() or 1
-    pyoracle.rrtmg_sw(sub, mcs, icld=3, iaer=10, native=True, nthreads=cores)
+    pyoracle.rrtmg_sw(sub, mcs, icld=3, iaer=10, tuned=True, nthreads=cores)
     t0, reps = time.perf_counter(), 0
     while reps < 3 or time.perf_counter() - t0 < 5.0:
-        pyoracle.rrtmg_sw(sub, mcs, icld=3, iaer=10, native=True, nthreads=cores)
+        pyoracle.rrtmg_sw(sub, mcs, icld=3, iaer=10, tuned=True, nthreads=cores)
         reps += 1
     dt = time.perf_counter() - t0
     res["cpu_oracle"] = {"value": nc * reps / dt, "unit": "columns/s", "cores": cores, "kind": "port",
@@ -1124,7 +1124,7 @@ def cpu_configs(seconds: float = 5.0) -> dict:
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
 
-    pyoracle.build(native=True)
+    pyoracle.build(tuned=True)
     cores = os.cpu_count() or 1
     out = {}
     for name, ncol in (("oracle_64x64x38", None), ("drop_in_360x300x45", 8192)):
@@ -1133,7 +1133,7 @@ def cpu_configs(seconds: float = 5.0) -> dict:
         n = st["play"].shape[0]
         done, reps, t0 = 0, 0, time.perf_counter()
         while reps < 3 or time.perf_counter() - t0 < seconds:
-            pyoracle.rrtmg_lw(st, mc, nthreads=cores, native=True)
+            pyoracle.rrtmg_lw(st, mc, nthreads=cores, tuned=True)
             done += n
             reps += 1
         dt = time.perf_counter() - t0

@@ -19,20 +19,20 @@ _lib = {}
 _D = np.ctypeslib.ndpointer(dtype=np.float64, flags="F_CONTIGUOUS")
 
 
-def build(native: bool = False) -> str:
-    target = "native" if native else "all"
+def build(tuned: bool = False) -> str:
+    target = "tuned" if tuned else "all"
     subprocess.run(["make", "-s", "-C", HERE, target], check=True)
-    return os.path.join(HERE, "_build", "liblworacle_native.so" if native else "liblworacle.so")
+    return os.path.join(HERE, "_build", "liblworacle_tuned.so" if tuned else "liblworacle.so")
 
 
-def lib(native: bool = False):
-    key = "native" if native else "portable"
+def lib(tuned: bool = False):
+    key = "tuned" if tuned else "portable"
     if key in _lib:
         return _lib[key]
-    path = os.path.join(HERE, "_build", "liblworacle_native.so" if native else "liblworacle.so")
+    path = os.path.join(HERE, "_build", "liblworacle_tuned.so" if tuned else "liblworacle.so")
     src = os.path.join(HERE, "lw_oracle.cpp")
     if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
-        build(native)
+        build(tuned)
     L = C.CDLL(path)
     L.ora_init.restype = C.c_int
     L.ora_init.argtypes = [C.c_double, C.c_char_p, C.c_char_p]
@@ -59,9 +59,9 @@ CLOUD_ORDER = ["cldfmcl", "taucmcl", "ciwpmcl", "clwpmcl", "reicmcl", "relqmcl"]
 
 
 def rrtmg_lw(state: dict, mc: dict, icld: int = 3, idrv: int = 1, inflglw: int = 2,
-             iceflglw: int = 3, liqflglw: int = 1, nthreads: int = 1, native: bool = False) -> dict:
+             iceflglw: int = 3, liqflglw: int = 1, nthreads: int = 1, tuned: bool = False) -> dict:
     """Reference-order FP64 rrtmg_lw on Fortran-ordered arrays; returns the outputs."""
-    L = lib(native)
+    L = lib(tuned)
     ncol, nlay = state["play"].shape
     st = [_f(state[k]) for k in STATE_ORDER]
     cl = [_f(mc[k]) for k in CLOUD_ORDER]
@@ -88,13 +88,13 @@ def rrtmg_lw_rtrn(state: dict, idrv: int = 1, inflglw: int = 2, iceflglw: int = 
 
 
 def rrtmg_lw_nomcica(state: dict, icld: int = 2, idrv: int = 1, inflglw: int = 2, iceflglw: int = 3,
-                     liqflglw: int = 1, native: bool = False) -> dict:
+                     liqflglw: int = 1, tuned: bool = False) -> dict:
     """rrtmg_lw of the non-McICA driver (rrtmg_lw_rad.nomcica.f90) on
     band-level clouds: state['cldfrac'], 'ciwp', 'clwp', 'rei', 'rel' (ncol,
     nlay) and optional 'tauc_band' (16, ncol, nlay, read for inflag 0).
     icld 1: random overlap (rtrn); 0, 2, 3: maximum/random overlap (rtrnmr);
     other values become 2 (returned in out['icld'])."""
-    L = lib(native)
+    L = lib(tuned)
     ncol, nlay = state["play"].shape
     st = [_f(state[k]) for k in STATE_ORDER]
     tb = state.get("tauc_band")
@@ -263,14 +263,14 @@ SW_CLOUD = ["cldfmcl", "taucmcl", "ssacmcl", "asmcmcl", "fsfcmcl", "ciwpmcl", "c
 SW_OUT = ["swuflx", "swdflx", "swhr", "swuflxc", "swdflxc", "swhrc"]
 
 
-def sw_lib(native: bool = False, count: bool = False):
+def sw_lib(tuned: bool = False, count: bool = False):
     """The SW oracle (sw_oracle.cpp), built on first use and initialised with
     cpdair 1004; count=True: the copy whose arithmetic counts its operations
     (flop_count.h, single-threaded use)."""
-    key = "sw_count" if count else ("sw_native" if native else "sw")
+    key = "sw_count" if count else ("sw_tuned" if tuned else "sw")
     if key in _lib:
         return _lib[key]
-    name = "libsworacle_count.so" if count else ("libsworacle_native.so" if native else "libsworacle.so")
+    name = "libsworacle_count.so" if count else ("libsworacle_tuned.so" if tuned else "libsworacle.so")
     path = os.path.join(HERE, "_build", name)
     src = os.path.join(HERE, "sw_oracle.cpp")
     if not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
@@ -289,13 +289,13 @@ def sw_lib(native: bool = False, count: bool = False):
 
 def rrtmg_sw(state: dict, mc: dict | None, icld: int = 3, iaer: int = 10, adjes: float = 1.0, dyofyr: int = 0,
              scon: float = 1368.22, isolvar: int = -1, inflgsw: int = 2, iceflgsw: int = 3, liqflgsw: int = 1,
-             nthreads: int = 1, native: bool = False, _count: bool = False) -> dict:
+             nthreads: int = 1, tuned: bool = False, _count: bool = False) -> dict:
     """rrtmg_sw (rrtmg_sw_rad.f90:243) on Fortran-ordered arrays: state keys
     SW_STATE ((ncol, nlay), (ncol, nlay+1), (ncol,)), aerosols 'tauaer_sw',
     'ssaaer_sw', 'asmaer_sw' (ncol, nlay, 14), McICA arrays SW_CLOUD ((112,
     ncol, nlay); reicmcl/relqmcl (ncol, nlay)).  Returns the outputs, icld,
     iaer."""
-    L = sw_lib(native, count=_count)
+    L = sw_lib(tuned, count=_count)
     ncol, nlay = state["play"].shape
     st = [_f(state[k]) for k in SW_STATE]
     z3 = np.zeros((112, ncol, nlay), order="F")
