@@ -32,7 +32,41 @@ def case(name, ncol, nlay, seed, ptop=10.0, t_noise=2.0, h2o_sigma=0.3):
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrs)
 
 
+def sw_case(name, ncol, nlay, seed, permuteseed=5):
+    """The shortwave chain as BRAMS calls it: band cloud optics, the McICA
+    generator (mcica_subcol_sw), then rrtmg_sw with McICA clouds (icld 3),
+    aerosols (iaer 10), ice option 3, liquid option 1."""
+    st = make_state(ProfileSpec(ncol=ncol, nlay=nlay, seed=seed, t_noise=3.0, h2o_sigma=0.4, cloud_prob=0.7))
+    rng = np.random.default_rng(seed)
+    for k in ("asdir", "asdif", "aldir", "aldif"):
+        st[k] = rng.uniform(0.05, 0.6, ncol)
+    st["coszen"] = rng.uniform(0.05, 1.0, ncol)
+    st["coszen"][:2] = [1.0, -0.2]  # overhead sun and a night column
+    # aerosol and band optics are float32 values (stored as such, exactly)
+    f32 = lambda a: np.asfortranarray(a.astype(np.float32).astype(np.float64))  # noqa: E731
+    st["tauaer_sw"] = f32(rng.uniform(0.0, 0.05, (ncol, nlay, 14)))
+    st["ssaaer_sw"] = f32(rng.uniform(0.8, 0.99, (ncol, nlay, 14)))
+    st["asmaer_sw"] = f32(rng.uniform(0.5, 0.8, (ncol, nlay, 14)))
+    for k in ("rei", "rel"):
+        st[k] = np.asfortranarray(np.clip(st[k], 6.0, 50.0))
+    band = {"tauc": f32(rng.uniform(0.1, 10.0, (14, ncol, nlay))),
+            "ssac": f32(rng.uniform(0.8, 1.0, (14, ncol, nlay))),
+            "asmc": f32(rng.uniform(0.6, 0.9, (14, ncol, nlay))),
+            "fsfc": f32(rng.uniform(0.0, 0.5, (14, ncol, nlay)))}
+    mc = pyoracle.mcica_subcol_sw(st, band, 3, permuteseed)
+    out = pyoracle.rrtmg_sw(st, mc, icld=3, iaer=10)
+    arrs = {f"in_{k}": (v.astype(np.float32) if k.endswith("aer_sw") else v) for k, v in st.items()}
+    arrs.update({f"band_{k}": v.astype(np.float32) for k, v in band.items()})
+    # the generator's draws, as the cloudy/clear mask of the sub-columns (the
+    # other McICA arrays follow from it, the band optics and the layer state)
+    arrs["mc_cldfmcl"] = mc["cldfmcl"].astype(np.uint8)
+    arrs.update({f"out_{k}": v for k, v in out.items() if isinstance(v, np.ndarray)})
+    arrs["permuteseed"] = np.array(permuteseed)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrs)
+
+
 def main():
+    sw_case("sw_8x45", 8, 45, seed=20240602)
     case("lw_16x38", 16, 38, seed=20240601)
     case("lw_8x60_top5hpa", 8, 60, seed=77, ptop=5.0, t_noise=4.0, h2o_sigma=0.5)
     seeds = np.array([1, 5489, 12345, 2**31 - 1], dtype=np.int64)

@@ -1,5 +1,7 @@
 """Oracle against the committed golden fixtures (CPU) and the CUDA library
-against the same fixtures (GPU)."""
+against the same fixtures (GPU): two longwave cases (McICA sub-columns and
+outputs) and the shortwave chain (the generator's sub-column mask from band
+cloud optics, then rrtmg_sw with McICA clouds and aerosols)."""
 import os
 
 import numpy as np
@@ -51,3 +53,45 @@ def test_gpu_matches_golden(ctx, name):
         assert np.abs(out[k] - ref[k]).max() <= 0.05, k
     for k in ("hr", "hrc"):
         assert np.abs(out[k] - ref[k]).max() <= 0.01, k
+
+
+SW_OUTS = ["swuflx", "swdflx", "swuflxc", "swdflxc", "swhr", "swhrc"]
+
+
+def _load_sw(name="sw_8x45"):
+    z = np.load(os.path.join(G, name + ".npz"))
+    st = {k[3:]: np.asfortranarray(z[k].astype(np.float64)) for k in z.files if k.startswith("in_")}
+    band = {k[5:]: np.asfortranarray(z[k].astype(np.float64)) for k in z.files if k.startswith("band_")}
+    out = {k[4:]: z[k] for k in z.files if k.startswith("out_")}
+    return st, band, z["mc_cldfmcl"].astype(np.float64), int(z["permuteseed"]), out
+
+
+def test_oracle_reproduces_sw_golden():
+    st, band, cldf, seed, ref = _load_sw()
+    mc = pyoracle.mcica_subcol_sw(st, band, 3, seed)
+    assert np.array_equal(mc["cldfmcl"], cldf)
+    assert 0.05 < cldf.mean() < 0.9
+    out = pyoracle.rrtmg_sw(st, mc, icld=3, iaer=10)
+    for k in SW_OUTS:
+        assert np.allclose(out[k], ref[k], rtol=1e-10, atol=1e-10), k
+    assert ref["swdflx"][1].max() < 1e-6    # the night column (cos zenith floored at 1e-10)
+    assert ref["swdflx"][0, -1] > 1000.0    # overhead sun: incoming flux at the top
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("bits", [64, 32])
+def test_gpu_matches_sw_golden(ctx, bits):
+    st, band, cldf, seed, ref = _load_sw()
+    ctx.sw_ini(1004.0)
+    mc = ctx.mcica_subcol_sw(st, band, 3, seed)
+    assert np.array_equal(mc["cldfmcl"], cldf)
+    ctx.sw_set_precision(bits)
+    try:
+        out = ctx.rrtmg_sw(st, mc, icld=3, iaer=10)
+    finally:
+        ctx.sw_set_precision(32)
+    flux_tol, hr_tol = (1e-6, 1e-8) if bits == 64 else (0.05, 0.01)
+    for k in ("swuflx", "swdflx", "swuflxc", "swdflxc"):
+        assert np.abs(out[k] - ref[k]).max() <= flux_tol, k
+    for k in ("swhr", "swhrc"):
+        assert np.abs(out[k] - ref[k]).max() <= hr_tol, k
