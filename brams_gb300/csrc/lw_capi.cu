@@ -12,7 +12,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/gb_rrtmg_lw.h"
@@ -381,6 +384,32 @@ int gb_ctx_launch_batch(gb_lw_context* ctx, LwBatch& b, cudaStream_t stream) {
   return GB_LW_OK;
 }
 
+namespace {
+struct ConstHold {
+  std::vector<unsigned char> bytes;
+  int holders = 0;
+};
+std::mutex g_const_mu;
+std::map<std::pair<int, int>, ConstHold> g_const;  // (kind, device) -> the bytes live contexts hold
+}  // namespace
+
+bool gb_const_acquire(int kind, int device, const void* bytes, size_t n, bool* upload) {
+  std::lock_guard<std::mutex> lk(g_const_mu);
+  ConstHold& h = g_const[{kind, device}];
+  const unsigned char* b = static_cast<const unsigned char*>(bytes);
+  if (h.holders > 0 && (h.bytes.size() != n || std::memcmp(h.bytes.data(), b, n) != 0)) return false;
+  *upload = h.holders == 0;
+  if (h.holders == 0) h.bytes.assign(b, b + n);
+  ++h.holders;
+  return true;
+}
+
+void gb_const_release(int kind, int device) {
+  std::lock_guard<std::mutex> lk(g_const_mu);
+  auto it = g_const.find({kind, device});
+  if (it != g_const.end() && it->second.holders > 0) --it->second.holders;
+}
+
 extern "C" {
 
 int gb_rrtmg_lw_ini(double cpdair, const char* table_dir, int device, gb_lw_context** out) {
@@ -408,6 +437,16 @@ int gb_rrtmg_lw_ini(double cpdair, const char* table_dir, int device, gb_lw_cont
   }
   ctx->absliq0 = cloud64[ctx->tabs.c64_absliq0];
   ctx->abscld1 = cloud64[ctx->tabs.c64_abscld1];
+  bool upload = false;
+  if (!gb_const_acquire(GB_CONST_LW, device, &ctx->tabs, sizeof(GbTables), &upload)) {
+    std::fprintf(stderr,
+                 "gb_rrtmg_lw_ini: another context on device %d holds different longwave tables "
+                 "(cpdair or table files); the contexts of a device must agree on them\n",
+                 device);
+    delete ctx;
+    return GB_LW_E_TABLES;
+  }
+  ctx->lw_const_held = true;
   int dev_smem = 0;
   cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
   ctx->max_smem = (size_t)dev_smem;
@@ -421,7 +460,7 @@ int gb_rrtmg_lw_ini(double cpdair, const char* table_dir, int device, gb_lw_cont
   ctx->d_err_host = ctx->d_err + 1;
   if (cudaMemcpy(ctx->d_tables, blob.data(), blob.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(ctx->d_cloud64, cloud64.data(), cloud64.size() * 8, cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemset(ctx->d_err, 0, 8) != cudaSuccess || gb_lw_set_tables(ctx->tabs) != cudaSuccess ||
+      cudaMemset(ctx->d_err, 0, 8) != cudaSuccess || (upload && gb_lw_set_tables(ctx->tabs) != cudaSuccess) ||
       cudaStreamCreateWithFlags(&ctx->streams[0], cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&ctx->streams[1], cudaStreamNonBlocking) != cudaSuccess) {
     std::fprintf(stderr, "gb_rrtmg_lw_ini: %s\n", cudaGetErrorString(cudaGetLastError()));
@@ -457,6 +496,8 @@ int gb_rrtmg_lw_free(gb_lw_context* ctx) {
   cudaFree(ctx->d_sw_tables);
   cudaFree(ctx->d_sw_tables_f);
   cudaFree(ctx->d_sw_scratch);
+  if (ctx->lw_const_held) gb_const_release(GB_CONST_LW, ctx->device);
+  if (ctx->sw_const_held) gb_const_release(GB_CONST_SW, ctx->device);
   delete ctx;
   return GB_LW_OK;
 }

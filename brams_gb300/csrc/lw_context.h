@@ -68,7 +68,20 @@ struct gb_lw_context {
   double sw_scon = 0.0;  // rrsw_scon of the tables (parrrsw.f90)
   void* d_sw_scratch = nullptr;
   size_t sw_scratch_bytes = 0;
+  // this context's hold on its device's constant table blocks (see below)
+  bool lw_const_held = false, sw_const_held = false;
 };
+
+// The kernels' constant table blocks (the longwave GbTables, the shortwave
+// table directory of each precision's unit) exist once per device, while
+// tables are loaded per context, so every live context on a device must hold
+// the same bytes there (the same table files and cpdair).  gb_const_acquire
+// takes a hold for `kind` on `device`: false, with nothing changed, when
+// another live context there holds different bytes; *upload is set when no
+// context held the block, so that the caller uploads its bytes.
+enum GbConstKind { GB_CONST_LW = 0, GB_CONST_SW = 1 };
+bool gb_const_acquire(int kind, int device, const void* bytes, size_t n, bool* upload);
+void gb_const_release(int kind, int device);
 
 // records a CUDA error on the context; returns GB_LW_E_CUDA
 int gb_ctx_fail(gb_lw_context* c, cudaError_t e, const char* where);

@@ -162,21 +162,42 @@ int gb_sw_load(gb_lw_context* ctx, double cpdair, const char* table_dir) {
   S.bpadef = (float)S.bpade;
   std::vector<float> blobf(blob.begin(), blob.end());  // the fp32 kernels' copy (every entry is within float range)
   cudaSetDevice(ctx->device);
+  // the table directory is a constant block of the device: this context's
+  // earlier hold (a repeated call) ends, and a new one must agree with the
+  // other live contexts of the device
+  ctx->sw_ready = false;
+  if (ctx->sw_const_held) gb_const_release(GB_CONST_SW, ctx->device);
+  ctx->sw_const_held = false;
+  bool upload = false;
+  if (!gb_const_acquire(GB_CONST_SW, ctx->device, &S, sizeof(S), &upload)) {
+    ctx->last_error = "another context on this device holds different shortwave tables (cpdair or table files); "
+                      "the contexts of a device must agree on them";
+    return GB_LW_E_TABLES;
+  }
+  ctx->sw_const_held = true;
   cudaFree(ctx->d_sw_tables);
   cudaFree(ctx->d_sw_tables_f);
   ctx->d_sw_tables = nullptr;
   ctx->d_sw_tables_f = nullptr;
+  auto drop_hold = [&]() {  // a failed load holds nothing (a later context uploads its own bytes)
+    gb_const_release(GB_CONST_SW, ctx->device);
+    ctx->sw_const_held = false;
+  };
   if (cudaMalloc(&ctx->d_sw_tables, blob.size() * 8) != cudaSuccess ||
       cudaMalloc(&ctx->d_sw_tables_f, blobf.size() * 4) != cudaSuccess) {
     cudaGetLastError();
+    drop_hold();
     ctx->last_error = "device allocation of the SW tables failed";
     return GB_LW_E_NOMEM;
   }
   cudaError_t e = cudaMemcpy(ctx->d_sw_tables, blob.data(), blob.size() * 8, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(ctx->d_sw_tables_f, blobf.data(), blobf.size() * 4, cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = gbsw::sw_set_tab(S);
-  if (e == cudaSuccess) e = gb_sw_set_tab_f32(&S);
-  if (e != cudaSuccess) return gb_ctx_fail(ctx, e, "SW tables");
+  if (e == cudaSuccess && upload) e = gbsw::sw_set_tab(S);
+  if (e == cudaSuccess && upload) e = gb_sw_set_tab_f32(&S);
+  if (e != cudaSuccess) {
+    drop_hold();
+    return gb_ctx_fail(ctx, e, "SW tables");
+  }
   std::map<std::string, GbTableEntry> tab;
   if (!gb_read_container(path.c_str(), tab, err) || !tab.count("rrsw_scon")) {
     ctx->last_error = "SW table file lacks rrsw_scon";

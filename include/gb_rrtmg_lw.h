@@ -44,7 +44,7 @@ typedef struct gb_lw_context gb_lw_context;
 #define GB_LW_E_SW_UNSUPPORTED 14 /* option the SW path does not implement (see gb_rrtmg_sw)  */
 #define GB_LW_E_ARGS (-1)      /* invalid sizes, flags or null pointers                  */
 #define GB_LW_E_CUDA (-2)      /* CUDA runtime error (see gb_rrtmg_lw_last_error)        */
-#define GB_LW_E_TABLES (-3)    /* table files missing or malformed                       */
+#define GB_LW_E_TABLES (-3)    /* table files missing or malformed, or unlike another live context's on the device */
 #define GB_LW_E_NOMEM (-4)     /* device or pinned-host allocation failed                */
 #define GB_LW_E_SCRATCH (-5)   /* call too large for the fixed scratch of gb_mcica_subcol_lw_noalloc */
 
@@ -52,7 +52,12 @@ typedef struct gb_lw_context gb_lw_context;
  * mem_rrtm.f90:114).  Loads the tables from table_dir (NULL: the directory
  * installed next to this library) onto CUDA device `device` and returns a
  * context.  cpdair is the specific heat of dry air used in heatfac
- * (BRAMS: cp = 1004.). */
+ * (BRAMS: cp = 1004.).  The kernels keep part of the tables in constant
+ * memory, one copy per device: every live context of a device must be made
+ * from the same table files and cpdair (the reference, too, holds one set of
+ * tables per process).  A context whose tables differ from those of a live
+ * context on its device is refused with GB_LW_E_TABLES; once the last such
+ * context is freed, the device takes the next context's tables. */
 int gb_rrtmg_lw_ini(double cpdair, const char* table_dir, int device, gb_lw_context** ctx);
 
 /* Releases all device memory, streams and events of the context. */
@@ -381,7 +386,10 @@ int gb_rrtmg_lw_graph_destroy(gb_lw_graph* graph);
  * options inflag 0 or 2 with iceflag 1-3 and liqflag 1 (the reference
  * leaves the coefficients of ice option 0 and liquid option 0 unset).  The
  * arithmetic is the context's shortwave precision (gb_rrtmg_sw_set_precision:
- * fp32 solution with fp64 sums by default, or fp64 throughout).  tlev, tsfc
+ * fp32 solution with fp64 sums by default, or fp64 throughout).  As in
+ * gb_rrtmg_lw_ini, the live contexts of a device must load the same
+ * shortwave tables and cpdair: otherwise GB_LW_E_TABLES, and the context is
+ * left without shortwave tables.  tlev, tsfc
  * and n2ovmr are not used by the reference's
  * shortwave computation and may be NULL. */
 int gb_rrtmg_sw_ini(gb_lw_context* ctx, double cpdair, const char* table_dir);
