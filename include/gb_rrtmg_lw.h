@@ -13,8 +13,11 @@
  * conditions (GB_LW_E_*), reported instead of stopping the process;
  * negative values are argument, memory or CUDA errors.
  *
- * Threading: a context may be used by one host thread at a time.  Separate
- * contexts (or separate streams with the *_device entry points) run
+ * Threading: a context may be used by one host thread at a time, and its
+ * calls share the context's device scratch (taumol hand-over planes, McICA
+ * draws, the shortwave kernel's slot records, grown on demand), so the
+ * *_device calls of one context must not overlap on the device: issue them
+ * on one stream, or order the streams (events).  Separate contexts run
  * concurrently.
  */
 #ifndef GB_RRTMG_LW_H
