@@ -375,3 +375,48 @@ int gb_mcica_subcol_sw(gb_lw_context* ctx, int ncol, int nlay, int icld, int per
   cudaFree(d);
   return rc;
 }
+
+int gb_cldprop_sw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int inflag, int iceflag, int liqflag,
+                         const double* cldfrac, const double* tauc, const double* ssac, const double* asmc,
+                         const double* fsfc, const double* ciwp, const double* clwp, const double* rei,
+                         const double* rel, double* taucloud, double* ssacloud, double* asmcloud, double* taucldorig,
+                         int64_t ld, int* d_col_status) {
+  if (!ctx || ncol < 0 || nlay < 1 || nlay > GB_MAXLAY || ld < ncol || inflag < 0 || inflag > 2 || iceflag < 0 ||
+      iceflag > 3 || liqflag < 0 || liqflag > 1 || !cldfrac || !ciwp || !clwp || !rei || !rel || !taucloud ||
+      !ssacloud || !asmcloud || (inflag == 0 && (!tauc || !ssac || !asmc || !fsfc)))
+    return GB_LW_E_ARGS;
+  if (!ctx->sw_ready) {
+    ctx->last_error = "gb_rrtmg_sw_ini has not been called on this context";
+    return GB_LW_E_ARGS;
+  }
+  if (ncol == 0) return GB_LW_OK;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = d_col_status ? cudaMemsetAsync(d_col_status, 0, sizeof(int) * (size_t)ncol, st) : cudaSuccess;
+  if (e != cudaSuccess) return gb_ctx_fail(ctx, e, "cldprop_sw status");
+  CldpropSwArgs a;
+  a.ncol = ncol;
+  a.nlay = nlay;
+  a.ld = ld;
+  a.inflag = inflag;
+  a.iceflag = iceflag;
+  a.liqflag = liqflag;
+  a.cldfrac = cldfrac;
+  a.tauc = tauc;
+  a.ssac = ssac;
+  a.asmc = asmc;
+  a.fsfc = fsfc;
+  a.ciwp = ciwp;
+  a.clwp = clwp;
+  a.rei = rei;
+  a.rel = rel;
+  a.taucldorig = taucldorig;
+  a.taucloud = taucloud;
+  a.ssacloud = ssacloud;
+  a.asmcloud = asmcloud;
+  a.col_err = d_col_status;
+  a.err_flag = ctx->d_err;
+  e = gb_cldprop_sw_launch(a, ctx->d_sw_tables, st);
+  if (e != cudaSuccess) return gb_ctx_fail(ctx, e, "cldprop_sw launch");
+  return GB_LW_OK;
+}

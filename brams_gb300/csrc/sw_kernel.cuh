@@ -698,6 +698,7 @@ __device__ int cloud_cell(const R* __restrict__ T, const SwArgs& a, int band, do
       if (index == (f3 ? 46 : 43)) index = f3 ? 45 : 42;
       const R fint = factor - (R)index;
       const int rows = f3 ? 46 : 43;
+      index = index < 1 ? 1 : (index > rows - 1 ? rows - 1 : index);  // in the table for any input (a NaN radius)
       const int oe = f3 ? c_S.extice3 : c_S.extice2, os = f3 ? c_S.ssaice3 : c_S.ssaice2,
                 og = f3 ? c_S.asyice3 : c_S.asyice2;
       extcoice = c2(oe, rows, index) + fint * (c2(oe, rows, index + 1) - c2(oe, rows, index));

@@ -23,6 +23,19 @@ struct SwArgs {
   int* err_flag;  // required: max status over the launch
 };
 
+// cldprop_sw on device arrays: inputs (ld, nlay) and (14, ld, nlay); outputs (14, ld, nlay)
+struct CldpropSwArgs {
+  int ncol, nlay;
+  long long ld;
+  int inflag, iceflag, liqflag;
+  const double *cldfrac, *tauc, *ssac, *asmc, *fsfc, *ciwp, *clwp, *rei, *rel;  // tauc..fsfc may be NULL (zeros)
+  double *taucldorig, *taucloud, *ssacloud, *asmcloud;                          // taucldorig may be NULL
+  int* col_err;   // optional per-column status (ncol)
+  int* err_flag;  // required: max status over the launch
+};
+// launches it on the fp64 tables of the context's shortwave load
+cudaError_t gb_cldprop_sw_launch(const CldpropSwArgs& a, const double* d_tables, cudaStream_t stream);
+
 struct gb_lw_context;
 // loads sw_tables.gbsw of table_dir (NULL: the context's table directory) into the context
 int gb_sw_load(gb_lw_context* ctx, double cpdair, const char* table_dir);

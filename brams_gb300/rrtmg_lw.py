@@ -51,6 +51,7 @@ EXPORTS = [
     "gb_rtm_ozone_load", "gb_rtm_ozone_free", "gb_rtm_ozone_lw",
     "gb_rrtmg_lw_shard_plan", "gb_rrtmg_lw_grid_slice", "gb_rrtmg_lw_nomcica", "gb_rrtmg_lw_nomcica_device",
     "gb_rrtmg_sw_ini", "gb_rrtmg_sw_set_precision", "gb_rrtmg_sw", "gb_rrtmg_sw_device", "gb_mcica_subcol_sw", "gb_mcica_subcol_sw_device",
+    "gb_cldprop_sw_device",
 ]
 MLP_MMA_SYNC, MLP_TCGEN05 = 0, 1
 MLP_NPARAM = 72352
@@ -160,6 +161,7 @@ def load_library(path: str = LIB_PATH):
         L.gb_rrtmg_sw_device.argtypes = [P, P, I, I, IP, IP] + SWA + [LL, LL, P]
         L.gb_mcica_subcol_sw.argtypes = [P, I, I, I, I, IP] + [P] * 11 + [P] * 9 + [LL, I]
         L.gb_mcica_subcol_sw_device.argtypes = [P, P, I, I, I, I, IP] + [P] * 11 + [P] * 9 + [LL, I]
+        L.gb_cldprop_sw_device.argtypes = [P, P, I, I, I, I, I] + [P] * 9 + [P] * 4 + [LL, P]
         L.gb_rrtmg_lw_shard_plan.argtypes = [I, IP, IP, I, I, C.POINTER(LL), C.POINTER(LL)]
         L.gb_rrtmg_lw_grid_slice.argtypes = [GP, LL, LL, GP]
         U64, F = C.c_uint64, C.c_float
@@ -395,6 +397,18 @@ class Context:
         _check(self.L, self.h, self.L.gb_cldprop_lw_device(
             self.h, _ptr(stream or 0), ncol, nlay, inflag, iceflag, liqflag, g("cldfrac"), g("tauc"), g("ciwp"),
             g("clwp"), g("rei"), g("rel"), g("taucloud"), ld if ld is not None else ncol, g("d_col_status")))
+
+    def cldprop_sw_device(self, ncol: int, nlay: int, ptrs: dict, inflag: int = 2, iceflag: int = 3,
+                          liqflag: int = 1, ld: int | None = None, stream=None) -> None:
+        """cldprop_sw (rrtmg_sw_cldprop.f90:53) on device arrays: ptrs holds cldfrac, ciwp, clwp, rei,
+        rel ((ld, nlay) memory order), optional tauc, ssac, asmc, fsfc (14, ld, nlay), outputs
+        taucloud, ssacloud, asmcloud and optional taucldorig (14, ld, nlay), optional d_col_status
+        (ncol int32)."""
+        g = lambda k: _ptr(ptrs.get(k))
+        _check(self.L, self.h, self.L.gb_cldprop_sw_device(
+            self.h, _ptr(stream or 0), ncol, nlay, inflag, iceflag, liqflag, g("cldfrac"), g("tauc"), g("ssac"),
+            g("asmc"), g("fsfc"), g("ciwp"), g("clwp"), g("rei"), g("rel"), g("taucloud"), g("ssacloud"),
+            g("asmcloud"), g("taucldorig"), ld if ld is not None else ncol, g("d_col_status")))
 
     PACK_IN = ("pi0", "pp", "theta", "rv", "rlongup", "albedt", "cldf", "lwl", "iwl", "rel", "rei")
     PACK_OUT = ("play", "plev", "tlay", "tlev", "tsfc", "h2ovmr", "co2vmr", "ch4vmr", "n2ovmr", "o2vmr", "cfc11vmr",

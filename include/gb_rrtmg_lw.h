@@ -449,6 +449,25 @@ int gb_mcica_subcol_sw_device(gb_lw_context* ctx, void* stream, int ncol, int nl
                               double* cldfmcl, double* ciwpmcl, double* clwpmcl, double* reicmcl, double* relqmcl,
                               double* taucmcl, double* ssacmcl, double* asmcmcl, double* fsfcmcl, int64_t ld,
                               int seed_per_column);
+/* cldprop_sw (rrtmg_sw_cldprop.f90:53-365) on DEVICE arrays for ncol
+ * columns, as BRAMS calls it per column before mcica_subcol_sw
+ * (rtm_driver.f90:1356-1368): cldfrac, ciwp, clwp, rei, rel are (ld, nlay);
+ * tauc, ssac, asmc, fsfc (14, ld, nlay) are the reference's inflag-0 inputs
+ * (required for inflag 0; otherwise NULL reads as zeros, which the driver
+ * passes).  Outputs, (14, ld, nlay) with the band fastest -- the layout
+ * gb_mcica_subcol_sw takes as tauc ssac asmc: taucloud (delta-scaled),
+ * ssacloud, asmcloud (delta-scaled) and taucldorig (may be NULL); a clear
+ * layer gets 0, 1, 0 and the input tauc.  fp64 with the reference's
+ * operations.  A layer the reference STOPs on keeps the clear values and
+ * sets d_col_status (may be NULL) to the code of that STOP (radius bounds,
+ * GB_LW_E_SW_OPTICS, GB_LW_E_SW_UNSUPPORTED for ice option 0 or liquid
+ * option 0 with a nonzero path), and the context's status.  Needs the
+ * shortwave tables (gb_rrtmg_sw_ini). */
+int gb_cldprop_sw_device(gb_lw_context* ctx, void* stream, int ncol, int nlay, int inflag, int iceflag, int liqflag,
+                         const double* cldfrac, const double* tauc, const double* ssac, const double* asmc,
+                         const double* fsfc, const double* ciwp, const double* clwp, const double* rei,
+                         const double* rel, double* taucloud, double* ssacloud, double* asmcloud, double* taucldorig,
+                         int64_t ld, int* d_col_status);
 
 /* ---------------------------------------------------------------------------
  * Multi-GPU column shards (host only; no device call).  BRAMS gives each MPI

@@ -328,6 +328,39 @@ def sw_flops_per_column(state: dict, mc: dict | None, **kw) -> float:
     return L.ora_flops(-1) / state["play"].shape[0]
 
 
+SW_CLDPROP_OUT = ["taucldorig", "taucloud", "ssacloud", "asmcloud"]
+
+
+def cldprop_sw_columns(state: dict, band_in: dict | None = None, inflag: int = 2, iceflag: int = 3,
+                       liqflag: int = 1) -> tuple[dict, np.ndarray]:
+    """BRAMS's per-column cldprop_sw call (rtm_driver.f90:1356-1368): state
+    cldfrac ciwp clwp rei rel (ncol, nlay); band_in tauc ssac asmc fsfc
+    (14, ncol, nlay) (None: zeros, as the driver passes for inflag 2).
+    Returns taucldorig taucloud ssacloud asmcloud (14, ncol, nlay) -- the
+    layout mcica_subcol_sw takes -- and the status of each column (0, or
+    the code of the STOP the reference reaches; that column's outputs are
+    then left 0)."""
+    L = sw_lib()
+    ncol, nlay = state["cldfrac"].shape
+    z = np.zeros((14, ncol, nlay))
+    bi = {k: (band_in[k] if band_in is not None and k in band_in else z) for k in ("tauc", "ssac", "asmc", "fsfc")}
+    out = {k: np.zeros((14, ncol, nlay), order="F") for k in SW_CLDPROP_OUT}
+    status = np.zeros(ncol, dtype=np.int64)
+    tmp = {k: np.zeros((nlay, 14), order="F") for k in SW_CLDPROP_OUT}
+    col = lambda a, i: np.ascontiguousarray(a[i, :], dtype=np.float64)  # noqa: E731
+    for i in range(ncol):
+        ins = [np.asfortranarray(bi[k][:, i, :], dtype=np.float64) for k in ("tauc", "ssac", "asmc", "fsfc")]
+        rc = L.ora_cldprop_sw(C.c_int(nlay), C.c_int(inflag), C.c_int(iceflag), C.c_int(liqflag),
+                              _p(col(state["cldfrac"], i)), *[_p(a) for a in ins],
+                              *[_p(col(state[k], i)) for k in ("ciwp", "clwp", "rei", "rel")],
+                              *[_p(tmp[k]) for k in SW_CLDPROP_OUT])
+        status[i] = rc
+        if rc == 0:
+            for k in SW_CLDPROP_OUT:
+                out[k][:, i, :] = tmp[k].T
+    return out, status
+
+
 def mcica_subcol_sw(state: dict, band: dict, icld: int, permuteseed: int, irng: int = 1) -> dict:
     """mcica_subcol_sw (mcica_subcol_gen_sw.f90:181): one call over all columns."""
     L = lib()

@@ -6,8 +6,9 @@
 // (rrtmg_sw_cldprmc.f90:43-338), setcoef_sw (rrtmg_sw_setcoef.f90:27-240),
 // taumol_sw (rrtmg_sw_taumol.f90:50-1787), spcvmc_sw (rrtmg_sw_spcvmc.f90:
 // 30-664), reftra_sw (rrtmg_sw_reftra.f90:27-330), vrtqdr_sw
-// (rrtmg_sw_vrtqdr.f90:24-171) and the lookup table of rrtmg_sw_ini
-// (rrtmg_sw_init.f90:99-118).  Tables come from sw_tables.gbsw, which
+// (rrtmg_sw_vrtqdr.f90:24-171), the lookup table of rrtmg_sw_ini
+// (rrtmg_sw_init.f90:99-118) and the band cloud optics cldprop_sw
+// (rrtmg_sw_cldprop.f90:53-365) the driver feeds to the McICA generator.  Tables come from sw_tables.gbsw, which
 // brams_gb300/data/extract_sw_tables.py extracts from the reference source
 // and reduces with the reference's cmbgb routines.
 //
@@ -1172,6 +1173,156 @@ int ora_rrtmg_sw(int ncol, int nlay, int* icld, int* iaer, const double* play, c
   }
   for (int e : err)
     if (e) return e;
+  return 0;
+}
+
+// cldprop_sw (rrtmg_sw_cldprop.f90:53-365): the band cloud optics of one
+// column, which BRAMS computes per column and hands to mcica_subcol_sw
+// (rtm_driver.f90:1356-1368).  Inputs cldfrac ciwp clwp rei rel (nlayers);
+// tauc ssac asmc fsfc (14, nlayers), read for inflag 0 (tauc also for the
+// cloudy test); outputs taucldorig taucloud ssacloud asmcloud (nlayers, 14),
+// the reference's (nlayers, 16:29) columns.  Returns the code of the first
+// STOP the reference reaches (outputs of the layers before it are written),
+// ERR_UNSUPPORTED where the reference would read coefficients it never set
+// (iceflag 0, liqflag 0 with a nonzero water path).
+int ora_cldprop_sw(int nlayers, int inflag, int iceflag, int liqflag, const double* cldfrac, const double* tauc,
+                   const double* ssac, const double* asmc, const double* fsfc, const double* ciwp, const double* clwp,
+                   const double* rei, const double* rel, double* taucldorig, double* taucloud, double* ssacloud,
+                   double* asmcloud) {
+  if (!g_ready) return ERR_NOT_INIT;
+  const double eps = 1.e-06, cldmin = 1.e-20;
+  auto IN = [&](const double* v, int ib, int lay) { return v[(ib - 16) + NBND * (lay - 1)]; };  // (ib-15, lay)
+  auto OUT = [&](double* v, int lay, int ib) -> double& { return v[(lay - 1) + nlayers * (ib - 16)]; };
+  std::vector<double> tauctot(nlayers + 1, 0.0);
+  for (int lay = 1; lay <= nlayers; ++lay)
+    for (int ib = 16; ib <= 29; ++ib) {
+      OUT(taucldorig, lay, ib) = IN(tauc, ib, lay);
+      OUT(taucloud, lay, ib) = 0.0;
+      OUT(ssacloud, lay, ib) = 1.0;
+      OUT(asmcloud, lay, ib) = 0.0;
+      tauctot[lay] = tauctot[lay] + IN(tauc, ib, lay);
+    }
+  double extcoice[30], ssacoice[30], gice[30], forwice[30], fdelta[30];
+  double extcoliq[30], ssacoliq[30], gliq[30], forwliq[30];
+  for (int lay = 1; lay <= nlayers; ++lay) {
+    const double cwp = ciwp[lay - 1] + clwp[lay - 1];
+    if (!(cldfrac[lay - 1] >= cldmin && (cwp >= cldmin || tauctot[lay] >= cldmin))) continue;
+    if (inflag == 0) {
+      for (int ib = 16; ib <= 29; ++ib) {
+        const double taucldorig_a = IN(tauc, ib, lay);
+        const double ffp = IN(fsfc, ib, lay);
+        const double ffp1 = 1.0 - ffp;
+        const double ffpssa = 1.0 - ffp * IN(ssac, ib, lay);
+        const double ssacloud_a = ffp1 * IN(ssac, ib, lay) / ffpssa;
+        const double taucloud_a = ffpssa * taucldorig_a;
+        OUT(taucldorig, lay, ib) = taucldorig_a;
+        OUT(ssacloud, lay, ib) = ssacloud_a;
+        OUT(taucloud, lay, ib) = taucloud_a;
+        OUT(asmcloud, lay, ib) = (IN(asmc, ib, lay) - ffp) / (ffp1);
+      }
+    } else if (inflag == 2) {
+      const double radice = rei[lay - 1];
+      if (ciwp[lay - 1] == 0.0) {
+        for (int ib = 16; ib <= 29; ++ib) extcoice[ib] = ssacoice[ib] = gice[ib] = forwice[ib] = 0.0;
+      } else if (iceflag == 1) {
+        if (radice < 13.0 || radice > 130.0) return ERR_ICE_BOUNDS;
+        for (int ib = 16; ib <= 29; ++ib) {
+          const double w2 = wavenum2[ib - 16];
+          int icx = 0;
+          if (w2 > 1.43e04) icx = 1;
+          else if (w2 > 7.7e03) icx = 2;
+          else if (w2 > 5.3e03) icx = 3;
+          else if (w2 > 4.0e03) icx = 4;
+          else if (w2 >= 2.5e03) icx = 5;
+          extcoice[ib] = abari[icx - 1] + bbari[icx - 1] / radice;
+          ssacoice[ib] = 1.0 - cbari[icx - 1] - dbari[icx - 1] * radice;
+          gice[ib] = ebari[icx - 1] + fbari[icx - 1] * radice;
+          if (gice[ib] >= 1.0) gice[ib] = 1.0 - eps;
+          forwice[ib] = gice[ib] * gice[ib];
+          if (extcoice[ib] < 0.0 || ssacoice[ib] > 1.0 || ssacoice[ib] < 0.0 || gice[ib] > 1.0 || gice[ib] < 0.0)
+            return ERR_OPTICS;
+        }
+      } else if (iceflag == 2) {
+        if (radice < 5.0 || radice > 131.0) return ERR_ICE_BOUNDS;
+        const double factor = (radice - 2.0) / 3.0;
+        int index = (int)factor;
+        if (index == 43) index = 42;
+        const double fint = factor - (double)index;
+        for (int ib = 16; ib <= 29; ++ib) {
+          extcoice[ib] = C2(extice2, 43, index, ib) + fint * (C2(extice2, 43, index + 1, ib) - C2(extice2, 43, index, ib));
+          ssacoice[ib] = C2(ssaice2, 43, index, ib) + fint * (C2(ssaice2, 43, index + 1, ib) - C2(ssaice2, 43, index, ib));
+          gice[ib] = C2(asyice2, 43, index, ib) + fint * (C2(asyice2, 43, index + 1, ib) - C2(asyice2, 43, index, ib));
+          forwice[ib] = gice[ib] * gice[ib];
+          if (extcoice[ib] < 0.0 || ssacoice[ib] > 1.0 || ssacoice[ib] < 0.0 || gice[ib] > 1.0 || gice[ib] < 0.0)
+            return ERR_OPTICS;
+        }
+      } else if (iceflag == 3) {
+        if (radice < 5.0 || radice > 140.0) return ERR_DGE_BOUNDS;
+        const double factor = (radice - 2.0) / 3.0;
+        int index = (int)factor;
+        if (index == 46) index = 45;
+        const double fint = factor - (double)index;
+        for (int ib = 16; ib <= 29; ++ib) {
+          extcoice[ib] = C2(extice3, 46, index, ib) + fint * (C2(extice3, 46, index + 1, ib) - C2(extice3, 46, index, ib));
+          ssacoice[ib] = C2(ssaice3, 46, index, ib) + fint * (C2(ssaice3, 46, index + 1, ib) - C2(ssaice3, 46, index, ib));
+          gice[ib] = C2(asyice3, 46, index, ib) + fint * (C2(asyice3, 46, index + 1, ib) - C2(asyice3, 46, index, ib));
+          fdelta[ib] = C2(fdlice3, 46, index, ib) + fint * (C2(fdlice3, 46, index + 1, ib) - C2(fdlice3, 46, index, ib));
+          if (fdelta[ib] < 0.0 || fdelta[ib] > 1.0) return ERR_OPTICS;
+          forwice[ib] = fdelta[ib] + 0.5 / ssacoice[ib];
+          if (forwice[ib] > gice[ib]) forwice[ib] = gice[ib];
+          if (extcoice[ib] < 0.0 || ssacoice[ib] > 1.0 || ssacoice[ib] < 0.0 || gice[ib] > 1.0 || gice[ib] < 0.0)
+            return ERR_OPTICS;
+        }
+      } else {
+        return ERR_UNSUPPORTED;
+      }
+      if (clwp[lay - 1] == 0.0) {
+        for (int ib = 16; ib <= 29; ++ib) extcoliq[ib] = ssacoliq[ib] = gliq[ib] = forwliq[ib] = 0.0;
+      } else if (liqflag == 1) {
+        const double radliq = rel[lay - 1];
+        if (radliq < 2.5 || radliq > 60.0) return ERR_LIQ_BOUNDS;
+        int index = (int)(radliq - 1.5);
+        if (index == 0) index = 1;
+        if (index == 58) index = 57;
+        const double fint = radliq - 1.5 - (double)index;
+        for (int ib = 16; ib <= 29; ++ib) {
+          extcoliq[ib] = C2(extliq1, 58, index, ib) + fint * (C2(extliq1, 58, index + 1, ib) - C2(extliq1, 58, index, ib));
+          ssacoliq[ib] = C2(ssaliq1, 58, index, ib) + fint * (C2(ssaliq1, 58, index + 1, ib) - C2(ssaliq1, 58, index, ib));
+          if (fint < 0.0 && ssacoliq[ib] > 1.0) ssacoliq[ib] = C2(ssaliq1, 58, index, ib);
+          gliq[ib] = C2(asyliq1, 58, index, ib) + fint * (C2(asyliq1, 58, index + 1, ib) - C2(asyliq1, 58, index, ib));
+          forwliq[ib] = gliq[ib] * gliq[ib];
+          if (extcoliq[ib] < 0.0 || ssacoliq[ib] > 1.0 || ssacoliq[ib] < 0.0 || gliq[ib] > 1.0 || gliq[ib] < 0.0)
+            return ERR_OPTICS;
+        }
+      } else {
+        return ERR_UNSUPPORTED;
+      }
+      for (int ib = 16; ib <= 29; ++ib) {
+        const double tauliqorig = clwp[lay - 1] * extcoliq[ib];
+        const double tauiceorig = ciwp[lay - 1] * extcoice[ib];
+        OUT(taucldorig, lay, ib) = tauliqorig + tauiceorig;
+        const double ssaliq = ssacoliq[ib] * (1.0 - forwliq[ib]) / (1.0 - forwliq[ib] * ssacoliq[ib]);
+        const double tauliq = (1.0 - forwliq[ib] * ssacoliq[ib]) * tauliqorig;
+        const double ssaice = ssacoice[ib] * (1.0 - forwice[ib]) / (1.0 - forwice[ib] * ssacoice[ib]);
+        const double tauice = (1.0 - forwice[ib] * ssacoice[ib]) * tauiceorig;
+        const double scatliq = ssaliq * tauliq;
+        double scatice = ssaice * tauice;
+        OUT(taucloud, lay, ib) = tauliq + tauice;
+        if (OUT(taucloud, lay, ib) == 0.0) OUT(taucloud, lay, ib) = cldmin;
+        if (scatice == 0.0) scatice = cldmin;
+        OUT(ssacloud, lay, ib) = (scatliq + scatice) / OUT(taucloud, lay, ib);
+        if (iceflag == 3) {
+          OUT(asmcloud, lay, ib) = (1.0 / (scatliq + scatice)) *
+                                   (scatliq * (gliq[ib] - forwliq[ib]) / (1.0 - forwliq[ib]) +
+                                    scatice * ((gice[ib] - forwice[ib]) / (1.0 - forwice[ib])));
+        } else {
+          OUT(asmcloud, lay, ib) = (scatliq * (gliq[ib] - forwliq[ib]) / (1.0 - forwliq[ib]) +
+                                    scatice * (gice[ib] - forwice[ib]) / (1.0 - forwice[ib])) /
+                                   (scatliq + scatice);
+        }
+      }
+    }
+  }
   return 0;
 }
 

@@ -287,6 +287,60 @@ def test_radius_bounds_are_decided_on_the_double_inputs(swctx, bits):
         assert e.value.code == code, (key, edge)
 
 
+# ---------------------------------------------------------------- cldprop_sw (oracle)
+def test_oracle_cldprop_sw_clear_layers_and_direct_input():
+    """Clear layers keep (taucldorig = tauc, 0, 1, 0); with direct input
+    (inflag 0) the band values are the delta scaling of rrtmg_sw_cldprop.f90:
+    161-176 of the inputs."""
+    st = make_state(ProfileSpec(ncol=5, nlay=20, seed=8, cloud_prob=0.6))
+    rng = np.random.default_rng(8)
+    bi = {"tauc": rng.uniform(0.1, 5.0, (14, 5, 20)), "ssac": rng.uniform(0.8, 0.999, (14, 5, 20)),
+          "asmc": rng.uniform(0.6, 0.9, (14, 5, 20)), "fsfc": rng.uniform(0.0, 0.4, (14, 5, 20))}
+    o, status = pyoracle.cldprop_sw_columns(st, bi, inflag=0)
+    assert (status == 0).all()
+    cloudy = (st["cldfrac"] >= 1e-20)[None].repeat(14, 0)  # tauc > 0 everywhere, so the cloud fraction decides
+    assert cloudy.any() and (~cloudy).any()
+    f, w, t, g = bi["fsfc"], bi["ssac"], bi["tauc"], bi["asmc"]
+    assert np.array_equal(o["taucloud"][cloudy], ((1.0 - f * w) * t)[cloudy])
+    assert np.array_equal(o["ssacloud"][cloudy], ((1.0 - f) * w / (1.0 - f * w))[cloudy])
+    assert np.array_equal(o["asmcloud"][cloudy], ((g - f) / (1.0 - f))[cloudy])
+    assert np.array_equal(o["taucldorig"], t)
+    for k, v in (("taucloud", 0.0), ("ssacloud", 1.0), ("asmcloud", 0.0)):
+        assert (o[k][~cloudy] == v).all(), k
+
+
+@pytest.mark.parametrize("iceflag", [1, 2, 3])
+def test_oracle_cldprop_sw_water_paths(iceflag):
+    """Optics from water paths (inflag 2): delta scaling only lowers the
+    optical depth, albedos in (0, 1], asymmetries in [0, 1); the band values
+    feed mcica_subcol_sw in its (14, ncol, nlay) layout."""
+    st = make_state(ProfileSpec(ncol=6, nlay=30, seed=20 + iceflag, cloud_prob=0.7))
+    rng = np.random.default_rng(iceflag)
+    lo, hi = {1: (13.0, 130.0), 2: (5.0, 131.0), 3: (5.0, 140.0)}[iceflag]
+    st["rei"] = np.asfortranarray(rng.uniform(lo, hi, st["rei"].shape))
+    st["rel"] = np.asfortranarray(rng.uniform(2.5, 60.0, st["rel"].shape))
+    o, status = pyoracle.cldprop_sw_columns(st, iceflag=iceflag)
+    assert (status == 0).all()
+    cl = o["taucloud"] > 0
+    assert cl.any()
+    assert (o["taucloud"][cl] <= o["taucldorig"][cl] * (1 + 1e-12)).all()
+    assert (o["ssacloud"][cl] > 0).all() and (o["ssacloud"][cl] <= 1.0).all()
+    assert (o["asmcloud"][cl] >= 0).all() and (o["asmcloud"][cl] < 1.0).all()
+    band = {"tauc": o["taucloud"], "ssac": o["ssacloud"], "asmc": o["asmcloud"], "fsfc": np.zeros_like(o["taucloud"])}
+    mc = pyoracle.mcica_subcol_sw(st, band, 3, 9)
+    ngb = np.repeat(np.arange(14), NGS)
+    cloudy = mc["cldfmcl"] == 1.0
+    assert np.array_equal(mc["taucmcl"][cloudy], o["taucloud"][ngb][cloudy])
+
+
+def test_oracle_cldprop_sw_stops_on_a_radius_out_of_bounds():
+    st = make_state(ProfileSpec(ncol=3, nlay=12, seed=5, cloud_prob=1.0))
+    st["rei"] = np.asfortranarray(np.full(st["rei"].shape, 150.0))
+    _, status = pyoracle.cldprop_sw_columns(st, iceflag=3)
+    icy = ((st["cldfrac"] >= 1e-20) & (st["ciwp"] > 0)).any(axis=1)
+    assert (status[icy] == 5).all() and (status[~icy] == 0).all()  # 'ICE GENERALIZED EFFECTIVE SIZE OUT OF BOUNDS'
+
+
 # ---------------------------------------------------------------- McICA for the shortwave
 def _sw_band(st, seed=3):
     ncol, nlay = st["play"].shape
