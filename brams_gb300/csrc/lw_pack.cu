@@ -130,6 +130,40 @@ __global__ void __launch_bounds__(128) unpack_kernel(UnpackArgs a) {
   a.fthrd[c3 + a.mzp - 1] = f;
 }
 
+// the shortwave-only inputs and output of the same loops: coszen and the
+// four albedos per packed column (:989, :992-996; the albedos stay 0 on the
+// first call, as allocated at :933-936), and rshort from the surface
+// downward shortwave flux, 0 below 0.5 W m-2 (:1448-1449)
+struct PackSwArgs {
+  int mxp, ia, ja, ni, ncol, firsttime;
+  const float *cosz, *albedt;
+  double *coszen, *asdir, *asdif, *aldir, *aldif;
+};
+__global__ void __launch_bounds__(128) pack_sw_kernel(PackSwArgs a) {
+  const int noc = blockIdx.x * blockDim.x + threadIdx.x;
+  if (noc >= a.ncol) return;
+  const long long c2 = (long long)(a.ia - 1 + noc % a.ni) + (long long)a.mxp * (a.ja - 1 + noc / a.ni);
+  a.coszen[noc] = (double)a.cosz[c2];
+  const double al = a.firsttime ? 0.0 : (double)a.albedt[c2];
+  a.asdir[noc] = al;
+  a.aldir[noc] = al;
+  a.asdif[noc] = al;
+  a.aldif[noc] = al;
+}
+
+struct UnpackSwArgs {
+  int mxp, ia, ja, ni, ncol;
+  const double* swdflx;
+  float* rshort;
+};
+__global__ void __launch_bounds__(128) unpack_sw_kernel(UnpackSwArgs a) {
+  const int noc = blockIdx.x * blockDim.x + threadIdx.x;
+  if (noc >= a.ncol) return;
+  const long long c2 = (long long)(a.ia - 1 + noc % a.ni) + (long long)a.mxp * (a.ja - 1 + noc / a.ni);
+  const double f = a.swdflx[noc];
+  a.rshort[c2] = f < 0.5 ? 0.0f : (float)f;
+}
+
 bool box_ok(int mzp, int mxp, int myp, int ia, int iz, int ja, int jz) {
   return mzp >= 3 && mxp >= 1 && myp >= 1 && ia >= 1 && iz >= ia && iz <= mxp && ja >= 1 && jz >= ja && jz <= myp &&
          (long long)(iz - ia + 1) * (jz - ja + 1) <= 0x7FFFFFFFLL;
@@ -185,4 +219,33 @@ int gb_rtm_unpack_lw_device(gb_lw_context* ctx, void* stream, int mzp, int mxp, 
   gbpk::unpack_kernel<<<(ncol + 127) / 128, 128, 0, (cudaStream_t)stream>>>(a);
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? GB_LW_OK : gb_ctx_fail(ctx, e, "tendency write-back launch");
+}
+
+int gb_rtm_pack_sw_device(gb_lw_context* ctx, void* stream, int mxp, int myp, int ia, int iz, int ja, int jz,
+                          int firsttime, const float* cosz, const float* albedt, double* coszen, double* asdir,
+                          double* asdif, double* aldir, double* aldif) {
+  if (!ctx || !gbpk::box_ok(3, mxp, myp, ia, iz, ja, jz) || !cosz || !albedt || !coszen || !asdir || !asdif ||
+      !aldir || !aldif)
+    return GB_LW_E_ARGS;
+  const int ni = iz - ia + 1, ncol = ni * (jz - ja + 1);
+  cudaSetDevice(ctx->device);
+  gbpk::PackSwArgs a{};
+  a.mxp = mxp, a.ia = ia, a.ja = ja, a.ni = ni, a.ncol = ncol, a.firsttime = firsttime != 0;
+  a.cosz = cosz, a.albedt = albedt, a.coszen = coszen, a.asdir = asdir, a.asdif = asdif, a.aldir = aldir;
+  a.aldif = aldif;
+  gbpk::pack_sw_kernel<<<(ncol + 127) / 128, 128, 0, (cudaStream_t)stream>>>(a);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? GB_LW_OK : gb_ctx_fail(ctx, e, "shortwave packing launch");
+}
+
+int gb_rtm_unpack_sw_device(gb_lw_context* ctx, void* stream, int mxp, int myp, int ia, int iz, int ja, int jz,
+                            const double* swdflx, float* rshort) {
+  if (!ctx || !gbpk::box_ok(3, mxp, myp, ia, iz, ja, jz) || !swdflx || !rshort) return GB_LW_E_ARGS;
+  const int ni = iz - ia + 1, ncol = ni * (jz - ja + 1);
+  cudaSetDevice(ctx->device);
+  gbpk::UnpackSwArgs a{};
+  a.mxp = mxp, a.ia = ia, a.ja = ja, a.ni = ni, a.ncol = ncol, a.swdflx = swdflx, a.rshort = rshort;
+  gbpk::unpack_sw_kernel<<<(ncol + 127) / 128, 128, 0, (cudaStream_t)stream>>>(a);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? GB_LW_OK : gb_ctx_fail(ctx, e, "shortwave write-back launch");
 }

@@ -51,7 +51,7 @@ EXPORTS = [
     "gb_rtm_ozone_load", "gb_rtm_ozone_free", "gb_rtm_ozone_lw",
     "gb_rrtmg_lw_shard_plan", "gb_rrtmg_lw_grid_slice", "gb_rrtmg_lw_nomcica", "gb_rrtmg_lw_nomcica_device",
     "gb_rrtmg_sw_ini", "gb_rrtmg_sw_set_precision", "gb_rrtmg_sw", "gb_rrtmg_sw_device", "gb_mcica_subcol_sw", "gb_mcica_subcol_sw_device",
-    "gb_cldprop_sw_device",
+    "gb_cldprop_sw_device", "gb_rtm_pack_sw_device", "gb_rtm_unpack_sw_device",
 ]
 MLP_MMA_SYNC, MLP_TCGEN05 = 0, 1
 MLP_NPARAM = 72352
@@ -141,6 +141,8 @@ def load_library(path: str = LIB_PATH):
         L.gb_cldprop_lw_device.argtypes = [P, P, I, I, I, I, I] + [P] * 7 + [LL, P]
         L.gb_rtm_pack_lw_device.argtypes = [P, P] + [I] * 9 + [P] * 31 + [LL]
         L.gb_rtm_unpack_lw_device.argtypes = [P, P] + [I] * 7 + [P] * 3 + [LL, LL, P, P]
+        L.gb_rtm_pack_sw_device.argtypes = [P, P] + [I] * 7 + [P] * 7
+        L.gb_rtm_unpack_sw_device.argtypes = [P, P] + [I] * 6 + [P] * 2
         L.gb_rtm_ozone_load.argtypes = [C.c_char_p, C.POINTER(P)]
         L.gb_rtm_ozone_free.argtypes = [P]
         L.gb_rtm_ozone_lw.argtypes = [P, I, I, P, LL, P, I, P, LL]
@@ -436,6 +438,22 @@ class Context:
             self.h, _ptr(stream or 0), mzp, mxp, myp, ia, iz, ja, jz, _ptr(hr), _ptr(swhr), _ptr(dflx),
             ld_hr if ld_hr is not None else ncol, ld_flx if ld_flx is not None else ncol, _ptr(fthrd),
             _ptr(rlong)))
+
+    def rtm_pack_sw_device(self, mxp: int, myp: int, box, cosz, albedt, out: dict, firsttime: bool = False,
+                           stream=None) -> None:
+        """gb_rtm_pack_sw_device: BRAMS's cosz and albedt (float32 (mxp, myp)) into coszen and
+        the albedos asdir, asdif, aldir, aldif (float64 (ncol) device arrays in out)."""
+        ia, iz, ja, jz = box
+        _check(self.L, self.h, self.L.gb_rtm_pack_sw_device(
+            self.h, _ptr(stream or 0), mxp, myp, ia, iz, ja, jz, 1 if firsttime else 0, _ptr(cosz), _ptr(albedt),
+            *[_ptr(out[k]) for k in ("coszen", "asdir", "asdif", "aldir", "aldif")]))
+
+    def rtm_unpack_sw_device(self, mxp: int, myp: int, box, swdflx, rshort, stream=None) -> None:
+        """gb_rtm_unpack_sw_device: the surface downward shortwave flux (the first ncol values of
+        swdflx) into BRAMS's rshort (float32 (mxp, myp)), 0 below 0.5 W m-2."""
+        ia, iz, ja, jz = box
+        _check(self.L, self.h, self.L.gb_rtm_unpack_sw_device(
+            self.h, _ptr(stream or 0), mxp, myp, ia, iz, ja, jz, _ptr(swdflx), _ptr(rshort)))
 
     def mcica_subcol_lw_device(self, ncol: int, nlay: int, ptrs: dict, icld: int, permuteseed: int, irng: int = 1,
                                seed_per_column: bool = True, stream=None, ld: int | None = None) -> None:

@@ -238,6 +238,20 @@ int gb_rtm_unpack_lw_device(gb_lw_context* ctx, void* stream, int mzp, int mxp, 
                             int jz, const double* hr, const double* swhr, const double* dflx, int64_t ld_hr,
                             int64_t ld_flx, float* fthrd, float* rlong);
 
+/* The shortwave-only parts of the same packing and write-back on DEVICE
+ * arrays: coszen(column) = cosz(i, j) and the four albedos asdir asdif aldir
+ * aldif = albedt(i, j), 0 when firsttime is nonzero (rtm_driver.f90:989,
+ * 992-996), all (ncol) with the columns in the packing order; and
+ * rshort(i, j) = swdflx(column, 1), 0 where that flux is below 0.5 W m-2
+ * (:1448-1449).  cosz, albedt and rshort are BRAMS's float fields
+ * (mxp, myp); swdflx is the first level of rrtmg_sw's output (its first
+ * ncol values). */
+int gb_rtm_pack_sw_device(gb_lw_context* ctx, void* stream, int mxp, int myp, int ia, int iz, int ja, int jz,
+                          int firsttime, const float* cosz, const float* albedt, double* coszen, double* asdir,
+                          double* asdif, double* aldir, double* aldif);
+int gb_rtm_unpack_sw_device(gb_lw_context* ctx, void* stream, int mxp, int myp, int ia, int iz, int ja, int jz,
+                            const double* swdflx, float* rshort);
+
 /* Diagnostics (no counterpart in the reference's interface): runs the same
  * column kernel on host arrays (tight layout, ld = ncol) and also returns
  * the gas-plus-aerosol optical depth taut and the Planck fraction of every

@@ -8,7 +8,9 @@ Follows ``radrrtmdrv`` in src/brams/radiate/rtm_driver.f90:
   * the extrapolated top level, :1045-1050;
   * layer and interface values, :1052-1076;
   * fixed trace gases and vapour volume mixing ratios, :1176-1231;
-  * theta tendency and surface longwave flux out, :1443-1456.
+  * theta tendency and surface longwave flux out, :1443-1456;
+  * the shortwave-only inputs (cosine of the zenith angle, albedos), :989,
+    :992-996, and the surface shortwave flux out, :1448-1449.
 BRAMS holds its fields and constants in default real (float32); the
 statements mix them with real(8) exactly as below (each float32 operation is
 rounded to float32 before it meets a double).  Ozone, aerosols and the
@@ -127,3 +129,26 @@ def unpack_lw(hr, dflx, swhr, mzp, mxp, myp, ia, iz, ja, jz, fthrd=None, rlong=N
     fthrd[0, i, j] = fthrd[1, i, j]
     fthrd[mzp - 1, i, j] = fthrd[mzp - 2, i, j]
     return fthrd, rlong
+
+
+def pack_sw(cosz, albedt, ia, iz, ja, jz, firsttime=False):
+    """BRAMS's cosz and albedt (float32 (mxp, myp)) -> coszen and the four
+    albedos of rrtmg_sw (ncol,) float64 (:989, :992-996; the albedos keep the
+    0 they are allocated with on the first call, :933-936)."""
+    i, j = column_index(cosz.shape[0], cosz.shape[1], ia, iz, ja, jz)
+    out = {"coszen": f8(cosz[i, j])}
+    al = np.zeros(i.size) if firsttime else f8(albedt[i, j])
+    for k in ("asdir", "aldir", "asdif", "aldif"):
+        out[k] = al.copy()
+    return out
+
+
+def unpack_sw(swdflx, mxp, myp, ia, iz, ja, jz, rshort=None):
+    """The surface downward shortwave flux into BRAMS's float32 rshort
+    (:1448-1449): 0 where swdflx(:, 1) < 0.5.  Columns outside the packed
+    range keep rshort as given."""
+    rshort = np.zeros((mxp, myp), np.float32) if rshort is None else rshort.copy()
+    i, j = column_index(mxp, myp, ia, iz, ja, jz)
+    v = swdflx[:, 0]
+    rshort[i, j] = np.where(v < 0.5, f4(0.0), f4(v))
+    return rshort

@@ -56,3 +56,22 @@ def test_write_back_copies_the_end_levels_and_leaves_other_columns():
     assert col[0] == col[1] and col[mzp - 1] == col[mzp - 2]
     assert (fthrd[:, 0, :] == 7.0).all() and (fthrd[:, :, 0] == 7.0).all()
     assert rlong[0, 0] == 9.0 and rlong[1, 1] == np.float32(dflx[0, 0])
+
+
+def test_shortwave_inputs_and_surface_flux():
+    """coszen and the four albedos per packed column (albedos 0 on the first
+    call), and rshort from the surface downward shortwave flux, 0 below
+    0.5 W m-2, other columns untouched."""
+    rs = np.random.default_rng(4)
+    cosz = rs.uniform(-0.3, 1.0, (5, 4)).astype(np.float32)
+    albedt = rs.uniform(0.05, 0.6, (5, 4)).astype(np.float32)
+    p = BP.pack_sw(cosz, albedt, 2, 4, 2, 3)
+    assert p["coszen"][0] == np.float64(cosz[1, 1]) and p["coszen"].size == 6
+    for k in ("asdir", "asdif", "aldir", "aldif"):
+        assert np.array_equal(p[k], p["asdir"]) and p[k][3] == np.float64(albedt[1, 2])
+    p0 = BP.pack_sw(cosz, albedt, 2, 4, 2, 3, firsttime=True)
+    assert (p0["asdir"] == 0.0).all() and np.array_equal(p0["coszen"], p["coszen"])
+    swdflx = np.array([[800.0], [0.49], [0.5], [1e-9], [350.25], [12.0]])
+    r = BP.unpack_sw(swdflx, 5, 4, 2, 4, 2, 3, np.full((5, 4), 3.0, np.float32))
+    assert r[1, 1] == np.float32(800.0) and r[2, 1] == 0.0 and r[3, 1] == np.float32(0.5) and r[1, 2] == 0.0
+    assert r[0, 0] == 3.0 and r[4, 3] == 3.0

@@ -1,5 +1,6 @@
 """BRAMS's column packing and tendency write-back on the device
-(gb_rtm_pack_lw_device / gb_rtm_unpack_lw_device) against the CPU
+(gb_rtm_pack_lw_device / gb_rtm_unpack_lw_device, and the shortwave-only
+gb_rtm_pack_sw_device / gb_rtm_unpack_sw_device) against the CPU
 restatement (oracle/brams_pack.py), and the whole caller-side path: model
 state in, packed on the device, cldprop and the fused-cloud solver, theta
 tendency out, against the same chain on the FP64 oracle."""
@@ -129,3 +130,29 @@ def test_model_state_in_theta_tendency_out(ctx):
     assert np.abs(got_f - ref_f).max() <= 0.01 / 86400.0, float(np.abs(got_f - ref_f).max() * 86400.0)
     assert np.abs(got_r - ref_r).max() <= 0.05
     assert np.abs(ref_f).max() > 1e-6  # the tendency is not trivially zero
+
+
+@pytest.mark.parametrize("firsttime", [False, True])
+def test_shortwave_pack_and_unpack_match_oracle(ctx, firsttime):
+    import torch
+
+    mxp, myp, box = 9, 7, (2, 8, 3, 7)
+    rs = np.random.default_rng(17)
+    cosz = rs.uniform(-0.3, 1.0, (mxp, myp)).astype(np.float32)
+    albedt = rs.uniform(0.05, 0.6, (mxp, myp)).astype(np.float32)
+    ref = BP.pack_sw(cosz, albedt, *box, firsttime=firsttime)
+    ncol = ref["coszen"].size
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a.T)).cuda()  # noqa: E731
+    out = {k: torch.full((ncol,), -7.0, dtype=torch.float64, device="cuda") for k in ref}
+    ctx.rtm_pack_sw_device(mxp, myp, box, dev(cosz), dev(albedt), out, firsttime=firsttime)
+    swdflx = rs.uniform(0.0, 900.0, (ncol + 2, 4))
+    swdflx[::5, 0] = rs.uniform(0.0, 0.6, swdflx[::5, 0].shape)  # fluxes around the 0.5 W m-2 cut
+    r0 = np.full((mxp, myp), 2.0, np.float32)
+    want = BP.unpack_sw(swdflx[:ncol], mxp, myp, *box, r0)
+    rsh = dev(r0)
+    ctx.rtm_unpack_sw_device(mxp, myp, box, dev(swdflx[:, 0].copy()), rsh)
+    torch.cuda.synchronize()
+    assert ctx.sync_status() == 0
+    for k in ref:
+        assert np.array_equal(out[k].cpu().numpy(), ref[k]), k
+    assert np.array_equal(rsh.cpu().numpy().T, want)
