@@ -65,7 +65,36 @@ def sw_case(name, ncol, nlay, seed, permuteseed=5):
     np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrs)
 
 
+def nomcica_case(name, ncol, nlay, seed):
+    """The non-McICA driver (rrtmg_lw_rad.nomcica.f90) on layer clouds: the
+    first columns carry designed fraction profiles (growing, shrinking and
+    equal neighbours, blocks at the surface and the top, overcast layers,
+    fractions between cldprop's 1e-20 and the transfer's 1e-6 tests); the
+    outputs of random (icld 1) and maximum/random (icld 2) overlap."""
+    st = make_state(ProfileSpec(ncol=ncol, nlay=nlay, seed=seed, t_noise=3.0, h2o_sigma=0.4, cloud_prob=0.6))
+    cf = st["cldfrac"].copy()
+    designed = [(5, [0.3, 0.6, 0.45, 0.7, 0.7, 0.2]), (nlay - 2, [0.8, 0.5]), (0, [0.4, 0.6, 0.6, 0.3]),
+                (8, [5e-7, 0.3, 5e-7, 0.0, 0.6]), (3, [1.0, 1.0, 0.5, 1.0])]
+    for c, (l0, prof) in enumerate(designed):
+        cf[c] = 0.0
+        cf[c, l0:l0 + len(prof)] = prof
+    rng = np.random.default_rng(seed)
+    cloudy = cf > 0
+    st["cldfrac"] = np.asfortranarray(cf)
+    st["clwp"] = np.asfortranarray(np.where(cloudy & (st["tlay"] > 240.0), rng.uniform(5.0, 80.0, cf.shape), 0.0))
+    st["ciwp"] = np.asfortranarray(np.where(cloudy & (st["tlay"] < 268.0), rng.uniform(2.0, 40.0, cf.shape), 0.0))
+    st["rel"] = np.asfortranarray(rng.uniform(4.0, 20.0, cf.shape))
+    st["rei"] = np.asfortranarray(rng.uniform(20.0, 80.0, cf.shape))
+    st["tauaer"] = np.asfortranarray(rng.uniform(0.0, 0.02, st["tauaer"].shape))
+    arrs = {f"in_{k}": v for k, v in st.items()}
+    for icld in (1, 2):
+        out = pyoracle.rrtmg_lw_nomcica(st, icld)
+        arrs.update({f"out{icld}_{k}": v for k, v in out.items() if isinstance(v, np.ndarray)})
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrs)
+
+
 def main():
+    nomcica_case("lw_nomcica_10x38", 10, 38, seed=20240603)
     sw_case("sw_8x45", 8, 45, seed=20240602)
     case("lw_16x38", 16, 38, seed=20240601)
     case("lw_8x60_top5hpa", 8, 60, seed=77, ptop=5.0, t_noise=4.0, h2o_sigma=0.5)

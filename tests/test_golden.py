@@ -95,3 +95,33 @@ def test_gpu_matches_sw_golden(ctx, bits):
         assert np.abs(out[k] - ref[k]).max() <= flux_tol, k
     for k in ("swhr", "swhrc"):
         assert np.abs(out[k] - ref[k]).max() <= hr_tol, k
+
+
+def _load_nomcica(name="lw_nomcica_10x38"):
+    z = np.load(os.path.join(G, name + ".npz"))
+    st = {k[3:]: np.asfortranarray(z[k]) for k in z.files if k.startswith("in_")}
+    outs = {icld: {k[5:]: z[k] for k in z.files if k.startswith(f"out{icld}_")} for icld in (1, 2)}
+    return st, outs
+
+
+@pytest.mark.parametrize("icld", [1, 2])
+def test_oracle_reproduces_nomcica_golden(icld):
+    st, outs = _load_nomcica()
+    out = pyoracle.rrtmg_lw_nomcica(st, icld)
+    for k in OUTS:
+        assert np.allclose(out[k], outs[icld][k], rtol=1e-10, atol=1e-10), k
+    assert np.abs(out["dflx"] - out["dflxc"]).max() > 1.0  # the clouds are seen
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("icld", [1, 2])
+def test_gpu_matches_nomcica_golden(ctx, icld):
+    st, outs = _load_nomcica()
+    out = ctx.rrtmg_lw_nomcica(st, icld)
+    ref = outs[icld]
+    for k in ("uflx", "dflx", "uflxc", "dflxc"):
+        assert np.abs(out[k] - ref[k]).max() <= 0.05, k
+    for k in ("hr", "hrc"):
+        assert np.abs(out[k] - ref[k]).max() <= 0.01, k
+    for k in ("duflx_dt", "duflxc_dt"):
+        assert np.abs(out[k] - ref[k]).max() <= 1e-3, k
