@@ -1176,6 +1176,43 @@ int ora_rrtmg_sw(int ncol, int nlay, int* icld, int* iaer, const double* play, c
   return 0;
 }
 
+// cldprmc_sw alone on one column's McICA cells (for cross-checks of the two
+// cloud-optics restatements): cldfmc taucmc ssacmc asmcmc fsfcmc ciwpmc
+// clwpmc (112, nlayers), reicmc relqmc (nlayers); outputs taormc taucmc
+// ssacmc asmcmc (112, nlayers).  Returns cldprmc_sw's status.
+int ora_cldprmc_sw_column(int nlayers, int inflag, int iceflag, int liqflag, const double* cldfmc,
+                          const double* taucmc, const double* ssacmc, const double* asmcmc, const double* fsfcmc,
+                          const double* ciwpmc, const double* clwpmc, const double* reicmc, const double* relqmc,
+                          double* taormc_out, double* taucmc_out, double* ssacmc_out, double* asmcmc_out) {
+  if (!g_ready) return ERR_NOT_INIT;
+  Col c;
+  c.alloc(nlayers);
+  for (int lay = 1; lay <= nlayers; ++lay) {
+    for (int ig = 1; ig <= NGPT; ++ig) {
+      const int i = (ig - 1) + NGPT * (lay - 1);
+      c.CM(c.cldfmc, ig, lay) = cldfmc[i];
+      c.CM(c.taucmc, ig, lay) = taucmc[i];
+      c.CM(c.ssacmc, ig, lay) = ssacmc[i];
+      c.CM(c.asmcmc, ig, lay) = asmcmc[i];
+      c.CM(c.fsfcmc, ig, lay) = fsfcmc[i];
+      c.CM(c.ciwpmc, ig, lay) = ciwpmc[i];
+      c.CM(c.clwpmc, ig, lay) = clwpmc[i];
+    }
+    c.reicmc[lay] = reicmc[lay - 1];
+    c.relqmc[lay] = relqmc[lay - 1];
+  }
+  const int err = cldprmc_sw(c, inflag, iceflag, liqflag);
+  for (int lay = 1; lay <= nlayers; ++lay)
+    for (int ig = 1; ig <= NGPT; ++ig) {
+      const int i = (ig - 1) + NGPT * (lay - 1);
+      taormc_out[i] = c.CM(c.taormc, ig, lay);
+      taucmc_out[i] = c.CM(c.taucmc, ig, lay);
+      ssacmc_out[i] = c.CM(c.ssacmc, ig, lay);
+      asmcmc_out[i] = c.CM(c.asmcmc, ig, lay);
+    }
+  return err;
+}
+
 // cldprop_sw (rrtmg_sw_cldprop.f90:53-365): the band cloud optics of one
 // column, which BRAMS computes per column and hands to mcica_subcol_sw
 // (rtm_driver.f90:1356-1368).  Inputs cldfrac ciwp clwp rei rel (nlayers);

@@ -333,6 +333,45 @@ def test_oracle_cldprop_sw_water_paths(iceflag):
     assert np.array_equal(mc["taucmcl"][cloudy], o["taucloud"][ngb][cloudy])
 
 
+@pytest.mark.parametrize("inflag,iceflag", [(2, 1), (2, 2), (2, 3), (0, 3)])
+def test_the_two_cloud_optics_restatements_agree(inflag, iceflag):
+    """cldprop_sw (rrtmg_sw_cldprop.f90, per band and layer) and cldprmc_sw
+    (rrtmg_sw_cldprmc.f90, per g-point and layer), restated from two
+    reference files, give every overcast g-point exactly its band's values."""
+    import ctypes as C
+
+    ncol, nlay = 4, 24
+    st = make_state(ProfileSpec(ncol=ncol, nlay=nlay, seed=30 + iceflag, cloud_prob=0.7))
+    rng = np.random.default_rng(iceflag)
+    lo, hi = {1: (13.0, 130.0), 2: (5.0, 131.0), 3: (5.0, 140.0)}[iceflag]
+    st["rei"] = np.asfortranarray(rng.uniform(lo, hi, (ncol, nlay)))
+    st["rel"] = np.asfortranarray(rng.uniform(2.5, 60.0, (ncol, nlay)))
+    bi = {"tauc": rng.uniform(0.1, 5.0, (14, ncol, nlay)), "ssac": rng.uniform(0.8, 0.999, (14, ncol, nlay)),
+          "asmc": rng.uniform(0.6, 0.9, (14, ncol, nlay)), "fsfc": rng.uniform(0.0, 0.4, (14, ncol, nlay))}
+    band, status = pyoracle.cldprop_sw_columns(st, bi if inflag == 0 else None, inflag, iceflag, 1)
+    assert (status == 0).all()
+    L = pyoracle.sw_lib()
+    ngb = np.repeat(np.arange(14), NGS)
+    p = pyoracle._p
+    for i in range(ncol):
+        over = (st["cldfrac"][i] >= 1e-20).astype(np.float64)
+        g_in = lambda a: np.asfortranarray(np.broadcast_to(a, (112, nlay)), dtype=np.float64)  # noqa: E731
+        cm = {"cldfmc": g_in(over), "ciwpmc": g_in(st["ciwp"][i] * over), "clwpmc": g_in(st["clwp"][i] * over)}
+        for k in ("tauc", "ssac", "asmc", "fsfc"):
+            cm[k + "mc"] = g_in(bi[k][ngb, i, :] if inflag == 0 else np.zeros((112, nlay)))
+        outs = [np.zeros((112, nlay), order="F") for _ in range(4)]
+        rc = L.ora_cldprmc_sw_column(C.c_int(nlay), C.c_int(inflag), C.c_int(iceflag), C.c_int(1),
+                                     *[p(cm[k]) for k in ("cldfmc", "taucmc", "ssacmc", "asmcmc", "fsfcmc",
+                                                          "ciwpmc", "clwpmc")],
+                                     p(np.ascontiguousarray(st["rei"][i])), p(np.ascontiguousarray(st["rel"][i])),
+                                     *[p(o) for o in outs])
+        assert rc == 0
+        cloudy = over.astype(bool)
+        assert cloudy.any()
+        for o, k in zip(outs, ("taucldorig", "taucloud", "ssacloud", "asmcloud")):
+            assert np.array_equal(o[:, cloudy], band[k][ngb, i][:, cloudy]), k
+
+
 def test_oracle_cldprop_sw_stops_on_a_radius_out_of_bounds():
     st = make_state(ProfileSpec(ncol=3, nlay=12, seed=5, cloud_prob=1.0))
     st["rei"] = np.asfortranarray(np.full(st["rei"].shape, 150.0))
