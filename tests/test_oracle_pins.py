@@ -4,7 +4,9 @@ The reference ships no tests, golden vectors or fixtures for this path, and
 its k-distribution data and a Fortran compiler are absent here, so the
 oracle is pinned by: published Mersenne-twister outputs, the lookup-table
 formulas of rrtmg_lw_ini, analytic radiative-transfer limits, and internal
-consistency (heating rate = heatfac * dF/dp, clear == total without clouds).
+consistency (heating rate = heatfac * dF/dp, clear == total without clouds),
+and the agreement of two restatements of the same physics from separate
+reference files (cldprop per band, cldprmc per g-point).
 """
 import numpy as np
 import pytest
@@ -164,3 +166,31 @@ def test_oracle_rejects_like_reference():
         bad["relqmcl"] = np.asfortranarray(np.full_like(mc["relqmcl"], 1.0))
         with pytest.raises(RuntimeError, match="LIQUID EFFECTIVE RADIUS"):
             pyoracle.rrtmg_lw(st, bad)
+
+
+LW_NG = [10, 12, 16, 14, 16, 8, 12, 8, 12, 6, 8, 8, 4, 2, 2, 2]
+
+
+@pytest.mark.parametrize("iceflag,liqflag", [(2, 1), (3, 1)])
+def test_lw_cloud_optics_restatements_agree(iceflag, liqflag):
+    """cldprop (per band, rrtmg_lw_cldprop.f90) and cldprmc (per g-point,
+    rrtmg_lw_cldprmc.f90), restated from two reference files: for overcast
+    layers every g-point's cloud optical depth equals its band's (options
+    with 16 cloud bands)."""
+    ncol, nlay = 3, 20
+    st = make_state(ProfileSpec(ncol=ncol, nlay=nlay, seed=40 + iceflag, cloud_prob=0.7))
+    rng = np.random.default_rng(iceflag)
+    lo, hi = {2: (5.0, 131.0), 3: (5.0, 140.0)}[iceflag]
+    st["rei"] = np.asfortranarray(rng.uniform(lo, hi, (ncol, nlay)))
+    st["rel"] = np.asfortranarray(rng.uniform(2.5, 60.0, (ncol, nlay)))
+    band = pyoracle.cldprop_columns(st, 2, iceflag, liqflag)
+    over = (st["cldfrac"] >= 1e-20).astype(np.float64)
+    g = lambda a: np.asfortranarray(np.broadcast_to(a[None], (140, ncol, nlay)), dtype=np.float64)  # noqa: E731
+    mc = {"cldfmcl": g(over), "ciwpmcl": g(st["ciwp"] * over), "clwpmcl": g(st["clwp"] * over),
+          "taucmcl": g(np.zeros((ncol, nlay))), "reicmcl": st["rei"], "relqmcl": st["rel"]}
+    ngb = np.repeat(np.arange(16), LW_NG)
+    for i in range(ncol):
+        im = pyoracle.column_intermediates(st, mc, i + 1, icld=3, inflglw=2, iceflglw=iceflag, liqflglw=liqflag)
+        cloudy = over[i].astype(bool) & ((st["ciwp"][i] + st["clwp"][i]) >= 1e-20)
+        assert cloudy.any()
+        assert np.array_equal(im["taucmc"][:, cloudy], band[ngb, i][:, cloudy])
