@@ -31,6 +31,37 @@ def test_library_exports_every_declared_symbol():
     assert sorted(EXPORTS) == names
 
 
+def test_header_is_c_and_every_declared_function_links(tmp_path):
+    """include/gb_rrtmg_lw.h is plain C (C89 and C99, pedantic) and C++, and a
+    C program that takes the address of every declared function links
+    against the library (C linkage, the header's names)."""
+    import shutil
+    import subprocess
+
+    from brams_gb300.build import build
+
+    gcc, gxx = shutil.which("gcc"), shutil.which("g++")
+    if not gcc or not gxx:
+        pytest.skip("no host C compiler")
+    lib = build()
+    inc = os.path.join(ROOT, "include")
+    hdr = os.path.join(inc, "gb_rrtmg_lw.h")
+    for cmd in ([gcc, "-std=c89", "-pedantic", "-Wall", "-Werror", "-fsyntax-only", "-x", "c", hdr],
+                [gcc, "-std=c99", "-pedantic", "-Wall", "-Werror", "-fsyntax-only", "-x", "c", hdr],
+                [gxx, "-std=c++11", "-pedantic", "-Wall", "-Werror", "-fsyntax-only", "-x", "c++", hdr]):
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, (cmd[1], r.stderr)
+    names = _declared()
+    src = tmp_path / "abi.c"
+    src.write_text('#include "gb_rrtmg_lw.h"\n#include <stdio.h>\nint main(void) {\n  void (*fns[])(void) = {\n'
+                   + ",\n".join(f"    (void (*)(void)){n}" for n in names)
+                   + '\n  };\n  printf("%d\\n", (int)(sizeof fns / sizeof fns[0]));\n  return 0;\n}\n')
+    r = subprocess.run([gcc, "-std=c99", "-pedantic", "-Wall", "-Werror", "-I", inc, str(src), "-L",
+                        os.path.dirname(lib), "-lgb_rrtmg_lw", "-Wl,--allow-shlib-undefined", "-o",
+                        str(tmp_path / "abi")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_library_init_without_gpu_fails_cleanly():
     import torch
 
