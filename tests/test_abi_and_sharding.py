@@ -62,6 +62,26 @@ def test_header_is_c_and_every_declared_function_links(tmp_path):
     assert r.returncode == 0, r.stderr
 
 
+def test_integration_guide_interfaces_match_the_header():
+    """Every Fortran bind(C) interface INTEGRATION.md shows a maintainer has
+    the argument list (names, order) of the header's prototype."""
+    guide = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "gb_rrtmg_lw.h")).read(), flags=re.S)
+    protos = {}
+    for m in re.finditer(r"\b(?:int|size_t)\s+(gb_\w+)\s*\((.*?)\);", hdr, flags=re.S):
+        params = [q.strip() for q in m.group(2).split(",") if q.strip() and q.strip() != "void"]
+        protos[m.group(1)] = [re.findall(r"(\w+)\s*$", q)[0].lower() for q in params]
+    found = 0
+    for m in re.finditer(r"function\s+(gb_\w+)\s*\((.*?)\)\s*&?\s*bind\(C(?:,\s*name=\"(\w+)\")?\)", guide,
+                         flags=re.S):
+        name, args, cname = m.group(1), m.group(2), m.group(3) or m.group(1)  # bind(C) alone: the Fortran name
+        assert name == cname and name in protos, name
+        fargs = [a.strip().lower() for a in args.replace("&", "").split(",") if a.strip()]
+        assert fargs == protos[name], (name, fargs, protos[name])
+        found += 1
+    assert found >= 15
+
+
 def test_library_init_without_gpu_fails_cleanly():
     import torch
 
