@@ -140,6 +140,41 @@ def test_scattering_atmosphere_conserves_energy():
     assert np.abs(o["swhr"]).max() < 1e-6
 
 
+@pytest.mark.parametrize("scale,laytrop", [(1.0, None), (0.08, 0), (None, "all")])
+def test_columns_wholly_above_or_below_the_tropopause_switch(scale, laytrop):
+    """Columns whose layers all lie above (laytrop 0) or all below (laytrop =
+    nlay) the lower/upper switch at log p = 4.56: the solar-layer searches of
+    the bands take their other branch (the reference reads jp(0) or
+    jp(nlayers+1) there, taken as 0).  Fluxes stay finite and the column
+    absorbs (net flux falls downward).  The incoming flux is the solar source
+    for a full column; a band whose solar-source layer the column never
+    reaches gets none (the reference leaves its source unset; the
+    restatement takes 0), so a squeezed column receives less."""
+    st = sw_state(ncol=6, nlay=30, seed=44)
+    if scale is None:  # squeeze the column between the surface and 200 hPa
+        for k in ("play", "plev"):
+            p = st[k]
+            st[k] = np.asfortranarray(p[:, :1] - (p[:, :1] - p) * (p[:, :1] - 200.0) / (p[:, :1] - p[:, -1:]))
+    elif scale != 1.0:
+        for k in ("play", "plev"):
+            st[k] = np.asfortranarray(st[k] * scale)
+    lp = np.log(st["play"])
+    if laytrop == 0:
+        assert (lp <= 4.56).all()
+    elif laytrop == "all":
+        assert (lp > 4.56).all()
+    o = pyoracle.rrtmg_sw(st, None, icld=0, iaer=10)
+    for k in ("swuflx", "swdflx", "swhr"):
+        assert np.isfinite(o[k]).all(), k
+    net = o["swdflx"] - o["swuflx"]
+    assert (net[:, -1] >= net[:, 0] - 1e-9).all()
+    toa = o["swdflx"][:, -1] / st["coszen"]
+    if scale == 1.0:
+        assert np.allclose(toa, 1368.22, atol=0.01)
+    else:
+        assert (toa > 0.0).all() and (toa < 1368.22 - 1.0).all()
+
+
 def test_clouds_add_reflection():
     st = sw_state(cloud_prob=0.8)
     mc = sw_mcica(st)
