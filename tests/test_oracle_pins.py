@@ -194,3 +194,28 @@ def test_lw_cloud_optics_restatements_agree(iceflag, liqflag):
         cloudy = over[i].astype(bool) & ((st["ciwp"][i] + st["clwp"][i]) >= 1e-20)
         assert cloudy.any()
         assert np.array_equal(im["taucmc"][:, cloudy], band[ngb, i][:, cloudy])
+
+
+@pytest.mark.parametrize("squeeze", ["upper", "lower"])
+def test_lw_columns_wholly_above_or_below_the_lower_upper_switch(squeeze):
+    """Columns whose layers all lie above (laytrop 0) or all below (laytrop =
+    nlay) setcoef's switch at log p = 4.56 take one taumol branch throughout:
+    fluxes stay finite and positive and the heating rate is still
+    heatfac * dF/dp."""
+    st = make_state(ProfileSpec(ncol=4, nlay=30, seed=6))
+    for k in ("play", "plev"):
+        p = st[k]
+        if squeeze == "upper":
+            st[k] = np.asfortranarray(p * 0.08)
+        else:  # between the surface and 200 hPa
+            st[k] = np.asfortranarray(p[:, :1] - (p[:, :1] - p) * (p[:, :1] - 200.0) / (p[:, :1] - p[:, -1:]))
+    lp = np.log(st["play"])
+    assert (lp <= 4.56).all() if squeeze == "upper" else (lp > 4.56).all()
+    out = pyoracle.rrtmg_lw(st, _clear_mc(st))
+    _, _, _, heatfac, _ = pyoracle.lookup_tables()
+    fnet = out["uflx"] - out["dflx"]
+    dp = st["plev"][:, :-1] - st["plev"][:, 1:]
+    assert np.allclose(heatfac * (fnet[:, :-1] - fnet[:, 1:]) / dp, out["hr"], rtol=1e-12, atol=1e-12)
+    for k in ("uflx", "dflx", "hr"):
+        assert np.isfinite(out[k]).all(), k
+    assert (out["uflx"] > 0).all() and (out["dflx"][:, :-1] >= 0).all()
